@@ -1,0 +1,58 @@
+// Work-queue construction for the persistent batched kernels: a counting sort of
+// the matrices by order, largest first, split into the size bins of kBinMax.
+// Runs on the device so that the whole batched pipeline is graph-capturable and
+// needs no host round trip to read the orders.
+#include "gs_internal.h"
+
+namespace gsk {
+namespace {
+
+__global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, int count,
+                                                   int* __restrict__ order, int* __restrict__ sched) {
+  __shared__ int hist[kSmallMax + 1];
+  __shared__ int pos[kSmallMax + 1];
+  for (int i = threadIdx.x; i <= kSmallMax; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < count; b += blockDim.x) {
+    int n = ns[b];
+    n = n < 0 ? 0 : (n > kSmallMax ? kSmallMax : n);
+    atomicAdd(&hist[n], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    int bin = kNumBins - 1;
+    sched[3 * bin] = 0;
+    for (int n = kSmallMax; n >= 0; --n) {
+      while (bin > 0 && n <= bin_max(bin - 1)) {
+        sched[3 * bin + 1] = run;
+        --bin;
+        sched[3 * bin] = run;
+      }
+      pos[n] = run;
+      run += hist[n];
+    }
+    sched[3 * bin + 1] = run;
+    while (bin > 0) {  // empty low bins
+      --bin;
+      sched[3 * bin] = run;
+      sched[3 * bin + 1] = run;
+    }
+    for (int i = 0; i < kNumBins; ++i) sched[3 * i + 2] = 0;
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < count; b += blockDim.x) {
+    int n = ns[b];
+    n = n < 0 ? 0 : (n > kSmallMax ? kSmallMax : n);
+    order[atomicAdd(&pos[n], 1)] = b;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s) {
+  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched);
+  return cudaGetLastError();
+}
+
+}  // namespace gsk

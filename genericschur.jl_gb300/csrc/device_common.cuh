@@ -1,0 +1,204 @@
+// Device helpers shared by the Schur kernels: IEEE constants, the small
+// Householder reflectors used by the Francis sweeps, and the standard-form 2x2
+// Schur block.  Everything here runs in FP64 on the CUDA cores (sm_103a has no
+// FP64 tensor-core MMA kind that would be faster than DFMA on this part).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gsk {
+
+constexpr double kEps = 2.220446049250313e-16;       // eps(Float64) = 2^-52
+constexpr double kFmin = 2.2250738585072014e-308;    // floatmin(Float64)
+constexpr double kSafemin = 2.2250738585072014e-308; // safemin(Float64) (util.jl:5-12)
+
+// Block reductions over the whole CTA.  `red` is shared scratch of >= 32 entries.
+template <int NT>
+__device__ __forceinline__ double block_max(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v || w != w) ? w : v;
+  }
+  if constexpr (NT > 32) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    v = red[0];
+#pragma unroll
+    for (int i = 1; i < NT / 32; ++i) {
+      double w = red[i];
+      v = (w > v || w != w) ? w : v;
+    }
+    __syncthreads();
+  }
+  return v;
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if constexpr (NT > 32) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    v = red[0];
+#pragma unroll
+    for (int i = 1; i < NT / 32; ++i) v += red[i];
+    __syncthreads();
+  }
+  return v;
+}
+
+// safescale! multiplier sequence (util.jl:41-80, kept as written there): fills
+// mul[0..k) with the factors to apply in order and returns k (at most 8).
+__device__ inline int safescale_factors(double cfrom, double cto, double* mul) {
+  const double smlnum = kSafemin;
+  const double bignum = 1.0 / smlnum;
+  double cfromc = cfrom, ctoc = cto;
+  int k = 0;
+  bool done = false;
+  while (!done && k < 8) {
+    double cfrom1 = cfromc * smlnum;
+    double m;
+    if (cfrom1 == cfromc) {
+      m = ctoc / cfromc; done = true;
+    } else {
+      double cto1 = ctoc / bignum;
+      if (cto1 == ctoc) {
+        m = cto; done = true; cfromc = 1.0;
+      } else if (fabs(cfrom1) > fabs(ctoc) && ctoc != 0.0) {
+        m = smlnum; done = false; cfromc = 1.0;
+      } else if (fabs(cto1) > fabs(cfromc)) {
+        m = bignum; done = false; cfromc = cfrom1;
+      } else {
+        m = ctoc / cfromc; done = true;
+      }
+    }
+    mul[k++] = m;
+  }
+  return k;
+}
+
+// Real Householder reflector of length 2 or 3 (householder.jl:12-54 semantics):
+// given x = (alpha, x1[, x2]) returns tau and overwrites x with (beta, v1[, v2]).
+// The 2-norm uses one square root when all entries lie in a range where squaring
+// cannot over/underflow, and falls back to the scaled form otherwise.
+__device__ __forceinline__ double reflector_small(double& a, double& x1, double& x2, int nr) {
+  if (nr <= 1) return 0.0;
+  const double ax1 = fabs(x1), ax2 = (nr == 3) ? fabs(x2) : 0.0;
+  if (ax1 == 0.0 && ax2 == 0.0) return 0.0;
+  const double aa = fabs(a);
+  const double big = fmax(aa, fmax(ax1, ax2));
+  double beta;
+  if (big < 1.0e150 && big > 1.0e-150) {
+    beta = sqrt(fma(a, a, fma(x1, x1, x2 * x2)));
+  } else {
+    const double r = 1.0 / big;
+    const double sa = a * r, s1 = x1 * r, s2 = x2 * r;
+    beta = big * sqrt(fma(sa, sa, fma(s1, s1, s2 * s2)));
+  }
+  const double sfmin = 2.0 * kFmin / kEps;
+  beta = -copysign(beta, a);
+  int kount = 0;
+  if (fabs(beta) < sfmin) {
+    // underflow-guard rescaling loop (householder.jl:25-42)
+    const double rsfmin = 1.0 / sfmin;
+    double al = a;
+    do {
+      ++kount;
+      x1 *= rsfmin; x2 *= rsfmin; beta *= rsfmin; al *= rsfmin;
+    } while (fabs(beta) < sfmin && kount < 20);
+    a = al;
+    beta = -copysign(sqrt(fma(a, a, fma(x1, x1, x2 * x2))), a);
+  }
+  const double rb = 1.0 / beta;
+  const double t = 1.0 / (a - beta);
+  const double tau = (beta - a) * rb;
+  x1 *= t;
+  x2 *= t;
+  for (int j = 0; j < kount; ++j) beta *= sfmin;
+  a = beta;
+  return tau;
+}
+
+// Standard-form 2x2 real Schur block (dlanv2 logic, GenericSchur.jl:716-803).
+__device__ inline void gs2x2(double& a, double& b, double& c, double& d, double& cs, double& sn,
+                             double& w1r, double& w1i, double& w2r, double& w2i) {
+  auto sgn = [](double x) { return (x < 0.0) ? -1.0 : 1.0; };
+  const double half = 0.5;
+  const double small = 4.0 * kEps;
+  if (c == 0.0) {
+    cs = 1.0; sn = 0.0;
+  } else if (b == 0.0) {
+    cs = 0.0; sn = 1.0;
+    double ta = a; a = d; b = -c; c = 0.0; d = ta;
+  } else if ((a - d) == 0.0 && (b * c < 0.0)) {
+    cs = 1.0; sn = 0.0;
+  } else {
+    double asubd = a - d;
+    double p = half * asubd;
+    double bcmax = fmax(fabs(b), fabs(c));
+    double bcmis = fmin(fabs(b), fabs(c)) * sgn(b) * sgn(c);
+    double scale = fmax(fabs(p), bcmax);
+    double z = (p / scale) * p + (bcmax / scale) * bcmis;
+    if (z >= small) {
+      z = p + sqrt(scale) * sqrt(z) * sgn(p);
+      a = d + z;
+      d -= (bcmax / z) * bcmis;
+      double tau = hypot(c, z);
+      cs = z / tau;
+      sn = c / tau;
+      b -= c;
+      c = 0.0;
+    } else {
+      double sigma = b + c;
+      double tau = hypot(sigma, asubd);
+      cs = sqrt(half * (1.0 + fabs(sigma) / tau));
+      sn = -(p / (tau * cs)) * sgn(sigma);
+      double aa = a * cs + b * sn;
+      double bb = -a * sn + b * cs;
+      double cc = c * cs + d * sn;
+      double dd = -c * sn + d * cs;
+      a = aa * cs + cc * sn;
+      b = bb * cs + dd * sn;
+      c = -aa * sn + cc * cs;
+      d = -bb * sn + dd * cs;
+      double midad = half * (a + d);
+      a = midad;
+      d = a;
+      if (c != 0.0) {
+        if (b != 0.0) {
+          if (b * c >= 0.0) {
+            double sab = sqrt(fabs(b));
+            double sac = sqrt(fabs(c));
+            p = sab * sac * sgn(c);
+            tau = 1.0 / sqrt(fabs(b + c));
+            a = midad + p;
+            d = midad - p;
+            b -= c;
+            c = 0.0;
+            double cs1 = sab * tau;
+            double sn1 = sac * tau;
+            double ncs = cs * cs1 - sn * sn1;
+            double nsn = cs * sn1 + sn * cs1;
+            cs = ncs; sn = nsn;
+          }
+        } else {
+          b = -c; c = 0.0;
+          double ncs = -sn, nsn = cs;
+          cs = ncs; sn = nsn;
+        }
+      }
+    }
+  }
+  if (c == 0.0) {
+    w1r = a; w1i = 0.0; w2r = d; w2i = 0.0;
+  } else {
+    double rti = sqrt(fabs(b)) * sqrt(fabs(c));
+    w1r = a; w1i = rti; w2r = d; w2i = -rti;
+  }
+}
+
+}  // namespace gsk

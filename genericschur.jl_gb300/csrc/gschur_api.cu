@@ -1,0 +1,385 @@
+// C-ABI of the GB300 Schur engine (declared in include/gschur_gb300.h).
+//
+// Host glue only: argument checks, a device workspace arena, host<->device
+// staging, the fork/join of the size-bin kernels onto auxiliary streams and the
+// optional CUDA-graph replay.  All arithmetic runs in the kernels.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gschur_gb300.h"
+#include "gs_internal.h"
+
+using namespace gsk;
+
+struct gs_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaStream_t aux[kNumBins] = {};
+  cudaStream_t cap = nullptr;
+  cudaEvent_t fork = nullptr, join[kNumBins] = {};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  bool timed = false;
+  char* dws = nullptr;
+  size_t dws_cap = 0;
+  std::string err;
+  // cached graph of the batched launch sequence
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<long long> gkey;
+};
+
+namespace {
+
+int set_err(gs_context* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return set_err(ctx, GS_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));      \
+  } while (0)
+
+// Bump allocator over the context's device arena.
+struct Arena {
+  size_t off = 0;
+  template <class T> size_t take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    size_t at = off;
+    off += count * sizeof(T);
+    return at;
+  }
+};
+
+int ensure_ws(gs_context* ctx, size_t bytes) {
+  if (bytes <= ctx->dws_cap) return GS_OK;
+  if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; ctx->gkey.clear(); }
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->dws) CK(cudaFree(ctx->dws));
+  ctx->dws = nullptr;
+  ctx->dws_cap = 0;
+  size_t cap = std::max(bytes, (size_t)1 << 20);
+  cap = cap + cap / 4;
+  CK(cudaMalloc(&ctx->dws, cap));
+  ctx->dws_cap = cap;
+  return GS_OK;
+}
+
+// Fork the aux streams off `s`, run `body(aux)`, join back into `s`.
+template <class F> int fork_join(gs_context* ctx, cudaStream_t s, F body) {
+  CK(cudaEventRecord(ctx->fork, s));
+  for (int i = 0; i < kNumBins; ++i) CK(cudaStreamWaitEvent(ctx->aux[i], ctx->fork, 0));
+  cudaError_t e = body(ctx->aux);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  for (int i = 0; i < kNumBins; ++i) {
+    CK(cudaEventRecord(ctx->join[i], ctx->aux[i]));
+    CK(cudaStreamWaitEvent(s, ctx->join[i], 0));
+  }
+  return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs_version(void) { return 100; }
+
+int gs_create(gs_context** out, int device) {
+  if (!out) return GS_BADARG;
+  *out = nullptr;
+  gs_context* ctx = new gs_context();
+  ctx->device = device;
+  int rc = GS_OK;
+  do {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { rc = set_err(ctx, GS_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)); break; }
+    e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) { rc = set_err(ctx, GS_CUDA, "device query: %s", cudaGetErrorString(e)); break; }
+    if ((e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreate(&ctx->t0)) != cudaSuccess || (e = cudaEventCreate(&ctx->t1)) != cudaSuccess) {
+      rc = set_err(ctx, GS_CUDA, "stream/event create: %s", cudaGetErrorString(e));
+      break;
+    }
+    for (int i = 0; i < kNumBins && e == cudaSuccess; ++i) {
+      e = cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) { rc = set_err(ctx, GS_CUDA, "aux streams: %s", cudaGetErrorString(e)); break; }
+    ctx->stream = ctx->own;
+  } while (0);
+  if (rc != GS_OK) {
+    // keep the context so that gs_last_error can report; compute calls will fail
+    *out = ctx;
+    return rc;
+  }
+  *out = ctx;
+  return GS_OK;
+}
+
+int gs_destroy(gs_context* ctx) {
+  if (!ctx) return GS_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->dws) cudaFree(ctx->dws);
+  for (int i = 0; i < kNumBins; ++i) {
+    if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+    if (ctx->join[i]) cudaEventDestroy(ctx->join[i]);
+  }
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->t0) cudaEventDestroy(ctx->t0);
+  if (ctx->t1) cudaEventDestroy(ctx->t1);
+  if (ctx->cap) cudaStreamDestroy(ctx->cap);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return GS_OK;
+}
+
+int gs_set_stream(gs_context* ctx, void* stream) {
+  if (!ctx) return GS_BADARG;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+  return GS_OK;
+}
+
+const char* gs_last_error(const gs_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+float gs_last_kernel_ms(const gs_context* ctx) {
+  if (!ctx || !ctx->timed) return -1.0f;
+  float ms = -1.0f;
+  if (cudaEventSynchronize(ctx->t1) != cudaSuccess) return -1.0f;
+  if (cudaEventElapsedTime(&ms, ctx->t0, ctx->t1) != cudaSuccess) return -1.0f;
+  return ms;
+}
+
+int gs_host_alloc(gs_context* ctx, void** ptr, size_t bytes) {
+  if (!ctx || !ptr) return GS_BADARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaHostAlloc(ptr, bytes, cudaHostAllocDefault));
+  return GS_OK;
+}
+
+int gs_host_free(gs_context* ctx, void* ptr) {
+  if (!ctx) return GS_BADARG;
+  if (ptr) CK(cudaFreeHost(ptr));
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched real
+// ---------------------------------------------------------------------------
+static int run_batched_real(gs_context* ctx, const RealBatch& bt, int* order, int* sched, unsigned flags,
+                            bool use_graph, const std::vector<long long>& key) {
+  auto enqueue = [&](cudaStream_t s) -> int {
+    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
+    return fork_join(ctx, s, [&](cudaStream_t* aux) {
+      return launch_schur_batched_real(bt, order, sched, ctx->num_sms, aux, kNumBins);
+    });
+  };
+  CK(cudaEventRecord(ctx->t0, ctx->stream));
+  if (use_graph) {
+    if (!ctx->gexec || ctx->gkey != key) {
+      if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+      CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue(ctx->cap);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(ctx->cap, &g);
+      if (rc != GS_OK) { if (g) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { ctx->gexec = nullptr; return set_err(ctx, GS_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+      ctx->gkey = key;
+    }
+    CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+  } else {
+    int rc = enqueue(ctx->stream);
+    if (rc != GS_OK) return rc;
+  }
+  CK(cudaEventRecord(ctx->t1, ctx->stream));
+  ctx->timed = true;
+  return GS_OK;
+}
+
+int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
+                         int32_t* status, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (count < 0 || count > (1LL << 30)) return set_err(ctx, GS_BADARG, "bad count %lld", (long long)count);
+  if (count == 0) return GS_OK;
+  const bool wantz = flags & GS_WANTZ;
+  if (!ns || !offs || !woffs || !A || !wr || !wi || !status || (wantz && !Z))
+    return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  RealBatch bt{};
+  bt.count = (int)count;
+  bt.wantz = wantz;
+  bt.scale = (flags & GS_SCALE) ? 1 : 0;
+  bt.maxiter_mult = 100;
+  Arena ar;
+  long long na = 0, nw = 0;
+  if (!dev) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int n = ns[b];
+      if (n < 0 || n > kSmallMax)
+        return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
+      if (offs[b] < 0 || woffs[b] < 0) return set_err(ctx, GS_BADARG, "matrix %lld: negative offset", (long long)b);
+      na = std::max(na, (long long)offs[b] + (long long)n * n);
+      nw = std::max(nw, (long long)woffs[b] + n);
+    }
+  }
+  const size_t o_order = ar.take<int>(count);
+  const size_t o_sched = ar.take<int>(3 * kNumBins);
+  size_t o_A = 0, o_Z = 0, o_wr = 0, o_wi = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
+  if (!dev) {
+    o_A = ar.take<double>(na);
+    o_Z = ar.take<double>(wantz ? na : 1);
+    o_wr = ar.take<double>(nw);
+    o_wi = ar.take<double>(nw);
+    o_ns = ar.take<int>(count);
+    o_offs = ar.take<long long>(count);
+    o_woffs = ar.take<long long>(count);
+    o_st = ar.take<int>(count);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  int* order = (int*)(base + o_order);
+  int* sched = (int*)(base + o_sched);
+  cudaStream_t s = ctx->stream;
+  if (!dev) {
+    bt.ns = (const int*)(base + o_ns);
+    bt.offs = (const long long*)(base + o_offs);
+    bt.woffs = (const long long*)(base + o_woffs);
+    bt.A = (double*)(base + o_A);
+    bt.Z = wantz ? (double*)(base + o_Z) : nullptr;
+    bt.wr = (double*)(base + o_wr);
+    bt.wi = (double*)(base + o_wi);
+    bt.status = (int*)(base + o_st);
+    CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(bt.A, A, sizeof(double) * na, cudaMemcpyHostToDevice, s));
+  } else {
+    bt.ns = ns;
+    bt.offs = (const long long*)offs;
+    bt.woffs = (const long long*)woffs;
+    bt.A = A;
+    bt.Z = wantz ? Z : nullptr;
+    bt.wr = wr;
+    bt.wi = wi;
+    bt.status = status;
+  }
+  std::vector<long long> key = {1, (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
+                                (long long)(uintptr_t)bt.ns, (long long)(uintptr_t)bt.wr,
+                                (long long)(uintptr_t)order, (long long)flags};
+  rc = run_batched_real(ctx, bt, order, sched, flags, (flags & GS_GRAPH) != 0, key);
+  if (rc) return rc;
+  if (dev) return GS_OK;
+  CK(cudaMemcpyAsync(A, bt.A, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
+  if (wantz) CK(cudaMemcpyAsync(Z, bt.Z, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wr, bt.wr, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wi, bt.wi, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(status, bt.status, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int64_t b = 0; b < count; ++b)
+    if (status[b] != GS_OK) return set_err(ctx, GS_UNCONVERGED, "matrix %lld: iteration limit reached", (long long)b);
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single real matrix: n <= 128 runs as a batch of one
+// ---------------------------------------------------------------------------
+int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
+                 double* wi, unsigned flags, int64_t maxiter) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  const bool wantz = flags & GS_WANTZ;
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
+  if (lda < std::max<int64_t>(n, 1) || (wantz && ldz < std::max<int64_t>(n, 1)))
+    return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
+  if (n == 0) return GS_OK;
+  if (!A || !wr || !wi || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
+  if (n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld > %d: large-matrix path not available", (long long)n, kSmallMax);
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  Arena ar;
+  const size_t o_A = ar.take<double>(n * n), o_Z = ar.take<double>(n * n);
+  const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n);
+  const size_t o_meta = ar.take<long long>(4), o_st = ar.take<int>(2);
+  const size_t o_order = ar.take<int>(1), o_sched = ar.take<int>(3 * kNumBins);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double* dA = (double*)(base + o_A);
+  double* dZ = (double*)(base + o_Z);
+  CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
+  long long meta_h[4] = {0, 0, 0, 0};  // offs, woffs, n (as int in first half of [2])
+  int n32 = (int)n;
+  long long* meta = (long long*)(base + o_meta);
+  CK(cudaMemcpyAsync(meta, meta_h, sizeof(meta_h), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(meta + 2, &n32, sizeof(int), cudaMemcpyHostToDevice, s));
+  RealBatch bt{};
+  bt.count = 1;
+  bt.ns = (const int*)(meta + 2);
+  bt.offs = meta;
+  bt.woffs = meta + 1;
+  bt.A = dA;
+  bt.Z = wantz ? dZ : nullptr;
+  bt.wr = (double*)(base + o_wr);
+  bt.wi = (double*)(base + o_wi);
+  bt.status = (int*)(base + o_st);
+  bt.wantz = wantz;
+  bt.scale = (flags & GS_SCALE) ? 1 : 0;
+  long long mi = maxiter > 0 ? maxiter : 100 * n;
+  bt.maxiter_mult = 100;
+  bt.maxiter_abs = mi;
+  rc = run_batched_real(ctx, bt, (int*)(base + o_order), (int*)(base + o_sched), flags, false, {});
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
+  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(double), dZ, n * sizeof(double), n * sizeof(double), n, out, s));
+  CK(cudaMemcpyAsync(wr, bt.wr, n * sizeof(double), out, s));
+  CK(cudaMemcpyAsync(wi, bt.wi, n * sizeof(double), out, s));
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, bt.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (st != GS_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit %lld reached", mi);
+  return GS_OK;
+}
+
+int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* w,
+                 unsigned flags, int64_t maxiter, int64_t maxinner) {
+  (void)A; (void)lda; (void)Z; (void)ldz; (void)w; (void)flags; (void)maxiter; (void)maxinner;
+  if (!ctx) return GS_BADARG;
+  return set_err(ctx, GS_BADARG, "complex path not built yet (n=%lld)", (long long)n);
+}
+
+int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, double* A, double* Z, double* w, int32_t* status, unsigned flags) {
+  (void)count; (void)ns; (void)offs; (void)woffs; (void)A; (void)Z; (void)w; (void)status; (void)flags;
+  if (!ctx) return GS_BADARG;
+  return set_err(ctx, GS_BADARG, "complex batched path not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+"""GB300 dense Schur engine — Python host mirror of GenericSchur.jl's API.
+
+Each function keeps the name, argument meaning and error behaviour of the
+GenericSchur.jl function it replaces (Julia's trailing `!` becomes a trailing
+underscore):
+
+  gschur(A)  / gschur_(A)      GenericSchur.jl:343 / 805-835 (real), 350-372 (complex)
+  schur(A)                      pirates.jl:8-10 (schur!) through the non-mutating wrapper
+  eigvals(A)                    pirates.jl:17-27
+  gschur_batched(...)           batched form, no reference counterpart
+
+Matrices are numpy arrays; they are handed to the C-ABI column-major (Julia's
+layout).  All arithmetic runs in the CUDA library; nothing here computes a
+decomposition, and there is no CPU fallback.
+"""
+from collections import namedtuple
+
+import numpy as np
+
+from . import _capi
+from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS_UNCONVERGED, GS_WANTZ, Context,
+                    GSError, get_context)
+
+__all__ = ["Schur", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_", "schur",
+           "eigvals", "gschur_batched", "get_context", "Context", "pack_batch", "unpack_batch"]
+
+# LinearAlgebra.Schur(T, Z, values)
+Schur = namedtuple("Schur", ["T", "Z", "values"])
+
+
+class UnconvergedException(RuntimeError):
+    """Iteration limit reached (GenericSchur.jl:39-45)."""
+
+
+class DimensionMismatch(ValueError):
+    """Non-square input or mismatched Z (GenericSchur.jl:523-525, LinearAlgebra.checksquare)."""
+
+
+class ArgumentError(ValueError):
+    """Invalid argument (GenericSchur.jl:206-210)."""
+
+
+def _raise(rc, ctx, what):
+    msg = "%s: %s" % (what, ctx.last_error())
+    if rc == GS_UNCONVERGED:
+        raise UnconvergedException("Convergence failure; " + msg)
+    if rc == GS_BADARG:
+        raise ArgumentError(msg)
+    raise GSError(rc, msg)
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def _checksquare(A):
+    if A.ndim != 2 or A.shape[0] != A.shape[1]:
+        raise DimensionMismatch("matrix is not square: dimensions are %s" % (A.shape,))
+    return A.shape[0]
+
+
+def gschur_(A, wantZ=True, scale=True, maxiter=None, maxinner=None, ctx=None):
+    """Destructive Schur decomposition: A (Fortran-ordered float64/complex128 array)
+    is overwritten by T.  Returns Schur(T, Z, values), T being A itself."""
+    n = _checksquare(A)
+    ctx = ctx or get_context()
+    if not (A.flags.f_contiguous and A.dtype in (np.float64, np.complex128)):
+        raise ArgumentError("gschur_ needs a Fortran-ordered float64 or complex128 array")
+    flags = (GS_WANTZ if wantZ else 0) | (GS_SCALE if scale else 0)
+    lib = ctx.lib
+    if A.dtype == np.complex128:
+        Z = np.zeros((n, n), dtype=np.complex128, order="F") if wantZ else None
+        w = np.zeros(n, dtype=np.complex128)
+        rc = lib.gs_schur_c64(ctx.handle, n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(w), flags,
+                              int(maxiter or 0), int(maxinner or 0))
+        if rc != GS_OK:
+            _raise(rc, ctx, "gschur")
+        return Schur(A, Z if wantZ else np.zeros((0, 0), dtype=np.complex128), w)
+    Z = np.zeros((n, n), dtype=np.float64, order="F") if wantZ else None
+    wr = np.zeros(n)
+    wi = np.zeros(n)
+    rc = lib.gs_schur_f64(ctx.handle, n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(wr), _ptr(wi), flags,
+                          int(maxiter or 0))
+    if rc != GS_OK:
+        _raise(rc, ctx, "gschur")
+    return Schur(A, Z if wantZ else np.zeros((0, 0)), wr + 1j * wi)
+
+
+def gschur(A, **kw):
+    """Schur decomposition of a copy of A (GenericSchur.jl:343)."""
+    A = np.asarray(A)
+    if A.dtype.kind in "iub":
+        raise TypeError("gschur is defined for floating-point element types only")
+    dt = np.complex128 if np.iscomplexobj(A) else np.float64
+    return gschur_(np.array(A, dtype=dt, order="F", copy=True), **kw)
+
+
+def schur(A, **kw):
+    """LinearAlgebra.schur through the pirated schur! (pirates.jl:8-10)."""
+    return gschur(A, **kw)
+
+
+def _eigsortby(w):
+    # LinearAlgebra.eigsortby: lexicographic by (real, imag)
+    return np.lexsort((w.imag, w.real))
+
+
+def eigvals(A, sortby="default", **kw):
+    """Eigenvalues via gschur!(A; wantZ=false) (pirates.jl:17-27)."""
+    S = gschur(A, wantZ=False, **kw)
+    w = S.values
+    if sortby is None:
+        return w
+    if sortby == "default":
+        return w[_eigsortby(w)]
+    return w[np.argsort([sortby(x) for x in w], kind="stable")]
+
+
+# ---------------------------------------------------------------------------
+# batched form
+# ---------------------------------------------------------------------------
+def pack_batch(mats, dtype=np.float64):
+    """Pack a list of square matrices column-major into one buffer.
+    Returns (packed, ns int32, offs int64, woffs int64)."""
+    ns = np.array([m.shape[0] for m in mats], dtype=np.int32)
+    sq = ns.astype(np.int64) ** 2
+    offs = np.zeros(len(mats), dtype=np.int64)
+    if len(mats) > 1:
+        offs[1:] = np.cumsum(sq)[:-1]
+    woffs = np.zeros(len(mats), dtype=np.int64)
+    if len(mats) > 1:
+        woffs[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+    packed = np.empty(int(sq.sum()), dtype=dtype)
+    for m, o, n in zip(mats, offs, ns):
+        packed[o:o + n * n] = np.asarray(m, dtype=dtype).ravel(order="F")
+    return packed, ns, offs, woffs
+
+
+def unpack_batch(packed, ns, offs):
+    return [packed[o:o + n * n].reshape((n, n), order="F") for o, n in zip(offs, ns)]
+
+
+def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ=True, scale=True, graph=False,
+                   ctx=None, raise_on_failure=True):
+    """gschur! over a ragged batch (orders <= 128) in one launch sequence.
+
+    Pass either `mats` (list of square arrays) or the packed form (packed, ns,
+    offs, woffs) as produced by pack_batch.  Returns (T_list, Z_list, values_list,
+    status) for `mats`, or (T_packed, Z_packed, w_packed, status) for packed input.
+    """
+    ctx = ctx or get_context()
+    lists = mats is not None
+    if lists:
+        for m in mats:
+            _checksquare(np.asarray(m))
+        cplx = any(np.iscomplexobj(m) for m in mats)
+        packed, ns, offs, woffs = pack_batch(mats, np.complex128 if cplx else np.float64)
+    else:
+        cplx = np.iscomplexobj(packed)
+        packed = np.array(packed, copy=True)
+    count = len(ns)
+    ns = np.ascontiguousarray(ns, dtype=np.int32)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    woffs = np.ascontiguousarray(woffs, dtype=np.int64)
+    nw = int(ns.sum()) if count else 0
+    nw = max(nw, int((woffs + ns).max()) if count else 0)
+    flags = (GS_WANTZ if wantZ else 0) | (GS_SCALE if scale else 0) | (GS_GRAPH if graph else 0)
+    status = np.zeros(count, dtype=np.int32)
+    Z = np.zeros_like(packed) if wantZ else None
+    lib = ctx.lib
+    if cplx:
+        w = np.zeros(nw, dtype=np.complex128)
+        rc = lib.gs_schur_batched_c64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), _ptr(packed), _ptr(Z),
+                                      _ptr(w), _ptr(status), flags)
+    else:
+        wr = np.zeros(nw)
+        wi = np.zeros(nw)
+        rc = lib.gs_schur_batched_f64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), _ptr(packed), _ptr(Z),
+                                      _ptr(wr), _ptr(wi), _ptr(status), flags)
+        w = wr + 1j * wi
+    if rc not in (GS_OK, GS_UNCONVERGED) or (rc == GS_UNCONVERGED and raise_on_failure):
+        _raise(rc, ctx, "gschur_batched")
+    if not lists:
+        return packed, Z, w, status
+    Ts = unpack_batch(packed, ns, offs)
+    Zs = unpack_batch(Z, ns, offs) if wantZ else [None] * count
+    ws = [w[o:o + n] for o, n in zip(woffs, ns)]
+    return Ts, Zs, ws, status

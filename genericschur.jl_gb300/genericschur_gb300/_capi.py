@@ -1,0 +1,128 @@
+"""ctypes binding of libgschur_gb300.so (declarations in include/gschur_gb300.h).
+
+The library is the product: there is no CPU fallback.  If the shared object is
+missing or cannot be loaded, every entry point raises.
+"""
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libgschur_gb300.so")
+
+GS_OK = 0
+GS_UNCONVERGED = 1
+GS_BADARG = 2
+GS_CUDA = 3
+
+GS_WANTZ = 1
+GS_SCALE = 2
+GS_DEVICE = 4
+GS_GRAPH = 8
+
+_i = ctypes.c_int
+_i64 = ctypes.c_int64
+_u = ctypes.c_uint
+_p = ctypes.c_void_p
+
+# name -> (restype, argtypes); kept in sync with include/gschur_gb300.h
+SIGNATURES = {
+    "gs_version": (_i, []),
+    "gs_create": (_i, [ctypes.POINTER(_p), _i]),
+    "gs_destroy": (_i, [_p]),
+    "gs_set_stream": (_i, [_p, _p]),
+    "gs_last_error": (ctypes.c_char_p, [_p]),
+    "gs_last_kernel_ms": (ctypes.c_float, [_p]),
+    "gs_host_alloc": (_i, [_p, ctypes.POINTER(_p), ctypes.c_size_t]),
+    "gs_host_free": (_i, [_p, _p]),
+    "gs_schur_f64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
+    "gs_schur_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _u, _i64, _i64]),
+    "gs_schur_batched_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_schur_batched_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path=None):
+    """Load the shared library (once) and attach the C signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            raise RuntimeError(
+                "libgschur_gb300.so not found at %s; build it with genericschur.jl_gb300/build_lib.py" % path)
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+class GSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class Context:
+    """A library context on one CUDA device (owns a stream and a workspace arena)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = _p()
+        rc = self.lib.gs_create(ctypes.byref(h), int(device))
+        self.handle = h
+        if rc != GS_OK:
+            msg = self.last_error()
+            raise GSError(rc, "gs_create failed: %s" % msg)
+        self.device = device
+
+    def last_error(self):
+        s = self.lib.gs_last_error(self.handle)
+        return s.decode() if s else ""
+
+    def set_stream(self, stream_ptr):
+        self.lib.gs_set_stream(self.handle, _p(stream_ptr) if stream_ptr else None)
+
+    def last_kernel_ms(self):
+        return float(self.lib.gs_last_kernel_ms(self.handle))
+
+    def host_alloc(self, nbytes):
+        p = _p()
+        rc = self.lib.gs_host_alloc(self.handle, ctypes.byref(p), ctypes.c_size_t(nbytes))
+        if rc != GS_OK:
+            raise GSError(rc, self.last_error())
+        return p.value
+
+    def host_free(self, ptr):
+        self.lib.gs_host_free(self.handle, _p(ptr))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gs_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_ctx = {}
+
+
+def get_context(device=0):
+    """Process-wide default context per device."""
+    c = _ctx.get(device)
+    if c is None:
+        c = Context(device)
+        _ctx[device] = c
+    return c

@@ -1,0 +1,120 @@
+/*
+ * gschur_gb300 — C-ABI of the GB300 dense Schur engine.
+ *
+ * Drop-in boundary for GenericSchur.jl's dense non-symmetric path: every entry
+ * point below names the reference function it replaces (file:line in the
+ * GenericSchur.jl source tree).  Matrices are column-major (Julia layout); complex
+ * data is interleaved (re, im) doubles, the memory layout of Julia's ComplexF64.
+ * Plain pointers and sizes only; no CUDA or torch types appear in the signatures.
+ *
+ * Pointers are host pointers unless GS_DEVICE is set in `flags`, in which case
+ * they are device pointers on the context's device and the call is asynchronous
+ * on the context's stream (results and per-matrix status are ready once the
+ * stream reaches that point).  Host-pointer calls are synchronous.
+ *
+ * Return codes mirror the reference's exceptions:
+ *   GS_OK           0  success
+ *   GS_UNCONVERGED  1  iteration limit reached   (UnconvergedException, GenericSchur.jl:39-45)
+ *   GS_BADARG       2  bad size / pointer        (DimensionMismatch / ArgumentError)
+ *   GS_CUDA         3  CUDA error; text from gs_last_error()
+ * There is no CPU fallback: without a usable GPU every compute entry returns GS_CUDA.
+ */
+#ifndef GSCHUR_GB300_H
+#define GSCHUR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GS_API __attribute__((visibility("default")))
+#else
+#define GS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS_OK 0
+#define GS_UNCONVERGED 1
+#define GS_BADARG 2
+#define GS_CUDA 3
+
+/* flags */
+#define GS_WANTZ 1u   /* accumulate Schur vectors (gschur!(A; wantZ=true), GenericSchur.jl:805-826) */
+#define GS_SCALE 2u   /* _scale! before and after (gschur!(A; scale=true), util.jl:14-29)          */
+#define GS_DEVICE 4u  /* all array arguments are device pointers; asynchronous                    */
+#define GS_GRAPH 8u   /* batched calls: replay a cached CUDA graph of the launch sequence         */
+
+typedef struct gs_context gs_context;
+
+/* Library version (integer, major*10000 + minor*100 + patch). */
+GS_API int gs_version(void);
+
+/* Create a context on CUDA device `device` with its own non-blocking stream.
+ * No reference counterpart (the reference keeps no state). */
+GS_API int gs_create(gs_context** ctx, int device);
+GS_API int gs_destroy(gs_context* ctx);
+
+/* Use the caller's CUDA stream (a cudaStream_t passed as void*; NULL restores the
+ * context's own stream). */
+GS_API int gs_set_stream(gs_context* ctx, void* stream);
+
+/* Text of the last error on this context (empty string if none). */
+GS_API const char* gs_last_error(const gs_context* ctx);
+
+/* Device time in milliseconds of the last compute call's kernel sequence
+ * (CUDA events on the context stream; host<->device copies excluded). */
+GS_API float gs_last_kernel_ms(const gs_context* ctx);
+
+/* Pinned host memory for fast host<->device staging. */
+GS_API int gs_host_alloc(gs_context* ctx, void** ptr, size_t bytes);
+GS_API int gs_host_free(gs_context* ctx, void* ptr);
+
+/* ---------------------------------------------------------------------------
+ * Real Schur decomposition of one n x n matrix.
+ * Replaces gschur!(A::StridedMatrix{<:AbstractFloat}; wantZ, scale, maxiter)
+ * (GenericSchur.jl:805-835, driving _hessenberg! hessenberg.jl:3-17,
+ * _materializeQ hessenberg.jl:150-166 and gschur!(H::Hessenberg, Z)
+ * GenericSchur.jl:513-699).
+ *   A   [in/out] n x n, leading dimension lda; overwritten by T (upper
+ *       quasi-triangular, 2x2 blocks in standard form, zeros below the first
+ *       subdiagonal), as the reference returns S.T.
+ *   Z   [out] n x n orthogonal Schur vectors, leading dimension ldz (GS_WANTZ).
+ *   wr, wi [out] eigenvalues, in the reference's order (S.values).
+ *   maxiter: iteration limit; <= 0 selects the reference default 100*n.
+ * ------------------------------------------------------------------------- */
+GS_API int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz,
+                 double* wr, double* wi, unsigned flags, int64_t maxiter);
+
+/* Complex Schur decomposition of one n x n ComplexF64 matrix.
+ * Replaces gschur!(A::StridedMatrix{Complex}) (GenericSchur.jl:350-372) with
+ * gschur!(H::Hessenberg{Complex}, Z) (GenericSchur.jl:194-335).
+ *   A [in/out] interleaved complex, overwritten by upper-triangular T.
+ *   w [out] n eigenvalues (interleaved complex) = diag(T).
+ *   maxiter / maxinner <= 0 select the reference defaults 100*n / 30*n. */
+GS_API int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz,
+                 double* w, unsigned flags, int64_t maxiter, int64_t maxinner);
+
+/* ---------------------------------------------------------------------------
+ * Batched forms (no reference counterpart: the reference handles one matrix per
+ * call; these run gschur! on every matrix of a ragged batch in one persistent
+ * launch sequence).  Matrix b has order ns[b] <= 128 and is stored column-major
+ * with leading dimension ns[b] at element offset offs[b] of A and Z; its
+ * eigenvalues start at element woffs[b] of wr/wi (or of w, complex).  status[b]
+ * receives GS_OK or GS_UNCONVERGED.  Returns GS_UNCONVERGED if any matrix failed
+ * (host-pointer mode) — the other matrices are still valid.
+ * ------------------------------------------------------------------------- */
+GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
+                         int32_t* status, unsigned flags);
+
+GS_API int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, double* A, double* Z, double* w, int32_t* status,
+                         unsigned flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSCHUR_GB300_H */

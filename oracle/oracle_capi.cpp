@@ -1,0 +1,211 @@
+// C entry points of the CPU oracle (test infrastructure only; see gschur_oracle.hpp).
+// Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg through
+// ctypes.  Complex arrays are interleaved (re, im) doubles, column-major.
+#include <cstring>
+#include <vector>
+#include "gschur_oracle.hpp"
+#include "eigvecs_oracle.hpp"
+
+using namespace orc;
+typedef cx<double> zc;
+
+extern "C" {
+
+int or_version(void) { return 1; }
+
+// ---- real, double --------------------------------------------------------
+int or_gschur_d(int n, double* a, int lda, double* z, int ldz, double* wr, double* wi, int wantz,
+                int scale, long long maxiter) {
+  if (maxiter <= 0) maxiter = 100LL * n;
+  return gschur_real<double>(n, a, lda, z, ldz, wr, wi, wantz != 0, scale != 0, maxiter);
+}
+
+int or_gschur_s(int n, float* a, int lda, float* z, int ldz, float* wr, float* wi, int wantz,
+                int scale, long long maxiter) {
+  if (maxiter <= 0) maxiter = 100LL * n;
+  return gschur_real<float>(n, a, lda, z, ldz, wr, wi, wantz != 0, scale != 0, maxiter);
+}
+
+// Hessenberg reduction + Q (hessenberg.jl:3-17, 150-166); a overwritten with H (reflectors
+// below the subdiagonal), tau n-1 entries, q n x n.
+int or_hessenberg_d(int n, double* a, int lda, double* tau, double* q, int ldq) {
+  hessenberg<double>(n, a, lda, tau);
+  if (q) materialize_q<double>(n, a, lda, tau, q, ldq);
+  return 0;
+}
+
+int or_hessenberg_z(int n, double* a, int lda, double* tau, double* q, int ldq) {
+  hessenberg<zc>(n, (zc*)a, lda, (zc*)tau);
+  if (q) materialize_q<zc>(n, (zc*)a, lda, (zc*)tau, (zc*)q, ldq);
+  return 0;
+}
+
+// ---- complex, double -----------------------------------------------------
+int or_gschur_z(int n, double* a, int lda, double* z, int ldz, double* w, int wantz, int scale,
+                long long maxiter, long long maxinner) {
+  if (maxiter <= 0) maxiter = 100LL * n;
+  if (maxinner <= 0) maxinner = 30LL * n;
+  return gschur_cplx<double>(n, (zc*)a, lda, (zc*)z, ldz, (zc*)w, wantz != 0, scale != 0, maxiter,
+                             maxinner);
+}
+
+// Complex Hessenberg QR on an already-Hessenberg H (GenericSchur.jl:194-335),
+// checksd = true (raises on a non-real subdiagonal: returns 2).
+int or_gschur_hess_z(int n, double* h, int ldh, double* z, int ldz, double* w, long long maxiter) {
+  if (maxiter <= 0) maxiter = 100LL * n;
+  return gschur_hess_cplx<double>(n, (zc*)h, ldh, (zc*)z, ldz, (zc*)w, maxiter, 30LL * n, true);
+}
+
+int or_gschur_hess_d(int n, double* h, int ldh, double* z, int ldz, double* wr, double* wi,
+                     long long maxiter) {
+  if (maxiter <= 0) maxiter = 100LL * n;
+  return gschur_hess_real<double>(n, h, ldh, z, ldz, wr, wi, maxiter);
+}
+
+// ---- quad precision (113-bit) ----------------------------------------------
+// Inputs/outputs in double; the whole decomposition runs in quad.  Also returns
+// the quad-precision residuals ||A - Z T Z^H||_F / ||A||_F and ||Z^H Z - I||_F.
+int or_gschur_q(int n, const double* a_in, double* t_out, double* z_out, double* wr, double* wi,
+                double* resid) {
+  std::vector<qreal> a((size_t)n * n), a0((size_t)n * n), z((size_t)n * n), qwr(n), qwi(n);
+  for (size_t i = 0; i < (size_t)n * n; ++i) a[i] = a0[i] = (qreal)a_in[i];
+  int st = gschur_real<qreal>(n, a.data(), n, z.data(), n, qwr.data(), qwi.data(), true, true,
+                              100LL * n);
+  if (st) return st;
+  for (size_t i = 0; i < (size_t)n * n; ++i) { t_out[i] = (double)a[i]; z_out[i] = (double)z[i]; }
+  for (int i = 0; i < n; ++i) { wr[i] = (double)qwr[i]; wi[i] = (double)qwi[i]; }
+  if (resid) {
+    // ||A - Z T Z^T||_F / ||A||_F and ||Z^T Z - I||_F in quad
+    std::vector<qreal> zt((size_t)n * n, 0);
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) {
+        qreal tkj = a[k + (size_t)j * n];
+        if (tkj == 0) continue;
+        for (int i = 0; i < n; ++i) zt[i + (size_t)j * n] += z[i + (size_t)k * n] * tkj;
+      }
+    qreal num = 0, den = 0, orth = 0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        qreal s = 0;
+        for (int k = 0; k < n; ++k) s += zt[i + (size_t)k * n] * z[j + (size_t)k * n];
+        qreal d = a0[i + (size_t)j * n] - s;
+        num += d * d;
+        den += a0[i + (size_t)j * n] * a0[i + (size_t)j * n];
+        qreal o = 0;
+        for (int k = 0; k < n; ++k) o += z[k + (size_t)i * n] * z[k + (size_t)j * n];
+        o -= (i == j) ? 1 : 0;
+        orth += o * o;
+      }
+    resid[0] = (double)(m_sqrt(num) / m_sqrt(den));
+    resid[1] = (double)m_sqrt(orth);
+  }
+  return 0;
+}
+
+// Complex quad: a_in interleaved complex double.
+int or_gschur_zq(int n, const double* a_in, double* t_out, double* z_out, double* w_out,
+                 double* resid) {
+  typedef cx<qreal> Q;
+  std::vector<Q> a((size_t)n * n), a0((size_t)n * n), z((size_t)n * n), w(n);
+  for (size_t i = 0; i < (size_t)n * n; ++i) a[i] = a0[i] = Q((qreal)a_in[2 * i], (qreal)a_in[2 * i + 1]);
+  int st = gschur_cplx<qreal>(n, a.data(), n, z.data(), n, w.data(), true, true, 100LL * n, 30LL * n);
+  if (st) return st;
+  for (size_t i = 0; i < (size_t)n * n; ++i) {
+    t_out[2 * i] = (double)a[i].re; t_out[2 * i + 1] = (double)a[i].im;
+    z_out[2 * i] = (double)z[i].re; z_out[2 * i + 1] = (double)z[i].im;
+  }
+  for (int i = 0; i < n; ++i) { w_out[2 * i] = (double)w[i].re; w_out[2 * i + 1] = (double)w[i].im; }
+  if (resid) {
+    std::vector<Q> zt((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k <= j; ++k) {
+        Q tkj = a[k + (size_t)j * n];
+        for (int i = 0; i < n; ++i) zt[i + (size_t)j * n] += z[i + (size_t)k * n] * tkj;
+      }
+    qreal num = 0, den = 0, orth = 0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        Q s;
+        for (int k = 0; k < n; ++k) s += zt[i + (size_t)k * n] * conj(z[j + (size_t)k * n]);
+        Q d = a0[i + (size_t)j * n] - s;
+        num += abs2(d);
+        den += abs2(a0[i + (size_t)j * n]);
+        Q o;
+        for (int k = 0; k < n; ++k) o += conj(z[k + (size_t)i * n]) * z[k + (size_t)j * n];
+        if (i == j) o -= Q(1);
+        orth += abs2(o);
+      }
+    resid[0] = (double)(m_sqrt(num) / m_sqrt(den));
+    resid[1] = (double)m_sqrt(orth);
+  }
+  return 0;
+}
+
+// ---- eigenvectors ------------------------------------------------------------
+// left = 0: right eigenvectors (vectors.jl:133-362 real / 45-131 complex);
+// left = 1: left eigenvectors (vectors.jl:462-698 / 372-460).
+// normalize = 1 applies _enormalize! (util.jl:572-592), as geigvecs does (vectors.jl:12-20).
+int or_eigvecs_d(int n, const double* t, const double* z, double* v, int left, int normalize) {
+  if (left) gleigvecs_real<double>(n, t, n, z, n, (zc*)v, n);
+  else geigvecs_real<double>(n, t, n, z, n, (zc*)v, n);
+  if (normalize) enormalize<double>(n, (zc*)v, n);
+  return 0;
+}
+
+int or_eigvecs_z(int n, const double* t, const double* z, double* v, int left, int normalize) {
+  std::vector<zc> tt((size_t)n * n);
+  std::memcpy(tt.data(), t, sizeof(zc) * (size_t)n * n);
+  if (left) gleigvecs_cplx<double>(n, tt.data(), n, (const zc*)z, n, (zc*)v, n);
+  else geigvecs_cplx<double>(n, tt.data(), n, (const zc*)z, n, (zc*)v, n);
+  if (normalize) enormalize<double>(n, (zc*)v, n);
+  return 0;
+}
+
+int or_triangularize_d(int n, const double* t, const double* z, double* tc, double* zc_out, double* w) {
+  triangularize<double>(n, t, n, z, n, (zc*)tc, (zc*)zc_out, (zc*)w);
+  return 0;
+}
+
+int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {
+  gs2x2<double>(h, cs, sn, &w[0], &w[1], &w[2], &w[3]);
+  return 0;
+}
+
+int or_reflector_d(double* x, int n, double* tau) {
+  *tau = reflector_real<double>(x, n);
+  return 0;
+}
+
+// ---- batched (CPU baseline) --------------------------------------------------
+// Ragged batch: matrix b has order ns[b], column-major at a + offs[b] (doubles, or
+// complex pairs for the _z form).  Runs the reference algorithm per matrix, OpenMP
+// over the batch.  Returns the number of matrices that failed to converge.
+int or_gschur_batched_d(int count, const long long* offs, const int* ns, double* a, double* z,
+                        double* wr, double* wi, const long long* woffs, int* status, int nthreads) {
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+  for (int b = 0; b < count; ++b) {
+    int n = ns[b];
+    int st = gschur_real<double>(n, a + offs[b], n, z + offs[b], n, wr + woffs[b], wi + woffs[b], true,
+                                 true, 100LL * n);
+    if (status) status[b] = st;
+    bad += (st != 0);
+  }
+  return bad;
+}
+
+int or_gschur_batched_z(int count, const long long* offs, const int* ns, double* a, double* z,
+                        double* w, const long long* woffs, int* status, int nthreads) {
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+  for (int b = 0; b < count; ++b) {
+    int n = ns[b];
+    int st = gschur_cplx<double>(n, (zc*)(a + 2 * offs[b]), n, (zc*)(z + 2 * offs[b]), n,
+                                 (zc*)(w + 2 * woffs[b]), true, true, 100LL * n, 30LL * n);
+    if (status) status[b] = st;
+    bad += (st != 0);
+  }
+  return bad;
+}
+
+}  // extern "C"

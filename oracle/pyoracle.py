@@ -1,0 +1,205 @@
+"""numpy front end of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module; the shipped library never does.  Matrices are numpy arrays in Fortran
+(column-major) order, like Julia's.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_i = ctypes.c_int
+_ll = ctypes.c_longlong
+_p = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        sig = {
+            "or_gschur_d": [_i, _p, _i, _p, _i, _p, _p, _i, _i, _ll],
+            "or_gschur_s": [_i, _p, _i, _p, _i, _p, _p, _i, _i, _ll],
+            "or_gschur_z": [_i, _p, _i, _p, _i, _p, _i, _i, _ll, _ll],
+            "or_gschur_hess_z": [_i, _p, _i, _p, _i, _p, _ll],
+            "or_gschur_hess_d": [_i, _p, _i, _p, _i, _p, _p, _ll],
+            "or_hessenberg_d": [_i, _p, _i, _p, _p, _i],
+            "or_hessenberg_z": [_i, _p, _i, _p, _p, _i],
+            "or_gschur_q": [_i, _p, _p, _p, _p, _p, _p],
+            "or_gschur_zq": [_i, _p, _p, _p, _p, _p],
+            "or_eigvecs_d": [_i, _p, _p, _p, _i, _i],
+            "or_eigvecs_z": [_i, _p, _p, _p, _i, _i],
+            "or_triangularize_d": [_i, _p, _p, _p, _p, _p],
+            "or_gs2x2_d": [_p, _p, _p, _p],
+            "or_reflector_d": [_p, _i, _p],
+            "or_gschur_batched_d": [_i, _p, _p, _p, _p, _p, _p, _p, _p, _i],
+            "or_gschur_batched_z": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _i
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _f(a, dtype):
+    return np.array(a, dtype=dtype, order="F", copy=True)
+
+
+class Unconverged(RuntimeError):
+    pass
+
+
+def gschur_real(A, wantZ=True, scale=True, maxiter=0, dtype=np.float64):
+    """Real Schur form (GenericSchur.jl:805-835).  Returns (T, Z, w)."""
+    A = _f(A, dtype)
+    n = A.shape[0]
+    Z = np.zeros((n, n), dtype=dtype, order="F")
+    wr = np.zeros(n, dtype=dtype)
+    wi = np.zeros(n, dtype=dtype)
+    fn = lib().or_gschur_d if dtype == np.float64 else lib().or_gschur_s
+    st = fn(n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(wr), _ptr(wi), int(wantZ), int(scale), maxiter)
+    if st == 1:
+        raise Unconverged("iteration limit reached")
+    return A, (Z if wantZ else None), wr + 1j * wi
+
+
+def gschur_cplx(A, wantZ=True, scale=True, maxiter=0, maxinner=0):
+    """Complex Schur form (GenericSchur.jl:350-372).  Returns (T, Z, w)."""
+    A = _f(A, np.complex128)
+    n = A.shape[0]
+    Z = np.zeros((n, n), dtype=np.complex128, order="F")
+    w = np.zeros(n, dtype=np.complex128)
+    st = lib().or_gschur_z(n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(w), int(wantZ), int(scale),
+                           maxiter, maxinner)
+    if st == 1:
+        raise Unconverged("iteration limit reached")
+    return A, (Z if wantZ else None), w
+
+
+def gschur(A, **kw):
+    if np.iscomplexobj(A):
+        return gschur_cplx(A, **kw)
+    return gschur_real(A, **kw)
+
+
+def gschur_hess_cplx(H, Z=None, maxiter=0):
+    """Complex Hessenberg QR with the subdiagonal check (GenericSchur.jl:194-335)."""
+    H = _f(H, np.complex128)
+    n = H.shape[0]
+    Zc = None if Z is None else _f(Z, np.complex128)
+    w = np.zeros(n, dtype=np.complex128)
+    st = lib().or_gschur_hess_z(n, _ptr(H), n, _ptr(Zc), n, _ptr(w), maxiter)
+    return st, H, Zc, w
+
+
+def hessenberg(A):
+    """Hessenberg reduction and Q (hessenberg.jl:3-17, 150-166).  Returns (Hfull, tau, Q)."""
+    cplx = np.iscomplexobj(A)
+    dt = np.complex128 if cplx else np.float64
+    A = _f(A, dt)
+    n = A.shape[0]
+    tau = np.zeros(max(n - 1, 1), dtype=dt)
+    Q = np.zeros((n, n), dtype=dt, order="F")
+    fn = lib().or_hessenberg_z if cplx else lib().or_hessenberg_d
+    fn(n, _ptr(A), n, _ptr(tau), _ptr(Q), n)
+    return A, tau[: max(n - 1, 0)], Q
+
+
+def gschur_quad(A):
+    """Real Schur in 113-bit arithmetic.  Returns (T, Z, w, (backward_err, orth_err))."""
+    A = _f(A, np.float64)
+    n = A.shape[0]
+    T = np.zeros((n, n), order="F")
+    Z = np.zeros((n, n), order="F")
+    wr = np.zeros(n)
+    wi = np.zeros(n)
+    res = np.zeros(2)
+    st = lib().or_gschur_q(n, _ptr(A), _ptr(T), _ptr(Z), _ptr(wr), _ptr(wi), _ptr(res))
+    if st:
+        raise Unconverged("iteration limit reached")
+    return T, Z, wr + 1j * wi, tuple(res)
+
+
+def gschur_cplx_quad(A):
+    A = _f(A, np.complex128)
+    n = A.shape[0]
+    T = np.zeros((n, n), dtype=np.complex128, order="F")
+    Z = np.zeros((n, n), dtype=np.complex128, order="F")
+    w = np.zeros(n, dtype=np.complex128)
+    res = np.zeros(2)
+    st = lib().or_gschur_zq(n, _ptr(A), _ptr(T), _ptr(Z), _ptr(w), _ptr(res))
+    if st:
+        raise Unconverged("iteration limit reached")
+    return T, Z, w, tuple(res)
+
+
+def eigvecs(T, Z, left=False, normalize=True):
+    """Eigenvectors from a Schur pair (vectors.jl:12-20 -> _geigvecs!/_gleigvecs!)."""
+    n = T.shape[0]
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    if np.iscomplexobj(T):
+        lib().or_eigvecs_z(n, _ptr(_f(T, np.complex128)), _ptr(_f(Z, np.complex128)), _ptr(V), int(left),
+                           int(normalize))
+    else:
+        lib().or_eigvecs_d(n, _ptr(_f(T, np.float64)), _ptr(_f(Z, np.float64)), _ptr(V), int(left),
+                           int(normalize))
+    return V
+
+
+def triangularize(T, Z):
+    """Real standard-form Schur -> complex triangular Schur (triang.jl:9-43)."""
+    n = T.shape[0]
+    Tc = np.zeros((n, n), dtype=np.complex128, order="F")
+    Zc = np.zeros((n, n), dtype=np.complex128, order="F")
+    w = np.zeros(n, dtype=np.complex128)
+    lib().or_triangularize_d(n, _ptr(_f(T, np.float64)), _ptr(_f(Z, np.float64)), _ptr(Tc), _ptr(Zc), _ptr(w))
+    return Tc, Zc, w
+
+
+def gs2x2(B):
+    """_gs2x2! (GenericSchur.jl:716-803) on a 2x2 block; returns (std block, cs, sn, w1, w2)."""
+    h = np.array([B[0, 0], B[0, 1], B[1, 0], B[1, 1]], dtype=np.float64)
+    cs = np.zeros(1)
+    sn = np.zeros(1)
+    w = np.zeros(4)
+    lib().or_gs2x2_d(_ptr(h), _ptr(cs), _ptr(sn), _ptr(w))
+    return np.array([[h[0], h[1]], [h[2], h[3]]]), cs[0], sn[0], w[0] + 1j * w[1], w[2] + 1j * w[3]
+
+
+def gschur_batched_real(mats, nthreads=1):
+    """Reference algorithm over a list of real matrices, OpenMP over the batch."""
+    ns = np.array([m.shape[0] for m in mats], dtype=np.int32)
+    offs = np.zeros(len(mats), dtype=np.int64)
+    offs[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+    woffs = np.zeros(len(mats), dtype=np.int64)
+    woffs[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+    a = np.concatenate([np.asarray(m, dtype=np.float64).ravel(order="F") for m in mats])
+    z = np.zeros_like(a)
+    wr = np.zeros(int(ns.sum()))
+    wi = np.zeros_like(wr)
+    st = np.zeros(len(mats), dtype=np.int32)
+    lib().or_gschur_batched_d(len(mats), _ptr(offs), _ptr(ns), _ptr(a), _ptr(z), _ptr(wr), _ptr(wi), _ptr(woffs),
+                              _ptr(st), nthreads)
+    return a, z, wr, wi, st, offs, woffs
+
+
+def gschur_batched_packed_real(count, offs, ns, a, z, wr, wi, woffs, status, nthreads):
+    """Same as gschur_batched_real on caller-owned packed buffers (no copies)."""
+    return lib().or_gschur_batched_d(count, _ptr(offs), _ptr(ns), _ptr(a), _ptr(z), _ptr(wr), _ptr(wi),
+                                     _ptr(woffs), _ptr(status), nthreads)
+
+
+def gschur_batched_packed_cplx(count, offs, ns, a, z, w, woffs, status, nthreads):
+    return lib().or_gschur_batched_z(count, _ptr(offs), _ptr(ns), _ptr(a), _ptr(z), _ptr(w), _ptr(woffs),
+                                     _ptr(status), nthreads)

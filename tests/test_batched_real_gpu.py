@@ -1,0 +1,122 @@
+"""GPU parity tests of the real FP64 Schur kernels against the CPU oracle.
+
+Criteria (spec parity bar, restating the reference's schurtest checks):
+T upper quasi-triangular with standard-form 2x2 blocks (test/real.jl:3-33),
+||A - Z T Z^T||_F / ||A||_F <= 10 n eps, ||Z^T Z - I||_F <= 10 n eps, eigenvalues
+consistent with T (test/testfuncs.jl:57-86) and matched to the oracle's within
+1e2 n eps ||A||_F / s_i.
+"""
+import numpy as np
+import pytest
+
+from common import EPS, assert_schur_real, eig_tolerances, match_eigenvalues, randn_matrix, godunov
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 2, 3, 4, 5, 7, 8, 16, 31, 32, 33, 47, 64, 65, 80, 96, 97, 111, 127, 128]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_single_random(gs, n):
+    rng = np.random.default_rng(1000 + n)
+    A = randn_matrix(rng, n)
+    S = gs.gschur(A)
+    assert_schur_real(A, S.T, S.Z, S.values)
+    w_ref, tol = eig_tolerances(A, po)
+    ok, worst = match_eigenvalues(S.values, w_ref, tol)
+    assert ok, "eigenvalue mismatch, worst err/tol = %.3g" % worst
+
+
+def test_batched_mixed_sizes(gs):
+    rng = np.random.default_rng(4)
+    ns = list(rng.integers(8, 129, size=200)) + [1, 2, 3, 128, 0]
+    mats = [randn_matrix(rng, int(n)) for n in ns]
+    Ts, Zs, ws, status = gs.gschur_batched(mats)
+    assert np.all(status == 0)
+    for A, T, Z, w in zip(mats, Ts, Zs, ws):
+        if A.shape[0] == 0:
+            continue
+        assert_schur_real(A, T, Z, w)
+    for idx in range(0, len(mats), 17):
+        A = mats[idx]
+        if A.shape[0] == 0:
+            continue
+        w_ref, tol = eig_tolerances(A, po)
+        ok, worst = match_eigenvalues(ws[idx], w_ref, tol)
+        assert ok, "matrix %d (n=%d): worst err/tol %.3g" % (idx, A.shape[0], worst)
+
+
+def test_batched_graph_replay_matches(gs):
+    rng = np.random.default_rng(5)
+    mats = [randn_matrix(rng, int(n)) for n in rng.integers(8, 129, size=64)]
+    packed, ns, offs, woffs = gs.pack_batch(mats)
+    T1, Z1, w1, s1 = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs, graph=True)
+    T2, Z2, w2, s2 = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs, graph=True)
+    T3, Z3, w3, s3 = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs, graph=False)
+    # same kernels, same inputs: identical results
+    np.testing.assert_array_equal(T1, T2)
+    np.testing.assert_array_equal(T1, T3)
+    np.testing.assert_array_equal(Z1, Z3)
+    np.testing.assert_array_equal(w1, w3)
+
+
+@pytest.mark.parametrize("n", [4, 32, 100])
+def test_orthogonal_normal(gs, n):
+    rng = np.random.default_rng(300 + n)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    S = gs.gschur(Q)
+    assert_schur_real(Q, S.T, S.Z, S.values)
+    assert np.linalg.norm(np.triu(S.T, 2)) / (n * np.linalg.norm(Q) * EPS) < 10
+
+
+@pytest.mark.parametrize("n", [4, 32, 128])
+def test_jordan(gs, n):
+    A = np.diag(np.ones(n - 1), 1) + np.eye(n)
+    S = gs.gschur(A)
+    assert_schur_real(A, S.T, S.Z, S.values, tol=20.0)
+
+
+@pytest.mark.parametrize("s", [1e-300, 1e-200, 1e200, 1e300])
+def test_extreme_scaling(gs, s):
+    rng = np.random.default_rng(8)
+    n = 24
+    A0 = rng.standard_normal((n, n))
+    A = s * A0
+    S = gs.gschur(A)
+    assert np.all(np.tril(S.T, -2) == 0)
+    be = np.linalg.norm(A0 - S.Z @ (S.T / s) @ S.Z.T) / np.linalg.norm(A0)
+    assert be <= 10 * n * EPS
+    assert np.linalg.norm(S.Z.T @ S.Z - np.eye(n)) <= 10 * n * EPS
+
+
+def test_special_matrices(gs):
+    for A in [np.zeros((6, 6)), np.eye(9), np.diag(np.arange(1.0, 11.0)), np.triu(np.ones((12, 12))),
+              np.diag(np.ones(15), -1)]:
+        S = gs.gschur(A)
+        assert_schur_real(A, S.T, S.Z, S.values, tol=20.0)
+
+
+def test_godunov_double(gs):
+    A, vals, econd = godunov()
+    S = gs.gschur(A)
+    assert_schur_real(A, S.T, S.Z, S.values)
+    # in double precision the eigenvalues are only good to ~ eps * econd * ||A||
+    assert np.allclose(np.sort(S.values.real), vals, atol=1e-1)
+
+
+def test_wantz_false_and_eigvals(gs):
+    rng = np.random.default_rng(13)
+    A = rng.standard_normal((40, 40))
+    S1 = gs.gschur(A)
+    S0 = gs.gschur(A, wantZ=False)
+    np.testing.assert_array_equal(S0.T, S1.T)
+    w = gs.eigvals(A)
+    assert np.all(np.diff(w.real) >= 0)
+
+
+def test_unconverged_status(gs):
+    rng = np.random.default_rng(14)
+    A = rng.standard_normal((20, 20))
+    with pytest.raises(gs.UnconvergedException):
+        gs.gschur(A, maxiter=3)

@@ -1,0 +1,171 @@
+"""Pin the CPU oracle against the reference's own known answers and property tests.
+
+The oracle is the checker for every GPU parity test, so it is validated here
+first, on the CPU:
+  * Godunov's matrix, exact eigenvalues {-4,-2,-1,0,1,2,4} (test/testfuncs.jl:127-142,
+    test/real.jl:142-157, test/complex.jl:139-154), in 113-bit arithmetic;
+  * schurtest / hesstest / vectest properties (test/real.jl, test/complex.jl,
+    test/testfuncs.jl) on random, Jordan, orthogonal and scaled matrices;
+  * the near-degenerate _gs2x2! case (test/real.jl:311-317);
+  * the non-real-subdiagonal ArgumentError (test/errors.jl:1-5);
+  * the committed golden fixtures (tests/golden, made by make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, checkblocks, godunov, orth_error,
+                    randn_matrix)
+from oracle import pyoracle as po
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_godunov_real_quad():
+    A, vals, econd = godunov()
+    T, Z, w, (be, oe) = po.gschur_quad(A)
+    # reference tolerance: delta < 100 eps(80-bit) ||A||, t = 3 delta econd (test/real.jl:148-151)
+    delta = be * np.linalg.norm(A)
+    assert delta < 100 * 2.0 ** -79 * np.linalg.norm(A)
+    t = 3 * delta * econd
+    got = np.sort(w.real)
+    assert np.all(np.abs(w.imag) <= t)
+    assert np.allclose(got, vals, atol=max(t, 1e-12))
+
+
+def test_godunov_complex_quad():
+    A, vals, econd = godunov()
+    T, Z, w, (be, oe) = po.gschur_cplx_quad(A.astype(np.complex128))
+    delta = be * np.linalg.norm(A)
+    assert delta < 100 * 2.0 ** -79 * np.linalg.norm(A)
+    t = 3 * delta * econd
+    got = w[np.lexsort((w.imag, w.real))]
+    assert np.allclose(got, vals, atol=max(t, 1e-12))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 32, 64])
+def test_oracle_real_random(n):
+    rng = np.random.default_rng(100 + n)
+    A = rng.random((n, n))
+    T, Z, w = po.gschur_real(A)
+    assert_schur_real(A, T, Z, w, tol=10.0)
+    # eigenvalues agree with LAPACK (third-party cross-check)
+    ev = np.linalg.eigvals(A)
+    assert np.allclose(np.sort_complex(ev), np.sort_complex(w), atol=1e-10 * max(1, np.abs(ev).max()))
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 32])
+def test_oracle_complex_random(n):
+    rng = np.random.default_rng(200 + n)
+    A = rng.random((n, n)) + 1j * rng.random((n, n))
+    T, Z, w = po.gschur_cplx(A)
+    assert_schur_cplx(A, T, Z, w, tol=10.0)
+
+
+@pytest.mark.parametrize("n", [4, 32])
+def test_oracle_orthogonal_normal(n):
+    # random orthogonal: Schur form is block diagonal (test/real.jl:133-138)
+    rng = np.random.default_rng(300 + n)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    T, Z, w = po.gschur_real(Q)
+    assert_schur_real(Q, T, Z, w, tol=10.0)
+    assert np.linalg.norm(np.triu(T, 2)) / (n * np.linalg.norm(Q) * EPS) < 10
+
+
+@pytest.mark.parametrize("n", [4, 32])
+def test_oracle_jordan(n):
+    A = np.diag(np.ones(n - 1), 1) + np.eye(n)  # test/real.jl:180-191
+    T, Z, w = po.gschur_real(A)
+    assert_schur_real(A, T, Z, w, tol=20.0)
+
+
+@pytest.mark.parametrize("scale", [100 * np.finfo(float).tiny, np.finfo(float).max / 100])
+def test_oracle_hessenberg_extreme_scale(scale):
+    # hesstest with tiny and huge entries (test/real.jl:104-116)
+    rng = np.random.default_rng(7)
+    n = 32
+    A = scale * rng.random((n, n))
+    H, tau, Q = po.hessenberg(A)
+    HH = np.triu(H, -1)
+    As, HHs = A / scale, HH / scale
+    assert np.linalg.norm(As - Q @ HHs @ Q.T) / (n * np.linalg.norm(As) * EPS) < 10
+    assert np.linalg.norm(np.eye(n) - Q @ Q.T) / (n * EPS) < 10
+
+
+def test_oracle_scaled_schur():
+    # _scale! path: entries near overflow and underflow (test/real.jl:178, magns)
+    rng = np.random.default_rng(8)
+    for s in (1e-300, 1e300):
+        A = s * rng.standard_normal((16, 16))
+        T, Z, w = po.gschur_real(A)
+        be = np.linalg.norm(A / s - Z @ (T / s) @ Z.T) / np.linalg.norm(A / s)
+        assert be <= 10 * 16 * EPS
+        assert orth_error(Z) <= 10 * 16 * EPS
+
+
+@pytest.mark.parametrize("n", [2, 5, 32])
+def test_oracle_vectest(n):
+    rng = np.random.default_rng(400 + n)
+    for cplx in (False, True):
+        A = randn_matrix(rng, n, cplx)
+        T, Z, w = po.gschur(A)
+        VR = po.eigvecs(T, Z, left=False)
+        VL = po.eigvecs(T, Z, left=True)
+        nA = np.linalg.norm(A)
+        assert np.linalg.norm(A @ VR - VR @ np.diag(w)) / (n * nA * EPS) < 20
+        assert np.linalg.norm(A.conj().T @ VL - VL @ np.diag(w.conj())) / (n * nA * EPS) < 20
+        # _enormalize!: unit norm, largest entry real (util.jl:572-592)
+        assert np.all(np.abs(np.linalg.norm(VR, axis=0) - 1) / (n * EPS) < 10)
+        for j in range(n):
+            assert VR[np.argmax(np.abs(VR[:, j])), j].imag == 0
+
+
+def test_oracle_triangularize():
+    rng = np.random.default_rng(9)
+    n = 32
+    A = rng.standard_normal((n, n))
+    T, Z, w = po.gschur_real(A)
+    Tc, Zc, wc = po.triangularize(T, Z)
+    assert np.all(np.tril(Tc, -1) == 0)
+    assert np.linalg.norm(A - Zc @ Tc @ Zc.conj().T) / (n * np.linalg.norm(A) * EPS) < 10
+    assert np.linalg.norm(np.eye(n) - Zc @ Zc.conj().T) / (n * EPS) < 10
+    assert np.array_equal(np.sort_complex(wc), np.sort_complex(np.diag(Tc)))
+
+
+def test_oracle_gs2x2_near_degenerate():
+    # test/real.jl:311-317
+    rng = np.random.default_rng(10)
+    l1, l2 = 1 + 2 * EPS, 1 - 2 * EPS
+    B = np.diag([l1, l2]) + (EPS / 4) * rng.random((2, 2))
+    Bs, cs, sn, w1, w2 = po.gs2x2(B)
+    assert abs(max(w1.real, w2.real) - l1) < 2 * EPS
+    assert abs(min(w1.real, w2.real) - l2) < 2 * EPS
+
+
+def test_oracle_nonreal_subdiagonal_raises():
+    # test/errors.jl:2-5
+    n = 5
+    rng = np.random.default_rng(11)
+    A = np.diag(np.full(n - 1, -1.0 + 1.0j), -1) + np.triu(rng.random((n, n)))
+    st, _, _, _ = po.gschur_hess_cplx(A)
+    assert st == 2
+
+
+def test_oracle_unconverged():
+    rng = np.random.default_rng(12)
+    with pytest.raises(po.Unconverged):
+        po.gschur_real(rng.standard_normal((16, 16)), maxiter=2)
+
+
+def test_oracle_golden_fixtures():
+    """The oracle reproduces the committed golden outputs bit for bit."""
+    path = os.path.join(GOLDEN, "oracle_golden.npz")
+    g = np.load(path)
+    for key in [k for k in g.files if k.startswith("A_")]:
+        tag = key[2:]
+        A = g[key]
+        T, Z, w = po.gschur(A)
+        np.testing.assert_array_equal(T, g["T_" + tag])
+        np.testing.assert_array_equal(Z, g["Z_" + tag])
+        np.testing.assert_array_equal(w, g["w_" + tag])
