@@ -1,0 +1,335 @@
+"""Benchmark of the batched real FP64 Schur decomposition (the headline workload).
+
+Workload: 20,000 real Float64 matrices, orders iid uniform in [8, 128], entries iid
+N(0,1), seed 4 (one batch per rank); each step is one gschur! over the whole batch
+returning T, Z and the eigenvalues.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is matrices/s with the inputs resident in HBM (CUDA events on the launch
+stream; the step includes restoring A, which the decomposition overwrites);
+`e2e` is the same metric through the C-ABI with pinned host buffers, host<->device
+copies inside the timed region.  `--impl reference` times the CPU restatement of
+the reference algorithm (the oracle) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "genericschur.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "batched Schur matrices/s & n=4096 Schur time: mixed vs FP64, same backward err"
+UNIT = "matrices/s"
+COUNT, SEED = 20000, 4
+WORKLOAD = "batched real FP64 Schur (T, Z, eigenvalues): 20000 matrices, n~U{8..128}, N(0,1), seed 4"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=COUNT)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="plain stream launches instead of the CUDA graph")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch, dev):
+    """Measured FP64 peak: cuBLAS DGEMM 4096^3 (best of 5), the FP64 analogue of the
+    driver's cuBLAS bf16 figure."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * 4096.0 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_baseline_sample(count, seed, budget_s=15.0):
+    """Oracle (C++ restatement of the reference algorithm), OpenMP over the batch on
+    all host cores, on a bounded sample of the same workload."""
+    from oracle import pyoracle as po
+    from genericschur_gb300.workloads import batched_real
+    threads = os.cpu_count() or 1
+    # calibrate on a small sample, then size the sample for ~budget_s
+    pk, ns, offs, woffs = batched_real(count=64, seed=seed + 1000)
+    t = time.perf_counter()
+    _run_oracle(po, pk, ns, offs, woffs, threads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    m = int(min(count, max(64, 64 * budget_s / dt)))
+    pk, ns, offs, woffs = batched_real(count=m, seed=seed)
+    t = time.perf_counter()
+    bad = _run_oracle(po, pk, ns, offs, woffs, threads)
+    dt = time.perf_counter() - t
+    return {"value": m / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "first %d matrices of the seed-%d batch (same size law), %d failed" % (m, seed, bad),
+            "seconds": dt}
+
+
+def _run_oracle(po, pk, ns, offs, woffs, threads):
+    a = pk.copy()
+    z = np.zeros_like(a)
+    nw = int(ns.sum())
+    wr = np.zeros(nw)
+    wi = np.zeros(nw)
+    st = np.zeros(len(ns), dtype=np.int32)
+    return po.gschur_batched_packed_real(len(ns), offs, ns, a, z, wr, wi, woffs, st, threads)
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build()
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline_sample(args.count, SEED, budget_s=8.0)
+        if i >= args.warmup:
+            samples.append(r)
+    v = float(np.mean([s["value"] for s in samples]))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": float(np.mean([s["seconds"] for s in samples]) * 1e3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "batch": args.count, "seed": SEED},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": samples[0]["cores"], "kind": "port",
+                            "sample": samples[0]["sample"] + "; C++ restatement of GenericSchur.jl's gschur! "
+                                      "(Julia is absent on this machine), OpenMP over the batch"},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import build_lib
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build_lib.build()
+    import genericschur_gb300 as gs
+    from genericschur_gb300 import _capi
+    from genericschur_gb300.workloads import batched_real, real_flops
+
+    ctx = gs.Context(local)
+    packed, ns, offs, woffs = batched_real(count=args.count, seed=SEED + rank)
+    nw = int(ns.sum())
+    count = len(ns)
+    flops = real_flops(ns)
+    # device-resident buffers
+    dA0 = torch.from_numpy(packed).to(dev)
+    dA = torch.empty_like(dA0)
+    dZ = torch.empty_like(dA0)
+    dwr = torch.empty(nw, dtype=torch.float64, device=dev)
+    dwi = torch.empty(nw, dtype=torch.float64, device=dev)
+    dns = torch.from_numpy(ns).to(dev)
+    doffs = torch.from_numpy(offs).to(dev)
+    dwoffs = torch.from_numpy(woffs).to(dev)
+    dst = torch.empty(count, dtype=torch.int32, device=dev)
+    # a dedicated (non-default) stream: the library and the CUDA events share it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | (0 if args.no_graph else _capi.GS_GRAPH)
+    lib = ctx.lib
+
+    def step():
+        dA.copy_(dA0)
+        rc = lib.gs_schur_batched_f64(ctx.handle, count, dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
+                                      dA.data_ptr(), dZ.data_ptr(), dwr.data_ptr(), dwi.data_ptr(), dst.data_ptr(),
+                                      flags)
+        if rc != 0:
+            raise RuntimeError("gs_schur_batched_f64 failed: %s" % ctx.last_error())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    bad = int((dst != 0).sum().item())
+    # per-launch kernel time of the batched Schur sequence (dominant kernel), events on its stream
+    kms = []
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    # kernel-only time per launch (CUDA events recorded by the library around its kernels)
+    for _ in range(2):
+        step()
+        torch.cuda.synchronize()
+        kms.append(ctx.last_kernel_ms())
+    ms = ms_total / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * count / (ms * 1e-3)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(ctx, packed, ns, offs, woffs, steps=max(1, min(args.steps, 3)))
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    peak = fp64_peak_tflops(torch, dev)
+    kernel_ms = float(np.mean(kms))
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": None,
+            "peak_source": "measured: cuBLAS DGEMM 4096^3 in this run (FP64 FMA pipe; no FP64 tensor-core path "
+                           "is faster on GB300)",
+            "algorithmic": "25 n^3 FLOP per matrix, summed over the batch (%.4g FLOP per launch)" % flops,
+            "kernel_ms": kernel_ms}
+    cpu = None if args.no_cpu else cpu_baseline_sample(args.count, SEED)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "batch_per_gpu": count, "seed": SEED,
+                      "l2": "inputs (%.0f MB of A per step) larger than L2; A restored from a pristine copy each "
+                            "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
+           "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+           "gpu_launches": 5 * args.steps, "unconverged": bad}
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def measure_e2e(ctx, packed, ns, offs, woffs, steps):
+    """Same metric through the C-ABI with pinned host buffers (copies included)."""
+    import ctypes
+    from genericschur_gb300 import _capi
+    count = len(ns)
+    nw = int(ns.sum())
+    nbytes = packed.nbytes
+    hp = [ctx.host_alloc(nbytes) for _ in range(2)]
+    hw = [ctx.host_alloc(nw * 8) for _ in range(2)]
+    hs = ctx.host_alloc(count * 4)
+    try:
+        A = np.ctypeslib.as_array((ctypes.c_double * packed.size).from_address(hp[0]))
+        Z = np.ctypeslib.as_array((ctypes.c_double * packed.size).from_address(hp[1]))
+        ctx.set_stream(None)
+        flags = _capi.GS_WANTZ | _capi.GS_SCALE
+        times = []
+        for i in range(steps + 1):
+            A[:] = packed
+            t = time.perf_counter()
+            rc = ctx.lib.gs_schur_batched_f64(ctx.handle, count, ns.ctypes.data, offs.ctypes.data,
+                                              woffs.ctypes.data, hp[0], hp[1], hw[0], hw[1], hs, flags)
+            dt = time.perf_counter() - t
+            if rc != 0:
+                raise RuntimeError(ctx.last_error())
+            if i > 0:
+                times.append(dt)
+        dt = float(np.mean(times))
+        h2d = nbytes + ns.nbytes + offs.nbytes + woffs.nbytes
+        d2h = 2 * nbytes + 2 * nw * 8 + count * 4
+        return {"value": count / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "seconds_per_step": dt}
+    finally:
+        for p in hp + hw + [hs]:
+            ctx.host_free(p)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -202,3 +202,79 @@ __device__ inline void gs2x2(double& a, double& b, double& c, double& d, double&
 }
 
 }  // namespace gsk
+
+// ---- complex FP64 helpers (double2 = (re, im)) -------------------------------
+namespace gsk {
+__device__ __forceinline__ double2 zmk(double r, double i) { return make_double2(r, i); }
+__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 zneg(double2 a) { return make_double2(-a.x, -a.y); }
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 zscal(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// a + b * c
+__device__ __forceinline__ double2 zfma(double2 b, double2 c, double2 a) {
+  return make_double2(fma(b.x, c.x, fma(-b.y, c.y, a.x)), fma(b.x, c.y, fma(b.y, c.x, a.y)));
+}
+// a - b * c
+__device__ __forceinline__ double2 zfms(double2 b, double2 c, double2 a) {
+  return make_double2(fma(-b.x, c.x, fma(b.y, c.y, a.x)), fma(-b.x, c.y, fma(-b.y, c.x, a.y)));
+}
+// a + conj(b) * c
+__device__ __forceinline__ double2 zfmac(double2 b, double2 c, double2 a) {
+  return make_double2(fma(b.x, c.x, fma(b.y, c.y, a.x)), fma(b.x, c.y, fma(-b.y, c.x, a.y)));
+}
+__device__ __forceinline__ double zabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ double zabs(double2 a) { return hypot(a.x, a.y); }
+// Smith's complex division
+__device__ inline double2 zdiv(double2 a, double2 b) {
+  if (fabs(b.y) <= fabs(b.x)) {
+    const double r = b.y / b.x, d = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const double r = b.x / b.y, d = b.y + b.x * r;
+  return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+// principal square root
+__device__ inline double2 zsqrt(double2 z) {
+  const double x = z.x, y = z.y;
+  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
+  const double t = sqrt((fabs(x) + hypot(x, y)) * 0.5);
+  if (x >= 0.0) return make_double2(t, y / (2.0 * t));
+  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
+// 2-element complex reflector (householder.jl:56-102 for length 2): returns tau,
+// overwrites (a, x1) with (beta, v1); beta is real.
+__device__ inline double2 zreflector2(double2& a, double2& x1) {
+  const double xnorm = hypot(x1.x, x1.y);
+  if (xnorm == 0.0 && a.y == 0.0) return make_double2(0.0, 0.0);
+  const double big = fmax(fmax(fabs(a.x), fabs(a.y)), xnorm);
+  double beta;
+  if (big < 1.0e150 && big > 1.0e-150) {
+    beta = sqrt(fma(a.x, a.x, fma(a.y, a.y, xnorm * xnorm)));
+  } else {
+    const double r = 1.0 / big, p = a.x * r, q = a.y * r, s = xnorm * r;
+    beta = big * sqrt(fma(p, p, fma(q, q, s * s)));
+  }
+  beta = -copysign(beta, a.x);
+  const double sfmin = kFmin / kEps;
+  int kount = 0;
+  if (fabs(beta) < sfmin) {
+    const double rsfmin = 1.0 / sfmin;
+    do {
+      ++kount;
+      x1 = zscal(x1, rsfmin); beta *= rsfmin; a = zscal(a, rsfmin);
+    } while (fabs(beta) < sfmin && kount < 20);
+    const double xn = hypot(x1.x, x1.y);
+    beta = -copysign(sqrt(fma(a.x, a.x, fma(a.y, a.y, xn * xn))), a.x);
+  }
+  const double2 tau = make_double2((beta - a.x) / beta, -a.y / beta);
+  const double2 t = zdiv(make_double2(1.0, 0.0), make_double2(a.x - beta, a.y));
+  x1 = zmul(x1, t);
+  for (int j = 0; j < kount; ++j) beta *= sfmin;
+  a = make_double2(beta, 0.0);
+  return tau;
+}
+}  // namespace gsk

@@ -47,6 +47,40 @@ struct CplxBatch {
   long long maxinner_abs;  // when > 0, overrides maxinner_mult
 };
 
+// Eigenvectors of complex Schur factors (T upper triangular), batched.  Matrix b
+// has order ns[b] <= 128 at element offset offs[b] of T, Z, VR, VL and scratch.
+constexpr int kEigSmem = 64;  // orders up to this keep the solution block in shared memory
+struct EigBatch {
+  int count;
+  const int* ns;
+  const long long* offs;
+  const double2* T;
+  const double2* Z;   // may be null: eigenvectors of T itself
+  double2* VR;        // right eigenvectors (null: skip)
+  double2* VL;        // left eigenvectors (null: skip)
+  double2* scratch;   // solution blocks of orders > kEigSmem
+  int normalize;      // apply _enormalize!
+  const long long* woffs;  // per-matrix offset into colmap (with colmap)
+  const int* colmap;       // optional: output column of eigenvector ki is colmap[woffs[b] + ki - 1]
+};
+size_t eigvecs_smem_bytes(int nmax);
+cudaError_t launch_eigvecs_batched(const EigBatch& eb, int nmax, int num_sms, cudaStream_t s);
+
+// Real quasi-triangular -> complex triangular Schur pairs (triang.jl:9-43).
+struct TriBatch {
+  int count;
+  const int* ns;
+  const long long* offs;   // element offsets of T/Z (real and complex buffers alike)
+  const long long* woffs;  // offsets of w / colmap
+  const double* Tr;
+  const double* Zr;        // may be null (identity)
+  double2* Tc;
+  double2* Zc;             // may be null
+  double2* w;              // may be null
+  int* colmap;             // may be null
+};
+cudaError_t launch_triangularize(const TriBatch& tb, int num_sms, cudaStream_t s);
+
 // Size bins of the persistent batched kernels.  `sched` holds, per bin, the
 // [start, end) range of that bin inside the sorted work order and a queue ticket
 // counter: sched[3*bin + {0,1,2}].

@@ -368,18 +368,408 @@ int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   return GS_OK;
 }
 
-int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* w,
-                 unsigned flags, int64_t maxiter, int64_t maxinner) {
-  (void)A; (void)lda; (void)Z; (void)ldz; (void)w; (void)flags; (void)maxiter; (void)maxinner;
-  if (!ctx) return GS_BADARG;
-  return set_err(ctx, GS_BADARG, "complex path not built yet (n=%lld)", (long long)n);
+// ---------------------------------------------------------------------------
+// complex: batched and single
+// ---------------------------------------------------------------------------
+static int run_batched_cplx(gs_context* ctx, const CplxBatch& bt, int* order, int* sched, bool use_graph,
+                            const std::vector<long long>& key) {
+  auto enqueue = [&](cudaStream_t s) -> int {
+    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
+    return fork_join(ctx, s, [&](cudaStream_t* aux) {
+      return launch_schur_batched_cplx(bt, order, sched, ctx->num_sms, aux, kNumBins);
+    });
+  };
+  CK(cudaEventRecord(ctx->t0, ctx->stream));
+  if (use_graph) {
+    if (!ctx->gexec || ctx->gkey != key) {
+      if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+      CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue(ctx->cap);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(ctx->cap, &g);
+      if (rc != GS_OK) { if (g) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { ctx->gexec = nullptr; return set_err(ctx, GS_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+      ctx->gkey = key;
+    }
+    CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+  } else {
+    int rc = enqueue(ctx->stream);
+    if (rc != GS_OK) return rc;
+  }
+  CK(cudaEventRecord(ctx->t1, ctx->stream));
+  ctx->timed = true;
+  return GS_OK;
 }
 
 int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* w, int32_t* status, unsigned flags) {
-  (void)count; (void)ns; (void)offs; (void)woffs; (void)A; (void)Z; (void)w; (void)status; (void)flags;
   if (!ctx) return GS_BADARG;
-  return set_err(ctx, GS_BADARG, "complex batched path not built yet");
+  ctx->err.clear();
+  if (count < 0 || count > (1LL << 30)) return set_err(ctx, GS_BADARG, "bad count %lld", (long long)count);
+  if (count == 0) return GS_OK;
+  const bool wantz = flags & GS_WANTZ;
+  if (!ns || !offs || !woffs || !A || !w || !status || (wantz && !Z))
+    return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  CplxBatch bt{};
+  bt.count = (int)count;
+  bt.wantz = wantz;
+  bt.scale = (flags & GS_SCALE) ? 1 : 0;
+  bt.maxiter_mult = 100;
+  bt.maxinner_mult = 30;
+  Arena ar;
+  long long na = 0, nw = 0;
+  if (!dev) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int n = ns[b];
+      if (n < 0 || n > kSmallMax)
+        return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
+      if (offs[b] < 0 || woffs[b] < 0) return set_err(ctx, GS_BADARG, "matrix %lld: negative offset", (long long)b);
+      na = std::max(na, (long long)offs[b] + (long long)n * n);
+      nw = std::max(nw, (long long)woffs[b] + n);
+    }
+  }
+  const size_t o_order = ar.take<int>(count);
+  const size_t o_sched = ar.take<int>(3 * kNumBins);
+  size_t o_A = 0, o_Z = 0, o_w = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
+  if (!dev) {
+    o_A = ar.take<double2>(na);
+    o_Z = ar.take<double2>(wantz ? na : 1);
+    o_w = ar.take<double2>(nw);
+    o_ns = ar.take<int>(count);
+    o_offs = ar.take<long long>(count);
+    o_woffs = ar.take<long long>(count);
+    o_st = ar.take<int>(count);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  int* order = (int*)(base + o_order);
+  int* sched = (int*)(base + o_sched);
+  cudaStream_t s = ctx->stream;
+  if (!dev) {
+    bt.ns = (const int*)(base + o_ns);
+    bt.offs = (const long long*)(base + o_offs);
+    bt.woffs = (const long long*)(base + o_woffs);
+    bt.A = (double2*)(base + o_A);
+    bt.Z = wantz ? (double2*)(base + o_Z) : nullptr;
+    bt.w = (double2*)(base + o_w);
+    bt.status = (int*)(base + o_st);
+    CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(bt.A, A, sizeof(double2) * na, cudaMemcpyHostToDevice, s));
+  } else {
+    bt.ns = ns;
+    bt.offs = (const long long*)offs;
+    bt.woffs = (const long long*)woffs;
+    bt.A = (double2*)A;
+    bt.Z = wantz ? (double2*)Z : nullptr;
+    bt.w = (double2*)w;
+    bt.status = status;
+  }
+  std::vector<long long> key = {2, (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
+                                (long long)(uintptr_t)bt.ns, (long long)(uintptr_t)bt.w,
+                                (long long)(uintptr_t)order, (long long)flags};
+  rc = run_batched_cplx(ctx, bt, order, sched, (flags & GS_GRAPH) != 0, key);
+  if (rc) return rc;
+  if (dev) return GS_OK;
+  CK(cudaMemcpyAsync(A, bt.A, sizeof(double2) * na, cudaMemcpyDeviceToHost, s));
+  if (wantz) CK(cudaMemcpyAsync(Z, bt.Z, sizeof(double2) * na, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(w, bt.w, sizeof(double2) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(status, bt.status, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int64_t b = 0; b < count; ++b)
+    if (status[b] != GS_OK) return set_err(ctx, GS_UNCONVERGED, "matrix %lld: iteration limit reached", (long long)b);
+  return GS_OK;
+}
+
+int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* w,
+                 unsigned flags, int64_t maxiter, int64_t maxinner) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  const bool wantz = flags & GS_WANTZ;
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
+  if (lda < std::max<int64_t>(n, 1) || (wantz && ldz < std::max<int64_t>(n, 1)))
+    return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
+  if (n == 0) return GS_OK;
+  if (!A || !w || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
+  if (n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld > %d: large-matrix path not available", (long long)n, kSmallMax);
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  Arena ar;
+  const size_t o_A = ar.take<double2>(n * n), o_Z = ar.take<double2>(n * n), o_w = ar.take<double2>(n);
+  const size_t o_meta = ar.take<long long>(4), o_st = ar.take<int>(2);
+  const size_t o_order = ar.take<int>(1), o_sched = ar.take<int>(3 * kNumBins);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double2* dA = (double2*)(base + o_A);
+  double2* dZ = (double2*)(base + o_Z);
+  const size_t es = sizeof(double2);
+  CK(cudaMemcpy2DAsync(dA, n * es, A, lda * es, n * es, n, in, s));
+  long long meta_h[4] = {0, 0, 0, 0};
+  int n32 = (int)n;
+  long long* meta = (long long*)(base + o_meta);
+  CK(cudaMemcpyAsync(meta, meta_h, sizeof(meta_h), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(meta + 2, &n32, sizeof(int), cudaMemcpyHostToDevice, s));
+  CplxBatch bt{};
+  bt.count = 1;
+  bt.ns = (const int*)(meta + 2);
+  bt.offs = meta;
+  bt.woffs = meta + 1;
+  bt.A = dA;
+  bt.Z = wantz ? dZ : nullptr;
+  bt.w = (double2*)(base + o_w);
+  bt.status = (int*)(base + o_st);
+  bt.wantz = wantz;
+  bt.scale = (flags & GS_SCALE) ? 1 : 0;
+  bt.maxiter_mult = 100;
+  bt.maxinner_mult = 30;
+  bt.maxiter_abs = maxiter > 0 ? maxiter : 0;
+  bt.maxinner_abs = maxinner > 0 ? maxinner : 0;
+  rc = run_batched_cplx(ctx, bt, (int*)(base + o_order), (int*)(base + o_sched), false, {});
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(A, lda * es, dA, n * es, n * es, n, out, s));
+  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * es, dZ, n * es, n * es, n, out, s));
+  CK(cudaMemcpyAsync(w, bt.w, n * es, out, s));
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, bt.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (st != GS_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit reached");
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// eigenvectors and triangularize
+// ---------------------------------------------------------------------------
+namespace {
+
+// Everything on device pointers: T/Z complex (Zc may be null), outputs VR/VL complex.
+int run_eigvecs(gs_context* ctx, int count, const int* ns, const long long* offs, const double2* T,
+                const double2* Z, double2* VR, double2* VL, double2* scratch, const long long* woffs,
+                const int* colmap, bool normalize) {
+  EigBatch eb{};
+  eb.count = count;
+  eb.ns = ns;
+  eb.offs = offs;
+  eb.T = T;
+  eb.Z = Z;
+  eb.VR = VR;
+  eb.VL = VL;
+  eb.scratch = scratch;
+  eb.normalize = normalize ? 1 : 0;
+  eb.woffs = woffs;
+  eb.colmap = colmap;
+  cudaError_t e = launch_eigvecs_batched(eb, kSmallMax, ctx->num_sms, ctx->stream);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "eigvecs launch: %s", cudaGetErrorString(e));
+  return GS_OK;
+}
+
+// Shared driver of the eigenvector entry points.  `real` selects real T/Z input
+// (triangularized first).  Host or device pointers per GS_DEVICE.
+int eigvecs_driver(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs, const int64_t* woffs,
+                   int64_t packed_len, int64_t w_len, const double* T, const double* Z, double* VR, double* VL,
+                   unsigned flags, bool real) {
+  if (count < 0) return set_err(ctx, GS_BADARG, "bad count");
+  if (count == 0) return GS_OK;
+  if (!ns || !offs || !T || (!VR && !VL) || (real && !woffs)) return set_err(ctx, GS_BADARG, "null array argument");
+  if (packed_len < 0 || w_len < 0) return set_err(ctx, GS_BADARG, "negative length");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  if (!dev) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int n = ns[b];
+      if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
+      if (offs[b] < 0 || offs[b] + (long long)n * n > packed_len) return set_err(ctx, GS_BADARG, "matrix %lld outside the packed buffer", (long long)b);
+      if (real && (woffs[b] < 0 || woffs[b] + n > w_len)) return set_err(ctx, GS_BADARG, "matrix %lld: eigenvalue offset outside w_len", (long long)b);
+    }
+  }
+  const size_t es = real ? sizeof(double) : sizeof(double2);
+  Arena ar;
+  size_t o_T = 0, o_Z = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_VR = 0, o_VL = 0;
+  const size_t o_X = ar.take<double2>(packed_len);
+  size_t o_Tc = 0, o_Zc = 0, o_map = 0;
+  if (real) {
+    o_Tc = ar.take<double2>(packed_len);
+    o_Zc = ar.take<double2>(Z ? packed_len : 1);
+    o_map = ar.take<int>(w_len);
+  }
+  if (!dev) {
+    o_T = ar.take<char>(es * packed_len);
+    o_Z = ar.take<char>(Z ? es * packed_len : 1);
+    o_ns = ar.take<int>(count);
+    o_offs = ar.take<long long>(count);
+    o_woffs = ar.take<long long>(real ? count : 1);
+    o_VR = ar.take<double2>(VR ? packed_len : 1);
+    o_VL = ar.take<double2>(VL ? packed_len : 1);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const int* d_ns = (const int*)ns;
+  const long long* d_offs = (const long long*)offs;
+  const long long* d_woffs = (const long long*)woffs;
+  const void* d_T = T;
+  const void* d_Z = Z;
+  double2* d_VR = (double2*)VR;
+  double2* d_VL = (double2*)VL;
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    if (real) CK(cudaMemcpyAsync(base + o_woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_T, T, es * packed_len, cudaMemcpyHostToDevice, s));
+    if (Z) CK(cudaMemcpyAsync(base + o_Z, Z, es * packed_len, cudaMemcpyHostToDevice, s));
+    d_ns = (const int*)(base + o_ns);
+    d_offs = (const long long*)(base + o_offs);
+    d_woffs = (const long long*)(base + o_woffs);
+    d_T = base + o_T;
+    d_Z = Z ? (const void*)(base + o_Z) : nullptr;
+    d_VR = VR ? (double2*)(base + o_VR) : nullptr;
+    d_VL = VL ? (double2*)(base + o_VL) : nullptr;
+  }
+  CK(cudaEventRecord(ctx->t0, s));
+  const double2* cT = (const double2*)d_T;
+  const double2* cZ = (const double2*)d_Z;
+  const int* cmap = nullptr;
+  if (real) {
+    TriBatch tb{};
+    tb.count = (int)count;
+    tb.ns = d_ns;
+    tb.offs = d_offs;
+    tb.woffs = d_woffs;
+    tb.Tr = (const double*)d_T;
+    tb.Zr = (const double*)d_Z;
+    tb.Tc = (double2*)(base + o_Tc);
+    tb.Zc = d_Z ? (double2*)(base + o_Zc) : nullptr;
+    tb.w = nullptr;
+    tb.colmap = (int*)(base + o_map);
+    cudaError_t e = launch_triangularize(tb, ctx->num_sms, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "triangularize launch: %s", cudaGetErrorString(e));
+    cT = tb.Tc;
+    cZ = tb.Zc;
+    cmap = tb.colmap;
+  }
+  rc = run_eigvecs(ctx, (int)count, d_ns, d_offs, cT, cZ, d_VR, d_VL, (double2*)(base + o_X), d_woffs, cmap,
+                   !(flags & GS_RAW));
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  if (dev) return GS_OK;
+  if (VR) CK(cudaMemcpyAsync(VR, d_VR, sizeof(double2) * packed_len, cudaMemcpyDeviceToHost, s));
+  if (VL) CK(cudaMemcpyAsync(VL, d_VL, sizeof(double2) * packed_len, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+}  // namespace
+
+int gs_eigvecs_c64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
+                   unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld outside [0, %d]", (long long)n, kSmallMax);
+  if (n == 0) return GS_OK;
+  if (flags & GS_DEVICE) return set_err(ctx, GS_BADARG, "gs_eigvecs_c64 with GS_DEVICE: use gs_eigvecs_batched_c64");
+  const int32_t n32 = (int32_t)n;
+  const int64_t zero = 0;
+  return eigvecs_driver(ctx, 1, &n32, &zero, nullptr, n * n, 0, T, Z, VR, VL, flags, false);
+}
+
+int gs_eigvecs_f64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
+                   unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld outside [0, %d]", (long long)n, kSmallMax);
+  if (n == 0) return GS_OK;
+  if (flags & GS_DEVICE) return set_err(ctx, GS_BADARG, "gs_eigvecs_f64 with GS_DEVICE: use gs_eigvecs_batched_f64");
+  const int32_t n32 = (int32_t)n;
+  const int64_t zero = 0;
+  return eigvecs_driver(ctx, 1, &n32, &zero, &zero, n * n, n, T, Z, VR, VL, flags, true);
+}
+
+int gs_eigvecs_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs, int64_t packed_len,
+                           const double* T, const double* Z, double* VR, double* VL, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  return eigvecs_driver(ctx, count, ns, offs, nullptr, packed_len, 0, T, Z, VR, VL, flags, false);
+}
+
+int gs_eigvecs_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                           const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T, const double* Z,
+                           double* VR, double* VL, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  return eigvecs_driver(ctx, count, ns, offs, woffs, packed_len, w_len, T, Z, VR, VL, flags, true);
+}
+
+int gs_triangularize_f64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* Tc, double* Zc,
+                         double* w, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
+  if (n == 0) return GS_OK;
+  if (!T || !Tc || (Zc && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_meta = ar.take<long long>(4);
+  size_t o_T = 0, o_Z = 0, o_Tc = 0, o_Zc = 0, o_w = 0;
+  if (!dev) {
+    o_T = ar.take<double>(nn);
+    o_Z = ar.take<double>(Z ? nn : 1);
+    o_Tc = ar.take<double2>(nn);
+    o_Zc = ar.take<double2>(Zc ? nn : 1);
+    o_w = ar.take<double2>(n);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  long long meta_h[4] = {0, 0, 0, 0};
+  int n32 = (int)n;
+  long long* meta = (long long*)(base + o_meta);
+  CK(cudaMemcpyAsync(meta, meta_h, sizeof(meta_h), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(meta + 2, &n32, sizeof(int), cudaMemcpyHostToDevice, s));
+  TriBatch tb{};
+  tb.count = 1;
+  tb.ns = (const int*)(meta + 2);
+  tb.offs = meta;
+  tb.woffs = meta + 1;
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_T, T, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (Z) CK(cudaMemcpyAsync(base + o_Z, Z, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    tb.Tr = (const double*)(base + o_T);
+    tb.Zr = Z ? (const double*)(base + o_Z) : nullptr;
+    tb.Tc = (double2*)(base + o_Tc);
+    tb.Zc = Zc ? (double2*)(base + o_Zc) : nullptr;
+    tb.w = w ? (double2*)(base + o_w) : nullptr;
+  } else {
+    tb.Tr = T;
+    tb.Zr = Z;
+    tb.Tc = (double2*)Tc;
+    tb.Zc = (double2*)Zc;
+    tb.w = (double2*)w;
+  }
+  tb.colmap = nullptr;
+  cudaError_t e = launch_triangularize(tb, ctx->num_sms, s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "triangularize launch: %s", cudaGetErrorString(e));
+  if (dev) return GS_OK;
+  CK(cudaMemcpyAsync(Tc, tb.Tc, nn * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  if (Zc) CK(cudaMemcpyAsync(Zc, tb.Zc, nn * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  if (w) CK(cudaMemcpyAsync(w, tb.w, n * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
 }
 
 }  // extern "C"

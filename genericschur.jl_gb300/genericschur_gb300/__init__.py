@@ -7,7 +7,11 @@ underscore):
   gschur(A)  / gschur_(A)      GenericSchur.jl:343 / 805-835 (real), 350-372 (complex)
   schur(A)                      pirates.jl:8-10 (schur!) through the non-mutating wrapper
   eigvals(A)                    pirates.jl:17-27
+  eigvecs(S; left) / geigvecs   pirates.jl:38-48 / vectors.jl:12-20
+  eigen(A)                      pirates.jl:63-89 (without balancing)
+  triangularize(S)              triang.jl:9-43
   gschur_batched(...)           batched form, no reference counterpart
+  geigvecs_batched(...)         batched eigenvectors, no reference counterpart
 
 Matrices are numpy arrays; they are handed to the C-ABI column-major (Julia's
 layout).  All arithmetic runs in the CUDA library; nothing here computes a
@@ -21,8 +25,12 @@ from . import _capi
 from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS_UNCONVERGED, GS_WANTZ, Context,
                     GSError, get_context)
 
-__all__ = ["Schur", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_", "schur",
-           "eigvals", "gschur_batched", "get_context", "Context", "pack_batch", "unpack_batch"]
+__all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_",
+           "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
+           "get_context", "Context", "pack_batch", "unpack_batch"]
+
+# LinearAlgebra.Eigen(values, vectors)
+Eigen = namedtuple("Eigen", ["values", "vectors"])
 
 # LinearAlgebra.Schur(T, Z, values)
 Schur = namedtuple("Schur", ["T", "Z", "values"])
@@ -186,3 +194,104 @@ def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ
     Zs = unpack_batch(Z, ns, offs) if wantZ else [None] * count
     ws = [w[o:o + n] for o, n in zip(woffs, ns)]
     return Ts, Zs, ws, status
+
+
+# ---------------------------------------------------------------------------
+# eigenvectors, triangularize, eigen
+# ---------------------------------------------------------------------------
+def _fc(a, dt):
+    return np.array(a, dtype=dt, order="F", copy=True)
+
+
+def geigvecs(S, left=False, normalize=True, ctx=None):
+    """Eigenvectors from a Schur decomposition (vectors.jl:12-20): right, or left
+    with left=True; columns ordered like S.values, unit 2-norm with the
+    largest-modulus entry real."""
+    ctx = ctx or get_context()
+    T = np.asarray(S.T)
+    n = _checksquare(T)
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    if n == 0:
+        return V
+    Z = S.Z if (S.Z is not None and np.asarray(S.Z).size) else None
+    flags = 0 if normalize else _capi.GS_RAW
+    outR, outL = (None, V) if left else (V, None)
+    if np.iscomplexobj(T):
+        Tc = _fc(T, np.complex128)
+        Zc = _fc(Z, np.complex128) if Z is not None else None
+        rc = ctx.lib.gs_eigvecs_c64(ctx.handle, n, _ptr(Tc), _ptr(Zc), _ptr(outR), _ptr(outL), flags)
+    else:
+        Tr = _fc(T, np.float64)
+        Zr = _fc(Z, np.float64) if Z is not None else None
+        rc = ctx.lib.gs_eigvecs_f64(ctx.handle, n, _ptr(Tr), _ptr(Zr), _ptr(outR), _ptr(outL), flags)
+    if rc != GS_OK:
+        _raise(rc, ctx, "geigvecs")
+    return V
+
+
+def eigvecs(S, left=False, ctx=None):
+    """LinearAlgebra.eigvecs(S::Schur; left) as pirated by the reference (pirates.jl:38-48)."""
+    return geigvecs(S, left=left, ctx=ctx)
+
+
+def triangularize(S, ctx=None):
+    """Real standard-form Schur -> complex triangular Schur (triang.jl:9-43)."""
+    ctx = ctx or get_context()
+    T = _fc(S.T, np.float64)
+    n = _checksquare(T)
+    Z = _fc(S.Z, np.float64) if (S.Z is not None and np.asarray(S.Z).size) else None
+    Tc = np.zeros((n, n), dtype=np.complex128, order="F")
+    Zc = np.zeros((n, n), dtype=np.complex128, order="F") if Z is not None else None
+    w = np.zeros(n, dtype=np.complex128)
+    rc = ctx.lib.gs_triangularize_f64(ctx.handle, n, _ptr(T), _ptr(Z), _ptr(Tc), _ptr(Zc), _ptr(w), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "triangularize")
+    return Schur(Tc, Zc if Zc is not None else np.zeros((0, 0), dtype=np.complex128), w)
+
+
+def eigen(A, permute=False, scale=False, sortby="default", ctx=None):
+    """Eigen decomposition (pirates.jl:63-89): Schur form, triangularize for real
+    input, right eigenvectors, _enormalize!, sort.  Balancing (permute/scale,
+    balance.jl) is not part of this engine; asking for it raises ArgumentError."""
+    if permute or scale:
+        raise ArgumentError("balancing is not implemented by the GB300 engine; call eigen(A, permute=False, scale=False)")
+    S = gschur(A, ctx=ctx)
+    if not np.iscomplexobj(S.T):
+        S = triangularize(S, ctx=ctx)
+    V = geigvecs(S, ctx=ctx)
+    w = S.values
+    if sortby is None:
+        return Eigen(w, V)
+    p = _eigsortby(w) if sortby == "default" else np.argsort([sortby(x) for x in w], kind="stable")
+    return Eigen(w[p], V[:, p])
+
+
+def geigvecs_batched(T_packed, Z_packed, ns, offs, woffs=None, left=False, normalize=True, ctx=None):
+    """Eigenvectors for a packed batch of Schur pairs (orders <= 128).  Returns the
+    packed complex eigenvector matrices."""
+    ctx = ctx or get_context()
+    ns = np.ascontiguousarray(ns, dtype=np.int32)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    count = len(ns)
+    plen = len(T_packed)
+    V = np.zeros(plen, dtype=np.complex128)
+    outR, outL = (None, V) if left else (V, None)
+    flags = 0 if normalize else _capi.GS_RAW
+    if np.iscomplexobj(T_packed):
+        T = np.ascontiguousarray(T_packed, dtype=np.complex128)
+        Z = np.ascontiguousarray(Z_packed, dtype=np.complex128) if Z_packed is not None else None
+        rc = ctx.lib.gs_eigvecs_batched_c64(ctx.handle, count, _ptr(ns), _ptr(offs), plen, _ptr(T), _ptr(Z), _ptr(outR),
+                                            _ptr(outL), flags)
+    else:
+        if woffs is None:
+            woffs = np.zeros(count, dtype=np.int64)
+            woffs[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+        woffs = np.ascontiguousarray(woffs, dtype=np.int64)
+        wlen = int((woffs + ns).max()) if count else 0
+        T = np.ascontiguousarray(T_packed, dtype=np.float64)
+        Z = np.ascontiguousarray(Z_packed, dtype=np.float64) if Z_packed is not None else None
+        rc = ctx.lib.gs_eigvecs_batched_f64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), plen, wlen, _ptr(T),
+                                            _ptr(Z), _ptr(outR), _ptr(outL), flags)
+    if rc != GS_OK:
+        _raise(rc, ctx, "geigvecs_batched")
+    return V

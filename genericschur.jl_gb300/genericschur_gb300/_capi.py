@@ -20,6 +20,7 @@ GS_WANTZ = 1
 GS_SCALE = 2
 GS_DEVICE = 4
 GS_GRAPH = 8
+GS_RAW = 16
 
 _i = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -40,6 +41,11 @@ SIGNATURES = {
     "gs_schur_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _u, _i64, _i64]),
     "gs_schur_batched_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_schur_batched_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_eigvecs_c64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
+    "gs_eigvecs_f64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
+    "gs_triangularize_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _u]),
+    "gs_eigvecs_batched_c64": (_i, [_p, _i64, _p, _p, _i64, _p, _p, _p, _p, _u]),
+    "gs_eigvecs_batched_f64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
 }
 
 _lib = None

@@ -1,0 +1,56 @@
+"""Seeded synthetic workloads with the sizes and value laws of the benchmark configs.
+
+The reference publishes no datasets; the configs name their inputs by law and
+seed, and these generators reproduce those laws with numpy's PCG64 streams (the
+reference's Julia randn stream cannot be reproduced outside Julia).
+"""
+import numpy as np
+
+from . import pack_batch
+
+
+def batch_sizes(count, seed, lo=8, hi=128):
+    """Orders iid uniform on the integers [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return rng.integers(lo, hi + 1, size=count).astype(np.int32)
+
+
+def batched_real(count=20000, seed=4, lo=8, hi=128):
+    """Packed batch of real N(0,1) matrices with orders ~ U{lo..hi}.
+    Returns (packed, ns, offs, woffs)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(lo, hi + 1, size=count).astype(np.int32)
+    sq = ns.astype(np.int64) ** 2
+    offs = np.zeros(count, dtype=np.int64)
+    offs[1:] = np.cumsum(sq)[:-1]
+    woffs = np.zeros(count, dtype=np.int64)
+    woffs[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+    packed = rng.standard_normal(int(sq.sum()))  # column-major per matrix by construction
+    return packed, ns, offs, woffs
+
+
+def batched_cplx(count=5000, seed=5, lo=8, hi=128):
+    """Packed batch of complex matrices, real and imaginary parts iid N(0, 1/2)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(lo, hi + 1, size=count).astype(np.int32)
+    sq = ns.astype(np.int64) ** 2
+    offs = np.zeros(count, dtype=np.int64)
+    offs[1:] = np.cumsum(sq)[:-1]
+    woffs = np.zeros(count, dtype=np.int64)
+    woffs[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+    m = int(sq.sum())
+    packed = (rng.standard_normal(m) + 1j * rng.standard_normal(m)) / np.sqrt(2.0)
+    return packed, ns, offs, woffs
+
+
+def real_flops(ns):
+    """Algorithmic FLOPs of a real Schur decomposition with Z: 25 n^3 per matrix."""
+    return 25.0 * float(np.sum(np.asarray(ns, dtype=np.float64) ** 3))
+
+
+def cplx_flops(ns):
+    """Complex Schur with Z: 25 n^3 complex operations = 100 n^3 real FLOPs."""
+    return 100.0 * float(np.sum(np.asarray(ns, dtype=np.float64) ** 3))
+
+
+__all__ = ["batch_sizes", "batched_real", "batched_cplx", "real_flops", "cplx_flops", "pack_batch"]

