@@ -278,3 +278,52 @@ __device__ inline double2 zreflector2(double2& a, double2& x1) {
   return tau;
 }
 }  // namespace gsk
+
+// ---- Newton-refined reciprocal and reciprocal square root ---------------------
+// Each FP64 instruction costs a full warp slot of the FP64 pipe on this part, so
+// the serial reflector math of the bulge chase is built from the hardware's
+// approximate seeds (rsqrt.approx / rcp.approx, ~23 correct bits) refined by two
+// Newton-Raphson steps each: y <- y + y (1 - s y^2) / 2 and r <- r + r (1 - d r),
+// which square the relative error per step (23 -> 46 -> past 53 bits).  Inputs are
+// kept inside [1e-290, 1e290] by the callers; extreme values take the scaled path.
+namespace gsk {
+__device__ __forceinline__ double rsqrt_nr(double s) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(s));
+  double h = s * y;
+  double e = fma(-h, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  h = s * y;
+  e = fma(-h, y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+__device__ __forceinline__ double rcp_nr(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
+// Real reflector of length 2 or 3 (householder.jl:12-54) in ~20 FP64 instructions:
+// with s = ||(a, x1, x2)||, beta = -sign(a) s, tau = (beta - a)/beta = 1 + |a|/s and
+// 1/(a - beta) = sign(a)/(|a| + s).  Falls back to reflector_small outside the safe
+// range.  Returns tau; (a, x1, x2) <- (beta, v1, v2).
+__device__ __forceinline__ double reflector_fast(double& a, double& x1, double& x2, int nr) {
+  if (nr < 3) x2 = 0.0;
+  const double xs = fma(x1, x1, x2 * x2);
+  if (xs == 0.0) return 0.0;
+  const double ss = fma(a, a, xs);
+  if (!(ss > 1.0e-290 && ss < 1.0e290)) return reflector_small(a, x1, x2, nr);
+  const double y = rsqrt_nr(ss);
+  const double s = ss * y;
+  const double aa = fabs(a);
+  const double tau = fma(aa, y, 1.0);
+  const double t = copysign(rcp_nr(aa + s), a);
+  x1 *= t;
+  x2 *= t;
+  a = -copysign(s, a);
+  return tau;
+}
+}  // namespace gsk

@@ -244,7 +244,7 @@ __device__ void eigvecs_one(const EigBatch& eb, int b, double2* smem) {
   const int ldt = n;  // unused by the packed accessor
   double2* T = smem;                                  // packed upper triangle, n(n+1)/2
   double* tn = (double*)(T + (size_t)n * (n + 1) / 2); // tnorms, n
-  double* red = tn + n;                               // 32
+  double* red = tn + ((n + 1) & ~1);                  // 32 (tn padded to an even count so Xs is 16-byte aligned)
   double2* Xs = (double2*)(red + 32);
   const bool xsmem = (n <= kEigSmem);
   double2* X = xsmem ? Xs : eb.scratch + off;         // X[i, ki] at (i-1)*ldx + ki-1
@@ -375,9 +375,16 @@ __global__ void __launch_bounds__(NT) k_eigvecs(EigBatch eb) {
 
 }  // namespace
 
+// Shared memory for orders up to nmax: packed T, tnorms (padded to an even count),
+// reduction scratch and, for orders <= kEigSmem, the solution block X.
 size_t eigvecs_smem_bytes(int nmax) {
-  const size_t x = nmax <= kEigSmem ? (size_t)nmax * nmax : 0;
-  return sizeof(double2) * ((size_t)nmax * (nmax + 1) / 2 + x) + sizeof(double) * (nmax + 32) + 64;
+  size_t need = 0;
+  for (int n = 1; n <= nmax; ++n) {
+    const size_t x = n <= kEigSmem ? (size_t)n * n : 0;
+    const size_t b = sizeof(double2) * ((size_t)n * (n + 1) / 2 + x) + sizeof(double) * (((n + 1) & ~1) + 32);
+    if (b > need) need = b;
+  }
+  return need + 64;
 }
 
 cudaError_t launch_eigvecs_batched(const EigBatch& eb, int nmax, int num_sms, cudaStream_t s) {

@@ -81,6 +81,19 @@ struct TriBatch {
 };
 cudaError_t launch_triangularize(const TriBatch& tb, int num_sms, cudaStream_t s);
 
+// Eigenvalue adjoint: grad = Y diag(gbar / conj(diag(Y^H X))) X^H per matrix.
+struct AdjBatch {
+  int count;
+  const int* ns;
+  const long long* offs;   // offsets of VR, VL, grad (complex elements)
+  const long long* woffs;  // offsets of gbar
+  const double2* VR;
+  const double2* VL;
+  const double2* gbar;
+  double2* grad;
+};
+cudaError_t launch_eig_adjoint(const AdjBatch& ab, int nmax, int num_sms, cudaStream_t s);
+
 // Size bins of the persistent batched kernels.  `sched` holds, per bin, the
 // [start, end) range of that bin inside the sorted work order and a queue ticket
 // counter: sched[3*bin + {0,1,2}].

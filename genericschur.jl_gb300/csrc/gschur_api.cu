@@ -772,4 +772,87 @@ int gs_triangularize_f64(gs_context* ctx, int64_t n, const double* T, const doub
   return GS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// eigenvalue adjoint
+// ---------------------------------------------------------------------------
+int gs_eig_adjoint_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                               const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
+                               const double* Z, const double* gbar, double* grad, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (count < 0 || packed_len < 0 || w_len < 0) return set_err(ctx, GS_BADARG, "negative size");
+  if (count == 0) return GS_OK;
+  if (!ns || !offs || !woffs || !T || !Z || !gbar || !grad) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  if (!dev) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int n = ns[b];
+      if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
+      if (offs[b] < 0 || offs[b] + (long long)n * n > packed_len) return set_err(ctx, GS_BADARG, "matrix %lld outside the packed buffer", (long long)b);
+      if (woffs[b] < 0 || woffs[b] + n > w_len) return set_err(ctx, GS_BADARG, "matrix %lld: eigenvalue offset outside w_len", (long long)b);
+    }
+  }
+  Arena ar;
+  const size_t o_X = ar.take<double2>(packed_len), o_VR = ar.take<double2>(packed_len), o_VL = ar.take<double2>(packed_len);
+  size_t o_T = 0, o_Z = 0, o_g = 0, o_G = 0, o_ns = 0, o_offs = 0, o_woffs = 0;
+  if (!dev) {
+    o_T = ar.take<double2>(packed_len);
+    o_Z = ar.take<double2>(packed_len);
+    o_g = ar.take<double2>(w_len);
+    o_G = ar.take<double2>(packed_len);
+    o_ns = ar.take<int>(count);
+    o_offs = ar.take<long long>(count);
+    o_woffs = ar.take<long long>(count);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const int* d_ns = ns;
+  const long long* d_offs = (const long long*)offs;
+  const long long* d_woffs = (const long long*)woffs;
+  const double2* d_T = (const double2*)T;
+  const double2* d_Z = (const double2*)Z;
+  const double2* d_g = (const double2*)gbar;
+  double2* d_G = (double2*)grad;
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_T, T, sizeof(double2) * packed_len, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_Z, Z, sizeof(double2) * packed_len, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_g, gbar, sizeof(double2) * w_len, cudaMemcpyHostToDevice, s));
+    d_ns = (const int*)(base + o_ns);
+    d_offs = (const long long*)(base + o_offs);
+    d_woffs = (const long long*)(base + o_woffs);
+    d_T = (const double2*)(base + o_T);
+    d_Z = (const double2*)(base + o_Z);
+    d_g = (const double2*)(base + o_g);
+    d_G = (double2*)(base + o_G);
+  }
+  CK(cudaEventRecord(ctx->t0, s));
+  double2* VR = (double2*)(base + o_VR);
+  double2* VL = (double2*)(base + o_VL);
+  rc = run_eigvecs(ctx, (int)count, d_ns, d_offs, d_T, d_Z, VR, VL, (double2*)(base + o_X), nullptr, nullptr, false);
+  if (rc) return rc;
+  AdjBatch ab{};
+  ab.count = (int)count;
+  ab.ns = d_ns;
+  ab.offs = d_offs;
+  ab.woffs = d_woffs;
+  ab.VR = VR;
+  ab.VL = VL;
+  ab.gbar = d_g;
+  ab.grad = d_G;
+  cudaError_t e = launch_eig_adjoint(ab, kSmallMax, ctx->num_sms, s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "adjoint launch: %s", cudaGetErrorString(e));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  if (dev) return GS_OK;
+  CK(cudaMemcpyAsync(grad, d_G, sizeof(double2) * packed_len, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
 }  // extern "C"

@@ -2,89 +2,60 @@
 //
 // Each CTA pulls matrix indices from its size bin's work queue (a ticket counter
 // in global memory) and runs, for one matrix:
-//   1. load + _scale! (util.jl:14-29), the matrix held in shared memory with an
-//      odd leading dimension so that row and column sweeps are bank-conflict free;
-//   2. Householder Hessenberg reduction (hessenberg.jl:3-17), reflector math as in
-//      householder.jl:12-54, lmul!/rmul! as householder.jl:140-172;
+//   1. load + _scale! (util.jl:14-29);
+//   2. Householder Hessenberg reduction (hessenberg.jl:3-17; reflector as in
+//      householder.jl:12-54, lmul!/rmul! as householder.jl:140-172), in shared
+//      memory for the small bins and in the L2-resident output buffer for the
+//      large ones;
 //   3. Q formation (hessenberg.jl:150-166) straight into the Z output, each thread
 //      owning whole rows of Z so that Z never needs a barrier;
 //   4. the real double-shift Francis iteration of gschur!(H::Hessenberg{<:Real}, Z)
-//      (GenericSchur.jl:513-699) with doubleShiftQR! (837-952) and _gs2x2! (716-803).
-//      The deflation scan and the start-row search run one candidate per thread;
-//      the bulge chase updates H in shared memory; the sweep's reflectors are
-//      logged and applied to Z rows afterwards in one streaming pass;
+//      (GenericSchur.jl:513-699) with doubleShiftQR! (837-952) and _gs2x2!
+//      (716-803) on a packed copy of H in shared memory (column j keeps rows
+//      1..j+3: the Hessenberg part and the two rows of the 3x3 bulge), which lets
+//      three 128x128 matrices share one SM;
 //   5. T, eigenvalues and status written back, undoing the scaling.
+//
+// Bulge chase, one barrier per step: warp 0 owns the near-diagonal block of step k
+// (left update of columns k..k+2, right update of rows k..k+3) and then computes
+// the reflector of step k+1 from column k, while the other warps apply step k to
+// the far columns (k+3..n) and far rows (1..k-1).  The two sets are disjoint, and
+// everything step k+1 reads was written by one side or the other before the
+// barrier.  Each sweep's reflectors are logged and applied to the Z rows in one
+// streaming pass afterwards (every thread owns rows of Z).
 #include "device_common.cuh"
 #include "gs_internal.h"
 
 namespace gsk {
 namespace {
 
+struct Refl {
+  double t1, t2, t3, v2, v3;
+};
+
 struct Ctl {
-  double v[3];          // start vector of the sweep
-  double t1, t2, t3, v2, v3;  // current reflector
-  double s[4];          // shifts r1r, r1i, r2r, r2i
-  double g[2];          // Givens cs, sn of a 2x2 deflation
+  double v[3];   // start vector of the sweep
+  Refl r[2];     // reflector of the current step / the next step
+  double s[4];   // shifts r1r, r1i, r2r, r2i
+  double g[2];   // Givens cs, sn of a 2x2 deflation
+  double blk[4]; // standardised 2x2 block
   int split;
   int mx;
 };
 
-// 1-based accessor into the shared copy of H.
-#define HH(i, j) H[((i) - 1) + ((j) - 1) * ldh]
+// Packed QR layout: column j (1-based) holds rows 1..j+3.
+__host__ __device__ __forceinline__ int rpk(int j) { return ((j - 1) * (j + 6)) >> 1; }
+
+#define AA(i, j) A[((i) - 1) + ((j) - 1) * lda]
+#define HH(i, j) H[rpk(j) + (i) - 1]
 
 template <int NT>
-__device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
+__device__ void hessenberg_real(int n, double* A, int lda, double* tau, double* red) {
   const int tid = threadIdx.x;
-  const int n = bt.ns[b];
-  if (n <= 0) {
-    if (tid == 0) bt.status[b] = ST_OK;
-    return;
-  }
-  const int ldh = n | 1;
-  double* H = smem;
-  double* tau = H + n * ldh;  // n-1 reflector scalars
-  double* lg = tau + n;       // 5 per chase step: t1, t2, t3, v2, v3
-  double* red = lg + 5 * n;   // reduction scratch (32)
-  double* __restrict__ Ag = bt.A + bt.offs[b];
-  double* __restrict__ Zg = bt.wantz ? bt.Z + bt.offs[b] : nullptr;
-  double* __restrict__ wr = bt.wr + bt.woffs[b];
-  double* __restrict__ wi = bt.wi + bt.woffs[b];
-
-  // ---- 1. load and scale --------------------------------------------------
-  double amax = 0.0;
-  for (int idx = tid; idx < n * n; idx += NT) {
-    const int i = idx % n, j = idx / n;
-    const double a = Ag[idx];
-    H[i + j * ldh] = a;
-    const double aa = fabs(a);
-    amax = (aa > amax || aa != aa) ? aa : amax;
-  }
-  amax = block_max<NT>(amax, red);
-  __syncthreads();
-  const double smlnum = sqrt(kSafemin) / kEps;
-  const double bignum = 1.0 / smlnum;
-  bool scaled = false;
-  double cscale = 1.0;
-  if (bt.scale) {
-    if (amax > 0.0 && amax < smlnum) { scaled = true; cscale = smlnum; }
-    else if (amax > bignum) { scaled = true; cscale = bignum; }
-  }
-  if (scaled) {
-    double mul[8];
-    const int nf = safescale_factors(amax, cscale, mul);
-    for (int f = 0; f < nf; ++f)
-      for (int idx = tid; idx < n * n; idx += NT) {
-        const int i = idx % n, j = idx / n;
-        H[i + j * ldh] *= mul[f];
-      }
-    __syncthreads();
-  }
-
-  // ---- 2. Hessenberg reduction ------------------------------------------------
   const double sfmin = 2.0 * kFmin / kEps;
   for (int i = 1; i <= n - 2; ++i) {
-    const int m = n - i;                 // reflector length: rows i+1..n
-    double* col = &HH(i + 1, i);         // col[0] = alpha, col[1..m-1] = x
+    const int m = n - i;          // reflector length: rows i+1..n
+    double* col = &AA(i + 1, i);  // col[0] = alpha, col[1..m-1] = x
     double lmax = 0.0;
     for (int r = 1 + tid; r < m; r += NT) lmax = fmax(lmax, fabs(col[r]));
     const double big = block_max<NT>(lmax, red);
@@ -133,7 +104,7 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
     if (tau_i == 0.0) continue;
     // lmul!(H', A[i+1:n, i+1:n]): one column per thread
     for (int j = i + 1 + tid; j <= n; j += NT) {
-      double* hj = &HH(i + 1, j);
+      double* hj = &AA(i + 1, j);
       double va0 = hj[0], va1 = 0.0;
       int r = 1;
       for (; r + 1 < m; r += 2) { va0 = fma(col[r], hj[r], va0); va1 = fma(col[r + 1], hj[r + 1], va1); }
@@ -145,27 +116,129 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
     __syncthreads();
     // rmul!(A[:, i+1:n], H): one row per thread
     for (int r = tid; r < n; r += NT) {
-      double* hr = &H[r + i * ldh];  // row r+1, column i+1
+      double* hr = &A[r + i * lda];  // row r+1, column i+1
       double x0 = hr[0], x1 = 0.0;
       int q = 1;
-      for (; q + 1 < m; q += 2) { x0 = fma(hr[q * ldh], col[q], x0); x1 = fma(hr[(q + 1) * ldh], col[q + 1], x1); }
-      if (q < m) x0 = fma(hr[q * ldh], col[q], x0);
+      for (; q + 1 < m; q += 2) { x0 = fma(hr[q * lda], col[q], x0); x1 = fma(hr[(q + 1) * lda], col[q + 1], x1); }
+      if (q < m) x0 = fma(hr[q * lda], col[q], x0);
       const double x = (x0 + x1) * tau_i;
       hr[0] -= x;
-      for (q = 1; q < m; ++q) hr[q * ldh] = fma(-x, col[q], hr[q * ldh]);
+      for (q = 1; q < m; ++q) hr[q * lda] = fma(-x, col[q], hr[q * lda]);
     }
     __syncthreads();
   }
+}
+
+// Apply reflector r (order 3) from the left to column j, rows k..k+2 of packed H.
+__device__ __forceinline__ void left3(double* H, int k, int j, const Refl& r) {
+  double* h = &HH(k, j);
+  const double ss = fma(r.v3, h[2], fma(r.v2, h[1], h[0]));
+  h[0] = fma(-ss, r.t1, h[0]);
+  h[1] = fma(-ss, r.t2, h[1]);
+  h[2] = fma(-ss, r.t3, h[2]);
+}
+// ... from the right to row i, columns k..k+2.
+__device__ __forceinline__ void right3(double* H, int k, int i, const Refl& r) {
+  double& h0 = HH(i, k);
+  double& h1 = HH(i, k + 1);
+  double& h2 = HH(i, k + 2);
+  const double ss = fma(r.v3, h2, fma(r.v2, h1, h0));
+  h0 = fma(-ss, r.t1, h0);
+  h1 = fma(-ss, r.t2, h1);
+  h2 = fma(-ss, r.t3, h2);
+}
+__device__ __forceinline__ void left2(double* H, int k, int j, const Refl& r) {
+  double* h = &HH(k, j);
+  const double ss = fma(r.v2, h[1], h[0]);
+  h[0] = fma(-ss, r.t1, h[0]);
+  h[1] = fma(-ss, r.t2, h[1]);
+}
+__device__ __forceinline__ void right2(double* H, int k, int i, const Refl& r) {
+  double& h0 = HH(i, k);
+  double& h1 = HH(i, k + 1);
+  const double ss = fma(r.v2, h1, h0);
+  h0 = fma(-ss, r.t1, h0);
+  h1 = fma(-ss, r.t2, h1);
+}
+
+// Reflector of chase step k (> mx) from column k-1, writing beta and the zeros
+// back into H (GenericSchur.jl:882-895); logged for the Z pass.
+__device__ __forceinline__ void make_refl(double* H, int k, int iend, Refl& out, double* lg) {
+  const int nr = min(3, iend - k + 1);
+  double a = HH(k, k - 1), x1 = HH(k + 1, k - 1), x2 = (nr == 3) ? HH(k + 2, k - 1) : 0.0;
+  const double t1 = reflector_fast(a, x1, x2, nr);
+  HH(k, k - 1) = a;
+  HH(k + 1, k - 1) = 0.0;
+  if (k < iend - 1) HH(k + 2, k - 1) = 0.0;
+  out.t1 = t1; out.v2 = x1; out.v3 = x2; out.t2 = t1 * x1; out.t3 = t1 * x2;
+  double* l = lg + 5 * (k - 1);
+  l[0] = t1; l[1] = out.t2; l[2] = out.t3; l[3] = x1; l[4] = x2;
+}
+
+template <int NT, bool HSMEM>
+__device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int n = bt.ns[b];
+  if (n <= 0) {
+    if (tid == 0) bt.status[b] = ST_OK;
+    return;
+  }
+  double* __restrict__ Ag = bt.A + bt.offs[b];
+  double* __restrict__ Zg = bt.wantz ? bt.Z + bt.offs[b] : nullptr;
+  double* __restrict__ wr = bt.wr + bt.woffs[b];
+  double* __restrict__ wi = bt.wi + bt.woffs[b];
+  const int lda = HSMEM ? (n | 1) : n;
+  const int hsz = HSMEM ? n * lda : rpk(n + 1);  // full (Hessenberg phase) or packed (QR phase)
+  const int hreg = max(hsz, rpk(n + 1));
+  double* H = smem;                 // packed H of the QR phase (and the full matrix before it, HSMEM)
+  double* tau = H + hreg;           // n-1 reflector scalars
+  double* lg = tau + n;             // 5 per chase step: t1, t2, t3, v2, v3
+  double* red = lg + 5 * n;         // reduction scratch (32)
+  double* A = HSMEM ? smem : Ag;    // where the Hessenberg reduction runs
+
+  // ---- 1. load and scale --------------------------------------------------
+  double amax = 0.0;
+  for (int idx = tid; idx < n * n; idx += NT) {
+    const int i = idx % n, j = idx / n;
+    const double a = Ag[idx];
+    if (HSMEM) A[i + j * lda] = a;
+    const double aa = fabs(a);
+    amax = (aa > amax || aa != aa) ? aa : amax;
+  }
+  amax = block_max<NT>(amax, red);
+  __syncthreads();
+  const double smlnum = sqrt(kSafemin) / kEps;
+  const double bignum = 1.0 / smlnum;
+  bool scaled = false;
+  double cscale = 1.0;
+  if (bt.scale) {
+    if (amax > 0.0 && amax < smlnum) { scaled = true; cscale = smlnum; }
+    else if (amax > bignum) { scaled = true; cscale = bignum; }
+  }
+  if (scaled) {
+    double mul[8];
+    const int nf = safescale_factors(amax, cscale, mul);
+    for (int f = 0; f < nf; ++f)
+      for (int idx = tid; idx < n * n; idx += NT) {
+        const int i = idx % n, j = idx / n;
+        A[i + j * lda] *= mul[f];
+      }
+    __syncthreads();
+  }
+
+  // ---- 2. Hessenberg reduction ------------------------------------------------
+  hessenberg_real<NT>(n, A, lda, tau, red);
 
   // ---- 3. Q formation into Z (row-owner threads, no barriers) ------------------
   if (Zg) {
     for (int r = tid; r < n; r += NT)
-      for (int j = 0; j < n; ++j) Zg[r + j * n] = (r == j) ? 1.0 : 0.0;
+      for (int j = 0; j < n; ++j) Zg[r + (long long)j * n] = (r == j) ? 1.0 : 0.0;
     for (int i = 1; i <= n - 2; ++i) {
       const double t = tau[i - 1];
       if (t == 0.0) continue;
       const int m = n - i;
-      const double* col = &HH(i + 1, i);
+      const double* col = &AA(i + 1, i);
       for (int r = tid; r < n; r += NT) {
         double* zr = Zg + r + (long long)i * n;  // Z[r+1, i+1]
         double s0 = zr[0], s1 = 0.0;
@@ -180,12 +253,21 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
   }
   __syncthreads();
 
-  // ---- 4. Francis double-shift QR ------------------------------------------------
-  for (int idx = tid; idx < n * n; idx += NT) {
-    const int i = idx % n, j = idx / n;
-    if (i > j + 1) H[i + j * ldh] = 0.0;  // triu!(HH, -1)
+  // ---- 4. pack H (Hessenberg part + bulge rows) into shared memory ----------------
+  if (HSMEM) {
+    // the full matrix occupies the same shared memory: route through the output buffer
+    for (int idx = tid; idx < n * n; idx += NT) {
+      const int i = idx % n, j = idx / n;
+      Ag[idx] = A[i + j * lda];
+    }
+    __syncthreads();
   }
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1 + tid; i <= j + 3; i += NT)
+      HH(i, j) = (i <= min(j + 1, n)) ? Ag[(i - 1) + (long long)(j - 1) * n] : 0.0;
   __syncthreads();
+
+  // ---- 5. Francis double-shift QR on packed H ------------------------------------------
   const double eps = kEps;
   const double smallnum = kFmin * ((double)n / eps);
   const long long maxiter = bt.maxiter_abs > 0 ? bt.maxiter_abs : (long long)bt.maxiter_mult * n;
@@ -285,6 +367,7 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
       }
       __syncthreads();
       const int mx = c.mx;
+      // reflector of the first step from the start vector
       if (tid == 0) {
         const double r1r = c.s[0], r1i = c.s[1], r2r = c.s[2], r2i = c.s[3];
         const int m = mx;
@@ -295,66 +378,43 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
         double v1 = h21s * (HH(m, m) + HH(m + 1, m + 1) - r1r - r2r);
         double v2 = h21s * HH(m + 2, m + 1);
         s = fabs(v0) + fabs(v1) + fabs(v2);
-        c.v[0] = v0 / s; c.v[1] = v1 / s; c.v[2] = v2 / s;
+        v0 /= s; v1 /= s; v2 /= s;
+        const int nr = min(3, iend - mx + 1);
+        const double t1 = reflector_fast(v0, v1, v2, nr);
+        if (mx > istart) HH(mx, mx - 1) *= (1.0 - t1);
+        Refl& r = c.r[0];
+        r.t1 = t1; r.v2 = v1; r.v3 = v2; r.t2 = t1 * v1; r.t3 = t1 * v2;
+        double* l = lg + 5 * (mx - 1);
+        l[0] = t1; l[1] = r.t2; l[2] = r.t3; l[3] = v1; l[4] = v2;
       }
-      // bulge chase (GenericSchur.jl:877-949)
-      for (int k = mx; k <= iend - 1; ++k) {
-        const int nr = min(3, iend - k + 1);
-        __syncthreads();
-        if (tid == 0) {
-          double a, x1, x2 = 0.0;
-          if (k > mx) {
-            a = HH(k, k - 1); x1 = HH(k + 1, k - 1);
-            if (nr == 3) x2 = HH(k + 2, k - 1);
-          } else {
-            a = c.v[0]; x1 = c.v[1]; x2 = (nr == 3) ? c.v[2] : 0.0;
-          }
-          const double t1 = reflector_small(a, x1, x2, nr);
-          if (k > mx) {
-            HH(k, k - 1) = a;
-            HH(k + 1, k - 1) = 0.0;
-            if (k < iend - 1) HH(k + 2, k - 1) = 0.0;
-          } else if (mx > istart) {
-            HH(k, k - 1) *= (1.0 - t1);
-          }
-          c.t1 = t1; c.v2 = x1; c.v3 = x2; c.t2 = t1 * x1; c.t3 = t1 * x2;
-          double* l = lg + 5 * (k - 1);
-          l[0] = t1; l[1] = t1 * x1; l[2] = t1 * x2; l[3] = x1; l[4] = x2;
-        }
-        __syncthreads();
-        const double t1 = c.t1, t2 = c.t2, t3 = c.t3, v2 = c.v2, v3 = c.v3;
-        if (nr == 3) {
-          for (int j = k + tid; j <= n; j += NT) {
-            double* hj = &HH(k, j);
-            const double ss = fma(v3, hj[2], fma(v2, hj[1], hj[0]));
-            hj[0] = fma(-ss, t1, hj[0]);
-            hj[1] = fma(-ss, t2, hj[1]);
-            hj[2] = fma(-ss, t3, hj[2]);
-          }
-          __syncthreads();
-          const int rl = min(k + 3, iend);
-          for (int r = 1 + tid; r <= rl; r += NT) {
-            double* hr = &HH(r, k);
-            const double ss = fma(v3, hr[2 * ldh], fma(v2, hr[ldh], hr[0]));
-            hr[0] = fma(-ss, t1, hr[0]);
-            hr[ldh] = fma(-ss, t2, hr[ldh]);
-            hr[2 * ldh] = fma(-ss, t3, hr[2 * ldh]);
-          }
+      __syncthreads();
+      // bulge chase (GenericSchur.jl:877-949), steps with a 3-element reflector
+      int cur = 0;
+      for (int k = mx; k <= iend - 2; ++k) {
+        const Refl r = c.r[cur];
+        if (warp == 0) {
+          // near block: left on columns k..k+2, then right on rows k..min(k+3, iend)
+          if (lane < 3) left3(H, k, k + lane, r);
+          __syncwarp();
+          if (lane < 4 && k + lane <= iend) right3(H, k, k + lane, r);
+          __syncwarp();
+          if (lane == 0) make_refl(H, k + 1, iend, c.r[cur ^ 1], lg);
         } else {
-          for (int j = k + tid; j <= n; j += NT) {
-            double* hj = &HH(k, j);
-            const double ss = fma(v2, hj[1], hj[0]);
-            hj[0] = fma(-ss, t1, hj[0]);
-            hj[1] = fma(-ss, t2, hj[1]);
-          }
-          __syncthreads();
-          for (int r = 1 + tid; r <= iend; r += NT) {
-            double* hr = &HH(r, k);
-            const double ss = fma(v2, hr[ldh], hr[0]);
-            hr[0] = fma(-ss, t1, hr[0]);
-            hr[ldh] = fma(-ss, t2, hr[ldh]);
-          }
+          const int ft = tid - 32;
+          constexpr int NF = NT - 32;
+          for (int j = k + 3 + ft; j <= n; j += NF) left3(H, k, j, r);
+          for (int i = 1 + ft; i <= k - 1; i += NF) right3(H, k, i, r);
         }
+        __syncthreads();
+        cur ^= 1;
+      }
+      // last step: 2-element reflector at k = iend-1 (left on columns k..n, right on rows 1..iend)
+      {
+        const int k = iend - 1;
+        const Refl r = c.r[cur];
+        for (int j = k + tid; j <= n; j += NT) left2(H, k, j, r);
+        __syncthreads();
+        for (int i = 1 + tid; i <= iend; i += NT) right2(H, k, i, r);
       }
       __syncthreads();
       // apply the sweep's reflectors to the Z rows each thread owns
@@ -390,7 +450,7 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
         gs2x2(a, bq, cc, d, cs, sn, w1r, w1i, w2r, w2i);
         wr[q - 1] = w2r; wi[q - 1] = w2i; wr[p - 1] = w1r; wi[p - 1] = w1i;
         c.g[0] = cs; c.g[1] = sn;
-        c.v[0] = a; c.v[1] = bq; c.v[2] = cc; c.s[0] = d;
+        c.blk[0] = a; c.blk[1] = bq; c.blk[2] = cc; c.blk[3] = d;
       }
       __syncthreads();
       const double cs = c.g[0], sn = c.g[1];
@@ -412,7 +472,7 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
           zp[n] = -sn * a1 + cs * a2;
         }
       if (tid == 0) {
-        HH(p, p) = c.v[0]; HH(p, q) = c.v[1]; HH(q, p) = c.v[2]; HH(q, q) = c.s[0];
+        HH(p, p) = c.blk[0]; HH(p, q) = c.blk[1]; HH(q, p) = c.blk[2]; HH(q, q) = c.blk[3];
         if (iend > 2) HH(iend - 1, iend - 2) = 0.0;
       }
     }
@@ -421,13 +481,13 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
   }
   __syncthreads();
 
-  // ---- 5. write back -----------------------------------------------------------
+  // ---- 6. write back -----------------------------------------------------------
   double mul[8];
   int nf = 0;
   if (scaled) nf = safescale_factors(cscale, amax, mul);
   for (int idx = tid; idx < n * n; idx += NT) {
     const int i = idx % n, j = idx / n;
-    double v = (i > j + 1) ? 0.0 : H[i + j * ldh];
+    double v = (i > j + 1) ? 0.0 : HH(i + 1, j + 1);
     for (int f = 0; f < nf; ++f) v *= mul[f];
     Ag[idx] = v;
   }
@@ -440,9 +500,10 @@ __device__ void solve_real(const RealBatch& bt, int b, double* smem, Ctl& c) {
   if (tid == 0) bt.status[b] = status;
   __syncthreads();
 }
+#undef AA
 #undef HH
 
-template <int NT>
+template <int NT, bool HSMEM>
 __global__ void __launch_bounds__(NT) k_schur_real(RealBatch bt, const int* __restrict__ order,
                                                    int* __restrict__ sched, int bin) {
   extern __shared__ double smem[];
@@ -455,23 +516,23 @@ __global__ void __launch_bounds__(NT) k_schur_real(RealBatch bt, const int* __re
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_real<NT>(bt, order[job], smem, c);
+    solve_real<NT, HSMEM>(bt, order[job], smem, c);
   }
 }
 
-template <int NT>
-cudaError_t launch_bin(const RealBatch& bt, const int* order, int* sched, int bin, int num_sms,
-                       cudaStream_t s) {
+template <int NT, bool HSMEM>
+cudaError_t launch_bin(const RealBatch& bt, const int* order, int* sched, int bin, int num_sms, cudaStream_t s) {
   const int nmax = bin_max(bin);
-  const size_t smem = sizeof(double) * ((size_t)nmax * (nmax | 1) + 6 * nmax + 32);
-  cudaError_t e = cudaFuncSetAttribute(k_schur_real<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t full = HSMEM ? (size_t)nmax * (nmax | 1) : 0;
+  const size_t hreg = full > (size_t)rpk(nmax + 1) ? full : (size_t)rpk(nmax + 1);
+  const size_t smem = sizeof(double) * (hreg + 6 * nmax + 32);
+  cudaError_t e = cudaFuncSetAttribute(k_schur_real<NT, HSMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_real<NT>, NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_real<NT, HSMEM>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  const int grid = num_sms * per_sm;
-  k_schur_real<NT><<<grid, NT, smem, s>>>(bt, order, sched, bin);
+  k_schur_real<NT, HSMEM><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin);
   return cudaGetLastError();
 }
 
@@ -481,10 +542,10 @@ cudaError_t launch_schur_batched_real(const RealBatch& bt, const int* order, int
                                       cudaStream_t* streams, int nstreams) {
   cudaError_t e;
   // largest bin first: it carries most of the work
-  if ((e = launch_bin<128>(bt, order, sched, 3, num_sms, streams[0 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<128>(bt, order, sched, 2, num_sms, streams[1 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<64>(bt, order, sched, 1, num_sms, streams[2 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<32>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
+  if ((e = launch_bin<128, false>(bt, order, sched, 3, num_sms, streams[0 % nstreams])) != cudaSuccess) return e;
+  if ((e = launch_bin<128, false>(bt, order, sched, 2, num_sms, streams[1 % nstreams])) != cudaSuccess) return e;
+  if ((e = launch_bin<64, true>(bt, order, sched, 1, num_sms, streams[2 % nstreams])) != cudaSuccess) return e;
+  if ((e = launch_bin<64, true>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

@@ -12,6 +12,7 @@ underscore):
   triangularize(S)              triang.jl:9-43
   gschur_batched(...)           batched form, no reference counterpart
   geigvecs_batched(...)         batched eigenvectors, no reference counterpart
+  eig_adjoint_batched(...)      eigenvalue adjoint (reverse-mode rule), no reference counterpart
 
 Matrices are numpy arrays; they are handed to the C-ABI column-major (Julia's
 layout).  All arithmetic runs in the CUDA library; nothing here computes a
@@ -27,6 +28,7 @@ from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS
 
 __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_",
            "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
+           "eig_adjoint_batched",
            "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
@@ -295,3 +297,25 @@ def geigvecs_batched(T_packed, Z_packed, ns, offs, woffs=None, left=False, norma
     if rc != GS_OK:
         _raise(rc, ctx, "geigvecs_batched")
     return V
+
+
+def eig_adjoint_batched(T_packed, Z_packed, ns, offs, woffs, gbar, ctx=None):
+    """Reverse-mode rule of A -> eigenvalues(A) for a packed batch of complex Schur
+    pairs: returns grad = dL/dRe(A) + i dL/dIm(A) (packed like T) given the
+    cotangents gbar = dL/dRe(l) + i dL/dIm(l) of the eigenvalues, ordered like
+    S.values.  Eigenvectors are recomputed on the GPU from (T, Z)."""
+    ctx = ctx or get_context()
+    ns = np.ascontiguousarray(ns, dtype=np.int32)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    woffs = np.ascontiguousarray(woffs, dtype=np.int64)
+    T = np.ascontiguousarray(T_packed, dtype=np.complex128)
+    Z = np.ascontiguousarray(Z_packed, dtype=np.complex128)
+    g = np.ascontiguousarray(gbar, dtype=np.complex128)
+    count = len(ns)
+    G = np.zeros(len(T), dtype=np.complex128)
+    wlen = int((woffs + ns).max()) if count else 0
+    rc = ctx.lib.gs_eig_adjoint_batched_c64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), len(T), wlen,
+                                            _ptr(T), _ptr(Z), _ptr(g), _ptr(G), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "eig_adjoint_batched")
+    return G

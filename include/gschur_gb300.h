@@ -151,6 +151,20 @@ GS_API int gs_eigvecs_batched_f64(gs_context* ctx, int64_t count, const int32_t*
                                   const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
                                   const double* Z, double* VR, double* VL, unsigned flags);
 
+/* ---------------------------------------------------------------------------
+ * Eigenvalue adjoint (no reference counterpart; the reverse-mode rule of
+ * A -> eigenvalues(A) built on the reference's eigenvector definitions).
+ * Given complex Schur pairs (T, Z) of a batch of matrices A_b and cotangents
+ * gbar_i = dL/dRe(l_i) + i dL/dIm(l_i) for their eigenvalues (in the order of
+ * S.values = diag(T)), returns grad_b = dL/dRe(A_b) + i dL/dIm(A_b)
+ *   = sum_i gbar_i y_i x_i^H / conj(y_i^H x_i),
+ * with x_i, y_i the right / left eigenvectors recomputed on the device from (T, Z)
+ * (_geigvecs!, vectors.jl:45-131; _gleigvecs!, vectors.jl:372-460).  Layout as in
+ * gs_eigvecs_batched_c64; gbar and the eigenvalues use woffs / w_len. */
+GS_API int gs_eig_adjoint_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                      const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
+                                      const double* Z, const double* gbar, double* grad, unsigned flags);
+
 #ifdef __cplusplus
 }
 #endif
