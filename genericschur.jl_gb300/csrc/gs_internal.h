@@ -1,6 +1,8 @@
 // Internal declarations shared by the kernel translation units and the C-ABI.
 #pragma once
+#include <cmath>
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace gsk {
@@ -93,6 +95,70 @@ struct AdjBatch {
   double2* grad;
 };
 cudaError_t launch_eig_adjoint(const AdjBatch& ab, int nmax, int num_sms, cudaStream_t s);
+
+// Large-matrix path (n > kSmallMax).
+constexpr int kMaxBulges = 32;  // bulges per multishift chain (one lane each)
+constexpr int kFarTile = 32;    // rows/columns per CTA of the far-update kernel
+template <class T>
+struct ChaseArgs {
+  T* H;          // n x n, leading dimension n
+  T* Z;          // may be null
+  int n;
+  int ilo, ihi;  // active block (1-based)
+  int B;         // bulges in the chain
+  int t0, w;     // first sweep step of this chunk and number of steps
+  int wlo, whi;  // window (1-based, inclusive)
+  const T* shifts;  // 4 per bulge: r1r, r1i, r2r, r2i
+  int* logk;     // w*B positions (0 = inactive)
+  T* logr;       // w*B*5 reflector scalars (t1, t1*v2, t1*v3, v2, v3)
+};
+template <class T> cudaError_t launch_chase_chunk(const ChaseArgs<T>& ca, int num_sms, cudaStream_t s);
+template <class T> cudaError_t launch_deflation_scan(const T* H, int n, int ilo, int ihi, int* out, cudaStream_t s);
+template <class T>
+cudaError_t launch_gemm(int m, int p, int q, const T* A, int lda, int transA, const T* B, int ldb, T* C, int ldc,
+                        cudaStream_t s);
+size_t hess_large_ws_elems(int n);
+template <class T> cudaError_t hessenberg_large(int n, T* A, int lda, T* Z, int ldz, T* tau_out, T* ws, cudaStream_t s);
+
+// One large real Schur decomposition (schur_large_host.cu).
+template <class T>
+struct LargeRun {
+  T* A;            // in: A; out: T (device, n x n, ld n)
+  T* Z;            // out: Schur vectors, or null
+  double* wr;      // out: eigenvalues (device, n)
+  double* wi;
+  int n;
+  int scale;
+  long long maxiter;  // bound on multishift sweeps (<= 0: 100 n)
+  void* ws;        // workspace of schur_large_ws_bytes(n, sizeof(T)) bytes
+  int num_sms;
+  cudaStream_t stream;
+  cudaError_t cuda_error;
+};
+size_t schur_large_ws_bytes(int n, size_t tsize);
+template <class T> int schur_large_run(LargeRun<T>& r);  // ST_OK, ST_UNCONVERGED, or -1 (cuda_error set)
+
+// Host copy of the safescale! factor sequence (util.jl:41-80, as written there).
+inline std::vector<double> safescale_factors_host(double cfrom, double cto) {
+  const double smlnum = 2.2250738585072014e-308, bignum = 1.0 / smlnum;
+  std::vector<double> f;
+  double cfromc = cfrom, ctoc = cto;
+  bool done = false;
+  while (!done && f.size() < 8) {
+    const double cfrom1 = cfromc * smlnum;
+    double m;
+    if (cfrom1 == cfromc) { m = ctoc / cfromc; done = true; }
+    else {
+      const double cto1 = ctoc / bignum;
+      if (cto1 == ctoc) { m = cto; done = true; cfromc = 1.0; }
+      else if (std::fabs(cfrom1) > std::fabs(ctoc) && ctoc != 0.0) { m = smlnum; done = false; cfromc = 1.0; }
+      else if (std::fabs(cto1) > std::fabs(cfromc)) { m = bignum; done = false; cfromc = cfrom1; }
+      else { m = ctoc / cfromc; done = true; }
+    }
+    f.push_back(m);
+  }
+  return f;
+}
 
 // Size bins of the persistent batched kernels.  `sched` holds, per bin, the
 // [start, end) range of that bin inside the sorted work order and a queue ticket

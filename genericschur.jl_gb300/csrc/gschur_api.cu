@@ -306,6 +306,53 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
 }
 
 // ---------------------------------------------------------------------------
+// large real matrix (n > 128): whole-GPU Hessenberg + multishift QR
+// ---------------------------------------------------------------------------
+static int schur_large_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
+                           double* wi, unsigned flags, int64_t maxiter) {
+  if (n > (1 << 16)) return set_err(ctx, GS_BADARG, "order %lld too large", (long long)n);
+  const bool wantz = flags & GS_WANTZ;
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_A = ar.take<double>(nn), o_Z = ar.take<double>(wantz ? nn : 1);
+  const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n);
+  const size_t o_ws = ar.take<char>(schur_large_ws_bytes((int)n, sizeof(double)));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double* dA = (double*)(base + o_A);
+  CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
+  LargeRun<double> r{};
+  r.A = dA;
+  r.Z = wantz ? (double*)(base + o_Z) : nullptr;
+  r.wr = (double*)(base + o_wr);
+  r.wi = (double*)(base + o_wi);
+  r.n = (int)n;
+  r.scale = (flags & GS_SCALE) ? 1 : 0;
+  r.maxiter = maxiter > 0 ? maxiter : 0;
+  r.ws = base + o_ws;
+  r.num_sms = ctx->num_sms;
+  r.stream = s;
+  r.cuda_error = cudaSuccess;
+  CK(cudaEventRecord(ctx->t0, s));
+  const int st = schur_large_run<double>(r);
+  if (st < 0) return set_err(ctx, GS_CUDA, "large Schur path: %s", cudaGetErrorString(r.cuda_error));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
+  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(double), r.Z, n * sizeof(double), n * sizeof(double), n, out, s));
+  CK(cudaMemcpyAsync(wr, r.wr, n * sizeof(double), out, s));
+  CK(cudaMemcpyAsync(wi, r.wi, n * sizeof(double), out, s));
+  CK(cudaStreamSynchronize(s));
+  if (st != ST_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit reached");
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // single real matrix: n <= 128 runs as a batch of one
 // ---------------------------------------------------------------------------
 int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
@@ -318,8 +365,8 @@ int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
     return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
   if (n == 0) return GS_OK;
   if (!A || !wr || !wi || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
-  if (n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld > %d: large-matrix path not available", (long long)n, kSmallMax);
   CK(cudaSetDevice(ctx->device));
+  if (n > kSmallMax) return schur_large_f64(ctx, n, A, lda, Z, ldz, wr, wi, flags, maxiter);
   const bool dev = flags & GS_DEVICE;
   Arena ar;
   const size_t o_A = ar.take<double>(n * n), o_Z = ar.take<double>(n * n);
@@ -851,6 +898,44 @@ int gs_eig_adjoint_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns
   ctx->timed = true;
   if (dev) return GS_OK;
   CK(cudaMemcpyAsync(grad, d_G, sizeof(double2) * packed_len, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Hessenberg reduction (hessenberg!, pirates.jl:232 -> _hessenberg!, hessenberg.jl:3-17)
+// ---------------------------------------------------------------------------
+int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* tau, double* Q, int64_t ldq,
+                      unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
+  if (lda < std::max<int64_t>(n, 1) || (Q && ldq < std::max<int64_t>(n, 1)))
+    return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
+  if (n == 0) return GS_OK;
+  if (!A || (n > 1 && !tau)) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_A = ar.take<double>(nn), o_Q = ar.take<double>(Q ? nn : 1), o_tau = ar.take<double>(n);
+  const size_t o_ws = ar.take<double>(hess_large_ws_elems((int)n));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double* dA = (double*)(base + o_A);
+  double* dQ = Q ? (double*)(base + o_Q) : nullptr;
+  double* dtau = (double*)(base + o_tau);
+  CK(cudaMemsetAsync(dtau, 0, n * sizeof(double), s));
+  CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
+  cudaError_t e = hessenberg_large<double>((int)n, dA, (int)n, dQ, (int)n, dtau, (double*)(base + o_ws), s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "hessenberg: %s", cudaGetErrorString(e));
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
+  if (Q) CK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), dQ, n * sizeof(double), n * sizeof(double), n, out, s));
+  if (n > 1) CK(cudaMemcpyAsync(tau, dtau, (n - 1) * sizeof(double), out, s));
   CK(cudaStreamSynchronize(s));
   return GS_OK;
 }

@@ -1,0 +1,311 @@
+// Host driver of the large-matrix (n > 128) real Schur path, templated on the
+// working precision T (double: the plain FP64 path; float: the first stage of the
+// mixed-precision path).
+//
+//   1. _scale! (util.jl:14-29) with a device max-reduction;
+//   2. Hessenberg reduction with Z accumulated (hessenberg_large.cu);
+//   3. QR: repeatedly take the bottom unreduced block [ilo, ihi] (deflation scan
+//      with the criterion of GenericSchur.jl:563-600).  Blocks of order <= 128 are
+//      finished by the small-matrix kernel in FP64 (it returns T_blk and the
+//      block's orthogonal factor U; the standard-form 2x2 blocks and the eigenvalue
+//      order of the reference come from it), and U is applied to the rest of H and
+//      to Z with GEMMs.  Larger blocks get multishift sweeps (schur_large.cu) whose
+//      2B shifts are the eigenvalues of the trailing 2B x 2B block, again computed
+//      by the small-matrix kernel;
+//   4. T = triu(H, -1), scaling undone.
+// The host reads two small values per sweep (the split position and the shifts).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "device_common.cuh"
+#include "gs_internal.h"
+
+namespace gsk {
+namespace {
+
+template <class T>
+__global__ void k_absmax_bits(const T* __restrict__ A, size_t cnt, unsigned long long* out) {
+  double m = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x) {
+    const double a = fabs((double)A[i]);
+    m = (a > m || a != a) ? a : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (w > m || w != w) ? w : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+template <class T>
+__global__ void k_scale(T* A, size_t cnt, double mul) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
+    A[i] = (T)((double)A[i] * mul);
+}
+
+template <class T>
+__global__ void k_triu1(T* H, int n) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const int i = idx % n, j = idx / n;
+  if (i > j + 1) H[idx] = T(0);
+}
+
+// dst (m x p, ld m) <- src (m x p, ld lds), converting element type
+template <class S, class D>
+__global__ void k_copy2d(int m, int p, const S* __restrict__ src, int lds, D* __restrict__ dst, int ldd) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)m * p) return;
+  const int i = idx % m, j = idx / m;
+  dst[(size_t)j * ldd + i] = (D)src[(size_t)j * lds + i];
+}
+
+template <class S, class D>
+cudaError_t copy2d(int m, int p, const S* src, int lds, D* dst, int ldd, cudaStream_t s) {
+  if (m <= 0 || p <= 0) return cudaSuccess;
+  const size_t tot = (size_t)m * p;
+  k_copy2d<S, D><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(m, p, src, lds, dst, ldd);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Workspace needed by schur_large_run<T>, in bytes.
+size_t schur_large_ws_bytes(int n, size_t tsize) {
+  const size_t nb = kSmallMax;
+  size_t b = 0;
+  b += tsize * hess_large_ws_elems(n) + 256;
+  b += sizeof(int) * 64 * kMaxBulges + tsize * 64 * kMaxBulges * 5 + 512;  // chase log
+  b += tsize * 4 * kMaxBulges + 256;                                        // shifts
+  b += 3 * sizeof(double) * nb * nb + 4 * sizeof(double) * nb + 1024;       // small solve blk, U, wr, wi, meta
+  b += sizeof(int) * (nb + 3 * kNumBins + 8) + 256;                         // order/sched/status/scan
+  b += tsize * (size_t)n * nb * 2 + tsize * nb * nb + 512;                  // GEMM temporaries, U in T
+  return b + 16 * 256;
+}
+
+template <class T>
+int schur_large_run(LargeRun<T>& r) {
+  const int n = r.n;
+  cudaStream_t s = r.stream;
+  cudaError_t e;
+#define CKL(...)                     \
+  do {                               \
+    e = (__VA_ARGS__);               \
+    if (e != cudaSuccess) {          \
+      r.cuda_error = e;              \
+      return -1;                     \
+    }                                \
+  } while (0)
+  // ---- carve the workspace
+  char* p = (char*)r.ws;
+  auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~size_t(255); return (void*)q; };
+  T* hws = (T*)take(sizeof(T) * hess_large_ws_elems(n));
+  int* logk = (int*)take(sizeof(int) * 64 * kMaxBulges);
+  T* logr = (T*)take(sizeof(T) * 64 * kMaxBulges * 5);
+  T* dshift = (T*)take(sizeof(T) * 4 * kMaxBulges);
+  const int nb = kSmallMax;
+  double* blk = (double*)take(sizeof(double) * nb * nb);
+  double* U = (double*)take(sizeof(double) * nb * nb);
+  double* bwr = (double*)take(sizeof(double) * nb);
+  double* bwi = (double*)take(sizeof(double) * nb);
+  long long* meta = (long long*)take(sizeof(long long) * 4);
+  int* order = (int*)take(sizeof(int) * (nb + 8));
+  int* sched = (int*)take(sizeof(int) * (3 * kNumBins + 4));
+  int* bstat = (int*)take(sizeof(int) * 4);
+  int* dscan = (int*)take(sizeof(int) * 4);
+  T* tmp = (T*)take(sizeof(T) * (size_t)n * nb);
+  T* tmp2 = (T*)take(sizeof(T) * (size_t)n * nb);
+  T* Ut = (T*)take(sizeof(T) * nb * nb);
+  unsigned long long* dmax = (unsigned long long*)take(sizeof(unsigned long long) * 2);
+  T* H = r.A;
+  T* Z = r.Z;
+  const size_t nn = (size_t)n * n;
+
+  // ---- 1. scale
+  double amax = 0.0, cscale = 1.0;
+  bool scaled = false;
+  if (r.scale) {
+    CKL(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
+    k_absmax_bits<T><<<4 * r.num_sms, 256, 0, s>>>(H, nn, dmax);
+    unsigned long long bits = 0;
+    CKL(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CKL(cudaStreamSynchronize(s));
+    std::memcpy(&amax, &bits, sizeof(amax));
+    const double smlnum = std::sqrt(2.2250738585072014e-308) / 2.220446049250313e-16;
+    const double bignum = 1.0 / smlnum;
+    if (amax > 0.0 && amax < smlnum) { scaled = true; cscale = smlnum; }
+    else if (amax > bignum) { scaled = true; cscale = bignum; }
+    if (scaled) {
+      // factor sequence of safescale! (util.jl:41-80), applied in order
+      for (double m : safescale_factors_host(amax, cscale)) k_scale<T><<<4 * r.num_sms, 256, 0, s>>>(H, nn, m);
+    }
+  }
+
+  // ---- 2. Hessenberg (+ Z)
+  CKL(hessenberg_large<T>(n, H, n, Z, n, nullptr, hws, s));
+  k_triu1<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(H, n);
+  CKL(cudaGetLastError());
+
+  // ---- 3. QR
+  auto small_solve = [&](int lo, int hi, bool wantU, double* wr_out, double* wi_out) -> int {
+    const int m = hi - lo + 1;
+    CKL(copy2d<T, double>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk, m, s));
+    long long mh[4] = {0, 0, 0, 0};
+    int m32 = m;
+    CKL(cudaMemcpyAsync(meta, mh, sizeof(mh), cudaMemcpyHostToDevice, s));
+    CKL(cudaMemcpyAsync(meta + 2, &m32, sizeof(int), cudaMemcpyHostToDevice, s));
+    RealBatch bt{};
+    bt.count = 1;
+    bt.ns = (const int*)(meta + 2);
+    bt.offs = meta;
+    bt.woffs = meta + 1;
+    bt.A = blk;
+    bt.Z = wantU ? U : nullptr;
+    bt.wr = wr_out;
+    bt.wi = wi_out;
+    bt.status = bstat;
+    bt.wantz = wantU;
+    bt.scale = 0;
+    bt.maxiter_mult = 100;
+    CKL(launch_bin_sort(bt.ns, 1, order, sched, s));
+    CKL(launch_schur_batched_real(bt, order, sched, r.num_sms, &s, 1));
+    return 0;
+  };
+
+  const int NMIN = kSmallMax;
+  int ihi = n;
+  long long sweeps = 0, since_defl = 0;
+  const long long max_sweeps = r.maxiter > 0 ? r.maxiter : 100LL * n;
+  std::vector<T> hsh(4 * kMaxBulges);
+  while (ihi >= 1) {
+    // bottom unreduced block
+    int kmax = 0;
+    if (ihi > 1) {
+      CKL(cudaMemsetAsync(dscan, 0, sizeof(int), s));
+      CKL(launch_deflation_scan<T>(H, n, 1, ihi, dscan, s));
+      CKL(cudaMemcpyAsync(&kmax, dscan, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CKL(cudaStreamSynchronize(s));
+    }
+    const int ilo = kmax > 0 ? kmax : 1;
+    if (kmax > 0) CKL(cudaMemsetAsync(H + (size_t)(ilo - 2) * n + (ilo - 1), 0, sizeof(T), s));
+    const int m = ihi - ilo + 1;
+    if (m <= NMIN) {
+      // finish the block with the small-matrix kernel; eigenvalues straight into wr/wi
+      if (small_solve(ilo, ihi, true, r.wr + (ilo - 1), r.wi + (ilo - 1))) return -1;
+      CKL(copy2d<double, T>(m, m, blk, m, H + (size_t)(ilo - 1) * n + (ilo - 1), n, s));
+      CKL(copy2d<double, T>(m, m, U, m, Ut, m, s));
+      // H[lo:hi, hi+1:n] <- U^T H[lo:hi, hi+1:n]
+      const int nr = n - ihi;
+      if (nr > 0) {
+        CKL(copy2d<T, T>(m, nr, H + (size_t)ihi * n + (ilo - 1), n, tmp, m, s));
+        CKL(launch_gemm<T>(m, nr, m, Ut, m, 1, tmp, m, H + (size_t)ihi * n + (ilo - 1), n, s));
+      }
+      // H[1:lo-1, lo:hi] <- H[1:lo-1, lo:hi] U
+      if (ilo > 1) {
+        CKL(copy2d<T, T>(ilo - 1, m, H + (size_t)(ilo - 1) * n, n, tmp, ilo - 1, s));
+        CKL(launch_gemm<T>(ilo - 1, m, m, tmp, ilo - 1, 0, Ut, m, H + (size_t)(ilo - 1) * n, n, s));
+      }
+      // Z[:, lo:hi] <- Z[:, lo:hi] U
+      if (Z) {
+        CKL(copy2d<T, T>(n, m, Z + (size_t)(ilo - 1) * n, n, tmp, n, s));
+        CKL(launch_gemm<T>(n, m, m, tmp, n, 0, Ut, m, Z + (size_t)(ilo - 1) * n, n, s));
+      }
+      int st = 0;
+      CKL(cudaMemcpyAsync(&st, bstat, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CKL(cudaStreamSynchronize(s));
+      if (st != ST_OK) return ST_UNCONVERGED;
+      ihi = ilo - 1;
+      since_defl = 0;
+      continue;
+    }
+    if (++sweeps > max_sweeps) return ST_UNCONVERGED;
+    // shifts: eigenvalues of the trailing 2B x 2B block
+    const int B = std::min(kMaxBulges, std::max(1, (m - 8) / 6));
+    const int ns = 2 * B;
+    std::vector<double> ewr(ns), ewi(ns);
+    ++since_defl;
+    if (since_defl % 6 == 0) {
+      // exceptional shifts (GenericSchur.jl:614-627 pattern) from the bottom entries
+      std::vector<T> hd(3 * ns + 3);
+      for (int b = 0; b < B; ++b) {
+        const int k = ihi - 2 * b;
+        T hkk, s1, s2;
+        CKL(cudaMemcpyAsync(&hkk, H + (size_t)(k - 1) * n + (k - 1), sizeof(T), cudaMemcpyDeviceToHost, s));
+        CKL(cudaMemcpyAsync(&s1, H + (size_t)(k - 2) * n + (k - 1), sizeof(T), cudaMemcpyDeviceToHost, s));
+        CKL(cudaMemcpyAsync(&s2, H + (size_t)(k - 3) * n + (k - 2), sizeof(T), cudaMemcpyDeviceToHost, s));
+        CKL(cudaStreamSynchronize(s));
+        const double sv = std::fabs((double)s1) + std::fabs((double)s2);
+        const double h11 = 0.75 * sv + (double)hkk;
+        // eigenvalues of [h11, -7/16 sv; sv, h11]: h11 +- i sv sqrt(7/16)
+        ewr[2 * b] = h11; ewi[2 * b] = sv * std::sqrt(7.0 / 16.0);
+        ewr[2 * b + 1] = h11; ewi[2 * b + 1] = -ewi[2 * b];
+      }
+    } else {
+      if (small_solve(ihi - ns + 1, ihi, false, bwr, bwi)) return -1;
+      CKL(cudaMemcpyAsync(ewr.data(), bwr, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+      CKL(cudaMemcpyAsync(ewi.data(), bwi, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+      CKL(cudaStreamSynchronize(s));
+    }
+    // pair the shifts: conjugate pairs stay together, real shifts are paired in order
+    std::vector<std::complex<double>> cpx, rl;
+    for (int q = 0; q < ns; ++q) {
+      if (ewi[q] > 0.0 && q + 1 < ns) { cpx.push_back({ewr[q], ewi[q]}); cpx.push_back({ewr[q + 1], ewi[q + 1]}); ++q; }
+      else if (ewi[q] == 0.0) rl.push_back({ewr[q], 0.0});
+    }
+    std::vector<std::complex<double>> sh(cpx);
+    for (auto& x : rl) sh.push_back(x);
+    while ((int)sh.size() < ns) sh.push_back(sh.empty() ? std::complex<double>(0.0, 0.0) : sh.back());
+    for (int b = 0; b < B; ++b) {
+      hsh[4 * b + 0] = (T)sh[2 * b].real();
+      hsh[4 * b + 1] = (T)sh[2 * b].imag();
+      hsh[4 * b + 2] = (T)sh[2 * b + 1].real();
+      hsh[4 * b + 3] = (T)sh[2 * b + 1].imag();
+    }
+    CKL(cudaMemcpyAsync(dshift, hsh.data(), sizeof(T) * 4 * B, cudaMemcpyHostToDevice, s));
+    // chase the chain through [ilo, ihi] in chunks
+    const int steps = (ihi - 1 - ilo) + 3 * (B - 1) + 1;
+    const int w = 32;
+    for (int t0 = 0; t0 < steps; t0 += w) {
+      const int wc = std::min(w, steps - t0);
+      const int kmin = std::max(ilo, ilo + t0 - 3 * (B - 1));
+      const int kmx = std::min(ihi - 1, ilo + t0 + wc - 1);
+      ChaseArgs<T> ca{};
+      ca.H = H;
+      ca.Z = Z;
+      ca.n = n;
+      ca.ilo = ilo;
+      ca.ihi = ihi;
+      ca.B = B;
+      ca.t0 = t0;
+      ca.w = wc;
+      ca.wlo = std::max(ilo, kmin - 1);
+      ca.whi = std::min(ihi, kmx + 3);
+      ca.shifts = dshift;
+      ca.logk = logk;
+      ca.logr = logr;
+      CKL(launch_chase_chunk<T>(ca, r.num_sms, s));
+    }
+  }
+
+  // ---- 4. unscale T and the eigenvalues
+  k_triu1<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(H, n);
+  CKL(cudaGetLastError());
+  if (scaled) {
+    for (double m : safescale_factors_host(cscale, amax)) {
+      k_scale<T><<<4 * r.num_sms, 256, 0, s>>>(H, nn, m);
+      k_scale<double><<<1, 256, 0, s>>>(r.wr, n, m);
+      k_scale<double><<<1, 256, 0, s>>>(r.wi, n, m);
+    }
+  }
+  CKL(cudaGetLastError());
+  return ST_OK;
+#undef CKL
+}
+
+template int schur_large_run<double>(LargeRun<double>&);
+template int schur_large_run<float>(LargeRun<float>&);
+
+}  // namespace gsk

@@ -10,6 +10,7 @@ underscore):
   eigvecs(S; left) / geigvecs   pirates.jl:38-48 / vectors.jl:12-20
   eigen(A)                      pirates.jl:63-89 (without balancing)
   triangularize(S)              triang.jl:9-43
+  hessenberg(A)                 pirates.jl:232 / hessenberg.jl:3-17, 150-166
   gschur_batched(...)           batched form, no reference counterpart
   geigvecs_batched(...)         batched eigenvectors, no reference counterpart
   eig_adjoint_batched(...)      eigenvalue adjoint (reverse-mode rule), no reference counterpart
@@ -28,7 +29,7 @@ from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS
 
 __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_",
            "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
-           "eig_adjoint_batched",
+           "eig_adjoint_batched", "hessenberg",
            "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
@@ -319,3 +320,18 @@ def eig_adjoint_batched(T_packed, Z_packed, ns, offs, woffs, gbar, ctx=None):
     if rc != GS_OK:
         _raise(rc, ctx, "eig_adjoint_batched")
     return G
+
+
+def hessenberg(A, ctx=None):
+    """Householder Hessenberg reduction (hessenberg.jl:3-17) and Q (hessenberg.jl:150-166).
+    Returns (Hpacked, tau, Q): Hpacked holds H on and above the first subdiagonal and
+    the reflectors below it, as the reference's Hessenberg object stores them."""
+    ctx = ctx or get_context()
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    n = _checksquare(A)
+    tau = np.zeros(max(n - 1, 1))
+    Q = np.zeros((n, n), order="F")
+    rc = ctx.lib.gs_hessenberg_f64(ctx.handle, n, _ptr(A), max(n, 1), _ptr(tau), _ptr(Q), max(n, 1), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "hessenberg")
+    return A, tau[:max(n - 1, 0)], Q

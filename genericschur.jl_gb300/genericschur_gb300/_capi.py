@@ -47,6 +47,7 @@ SIGNATURES = {
     "gs_eigvecs_batched_c64": (_i, [_p, _i64, _p, _p, _i64, _p, _p, _p, _p, _u]),
     "gs_eigvecs_batched_f64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
     "gs_eig_adjoint_batched_c64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
+    "gs_hessenberg_f64": (_i, [_p, _i64, _p, _i64, _p, _p, _i64, _u]),
 }
 
 _lib = None

@@ -165,6 +165,15 @@ GS_API int gs_eig_adjoint_batched_c64(gs_context* ctx, int64_t count, const int3
                                       const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
                                       const double* Z, const double* gbar, double* grad, unsigned flags);
 
+/* Hessenberg reduction with Q.  Replaces hessenberg!(A) (pirates.jl:232 ->
+ * _hessenberg!, hessenberg.jl:3-17) and _materializeQ (hessenberg.jl:150-166):
+ * A [in/out] is overwritten by H with the reflectors' essential parts below the
+ * first subdiagonal (the packed form of the reference's Hessenberg object), tau
+ * receives the n-1 reflector scalars, Q (may be NULL) the orthogonal factor with
+ * A = Q H Q^T.  Any n. */
+GS_API int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* tau, double* Q, int64_t ldq,
+                             unsigned flags);
+
 #ifdef __cplusplus
 }
 #endif
