@@ -49,6 +49,8 @@ SIGNATURES = {
     "gs_eig_adjoint_batched_c64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
     "gs_hessenberg_f64": (_i, [_p, _i64, _p, _i64, _p, _p, _i64, _u]),
 }
+# allocation-free entry point (include/gschur_gb300_noalloc.h)
+SIGNATURES["gs_schur_batched_f64_noalloc"] = (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u])
 
 _lib = None
 _lock = threading.Lock()
