@@ -327,3 +327,27 @@ __device__ __forceinline__ double reflector_fast(double& a, double& x1, double& 
   return tau;
 }
 }  // namespace gsk
+
+namespace gsk {
+// 2-element complex reflector (householder.jl:56-102) from Newton-refined seeds:
+// s = ||(a, x1)||, beta = -sign(Re a) s, tau = (1 + |Re a|/s, sign(Re a) Im a / s),
+// 1/(a - beta) = conj(d)/|d|^2 with d = (Re a + sign(Re a) s, Im a).  Falls back to
+// zreflector2 outside the safe range.
+__device__ __forceinline__ double2 zreflector2_fast(double2& a, double2& x1) {
+  if (x1.x == 0.0 && x1.y == 0.0 && a.y == 0.0) return make_double2(0.0, 0.0);
+  const double xs = fma(x1.x, x1.x, x1.y * x1.y);
+  const double ss = fma(a.x, a.x, fma(a.y, a.y, xs));
+  if (!(ss > 1.0e-290 && ss < 1.0e290)) return zreflector2(a, x1);
+  const double y = rsqrt_nr(ss);
+  const double s = ss * y;
+  const double aa = fabs(a.x);
+  const double sy = copysign(y, a.x);
+  const double2 tau = make_double2(fma(aa, y, 1.0), a.y * sy);
+  const double dr = a.x + copysign(s, a.x);
+  const double r = rcp_nr(fma(dr, dr, a.y * a.y));
+  const double2 t = make_double2(dr * r, -a.y * r);
+  x1 = zmul(x1, t);
+  a = make_double2(-copysign(s, a.x), 0.0);
+  return tau;
+}
+}  // namespace gsk

@@ -47,7 +47,10 @@ struct CplxBatch {
   int maxinner_mult; // maxinner = maxinner_mult * n (reference default 30)
   long long maxiter_abs;   // when > 0, overrides maxiter_mult
   long long maxinner_abs;  // when > 0, overrides maxinner_mult
+  double2* hws;            // packed-H workspace of the single-matrix large variant
 };
+cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* order, int* sched, cudaStream_t s);
+size_t cplx_large_hws_elems(int n);
 
 // Eigenvectors of complex Schur factors (T upper triangular), batched.  Matrix b
 // has order ns[b] <= 128 at element offset offs[b] of T, Z, VR, VL and scratch.
@@ -134,8 +137,13 @@ struct LargeRun {
   int num_sms;
   cudaStream_t stream;
   cudaError_t cuda_error;
+  int bulges;      // bulges per chain (<= kMaxBulges; 0: default)
+  int chunk;       // chase steps per chunk (<= 64; 0: default)
 };
 size_t schur_large_ws_bytes(int n, size_t tsize);
+// Tuning of the large path: GS_LARGE_BULGES / GS_LARGE_CHUNK environment variables
+// (read once per call), else the built-in defaults.
+void large_tuning(int n, int* bulges, int* chunk);
 template <class T> int schur_large_run(LargeRun<T>& r);  // ST_OK, ST_UNCONVERGED, or -1 (cuda_error set)
 
 // Host copy of the safescale! factor sequence (util.jl:41-80, as written there).
@@ -159,6 +167,18 @@ inline std::vector<double> safescale_factors_host(double cfrom, double cto) {
   }
   return f;
 }
+
+// FP64 refinement kernels of the mixed-precision form (refine.cu).
+cudaError_t launch_sylv_wave(int n, int N, int d, const double* At, const double* Att, double* W, double* Wt,
+                             const int* bs, const int* bz, double floor, cudaStream_t s);
+cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s);
+cudaError_t launch_transpose(int n, const double* A, double* B, cudaStream_t s);
+cudaError_t launch_lower_norm(int n, const double* At, const int* blk, double* out, int num_sms, cudaStream_t s);
+cudaError_t launch_block_triu(int n, const double* At, const int* blk, double* T, cudaStream_t s);
+cudaError_t launch_std_blocks(int n, int N, const int* bs, const int* bz, double* T, double* Z, double* cs_sn,
+                              double* wr, double* wi, cudaStream_t s);
+template <class S, class D> cudaError_t convert_array(const S* src, D* dst, size_t count, double scale, cudaStream_t s);
+cudaError_t launch_absmax(const double* A, size_t cnt, unsigned long long* out, int num_sms, cudaStream_t s);
 
 // Size bins of the persistent batched kernels.  `sched` holds, per bin, the
 // [start, end) range of that bin inside the sorted work order and a queue ticket

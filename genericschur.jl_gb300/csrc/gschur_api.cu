@@ -4,6 +4,7 @@
 // staging, the fork/join of the size-bin kernels onto auxiliary streams and the
 // optional CUDA-graph replay.  All arithmetic runs in the kernels.
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -14,6 +15,8 @@
 #include "gs_internal.h"
 
 using namespace gsk;
+
+static constexpr int kCplxLargeMax = 2048;  // single-CTA complex path for 128 < n <= this
 
 struct gs_context {
   int device = 0;
@@ -47,11 +50,11 @@ int set_err(gs_context* c, int code, const char* fmt, ...) {
   return code;
 }
 
-#define CK(call)                                                                          \
+#define CK(...)                                                                           \
   do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
+    cudaError_t e_ = (__VA_ARGS__);                                                       \
     if (e_ != cudaSuccess)                                                                \
-      return set_err(ctx, GS_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));      \
+      return set_err(ctx, GS_CUDA, "%s failed: %s", #__VA_ARGS__, cudaGetErrorString(e_)); \
   } while (0)
 
 // Bump allocator over the context's device arena.
@@ -338,6 +341,7 @@ static int schur_large_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, d
   r.num_sms = ctx->num_sms;
   r.stream = s;
   r.cuda_error = cudaSuccess;
+  large_tuning((int)n, &r.bulges, &r.chunk);
   CK(cudaEventRecord(ctx->t0, s));
   const int st = schur_large_run<double>(r);
   if (st < 0) return set_err(ctx, GS_CUDA, "large Schur path: %s", cudaGetErrorString(r.cuda_error));
@@ -546,11 +550,13 @@ int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
     return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
   if (n == 0) return GS_OK;
   if (!A || !w || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
-  if (n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld > %d: large-matrix path not available", (long long)n, kSmallMax);
+  if (n > kCplxLargeMax) return set_err(ctx, GS_BADARG, "order %lld > %d not supported for complex input", (long long)n, kCplxLargeMax);
   CK(cudaSetDevice(ctx->device));
   const bool dev = flags & GS_DEVICE;
+  const bool large = n > kSmallMax;
   Arena ar;
   const size_t o_A = ar.take<double2>(n * n), o_Z = ar.take<double2>(n * n), o_w = ar.take<double2>(n);
+  const size_t o_h = ar.take<double2>(large ? cplx_large_hws_elems((int)n) : 1);
   const size_t o_meta = ar.take<long long>(4), o_st = ar.take<int>(2);
   const size_t o_order = ar.take<int>(1), o_sched = ar.take<int>(3 * kNumBins);
   int rc = ensure_ws(ctx, ar.off);
@@ -583,8 +589,19 @@ int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   bt.maxinner_mult = 30;
   bt.maxiter_abs = maxiter > 0 ? maxiter : 0;
   bt.maxinner_abs = maxinner > 0 ? maxinner : 0;
-  rc = run_batched_cplx(ctx, bt, (int*)(base + o_order), (int*)(base + o_sched), false, {});
-  if (rc) return rc;
+  if (large) {
+    // one CTA, packed H in global memory (any order up to kCplxLargeMax)
+    bt.hws = (double2*)(base + o_h);
+    CK(cudaEventRecord(ctx->t0, s));
+    cudaError_t e = launch_bin_sort(bt.ns, 1, (int*)(base + o_order), (int*)(base + o_sched), s);
+    if (e == cudaSuccess) e = launch_schur_cplx_large(bt, (int)n, (int*)(base + o_order), (int*)(base + o_sched), s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "complex large launch: %s", cudaGetErrorString(e));
+    CK(cudaEventRecord(ctx->t1, s));
+    ctx->timed = true;
+  } else {
+    rc = run_batched_cplx(ctx, bt, (int*)(base + o_order), (int*)(base + o_sched), false, {});
+    if (rc) return rc;
+  }
   CK(cudaMemcpy2DAsync(A, lda * es, dA, n * es, n * es, n, out, s));
   if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * es, dZ, n * es, n * es, n, out, s));
   CK(cudaMemcpyAsync(w, bt.w, n * es, out, s));
@@ -937,6 +954,225 @@ int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double
   if (Q) CK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), dQ, n * sizeof(double), n * sizeof(double), n, out, s));
   if (n > 1) CK(cudaMemcpyAsync(tau, dtau, (n - 1) * sizeof(double), out, s));
   CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision: FP32 Schur on the GPU + FP64 refinement of the Schur pair
+// ---------------------------------------------------------------------------
+int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
+                       double* wi, unsigned flags, int64_t maxiter, double* info) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (lda < std::max<int64_t>(n, 1) || ldz < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
+  if (n == 0) return GS_OK;
+  if (!A || !Z || !wr || !wi) return set_err(ctx, GS_BADARG, "null array argument (Z is required)");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  const int N32 = (int)n;
+  Arena ar;
+  const size_t o_A0 = ar.take<double>(nn), o_A32 = ar.take<float>(nn), o_Z32 = ar.take<float>(nn);
+  const size_t o_Z = ar.take<double>(nn), o_T1 = ar.take<double>(nn), o_T2 = ar.take<double>(nn);
+  const size_t o_T3 = ar.take<double>(nn), o_W = ar.take<double>(nn), o_Wt = ar.take<double>(nn);
+  const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n), o_sub = ar.take<float>(n);
+  const size_t o_bs = ar.take<int>(n), o_bz = ar.take<int>(n), o_blk = ar.take<int>(n), o_cs = ar.take<double>(4 * n);
+  const size_t o_nrm = ar.take<double>(4), o_max = ar.take<unsigned long long>(2);
+  const size_t o_ws = ar.take<char>(schur_large_ws_bytes(N32, sizeof(float)));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double* A0 = (double*)(base + o_A0);
+  float* A32 = (float*)(base + o_A32);
+  float* Z32 = (float*)(base + o_Z32);
+  double* dZ = (double*)(base + o_Z);
+  double* T1 = (double*)(base + o_T1);
+  double* T2 = (double*)(base + o_T2);
+  double* T3 = (double*)(base + o_T3);
+  double* W = (double*)(base + o_W);
+  double* Wt = (double*)(base + o_Wt);
+  double* dwr = (double*)(base + o_wr);
+  double* dwi = (double*)(base + o_wi);
+  double* nrm = (double*)(base + o_nrm);
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy2DAsync(A0, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
+  cudaEvent_t e0, e1, e2;
+  CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1)); CK(cudaEventCreate(&e2));
+  CK(cudaEventRecord(e0, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  // exact power-of-two prescale to max|a| in [0.5, 1): FP32 range safety, undone at the end
+  double amax = 0.0;
+  {
+    unsigned long long* dmax = (unsigned long long*)(base + o_max);
+    CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
+    cudaError_t e = launch_absmax(A0, nn, dmax, ctx->num_sms, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "absmax: %s", cudaGetErrorString(e));
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::memcpy(&amax, &bits, sizeof(amax));
+  }
+  if (!(amax > 0.0) || !std::isfinite(amax)) {
+    // zero or non-finite input: the plain FP64 path handles it with the reference's semantics
+    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+    return gs_schur_f64(ctx, n, A, lda, Z, ldz, wr, wi, flags | GS_WANTZ, maxiter);
+  }
+  int ex = 0;
+  std::frexp(amax, &ex);
+  const double pre = std::ldexp(1.0, -ex);   // A0 * pre has max in [0.5, 1)
+  CK(convert_array<double, double>(A0, A0, nn, pre, s));
+  CK(convert_array<double, float>(A0, A32, nn, 1.0, s));
+  // ---- FP32 Schur
+  LargeRun<float> r{};
+  r.A = A32;
+  r.Z = Z32;
+  r.wr = dwr;
+  r.wi = dwi;
+  r.n = N32;
+  r.scale = 0;
+  r.maxiter = maxiter > 0 ? maxiter : 0;
+  r.ws = base + o_ws;
+  r.num_sms = ctx->num_sms;
+  r.stream = s;
+  r.cuda_error = cudaSuccess;
+  large_tuning(N32, &r.bulges, &r.chunk);
+  const int st = schur_large_run<float>(r);
+  if (st < 0) return set_err(ctx, GS_CUDA, "FP32 Schur stage: %s", cudaGetErrorString(r.cuda_error));
+  if (st != ST_OK) return set_err(ctx, GS_UNCONVERGED, "FP32 Schur stage: iteration limit reached");
+  CK(cudaEventRecord(e1, s));
+  // ---- block structure from the FP32 quasi-triangular form
+  std::vector<float> sub(n, 0.0f);
+  {
+    // subdiagonal T32[i+1, i] at element (i+1) + i*n
+    CK(cudaMemcpy2DAsync(sub.data(), sizeof(float), A32 + 1, (n + 1) * sizeof(float), sizeof(float), n - 1,
+                         cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  std::vector<int> bs, bz, blk(n);
+  for (int i = 0; i < n;) {
+    const int z = (i + 1 < n && sub[i] != 0.0f) ? 2 : 1;
+    bs.push_back(i);
+    bz.push_back(z);
+    for (int q = 0; q < z; ++q) blk[i + q] = (int)bs.size() - 1;
+    i += z;
+  }
+  const int NB = (int)bs.size();
+  int* dbs = (int*)(base + o_bs);
+  int* dbz = (int*)(base + o_bz);
+  int* dblk = (int*)(base + o_blk);
+  CK(cudaMemcpyAsync(dbs, bs.data(), sizeof(int) * NB, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dbz, bz.data(), sizeof(int) * NB, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dblk, blk.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  // ---- FP64 refinement
+  auto gemm = [&](int m, int p, int q, const double* Am, int la, int tA, const double* Bm, int lb, double* Cm, int lc) {
+    return launch_gemm<double>(m, p, q, Am, la, tA, Bm, lb, Cm, lc, s);
+  };
+  auto ns_step = [&]() -> cudaError_t {
+    // Z <- Z (1.5 I - 0.5 Z^T Z)
+    cudaError_t e = gemm(N32, N32, N32, dZ, N32, 1, dZ, N32, T1, N32);
+    if (e == cudaSuccess) e = launch_refine_elementwise(2, N32, nullptr, T1, 0.0, s);
+    if (e == cudaSuccess) e = gemm(N32, N32, N32, dZ, N32, 0, T1, N32, T2, N32);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dZ, T2, nn * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    return e;
+  };
+  auto form_At = [&]() -> cudaError_t {
+    // T3 = A0 Z; T1 = Z^T T3
+    cudaError_t e = gemm(N32, N32, N32, A0, N32, 0, dZ, N32, T3, N32);
+    if (e == cudaSuccess) e = gemm(N32, N32, N32, dZ, N32, 1, T3, N32, T1, N32);
+    return e;
+  };
+  CK(convert_array<float, double>(Z32, dZ, nn, 1.0, s));
+  // two Newton-Schulz steps take the FP32 factor's orthogonality error (~1e-6) below eps
+  cudaError_t e = ns_step();
+  if (e == cudaSuccess) e = ns_step();
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "orthonormalisation: %s", cudaGetErrorString(e));
+  // Convergence: the residual reaches the rounding level of forming Z^T A Z, or it stops
+  // shrinking (Newton converges quadratically, so a step that gains less than 4x is at
+  // the noise floor) while below the acceptance bound.  NaN or a growing residual means
+  // the FP32 eigenvalues were not separated enough for the Newton step.
+  const double eps = 2.220446049250313e-16;
+  const double tol = 4.0 * eps * std::sqrt((double)n);
+  const double accept = eps * (double)n;
+  const int maxit = 6;
+  double res = 0.0, prev = 0.0;
+  int its = 0;
+  bool conv = false;
+  for (;;) {
+    e = form_At();
+    if (e == cudaSuccess) e = cudaMemsetAsync(nrm, 0, 4 * sizeof(double), s);
+    if (e == cudaSuccess) e = launch_lower_norm(N32, T1, dblk, nrm, ctx->num_sms, s);
+    double hn[2] = {0.0, 0.0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "refinement residual: %s", cudaGetErrorString(e));
+    res = std::sqrt(hn[0]) / std::max(std::sqrt(hn[1]), 1e-300);
+    if (!(res == res)) break;
+    if (res <= tol) { conv = true; break; }
+    if (its > 0 && res > 0.25 * prev) { conv = res <= accept; break; }
+    if (its >= maxit) break;
+    prev = res;
+    ++its;
+    // block Sylvester solve for W, then Z <- Z (I + S), S = W - W^T
+    e = launch_transpose(N32, T1, T2, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(W, 0, nn * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(Wt, 0, nn * sizeof(double), s);
+    const double floor = 1e-3 * std::sqrt(hn[1]) * eps;
+    for (int d = 0; d <= NB - 2 && e == cudaSuccess; ++d) e = launch_sylv_wave(N32, NB, d, T1, T2, W, Wt, dbs, dbz, floor, s);
+    double wn[2] = {0.0, 0.0};
+    if (e == cudaSuccess) e = launch_lower_norm(N32, W, dblk, nrm + 2, ctx->num_sms, s);
+    if (e == cudaSuccess) e = launch_refine_elementwise(0, N32, W, T3, 1.0, s);  // T3 = I + S
+    if (e == cudaSuccess) e = gemm(N32, N32, N32, dZ, N32, 0, T3, N32, T2, N32);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dZ, T2, nn * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(wn, nrm + 2, sizeof(wn), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // Z (I + S) departs from orthogonality by |S|^2: re-orthonormalise unless that is below eps
+    if (e == cudaSuccess && !(std::sqrt(wn[1]) <= 1e-8)) e = ns_step();
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "refinement step: %s", cudaGetErrorString(e));
+  }
+  if (!conv) {
+    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+    if (flags & GS_NOFALLBACK)
+      return set_err(ctx, GS_UNCONVERGED, "refinement did not converge (residual %.3g after %d steps)", res, its);
+    // the FP32 eigenvalues were not separated enough: recompute in FP64 from the untouched input
+    const int rc2 = gs_schur_f64(ctx, n, A, lda, Z, ldz, wr, wi, (flags & ~GS_NOFALLBACK) | GS_WANTZ, maxiter);
+    if (info) {
+      info[0] = -1.0;
+      info[1] = res;
+      info[2] = 0.0;
+      info[3] = 0.0;
+    }
+    return rc2;
+  }
+  // ---- T = block-upper part of Z^T A Z (already in T1), standardise 2x2 blocks
+  double* dT = T2;
+  e = launch_block_triu(N32, T1, dblk, dT, s);
+  if (e == cudaSuccess) e = launch_std_blocks(N32, NB, dbs, dbz, dT, dZ, (double*)(base + o_cs), dwr, dwi, s);
+  // undo the prescale (exact power of two)
+  if (e == cudaSuccess) e = convert_array<double, double>(dT, dT, nn, 1.0 / pre, s);
+  if (e == cudaSuccess) e = convert_array<double, double>(dwr, dwr, n, 1.0 / pre, s);
+  if (e == cudaSuccess) e = convert_array<double, double>(dwi, dwi, n, 1.0 / pre, s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "final form: %s", cudaGetErrorString(e));
+  CK(cudaEventRecord(e2, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dT, n * sizeof(double), n * sizeof(double), n, out, s));
+  CK(cudaMemcpy2DAsync(Z, ldz * sizeof(double), dZ, n * sizeof(double), n * sizeof(double), n, out, s));
+  CK(cudaMemcpyAsync(wr, dwr, n * sizeof(double), out, s));
+  CK(cudaMemcpyAsync(wi, dwi, n * sizeof(double), out, s));
+  CK(cudaStreamSynchronize(s));
+  float ms1 = 0.f, ms2 = 0.f;
+  cudaEventElapsedTime(&ms1, e0, e1);
+  cudaEventElapsedTime(&ms2, e1, e2);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  if (info) {
+    info[0] = its;
+    info[1] = res;
+    info[2] = ms1;
+    info[3] = ms2;
+  }
   return GS_OK;
 }
 

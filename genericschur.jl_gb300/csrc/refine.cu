@@ -1,0 +1,282 @@
+// FP64 refinement of an approximate real Schur pair (the mixed-precision form).
+//
+// Given orthogonal Z (to working accuracy) and At = Z^T A Z = T + L, with T block
+// upper triangular in the 1x1/2x2 block structure of the low-precision Schur form and
+// L the (small) block-lower remainder, one Newton step looks for Q = I + S,
+// S = W - W^T skew with W block-lower, such that Q^T At Q is block upper triangular
+// to first order.  The block-lower part of T S - S T + L must vanish, which for
+// block rows p > q reads
+//     T_pp W_pq - W_pq T_qq = -L_pq - sum_{r>p} T_pr W_rq + sum_{r<q} W_pr T_rq,
+// a block triangular Sylvester equation (the iteration of Bujanovic, Kressner and
+// Schroeder, "Iterative refinement of Schur decompositions", Numer. Algorithms 2023).
+// It is solved by anti-diagonal waves over the block pairs: wave d holds the pairs
+// (p, q) = (N-1-d+q, q), which depend only on earlier waves.  One warp per pair: the
+// lanes split the two sums, lane 0 solves the (<= 4 x 4) Kronecker system of the pair.
+// Z is then updated to Z (I + S), which departs from orthogonality by O(|S|^2); a
+// Newton-Schulz step Z <- Z (3 I - Z^T Z) / 2 follows whenever |S| is above 1e-8.
+#include "device_common.cuh"
+#include "gs_internal.h"
+
+namespace gsk {
+namespace {
+
+// Solve the small system M x = r (m <= 4) with partial pivoting; tiny pivots are
+// replaced by +-floor so that (nearly) equal eigenvalues give a bounded correction.
+__device__ void small_solve(int m, double M[4][4], double r[4], double floor) {
+  for (int c = 0; c < m; ++c) {
+    int piv = c;
+    for (int i = c + 1; i < m; ++i)
+      if (fabs(M[i][c]) > fabs(M[piv][c])) piv = i;
+    if (piv != c) {
+      for (int j = 0; j < m; ++j) { double t = M[c][j]; M[c][j] = M[piv][j]; M[piv][j] = t; }
+      double t = r[c]; r[c] = r[piv]; r[piv] = t;
+    }
+    if (fabs(M[c][c]) < floor) M[c][c] = (M[c][c] < 0.0) ? -floor : floor;
+    for (int i = c + 1; i < m; ++i) {
+      const double f = M[i][c] / M[c][c];
+      for (int j = c; j < m; ++j) M[i][j] -= f * M[c][j];
+      r[i] -= f * r[c];
+    }
+  }
+  for (int c = m - 1; c >= 0; --c) {
+    double s = r[c];
+    for (int j = c + 1; j < m; ++j) s -= M[c][j] * r[j];
+    r[c] = s / M[c][c];
+  }
+}
+
+// One wave of the block Sylvester solve.  T: At (n x n, ld n) whose block-upper part
+// is T and block-lower part is L; Tt = At^T; W, Wt: the solution and its transpose
+// (zero-initialised); bs/bz: block start (0-based) and size of the N blocks.
+__global__ void __launch_bounds__(256) k_sylv_wave(int n, int N, int d, const double* __restrict__ At,
+                                                   const double* __restrict__ Att, double* __restrict__ W,
+                                                   double* __restrict__ Wt, const int* __restrict__ bs,
+                                                   const int* __restrict__ bz, double floor) {
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (q > d) return;
+  const int p = N - 1 - d + q;
+  const int sp = bs[p], zp = bz[p], sq = bs[q], zq = bz[q];
+  const int kp = sp + zp;  // sum_{r>p}: scalar k >= kp
+  double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+  // - sum_{k >= kp} T[i, k] W[k, j]   (T row i = Att column i)
+  for (int k = kp + lane; k < n; k += 32) {
+    for (int a = 0; a < zp; ++a) {
+      const double t = Att[(size_t)(sp + a) * n + k];
+      for (int b = 0; b < zq; ++b) acc[a][b] -= t * W[(size_t)(sq + b) * n + k];
+    }
+  }
+  // + sum_{k < sq} W[i, k] T[k, j]    (W row i = Wt column i)
+  for (int k = lane; k < sq; k += 32) {
+    for (int a = 0; a < zp; ++a) {
+      const double wv = Wt[(size_t)(sp + a) * n + k];
+      for (int b = 0; b < zq; ++b) acc[a][b] += wv * At[(size_t)(sq + b) * n + k];
+    }
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int o = 16; o > 0; o >>= 1) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o);
+  if (lane != 0) return;
+  // r = -L_pq + sums;  unknowns x = vec(W_pq) (column-major, zp x zq)
+  const int m = zp * zq;
+  double M[4][4] = {{0}}, r[4];
+  for (int b = 0; b < zq; ++b)
+    for (int a = 0; a < zp; ++a) r[a + b * zp] = -At[(size_t)(sq + b) * n + sp + a] + acc[a][b];
+  // (I_zq (x) T_pp - T_qq^T (x) I_zp) x = r
+  for (int b = 0; b < zq; ++b)
+    for (int a = 0; a < zp; ++a) {
+      const int row = a + b * zp;
+      for (int a2 = 0; a2 < zp; ++a2) M[row][a2 + b * zp] += At[(size_t)(sp + a2) * n + sp + a];   // T_pp[a, a2]
+      for (int b2 = 0; b2 < zq; ++b2) M[row][a + b2 * zp] -= At[(size_t)(sq + b) * n + sq + b2];    // T_qq[b2, b]
+    }
+  small_solve(m, M, r, floor);
+  for (int b = 0; b < zq; ++b)
+    for (int a = 0; a < zp; ++a) {
+      const double x = r[a + b * zp];
+      W[(size_t)(sq + b) * n + sp + a] = x;
+      Wt[(size_t)(sp + a) * n + sq + b] = x;
+    }
+}
+
+// S = W - W^T (+ I when add_identity), and block-lower norm accumulation helpers.
+__global__ void k_skew(int n, const double* __restrict__ W, double* __restrict__ S, double add_identity) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const int i = idx % n, j = idx / n;
+  S[idx] = W[idx] - W[(size_t)i * n + j] + (i == j ? add_identity : 0.0);
+}
+
+// E = I + S + S2/2 in place over S2.
+__global__ void k_exp2(int n, const double* __restrict__ S, double* __restrict__ S2) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const int i = idx % n, j = idx / n;
+  S2[idx] = (i == j ? 1.0 : 0.0) + S[idx] + 0.5 * S2[idx];
+}
+
+// Newton-Schulz factor: X <- 1.5 I - 0.5 X
+__global__ void k_ns_factor(int n, double* X) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const int i = idx % n, j = idx / n;
+  X[idx] = (i == j ? 1.5 : 0.0) - 0.5 * X[idx];
+}
+
+// transpose
+__global__ void k_transpose(int n, const double* __restrict__ A, double* __restrict__ B) {
+  __shared__ double t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = bx + threadIdx.x, c = by + k;
+    if (r < n && c < n) t[k][threadIdx.x] = A[(size_t)c * n + r];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = by + threadIdx.x, c = bx + k;
+    if (r < n && c < n) B[(size_t)c * n + r] = t[threadIdx.x][k];
+  }
+}
+
+// sum of squares of the block-lower part (entries (i, j) with block(i) > block(j)) and of all
+// entries, into out[0], out[1] (atomics on doubles: the norms only steer the iteration).
+__global__ void k_lower_norm(int n, const double* __restrict__ At, const int* __restrict__ blk, double* out) {
+  double sl = 0.0, sa = 0.0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (size_t)n * n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = idx % n, j = idx / n;
+    const double v = At[idx];
+    sa += v * v;
+    if (blk[i] > blk[j]) sl += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sl += __shfl_xor_sync(0xffffffffu, sl, o);
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+  }
+  if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], sl); atomicAdd(&out[1], sa); }
+}
+
+// T = block-upper part of At (zero below the block diagonal).
+__global__ void k_block_triu(int n, const double* __restrict__ At, const int* __restrict__ blk, double* __restrict__ T) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const int i = idx % n, j = idx / n;
+  T[idx] = (blk[i] > blk[j]) ? 0.0 : At[idx];
+}
+
+// Standardise every 2x2 diagonal block with _gs2x2! (GenericSchur.jl:716-803): the
+// rotations of different blocks act on disjoint index pairs.  Phase 0: compute
+// (cs, sn) and the eigenvalues; phase 1: rows; phase 2: columns of T and Z.
+__global__ void k_std_blocks(int n, int N, const int* __restrict__ bs, const int* __restrict__ bz, double* T,
+                             double* Z, double* cs_sn, double* wr, double* wi, int phase) {
+  const int b = blockIdx.x;
+  if (b >= N) return;
+  const int s = bs[b], z = bz[b];
+  if (z == 1) {
+    if (phase == 0 && threadIdx.x == 0) { wr[s] = T[(size_t)s * n + s]; wi[s] = 0.0; }
+    return;
+  }
+  const int p = s, q = s + 1;
+  if (phase == 0) {
+    if (threadIdx.x == 0) {
+      double a = T[(size_t)p * n + p], bb = T[(size_t)q * n + p], c = T[(size_t)p * n + q], d = T[(size_t)q * n + q];
+      double cs, sn, w1r, w1i, w2r, w2i;
+      gs2x2(a, bb, c, d, cs, sn, w1r, w1i, w2r, w2i);
+      cs_sn[4 * b] = cs; cs_sn[4 * b + 1] = sn;
+      wr[p] = w1r; wi[p] = w1i; wr[q] = w2r; wi[q] = w2i;
+      cs_sn[4 * b + 2] = a;  // keep the standardised block to write it back exactly
+      (void)bb; (void)c;
+      T[(size_t)p * n + p] = a; T[(size_t)q * n + p] = bb; T[(size_t)p * n + q] = c; T[(size_t)q * n + q] = d;
+    }
+    return;
+  }
+  const double cs = cs_sn[4 * b], sn = cs_sn[4 * b + 1];
+  if (phase == 1) {
+    // rows p, q of T, columns outside the block
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      if (j == p || j == q) continue;
+      const double a1 = T[(size_t)j * n + p], a2 = T[(size_t)j * n + q];
+      T[(size_t)j * n + p] = cs * a1 + sn * a2;
+      T[(size_t)j * n + q] = -sn * a1 + cs * a2;
+    }
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      if (i != p && i != q) {
+        const double a1 = T[(size_t)p * n + i], a2 = T[(size_t)q * n + i];
+        T[(size_t)p * n + i] = cs * a1 + sn * a2;
+        T[(size_t)q * n + i] = -sn * a1 + cs * a2;
+      }
+      if (Z) {
+        const double z1 = Z[(size_t)p * n + i], z2 = Z[(size_t)q * n + i];
+        Z[(size_t)p * n + i] = cs * z1 + sn * z2;
+        Z[(size_t)q * n + i] = -sn * z1 + cs * z2;
+      }
+    }
+  }
+}
+
+template <class S, class D>
+__global__ void k_convert(const S* __restrict__ src, D* __restrict__ dst, size_t count, double scale) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (D)((double)src[i] * scale);
+}
+
+}  // namespace
+
+template <class S, class D>
+cudaError_t convert_array(const S* src, D* dst, size_t count, double scale, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  k_convert<S, D><<<1024, 256, 0, s>>>(src, dst, count, scale);
+  return cudaGetLastError();
+}
+template cudaError_t convert_array<double, float>(const double*, float*, size_t, double, cudaStream_t);
+template cudaError_t convert_array<float, double>(const float*, double*, size_t, double, cudaStream_t);
+template cudaError_t convert_array<double, double>(const double*, double*, size_t, double, cudaStream_t);
+
+cudaError_t launch_sylv_wave(int n, int N, int d, const double* At, const double* Att, double* W, double* Wt,
+                             const int* bs, const int* bz, double floor, cudaStream_t s) {
+  const int pairs = d + 1;
+  const int wpb = 8;
+  k_sylv_wave<<<(pairs + wpb - 1) / wpb, 32 * wpb, 0, s>>>(n, N, d, At, Att, W, Wt, bs, bz, floor);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s) {
+  const size_t tot = (size_t)n * n;
+  const unsigned g = (unsigned)((tot + 255) / 256);
+  switch (op) {
+    case 0: k_skew<<<g, 256, 0, s>>>(n, a, b, x); break;
+    case 1: k_exp2<<<g, 256, 0, s>>>(n, a, b); break;
+    case 2: k_ns_factor<<<g, 256, 0, s>>>(n, b); break;
+    default: break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(int n, const double* A, double* B, cudaStream_t s) {
+  dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
+  k_transpose<<<g, b, 0, s>>>(n, A, B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lower_norm(int n, const double* At, const int* blk, double* out, int num_sms, cudaStream_t s) {
+  k_lower_norm<<<4 * num_sms, 256, 0, s>>>(n, At, blk, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_block_triu(int n, const double* At, const int* blk, double* T, cudaStream_t s) {
+  const size_t tot = (size_t)n * n;
+  k_block_triu<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, At, blk, T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_std_blocks(int n, int N, const int* bs, const int* bz, double* T, double* Z, double* cs_sn,
+                              double* wr, double* wi, cudaStream_t s) {
+  for (int ph = 0; ph < 3; ++ph) {
+    k_std_blocks<<<N, 128, 0, s>>>(n, N, bs, bz, T, Z, cs_sn, wr, wi, ph);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace gsk

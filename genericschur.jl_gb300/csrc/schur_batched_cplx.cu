@@ -20,10 +20,14 @@
 namespace gsk {
 namespace {
 
-struct CtlC {
-  double2 v[2];
+struct ZRefl {
   double2 t1, v2;
   double t2;
+};
+
+struct CtlC {
+  double2 v[2];
+  ZRefl r[2];
   double2 shift;
   double2 ph;   // phase factor t of the start-row fix-up
   double2 tail; // phase factor of the tail fix-up
@@ -144,10 +148,11 @@ __device__ void hessenberg_cplx(int n, double2* A, int ld, double2* tau, double*
 #undef AA
 }
 
-template <int NT, bool HSMEM>
+template <int NT, bool HSMEM, bool HGLOB>
 __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
   constexpr bool PACKED = !HSMEM;
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   const int n = bt.ns[b];
   if (n <= 0) {
     if (tid == 0) bt.status[b] = ST_OK;
@@ -158,8 +163,9 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
   double2* __restrict__ wg = bt.w + bt.woffs[b];
   const int ldh = HSMEM ? (n | 1) : n;
   const int hsize = HSMEM ? n * ldh : pk_off(n + 1);
-  double2* Hs = smem;
-  double2* tau = Hs + hsize;        // n
+  // packed H of the QR phase: shared memory, or (orders > 128) the global workspace
+  double2* Hs = HGLOB ? bt.hws : smem;
+  double2* tau = HGLOB ? smem : Hs + hsize;  // n
   double2* lg = tau + n;            // 3 per chase step: t1, v2, (t2, 0)
   double* red = (double*)(lg + 3 * n);
   double2* A = HSMEM ? Hs : Ag;     // where the Hessenberg reduction runs
@@ -330,24 +336,25 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
         c.v[0] = zdiv(h11s, make_double2(s, 0.0));
         c.v[1] = make_double2(h21 / s, 0.0);
         c.phase_on = 0;
+        c.ph = make_double2(1.0, 0.0);
       }
-      // chase (GenericSchur.jl:426-484)
-      for (int k = k0; k <= iend - 1; ++k) {
-        __syncthreads();
-        if (tid == 0) {
-          double2 a, x1;
-          if (k > k0) { a = H(k, k - 1); x1 = H(k + 1, k - 1); }
-          else { a = c.v[0]; x1 = c.v[1]; }
-          const double2 t1 = zreflector2(a, x1);
-          if (k > k0) { H(k, k - 1) = a; H(k + 1, k - 1) = make_double2(0.0, 0.0); }
-          c.t1 = t1; c.v2 = x1; c.t2 = zmul(t1, x1).x;
-          double2* l = lg + 3 * (k - 1);
-          l[0] = t1; l[1] = x1; l[2] = make_double2(c.t2, 0.0);
-        }
-        __syncthreads();
-        const double2 t1 = c.t1, v2 = c.v2;
-        const double t2 = c.t2;
-        for (int j = k + tid; j <= n; j += NT) {  // rows k, k+1; columns k..n
+      // chase (GenericSchur.jl:426-484).  The first step runs on its own (its phase
+      // fix-up changes the next reflector's inputs); after it, one barrier per step:
+      // warp 0 updates the 3x2 near block and computes the next reflector while the
+      // other warps update the far columns (k+2..n) and far rows (1..k-1).
+      if (tid == 0) {
+        double2 a = c.v[0], x1 = c.v[1];
+        const double2 t1 = zreflector2_fast(a, x1);
+        c.r[0].t1 = t1; c.r[0].v2 = x1; c.r[0].t2 = zmul(t1, x1).x;
+        double2* l = lg + 3 * (k0 - 1);
+        l[0] = t1; l[1] = x1; l[2] = make_double2(c.r[0].t2, 0.0);
+      }
+      __syncthreads();
+      {
+        const int k = k0;
+        const double2 t1 = c.r[0].t1, v2 = c.r[0].v2;
+        const double t2 = c.r[0].t2;
+        for (int j = k + tid; j <= n; j += NT) {
           const double2 h0 = H(k, j), h1 = H(k + 1, j);
           const double2 ss = zadd(zmul(zconj(t1), h0), zscal(h1, t2));
           H(k, j) = zsub(h0, ss);
@@ -355,13 +362,13 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
         }
         __syncthreads();
         const int rl = min(k + 2, iend);
-        for (int r = 1 + tid; r <= rl; r += NT) {  // columns k, k+1; rows 1..min(k+2, iend)
+        for (int r = 1 + tid; r <= rl; r += NT) {
           const double2 h0 = H(r, k), h1 = H(r, k + 1);
           const double2 ss = zadd(zmul(t1, h0), zscal(h1, t2));
           H(r, k) = zsub(h0, ss);
           H(r, k + 1) = zfms(ss, zconj(v2), h1);
         }
-        if (k == k0 && k0 > istart) {
+        if (k0 > istart) {
           // phase fix-up keeping H[k0+1, k0] real (GenericSchur.jl:461-482)
           __syncthreads();
           if (tid == 0) {
@@ -374,15 +381,77 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
           }
           __syncthreads();
           const double2 t = c.ph;
-          // rows j in [k0, iend] \ {k0+1}: H[j, j+1:n] *= t (one column per thread)
           for (int col = k0 + 1 + tid; col <= n; col += NT)
             for (int j = k0; j <= min(iend, col - 1); ++j)
               if (j != k0 + 1) H(j, col) = zmul(H(j, col), t);
           __syncthreads();
-          // columns j in [k0, iend] \ {k0+1}: H[1:j-1, j] *= conj(t)
           for (int j = k0 + tid; j <= iend; j += NT)
             if (j != k0 + 1)
               for (int r = 1; r <= j - 1; ++r) H(r, j) = zmul(H(r, j), zconj(t));
+        }
+        __syncthreads();
+        if (tid == 0 && k0 + 1 <= iend - 1) {
+          const int kk = k0 + 1;
+          double2 a = H(kk, kk - 1), x1 = H(kk + 1, kk - 1);
+          const double2 tn = zreflector2_fast(a, x1);
+          H(kk, kk - 1) = a;
+          H(kk + 1, kk - 1) = make_double2(0.0, 0.0);
+          c.r[1].t1 = tn; c.r[1].v2 = x1; c.r[1].t2 = zmul(tn, x1).x;
+          double2* l = lg + 3 * (kk - 1);
+          l[0] = tn; l[1] = x1; l[2] = make_double2(c.r[1].t2, 0.0);
+        }
+        __syncthreads();
+      }
+      {
+        int cur = 1;
+        for (int k = k0 + 1; k <= iend - 1; ++k) {
+          const ZRefl r = c.r[cur];
+          if (warp == 0) {
+            if (lane < 2) {  // left on columns k, k+1 (rows k, k+1)
+              const int j = k + lane;
+              const double2 h0 = H(k, j), h1 = H(k + 1, j);
+              const double2 ss = zadd(zmul(zconj(r.t1), h0), zscal(h1, r.t2));
+              H(k, j) = zsub(h0, ss);
+              H(k + 1, j) = zfms(ss, r.v2, h1);
+            }
+            __syncwarp();
+            if (lane < 3 && k + lane <= min(k + 2, iend)) {  // right on rows k..k+2 (columns k, k+1)
+              const int rr = k + lane;
+              const double2 h0 = H(rr, k), h1 = H(rr, k + 1);
+              const double2 ss = zadd(zmul(r.t1, h0), zscal(h1, r.t2));
+              H(rr, k) = zsub(h0, ss);
+              H(rr, k + 1) = zfms(ss, zconj(r.v2), h1);
+            }
+            __syncwarp();
+            if (lane == 0 && k + 1 <= iend - 1) {
+              const int kk = k + 1;
+              double2 a = H(kk, kk - 1), x1 = H(kk + 1, kk - 1);
+              const double2 tn = zreflector2_fast(a, x1);
+              H(kk, kk - 1) = a;
+              H(kk + 1, kk - 1) = make_double2(0.0, 0.0);
+              ZRefl& o = c.r[cur ^ 1];
+              o.t1 = tn; o.v2 = x1; o.t2 = zmul(tn, x1).x;
+              double2* l = lg + 3 * (kk - 1);
+              l[0] = tn; l[1] = x1; l[2] = make_double2(o.t2, 0.0);
+            }
+          } else {
+            const int ft = tid - 32;
+            constexpr int NF = NT - 32;
+            for (int j = k + 2 + ft; j <= n; j += NF) {
+              const double2 h0 = H(k, j), h1 = H(k + 1, j);
+              const double2 ss = zadd(zmul(zconj(r.t1), h0), zscal(h1, r.t2));
+              H(k, j) = zsub(h0, ss);
+              H(k + 1, j) = zfms(ss, r.v2, h1);
+            }
+            for (int rr = 1 + ft; rr <= k - 1; rr += NF) {
+              const double2 h0 = H(rr, k), h1 = H(rr, k + 1);
+              const double2 ss = zadd(zmul(r.t1, h0), zscal(h1, r.t2));
+              H(rr, k) = zsub(h0, ss);
+              H(rr, k + 1) = zfms(ss, zconj(r.v2), h1);
+            }
+          }
+          __syncthreads();
+          cur ^= 1;
         }
       }
       __syncthreads();
@@ -454,7 +523,7 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
   __syncthreads();
 }
 
-template <int NT, bool HSMEM>
+template <int NT, bool HSMEM, bool HGLOB>
 __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __restrict__ order,
                                                    int* __restrict__ sched, int bin) {
   extern __shared__ double2 smemz[];
@@ -467,7 +536,7 @@ __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __re
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_cplx<NT, HSMEM>(bt, order[job], smemz, c);
+    solve_cplx<NT, HSMEM, HGLOB>(bt, order[job], smemz, c);
   }
 }
 
@@ -476,17 +545,30 @@ cudaError_t launch_bin_c(const CplxBatch& bt, const int* order, int* sched, int 
   const int nmax = bin_max(bin);
   const size_t hsize = HSMEM ? (size_t)nmax * (nmax | 1) : (size_t)pk_off(nmax + 1);
   const size_t smem = sizeof(double2) * (hsize + 4 * nmax) + 32 * sizeof(double) + 64;
-  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<NT, HSMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<NT, HSMEM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM>, NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM, false>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  k_schur_cplx<NT, HSMEM><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin);
+  k_schur_cplx<NT, HSMEM, false><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin);
   return cudaGetLastError();
 }
 
 }  // namespace
+
+// One complex matrix of order n > 128: a single CTA of 256 threads, with the packed
+// H of the QR phase in the global workspace bt.hws (pk_off(n+1) entries).  The
+// matrix has gone through launch_bin_sort, which places it in the last bin.
+cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* order, int* sched, cudaStream_t s) {
+  const size_t smem = sizeof(double2) * (4 * (size_t)nmax) + 32 * sizeof(double) + 64;
+  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<256, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_schur_cplx<256, false, true><<<1, 256, smem, s>>>(bt, order, sched, kNumBins - 1);
+  return cudaGetLastError();
+}
+
+size_t cplx_large_hws_elems(int n) { return (size_t)pk_off(n + 1); }
 
 cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched, int num_sms,
                                       cudaStream_t* streams, int nstreams) {
@@ -494,7 +576,7 @@ cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int
   if ((e = launch_bin_c<128, false>(bt, order, sched, 3, num_sms, streams[0 % nstreams])) != cudaSuccess) return e;
   if ((e = launch_bin_c<128, false>(bt, order, sched, 2, num_sms, streams[1 % nstreams])) != cudaSuccess) return e;
   if ((e = launch_bin_c<64, true>(bt, order, sched, 1, num_sms, streams[2 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin_c<32, true>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
+  if ((e = launch_bin_c<64, true>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
   return cudaSuccess;
 }
 

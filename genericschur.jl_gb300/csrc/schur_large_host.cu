@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -72,6 +73,18 @@ cudaError_t copy2d(int m, int p, const S* src, int lds, D* dst, int ldd, cudaStr
 }
 
 }  // namespace
+
+void large_tuning(int n, int* bulges, int* chunk) {
+  const char* b = std::getenv("GS_LARGE_BULGES");
+  const char* c = std::getenv("GS_LARGE_CHUNK");
+  *bulges = b ? std::max(1, std::min(kMaxBulges, std::atoi(b))) : (n >= 1024 ? 16 : 12);
+  *chunk = c ? std::max(1, std::min(64, std::atoi(c))) : 16;
+}
+
+cudaError_t launch_absmax(const double* A, size_t cnt, unsigned long long* out, int num_sms, cudaStream_t s) {
+  k_absmax_bits<double><<<4 * num_sms, 256, 0, s>>>(A, cnt, out);
+  return cudaGetLastError();
+}
 
 // Workspace needed by schur_large_run<T>, in bytes.
 size_t schur_large_ws_bytes(int n, size_t tsize) {
@@ -223,7 +236,7 @@ int schur_large_run(LargeRun<T>& r) {
     }
     if (++sweeps > max_sweeps) return ST_UNCONVERGED;
     // shifts: eigenvalues of the trailing 2B x 2B block
-    const int B = std::min(kMaxBulges, std::max(1, (m - 8) / 6));
+    const int B = std::min(r.bulges > 0 ? r.bulges : kMaxBulges, std::max(1, (m - 8) / 6));
     const int ns = 2 * B;
     std::vector<double> ewr(ns), ewi(ns);
     ++since_defl;
@@ -267,7 +280,7 @@ int schur_large_run(LargeRun<T>& r) {
     CKL(cudaMemcpyAsync(dshift, hsh.data(), sizeof(T) * 4 * B, cudaMemcpyHostToDevice, s));
     // chase the chain through [ilo, ihi] in chunks
     const int steps = (ihi - 1 - ilo) + 3 * (B - 1) + 1;
-    const int w = 32;
+    const int w = r.chunk > 0 ? std::min(r.chunk, 64) : 32;
     for (int t0 = 0; t0 < steps; t0 += w) {
       const int wc = std::min(w, steps - t0);
       const int kmin = std::max(ilo, ilo + t0 - 3 * (B - 1));

@@ -29,7 +29,7 @@ from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS
 
 __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_",
            "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
-           "eig_adjoint_batched", "hessenberg",
+           "eig_adjoint_batched", "hessenberg", "gschur_mixed",
            "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
@@ -335,3 +335,28 @@ def hessenberg(A, ctx=None):
     if rc != GS_OK:
         _raise(rc, ctx, "hessenberg")
     return A, tau[:max(n - 1, 0)], Q
+
+
+def gschur_mixed(A, scale=True, maxiter=None, ctx=None, return_info=False, fallback=True):
+    """Real Schur decomposition computed in FP32 on the GPU and refined to FP64
+    accuracy (Newton refinement of the Schur pair).  Same outputs as gschur.
+    When FP32 does not separate the eigenvalues well enough for the refinement, the
+    decomposition is recomputed in FP64 (info["iterations"] == -1); with
+    fallback=False an UnconvergedException is raised instead."""
+    ctx = ctx or get_context()
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    n = _checksquare(A)
+    Z = np.zeros((n, n), order="F")
+    wr = np.zeros(n)
+    wi = np.zeros(n)
+    info = np.zeros(4)
+    flags = GS_WANTZ | (GS_SCALE if scale else 0) | (0 if fallback else _capi.GS_NOFALLBACK)
+    rc = ctx.lib.gs_schur_mixed_f64(ctx.handle, n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(wr), _ptr(wi), flags,
+                                    int(maxiter or 0), _ptr(info))
+    if rc != GS_OK:
+        _raise(rc, ctx, "gschur_mixed")
+    S = Schur(A, Z, wr + 1j * wi)
+    if return_info:
+        return S, {"iterations": int(info[0]), "residual": float(info[1]), "fp32_ms": float(info[2]),
+                   "refine_ms": float(info[3])}
+    return S

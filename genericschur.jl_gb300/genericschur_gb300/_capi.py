@@ -21,6 +21,7 @@ GS_SCALE = 2
 GS_DEVICE = 4
 GS_GRAPH = 8
 GS_RAW = 16
+GS_NOFALLBACK = 32
 
 _i = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -48,6 +49,7 @@ SIGNATURES = {
     "gs_eigvecs_batched_f64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
     "gs_eig_adjoint_batched_c64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
     "gs_hessenberg_f64": (_i, [_p, _i64, _p, _i64, _p, _p, _i64, _u]),
+    "gs_schur_mixed_f64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64, _p]),
 }
 # allocation-free entry point (include/gschur_gb300_noalloc.h)
 SIGNATURES["gs_schur_batched_f64_noalloc"] = (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u])

@@ -53,4 +53,31 @@ def cplx_flops(ns):
     return 100.0 * float(np.sum(np.asarray(ns, dtype=np.float64) ** 3))
 
 
-__all__ = ["batch_sizes", "batched_real", "batched_cplx", "real_flops", "cplx_flops", "pack_batch"]
+__all__ = ["batch_sizes", "batched_real", "batched_cplx", "real_flops", "cplx_flops", "pack_batch", "conditioned_matrix",
+           "large_real", "LARGE_SEEDS"]
+
+
+def conditioned_matrix(n=2048, seed=6, cond=1e3, lo=1e-3, hi=1e3):
+    """A = V diag(l) V^-1 with l real, |l| log-uniform in [lo, hi] with random signs,
+    and V Gaussian with its singular values replaced by a log-uniform spread from 1 to
+    cond (V = U diag(s) W^T from the SVD of a Gaussian matrix)."""
+    rng = np.random.default_rng(seed)
+    lam = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n)) * rng.choice([-1.0, 1.0], size=n)
+    G = rng.standard_normal((n, n))
+    U, _, Wt = np.linalg.svd(G)
+    s = np.exp(np.linspace(0.0, np.log(cond), n))
+    V = (U * s) @ Wt
+    Vinv = (Wt.T / s) @ U.T
+    return np.asfortranarray((V * lam) @ Vinv)
+
+
+LARGE_SEEDS = {4096: 1, 1024: 2, 2048: 3}
+
+
+def large_real(n=4096, seed=None):
+    """One real n x n matrix with iid N(0,1) entries (column-major); the default seeds
+    are 1 for n=4096, 2 for n=1024 and 3 for n=2048."""
+    if seed is None:
+        seed = LARGE_SEEDS.get(n, n)
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(rng.standard_normal((n, n)))

@@ -46,6 +46,7 @@ extern "C" {
 #define GS_DEVICE 4u  /* all array arguments are device pointers; asynchronous                    */
 #define GS_GRAPH 8u   /* batched calls: replay a cached CUDA graph of the launch sequence         */
 #define GS_RAW 16u    /* eigenvectors: skip _enormalize! (return the max-|re|+|im|-scaled vectors) */
+#define GS_NOFALLBACK 32u /* mixed precision: report GS_UNCONVERGED instead of recomputing in FP64   */
 
 typedef struct gs_context gs_context;
 
@@ -164,6 +165,22 @@ GS_API int gs_eigvecs_batched_f64(gs_context* ctx, int64_t count, const int32_t*
 GS_API int gs_eig_adjoint_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                                       const int64_t* woffs, int64_t packed_len, int64_t w_len, const double* T,
                                       const double* Z, const double* gbar, double* grad, unsigned flags);
+
+/* Mixed-precision real Schur (no reference counterpart; same outputs as
+ * gs_schur_f64).  The decomposition runs in FP32 on the GPU (Hessenberg reduction
+ * and multishift QR), then FP64 Newton refinement of the Schur pair restores FP64
+ * accuracy: Z is re-orthonormalised (Newton-Schulz), Z^T A Z is formed in FP64 and
+ * its block-lower part removed by solving the block triangular Sylvester equation
+ * of the Newton step; the 1x1/2x2 block structure is the FP32 form's, and the 2x2
+ * blocks are finally put in standard form with _gs2x2! (GenericSchur.jl:716-803).
+ * Z is required.  info (may be NULL) receives 4 doubles: refinement iterations,
+ * final ||blocklower(Z^T A Z)||_F / ||A||_F, FP32-stage ms, refinement ms.
+ * When the refinement cannot reach FP64 accuracy (eigenvalues that FP32 does not
+ * separate, e.g. tight clusters relative to ||A||), the decomposition is recomputed
+ * by gs_schur_f64 from the untouched input and info[0] = -1; with GS_NOFALLBACK
+ * the call returns GS_UNCONVERGED instead. */
+GS_API int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
+                              double* wi, unsigned flags, int64_t maxiter, double* info);
 
 /* Hessenberg reduction with Q.  Replaces hessenberg!(A) (pirates.jl:232 ->
  * _hessenberg!, hessenberg.jl:3-17) and _materializeQ (hessenberg.jl:150-166):

@@ -63,3 +63,16 @@ def test_large_wantz_false(gs):
     S1 = gs.gschur(A)
     S0 = gs.gschur(A, wantZ=False)
     np.testing.assert_array_equal(S0.T, S1.T)
+
+
+@pytest.mark.parametrize("n", [129, 256])
+def test_large_complex_schur(gs, n):
+    # the plain CPU-runnable workload's law: one n x n ComplexF64 matrix, re/im iid N(0, 1/2)
+    rng = np.random.default_rng(9700 + n)
+    A = randn_matrix(rng, n, cplx=True)
+    S = gs.gschur(A)
+    from common import assert_schur_cplx
+    assert_schur_cplx(A, S.T, S.Z, S.values)
+    w_ref, tol = eig_tolerances(A, po)
+    ok, worst = match_eigenvalues(S.values, w_ref, tol)
+    assert ok, "worst err/tol %.3g" % worst
