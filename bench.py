@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="plain stream launches instead of the CUDA graph")
+    ap.add_argument("--no-large", action="store_true", help="skip the n=4096 FP64 vs mixed-precision timing")
+    ap.add_argument("--large-n", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -274,6 +276,11 @@ def run_ours(args):
             "algorithmic": "25 n^3 FLOP per matrix, summed over the batch (%.4g FLOP per launch)" % flops,
             "kernel_ms": kernel_ms}
     cpu = None if args.no_cpu else cpu_baseline_sample(args.count, SEED)
+    per_matrix = measure_per_matrix(ctx, packed, ns, offs)
+    large = None
+    if not args.no_large:
+        ctx.set_stream(None)
+        large = measure_large(ctx, torch, dev, args.large_n)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -281,10 +288,75 @@ def run_ours(args):
                       "l2": "inputs (%.0f MB of A per step) larger than L2; A restored from a pristine copy each "
                             "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-           "gpu_launches": 5 * args.steps, "unconverged": bad}
+           "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
+           "large": large}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_large(ctx, torch, dev, n):
+    """The second half of the metric: one n x n real Schur decomposition (iid N(0,1),
+    seed 1 for n=4096) by the plain FP64 path and by the FP32 + FP64-refinement path,
+    each through the C-ABI with host buffers (copies included), with its backward
+    error ||A - Z T Z^T||_F / ||A||_F and orthogonality ||Z^T Z - I||_F in units of
+    n eps (computed on the GPU in FP64 after the timed call)."""
+    import ctypes
+    import genericschur_gb300 as gs
+    from genericschur_gb300.workloads import large_real, LARGE_SEEDS
+    A = large_real(n)
+    eps = np.finfo(np.float64).eps
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).to(dev).T  # column-major view
+
+    def errors(S):
+        T = torch.from_numpy(np.ascontiguousarray(S.T.T)).to(dev).T
+        Z = torch.from_numpy(np.ascontiguousarray(S.Z.T)).to(dev).T
+        be = torch.linalg.norm(dA - Z @ T @ Z.T) / torch.linalg.norm(dA)
+        oe = torch.linalg.norm(Z.T @ Z - torch.eye(n, dtype=torch.float64, device=dev))
+        return float(be) / (n * eps), float(oe) / (n * eps)
+
+    out = {"n": n, "seed": LARGE_SEEDS.get(n, n), "entries": "iid N(0,1)"}
+    t = time.perf_counter()
+    S = gs.gschur(A, ctx=ctx)
+    out["fp64_s"] = time.perf_counter() - t
+    out["fp64_kernel_ms"] = ctx.last_kernel_ms()
+    out["fp64_backward_err_n_eps"], out["fp64_orth_err_n_eps"] = errors(S)
+    t = time.perf_counter()
+    S, info = gs.gschur_mixed(A, ctx=ctx, return_info=True)
+    out["mixed_s"] = time.perf_counter() - t
+    out["mixed_kernel_ms"] = ctx.last_kernel_ms()
+    out["mixed_backward_err_n_eps"], out["mixed_orth_err_n_eps"] = errors(S)
+    out["mixed_refinement"] = info
+    out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
+    out["flops_25n3"] = 25.0 * n ** 3
+    return out
+
+
+def measure_per_matrix(ctx, packed, ns, offs, sample=200):
+    """The plain FP64 path one matrix per call (gs_schur_f64 with device buffers,
+    synchronised per call) on the first `sample` matrices of the batch: what a caller
+    without the batched form gets, for comparison with the persistent batched launch."""
+    import torch
+    from genericschur_gb300 import _capi
+    dev = torch.device("cuda", torch.cuda.current_device())
+    m = min(sample, len(ns))
+    mats = [torch.from_numpy(packed[offs[b]:offs[b] + int(ns[b]) ** 2].copy()).to(dev) for b in range(m)]
+    Z = torch.empty(128 * 128, dtype=torch.float64, device=dev)
+    wr = torch.empty(128, dtype=torch.float64, device=dev)
+    wi = torch.empty(128, dtype=torch.float64, device=dev)
+    flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for b in range(m):
+        n = int(ns[b])
+        rc = ctx.lib.gs_schur_f64(ctx.handle, n, mats[b].data_ptr(), n, Z.data_ptr(), n, wr.data_ptr(), wi.data_ptr(),
+                                  flags, 0)
+        if rc not in (0, 1):
+            raise RuntimeError(ctx.last_error())
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    return {"value": m / dt, "unit": UNIT, "sample": "first %d matrices of the batch, one gs_schur_f64 call each "
+            "(device buffers)" % m}
 
 
 def measure_e2e(ctx, packed, ns, offs, woffs, steps):

@@ -13,10 +13,10 @@ constexpr double kFmin = 2.2250738585072014e-308;    // floatmin(Float64)
 constexpr double kSafemin = 2.2250738585072014e-308; // safemin(Float64) (util.jl:5-12)
 
 // Block reductions over the whole CTA.  `red` is shared scratch of >= 32 entries.
-template <int NT>
-__device__ __forceinline__ double block_max(double v, double* red) {
+template <int NT, class V>
+__device__ __forceinline__ V block_max(V v, V* red) {
   for (int o = 16; o > 0; o >>= 1) {
-    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    V w = __shfl_xor_sync(0xffffffffu, v, o);
     v = (w > v || w != w) ? w : v;
   }
   if constexpr (NT > 32) {
@@ -27,7 +27,7 @@ __device__ __forceinline__ double block_max(double v, double* red) {
     v = red[0];
 #pragma unroll
     for (int i = 1; i < NT / 32; ++i) {
-      double w = red[i];
+      V w = red[i];
       v = (w > v || w != w) ? w : v;
     }
     __syncthreads();
@@ -35,8 +35,8 @@ __device__ __forceinline__ double block_max(double v, double* red) {
   return v;
 }
 
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* red) {
+template <int NT, class V>
+__device__ __forceinline__ V block_sum(V v, V* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if constexpr (NT > 32) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -350,4 +350,41 @@ __device__ __forceinline__ double2 zreflector2_fast(double2& a, double2& x1) {
   a = make_double2(-copysign(s, a.x), 0.0);
   return tau;
 }
+}  // namespace gsk
+
+namespace gsk {
+// FP32 counterpart of reflector_fast for the FP32 stage of the mixed-precision form:
+// the same closed form with the hardware reciprocal square root and a correctly
+// rounded reciprocal; outside [1e-30, 1e30] the FP64 scaled path takes over.
+__device__ __forceinline__ float reflector_fast(float& a, float& x1, float& x2, int nr) {
+  if (nr < 3) x2 = 0.0f;
+  if (x1 == 0.0f && x2 == 0.0f) return 0.0f;
+  const float ss = fmaf(a, a, fmaf(x1, x1, x2 * x2));
+  if (!(ss > 1.0e-30f && ss < 1.0e30f)) {
+    double ad = a, x1d = x1, x2d = x2;
+    const double t = reflector_small(ad, x1d, x2d, nr);
+    a = (float)ad; x1 = (float)x1d; x2 = (float)x2d;
+    return (float)t;
+  }
+  const float y = rsqrtf(ss);
+  const float s = ss * y;
+  const float aa = fabsf(a);
+  const float tau = fmaf(aa, y, 1.0f);
+  const float t = copysignf(__frcp_rn(aa + s), a);
+  x1 *= t;
+  x2 *= t;
+  a = -copysignf(s, a);
+  return tau;
+}
+
+// Floating-point constants of the working precision.
+template <class T> struct Prec;
+template <> struct Prec<double> {
+  static constexpr double eps = 2.220446049250313e-16, fmin = 2.2250738585072014e-308;
+  static constexpr double safe_lo = 1.0e-150, safe_hi = 1.0e150;
+};
+template <> struct Prec<float> {
+  static constexpr float eps = 1.1920929e-07f, fmin = 1.17549435e-38f;
+  static constexpr float safe_lo = 1.0e-15f, safe_hi = 1.0e15f;
+};
 }  // namespace gsk

@@ -16,21 +16,23 @@ enum : int { ST_OK = 0, ST_UNCONVERGED = 1, ST_BADARG = 2, ST_CUDA = 3 };
 // A ragged batch of column-major matrices in one packed buffer.  Matrix b has
 // order ns[b] and starts at element offs[b] of A and Z; its eigenvalues start at
 // woffs[b].  All pointers are device pointers.
-struct RealBatch {
+template <class T, class W = double>
+struct RealBatchT {
   int count;
   const int* ns;
   const long long* offs;
   const long long* woffs;
-  double* A;       // in: A; out: T (quasi-triangular, standard form)
-  double* Z;       // out: Schur vectors (ignored when wantz == 0)
-  double* wr;      // out: real parts of the eigenvalues
-  double* wi;      // out: imaginary parts
+  T* A;            // in: A; out: T (quasi-triangular, standard form)
+  T* Z;            // out: Schur vectors (ignored when wantz == 0)
+  W* wr;           // out: real parts of the eigenvalues
+  W* wi;           // out: imaginary parts
   int* status;     // out: ST_OK / ST_UNCONVERGED per matrix
   int wantz;
   int scale;
   int maxiter_mult;  // maxiter = maxiter_mult * n (reference default 100)
   long long maxiter_abs;  // when > 0, overrides maxiter_mult
 };
+using RealBatch = RealBatchT<double>;
 
 struct CplxBatch {
   int count;
@@ -69,6 +71,12 @@ struct EigBatch {
   const int* colmap;       // optional: output column of eigenvector ki is colmap[woffs[b] + ki - 1]
 };
 size_t eigvecs_smem_bytes(int nmax);
+// One matrix of any order (eigvecs_large.cu): workspace of eigvecs_large_ws_elems(n)
+// complex elements; cmap (optional) scatters eigenvector ki to column cmap[ki]; bad[0]
+// counts columns that overflowed.
+size_t eigvecs_large_ws_elems(int n);
+cudaError_t launch_eigvecs_large(int n, const double2* T, const double2* Z, double2* VR, double2* VL, int normalize,
+                                 const int* cmap, double2* ws, int* bad, cudaStream_t s);
 cudaError_t launch_eigvecs_batched(const EigBatch& eb, int nmax, int num_sms, cudaStream_t s);
 
 // Real quasi-triangular -> complex triangular Schur pairs (triang.jl:9-43).
@@ -123,6 +131,25 @@ cudaError_t launch_gemm(int m, int p, int q, const T* A, int lda, int transA, co
 size_t hess_large_ws_elems(int n);
 template <class T> cudaError_t hessenberg_large(int n, T* A, int lda, T* Z, int ldz, T* tau_out, T* ws, cudaStream_t s);
 
+// Aggressive early deflation on the trailing window of the active block (aed.cu).
+template <class T>
+struct AedArgs {
+  T* H;                   // n x n, ld n
+  int n;
+  int ilo;                // active block start (1-based)
+  int kwtop;              // window start (1-based); the window ends at ihi = kwtop + nw - 1
+  int nw;
+  const T* Tw;            // real Schur form of the window (nw x nw, ld nw)
+  T* V;                   // its Schur vectors; updated in place to the window's final transform
+  const int* win_status;  // status of the window's Schur decomposition
+  double* ewr;            // eigenvalues of the window's diagonal blocks (nw)
+  double* ewi;
+  double* wr;             // eigenvalue outputs of the whole matrix (deflated ones written)
+  double* wi;
+  int* out;               // [undeflated count, deflated count, H modified]
+};
+template <class T> cudaError_t launch_aed(const AedArgs<T>& g, cudaStream_t s);
+
 // One large real Schur decomposition (schur_large_host.cu).
 template <class T>
 struct LargeRun {
@@ -139,11 +166,15 @@ struct LargeRun {
   cudaError_t cuda_error;
   int bulges;      // bulges per chain (<= kMaxBulges; 0: default)
   int chunk;       // chase steps per chunk (<= 64; 0: default)
+  int shift_fp32;  // compute the sweep shifts with the FP32 small-matrix kernel
+  int aedw;        // aggressive-early-deflation window (<= 128; 0: off)
 };
 size_t schur_large_ws_bytes(int n, size_t tsize);
-// Tuning of the large path: GS_LARGE_BULGES / GS_LARGE_CHUNK environment variables
-// (read once per call), else the built-in defaults.
-void large_tuning(int n, int* bulges, int* chunk);
+// Tuning of the large path: GS_LARGE_BULGES / GS_LARGE_CHUNK / GS_LARGE_AEDW environment
+// variables (read once per call), else the built-in defaults for element size tsize.
+void large_tuning(int n, int* bulges, int* chunk, int* aedw, size_t tsize);
+// GS_LARGE_SHIFT32=1: shifts of the FP64 path from the FP32 small-matrix kernel.
+int large_shift_fp32();
 template <class T> int schur_large_run(LargeRun<T>& r);  // ST_OK, ST_UNCONVERGED, or -1 (cuda_error set)
 
 // Host copy of the safescale! factor sequence (util.jl:41-80, as written there).
@@ -173,6 +204,7 @@ cudaError_t launch_sylv_wave(int n, int N, int d, const double* At, const double
                              const int* bs, const int* bz, double floor, cudaStream_t s);
 cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s);
 cudaError_t launch_transpose(int n, const double* A, double* B, cudaStream_t s);
+cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s);
 cudaError_t launch_lower_norm(int n, const double* At, const int* blk, double* out, int num_sms, cudaStream_t s);
 cudaError_t launch_block_triu(int n, const double* At, const int* blk, double* T, cudaStream_t s);
 cudaError_t launch_std_blocks(int n, int N, const int* bs, const int* bz, double* T, double* Z, double* cs_sn,
@@ -190,7 +222,11 @@ __host__ __device__ constexpr int bin_max(int bin) { return 32 * (bin + 1); }  /
 // order first inside a bin; sched[] receives the bin ranges and zeroed counters.
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s);
 
-cudaError_t launch_schur_batched_real(const RealBatch& bt, const int* order, int* sched,
+// T = double: the FP64 batched kernel; T = float: the same algorithm in FP32 (the
+// Float32 entry points and the FP32 stage of the mixed-precision form).  W is the
+// type of the eigenvalue outputs.
+template <class T, class W>
+cudaError_t launch_schur_batched_real(const RealBatchT<T, W>& bt, const int* order, int* sched,
                                       int num_sms, cudaStream_t* streams, int nstreams);
 cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched,
                                       int num_sms, cudaStream_t* streams, int nstreams);

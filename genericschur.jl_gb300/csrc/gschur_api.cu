@@ -186,7 +186,9 @@ int gs_host_free(gs_context* ctx, void* ptr) {
 // ---------------------------------------------------------------------------
 // batched real
 // ---------------------------------------------------------------------------
-static int run_batched_real(gs_context* ctx, const RealBatch& bt, int* order, int* sched, unsigned flags,
+}  // extern "C"
+template <class T, class W>
+static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* order, int* sched, unsigned flags,
                             bool use_graph, const std::vector<long long>& key) {
   auto enqueue = [&](cudaStream_t s) -> int {
     cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, s);
@@ -220,9 +222,9 @@ static int run_batched_real(gs_context* ctx, const RealBatch& bt, int* order, in
   return GS_OK;
 }
 
-int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
-                         const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
-                         int32_t* status, unsigned flags) {
+template <class T>
+static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                   const int64_t* woffs, T* A, T* Z, T* wr, T* wi, int32_t* status, unsigned flags) {
   if (!ctx) return GS_BADARG;
   ctx->err.clear();
   if (count < 0 || count > (1LL << 30)) return set_err(ctx, GS_BADARG, "bad count %lld", (long long)count);
@@ -232,7 +234,7 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
     return set_err(ctx, GS_BADARG, "null array argument");
   CK(cudaSetDevice(ctx->device));
   const bool dev = flags & GS_DEVICE;
-  RealBatch bt{};
+  RealBatchT<T, T> bt{};
   bt.count = (int)count;
   bt.wantz = wantz;
   bt.scale = (flags & GS_SCALE) ? 1 : 0;
@@ -253,10 +255,10 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
   const size_t o_sched = ar.take<int>(3 * kNumBins);
   size_t o_A = 0, o_Z = 0, o_wr = 0, o_wi = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
   if (!dev) {
-    o_A = ar.take<double>(na);
-    o_Z = ar.take<double>(wantz ? na : 1);
-    o_wr = ar.take<double>(nw);
-    o_wi = ar.take<double>(nw);
+    o_A = ar.take<T>(na);
+    o_Z = ar.take<T>(wantz ? na : 1);
+    o_wr = ar.take<T>(nw);
+    o_wi = ar.take<T>(nw);
     o_ns = ar.take<int>(count);
     o_offs = ar.take<long long>(count);
     o_woffs = ar.take<long long>(count);
@@ -272,15 +274,15 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
     bt.ns = (const int*)(base + o_ns);
     bt.offs = (const long long*)(base + o_offs);
     bt.woffs = (const long long*)(base + o_woffs);
-    bt.A = (double*)(base + o_A);
-    bt.Z = wantz ? (double*)(base + o_Z) : nullptr;
-    bt.wr = (double*)(base + o_wr);
-    bt.wi = (double*)(base + o_wi);
+    bt.A = (T*)(base + o_A);
+    bt.Z = wantz ? (T*)(base + o_Z) : nullptr;
+    bt.wr = (T*)(base + o_wr);
+    bt.wi = (T*)(base + o_wi);
     bt.status = (int*)(base + o_st);
     CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(bt.A, A, sizeof(double) * na, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(bt.A, A, sizeof(T) * na, cudaMemcpyHostToDevice, s));
   } else {
     bt.ns = ns;
     bt.offs = (const long long*)offs;
@@ -291,16 +293,16 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
     bt.wi = wi;
     bt.status = status;
   }
-  std::vector<long long> key = {1, (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
+  std::vector<long long> key = {(long long)sizeof(T), (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
                                 (long long)(uintptr_t)bt.ns, (long long)(uintptr_t)bt.wr,
                                 (long long)(uintptr_t)order, (long long)flags};
   rc = run_batched_real(ctx, bt, order, sched, flags, (flags & GS_GRAPH) != 0, key);
   if (rc) return rc;
   if (dev) return GS_OK;
-  CK(cudaMemcpyAsync(A, bt.A, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
-  if (wantz) CK(cudaMemcpyAsync(Z, bt.Z, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(wr, bt.wr, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(wi, bt.wi, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(A, bt.A, sizeof(T) * na, cudaMemcpyDeviceToHost, s));
+  if (wantz) CK(cudaMemcpyAsync(Z, bt.Z, sizeof(T) * na, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wr, bt.wr, sizeof(T) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wi, bt.wi, sizeof(T) * nw, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(status, bt.status, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   for (int64_t b = 0; b < count; ++b)
@@ -308,30 +310,46 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
   return GS_OK;
 }
 
+extern "C" {
+int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
+                         int32_t* status, unsigned flags) {
+  return schur_batched_real_impl<double>(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
+}
+
+int gs_schur_batched_f32(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                         const int64_t* woffs, float* A, float* Z, float* wr, float* wi,
+                         int32_t* status, unsigned flags) {
+  return schur_batched_real_impl<float>(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
+}
+
 // ---------------------------------------------------------------------------
 // large real matrix (n > 128): whole-GPU Hessenberg + multishift QR
 // ---------------------------------------------------------------------------
-static int schur_large_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
-                           double* wi, unsigned flags, int64_t maxiter) {
+}  // extern "C"
+template <class T>
+static int schur_large_impl(gs_context* ctx, int64_t n, T* A, int64_t lda, T* Z, int64_t ldz, T* wr, T* wi,
+                            unsigned flags, int64_t maxiter) {
   if (n > (1 << 16)) return set_err(ctx, GS_BADARG, "order %lld too large", (long long)n);
   const bool wantz = flags & GS_WANTZ;
   const bool dev = flags & GS_DEVICE;
   const size_t nn = (size_t)n * n;
   Arena ar;
-  const size_t o_A = ar.take<double>(nn), o_Z = ar.take<double>(wantz ? nn : 1);
+  const size_t o_A = ar.take<T>(nn), o_Z = ar.take<T>(wantz ? nn : 1);
   const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n);
-  const size_t o_ws = ar.take<char>(schur_large_ws_bytes((int)n, sizeof(double)));
+  const size_t o_w32 = ar.take<T>(2 * n);
+  const size_t o_ws = ar.take<char>(schur_large_ws_bytes((int)n, sizeof(T)));
   int rc = ensure_ws(ctx, ar.off);
   if (rc) return rc;
   char* base = ctx->dws;
   cudaStream_t s = ctx->stream;
   const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  double* dA = (double*)(base + o_A);
-  CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
-  LargeRun<double> r{};
+  T* dA = (T*)(base + o_A);
+  CK(cudaMemcpy2DAsync(dA, n * sizeof(T), A, lda * sizeof(T), n * sizeof(T), n, in, s));
+  LargeRun<T> r{};
   r.A = dA;
-  r.Z = wantz ? (double*)(base + o_Z) : nullptr;
+  r.Z = wantz ? (T*)(base + o_Z) : nullptr;
   r.wr = (double*)(base + o_wr);
   r.wi = (double*)(base + o_wi);
   r.n = (int)n;
@@ -341,16 +359,21 @@ static int schur_large_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, d
   r.num_sms = ctx->num_sms;
   r.stream = s;
   r.cuda_error = cudaSuccess;
-  large_tuning((int)n, &r.bulges, &r.chunk);
+  large_tuning((int)n, &r.bulges, &r.chunk, &r.aedw, sizeof(T));
+  r.shift_fp32 = sizeof(T) == 8 ? large_shift_fp32() : 0;
   CK(cudaEventRecord(ctx->t0, s));
-  const int st = schur_large_run<double>(r);
+  const int st = schur_large_run<T>(r);
   if (st < 0) return set_err(ctx, GS_CUDA, "large Schur path: %s", cudaGetErrorString(r.cuda_error));
   CK(cudaEventRecord(ctx->t1, s));
   ctx->timed = true;
-  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
-  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(double), r.Z, n * sizeof(double), n * sizeof(double), n, out, s));
-  CK(cudaMemcpyAsync(wr, r.wr, n * sizeof(double), out, s));
-  CK(cudaMemcpyAsync(wi, r.wi, n * sizeof(double), out, s));
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(T), dA, n * sizeof(T), n * sizeof(T), n, out, s));
+  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(T), r.Z, n * sizeof(T), n * sizeof(T), n, out, s));
+  // eigenvalues are produced in FP64; the element type's copy is made on the device
+  T* w32 = (T*)(base + o_w32);
+  CK(convert_array<double, T>(r.wr, w32, n, 1.0, s));
+  CK(convert_array<double, T>(r.wi, w32 + n, n, 1.0, s));
+  CK(cudaMemcpyAsync(wr, w32, n * sizeof(T), out, s));
+  CK(cudaMemcpyAsync(wi, w32 + n, n * sizeof(T), out, s));
   CK(cudaStreamSynchronize(s));
   if (st != ST_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit reached");
   return GS_OK;
@@ -359,8 +382,9 @@ static int schur_large_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, d
 // ---------------------------------------------------------------------------
 // single real matrix: n <= 128 runs as a batch of one
 // ---------------------------------------------------------------------------
-int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
-                 double* wi, unsigned flags, int64_t maxiter) {
+template <class T>
+static int schur_real_impl(gs_context* ctx, int64_t n, T* A, int64_t lda, T* Z, int64_t ldz, T* wr, T* wi,
+                           unsigned flags, int64_t maxiter) {
   if (!ctx) return GS_BADARG;
   ctx->err.clear();
   const bool wantz = flags & GS_WANTZ;
@@ -370,11 +394,11 @@ int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   if (n == 0) return GS_OK;
   if (!A || !wr || !wi || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
   CK(cudaSetDevice(ctx->device));
-  if (n > kSmallMax) return schur_large_f64(ctx, n, A, lda, Z, ldz, wr, wi, flags, maxiter);
+  if (n > kSmallMax) return schur_large_impl<T>(ctx, n, A, lda, Z, ldz, wr, wi, flags, maxiter);
   const bool dev = flags & GS_DEVICE;
   Arena ar;
-  const size_t o_A = ar.take<double>(n * n), o_Z = ar.take<double>(n * n);
-  const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n);
+  const size_t o_A = ar.take<T>(n * n), o_Z = ar.take<T>(n * n);
+  const size_t o_wr = ar.take<T>(n), o_wi = ar.take<T>(n);
   const size_t o_meta = ar.take<long long>(4), o_st = ar.take<int>(2);
   const size_t o_order = ar.take<int>(1), o_sched = ar.take<int>(3 * kNumBins);
   int rc = ensure_ws(ctx, ar.off);
@@ -383,23 +407,23 @@ int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   cudaStream_t s = ctx->stream;
   const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  double* dA = (double*)(base + o_A);
-  double* dZ = (double*)(base + o_Z);
-  CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
+  T* dA = (T*)(base + o_A);
+  T* dZ = (T*)(base + o_Z);
+  CK(cudaMemcpy2DAsync(dA, n * sizeof(T), A, lda * sizeof(T), n * sizeof(T), n, in, s));
   long long meta_h[4] = {0, 0, 0, 0};  // offs, woffs, n (as int in first half of [2])
   int n32 = (int)n;
   long long* meta = (long long*)(base + o_meta);
   CK(cudaMemcpyAsync(meta, meta_h, sizeof(meta_h), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(meta + 2, &n32, sizeof(int), cudaMemcpyHostToDevice, s));
-  RealBatch bt{};
+  RealBatchT<T, T> bt{};
   bt.count = 1;
   bt.ns = (const int*)(meta + 2);
   bt.offs = meta;
   bt.woffs = meta + 1;
   bt.A = dA;
   bt.Z = wantz ? dZ : nullptr;
-  bt.wr = (double*)(base + o_wr);
-  bt.wi = (double*)(base + o_wi);
+  bt.wr = (T*)(base + o_wr);
+  bt.wi = (T*)(base + o_wi);
   bt.status = (int*)(base + o_st);
   bt.wantz = wantz;
   bt.scale = (flags & GS_SCALE) ? 1 : 0;
@@ -408,15 +432,26 @@ int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   bt.maxiter_abs = mi;
   rc = run_batched_real(ctx, bt, (int*)(base + o_order), (int*)(base + o_sched), flags, false, {});
   if (rc) return rc;
-  CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
-  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(double), dZ, n * sizeof(double), n * sizeof(double), n, out, s));
-  CK(cudaMemcpyAsync(wr, bt.wr, n * sizeof(double), out, s));
-  CK(cudaMemcpyAsync(wi, bt.wi, n * sizeof(double), out, s));
+  CK(cudaMemcpy2DAsync(A, lda * sizeof(T), dA, n * sizeof(T), n * sizeof(T), n, out, s));
+  if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * sizeof(T), dZ, n * sizeof(T), n * sizeof(T), n, out, s));
+  CK(cudaMemcpyAsync(wr, bt.wr, n * sizeof(T), out, s));
+  CK(cudaMemcpyAsync(wi, bt.wi, n * sizeof(T), out, s));
   int st = 0;
   CK(cudaMemcpyAsync(&st, bt.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (st != GS_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit %lld reached", mi);
   return GS_OK;
+}
+
+extern "C" {
+int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
+                 double* wi, unsigned flags, int64_t maxiter) {
+  return schur_real_impl<double>(ctx, n, A, lda, Z, ldz, wr, wi, flags, maxiter);
+}
+
+int gs_schur_f32(gs_context* ctx, int64_t n, float* A, int64_t lda, float* Z, int64_t ldz, float* wr, float* wi,
+                 unsigned flags, int64_t maxiter) {
+  return schur_real_impl<float>(ctx, n, A, lda, Z, ldz, wr, wi, flags, maxiter);
 }
 
 // ---------------------------------------------------------------------------
@@ -737,11 +772,100 @@ int eigvecs_driver(gs_context* ctx, int64_t count, const int32_t* ns, const int6
 
 }  // namespace
 
+// One matrix of order > 128: tiled back-substitution (eigvecs_large.cu); real input is
+// triangularised first.
+static int eigvecs_large_driver(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
+                                unsigned flags, bool real) {
+  if (!T || (!VR && !VL)) return set_err(ctx, GS_BADARG, "null array argument");
+  if (n > (1 << 16)) return set_err(ctx, GS_BADARG, "order %lld too large", (long long)n);
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  const size_t es = real ? sizeof(double) : sizeof(double2);
+  Arena ar;
+  const size_t o_ws = ar.take<double2>(eigvecs_large_ws_elems((int)n));
+  const size_t o_bad = ar.take<int>(4);
+  size_t o_T = 0, o_Z = 0, o_VR = 0, o_VL = 0, o_Tc = 0, o_Zc = 0, o_map = 0, o_meta = 0;
+  if (real) {
+    o_Tc = ar.take<double2>(nn);
+    o_Zc = ar.take<double2>(Z ? nn : 1);
+    o_map = ar.take<int>(n);
+    o_meta = ar.take<long long>(4);
+  }
+  if (!dev) {
+    o_T = ar.take<char>(es * nn);
+    o_Z = ar.take<char>(Z ? es * nn : 1);
+    o_VR = ar.take<double2>(VR ? nn : 1);
+    o_VL = ar.take<double2>(VL ? nn : 1);
+  }
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const void* d_T = T;
+  const void* d_Z = Z;
+  double2* d_VR = (double2*)VR;
+  double2* d_VL = (double2*)VL;
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_T, T, es * nn, cudaMemcpyHostToDevice, s));
+    if (Z) CK(cudaMemcpyAsync(base + o_Z, Z, es * nn, cudaMemcpyHostToDevice, s));
+    d_T = base + o_T;
+    d_Z = Z ? (const void*)(base + o_Z) : nullptr;
+    d_VR = VR ? (double2*)(base + o_VR) : nullptr;
+    d_VL = VL ? (double2*)(base + o_VL) : nullptr;
+  }
+  int* bad = (int*)(base + o_bad);
+  CK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  CK(cudaEventRecord(ctx->t0, s));
+  const double2* cT = (const double2*)d_T;
+  const double2* cZ = (const double2*)d_Z;
+  const int* cmap = nullptr;
+  if (real) {
+    long long meta_h[4] = {0, 0, 0, 0};
+    int n32 = (int)n;
+    long long* meta = (long long*)(base + o_meta);
+    CK(cudaMemcpyAsync(meta, meta_h, sizeof(meta_h), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(meta + 2, &n32, sizeof(int), cudaMemcpyHostToDevice, s));
+    TriBatch tb{};
+    tb.count = 1;
+    tb.ns = (const int*)(meta + 2);
+    tb.offs = meta;
+    tb.woffs = meta + 1;
+    tb.Tr = (const double*)d_T;
+    tb.Zr = (const double*)d_Z;
+    tb.Tc = (double2*)(base + o_Tc);
+    tb.Zc = d_Z ? (double2*)(base + o_Zc) : nullptr;
+    tb.w = nullptr;
+    tb.colmap = (int*)(base + o_map);
+    cudaError_t e = launch_triangularize(tb, ctx->num_sms, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "triangularize launch: %s", cudaGetErrorString(e));
+    cT = tb.Tc;
+    cZ = tb.Zc;
+    cmap = tb.colmap;
+  }
+  cudaError_t e = launch_eigvecs_large((int)n, cT, cZ, d_VR, d_VL, !(flags & GS_RAW), cmap,
+                                       (double2*)(base + o_ws), bad, s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "eigenvector kernels: %s", cudaGetErrorString(e));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  int nbad = 0;
+  CK(cudaMemcpyAsync(&nbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!dev) {
+    if (VR) CK(cudaMemcpyAsync(VR, d_VR, sizeof(double2) * nn, cudaMemcpyDeviceToHost, s));
+    if (VL) CK(cudaMemcpyAsync(VL, d_VL, sizeof(double2) * nn, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (nbad) return set_err(ctx, GS_UNCONVERGED, "%d eigenvector columns overflowed (no rescaling for n > %d)", nbad,
+                           kSmallMax);
+  return GS_OK;
+}
+
 int gs_eigvecs_c64(gs_context* ctx, int64_t n, const double* T, const double* Z, double* VR, double* VL,
                    unsigned flags) {
   if (!ctx) return GS_BADARG;
   ctx->err.clear();
-  if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld outside [0, %d]", (long long)n, kSmallMax);
+  if (n > kSmallMax) return eigvecs_large_driver(ctx, n, T, Z, VR, VL, flags, false);
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
   if (n == 0) return GS_OK;
   if (flags & GS_DEVICE) return set_err(ctx, GS_BADARG, "gs_eigvecs_c64 with GS_DEVICE: use gs_eigvecs_batched_c64");
   const int32_t n32 = (int32_t)n;
@@ -753,7 +877,8 @@ int gs_eigvecs_f64(gs_context* ctx, int64_t n, const double* T, const double* Z,
                    unsigned flags) {
   if (!ctx) return GS_BADARG;
   ctx->err.clear();
-  if (n < 0 || n > kSmallMax) return set_err(ctx, GS_BADARG, "order %lld outside [0, %d]", (long long)n, kSmallMax);
+  if (n > kSmallMax) return eigvecs_large_driver(ctx, n, T, Z, VR, VL, flags, true);
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
   if (n == 0) return GS_OK;
   if (flags & GS_DEVICE) return set_err(ctx, GS_BADARG, "gs_eigvecs_f64 with GS_DEVICE: use gs_eigvecs_batched_f64");
   const int32_t n32 = (int32_t)n;
@@ -1038,7 +1163,8 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   r.num_sms = ctx->num_sms;
   r.stream = s;
   r.cuda_error = cudaSuccess;
-  large_tuning(N32, &r.bulges, &r.chunk);
+  large_tuning(N32, &r.bulges, &r.chunk, &r.aedw, sizeof(float));
+  r.shift_fp32 = 0;
   const int st = schur_large_run<float>(r);
   if (st < 0) return set_err(ctx, GS_CUDA, "FP32 Schur stage: %s", cudaGetErrorString(r.cuda_error));
   if (st != ST_OK) return set_err(ctx, GS_UNCONVERGED, "FP32 Schur stage: iteration limit reached");
@@ -1070,12 +1196,22 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   auto gemm = [&](int m, int p, int q, const double* Am, int la, int tA, const double* Bm, int lb, double* Cm, int lc) {
     return launch_gemm<double>(m, p, q, Am, la, tA, Bm, lb, Cm, lc, s);
   };
+  // Z <- Z + Z X for a small correction X (|X| <= ~1e-6): the product only needs first-order
+  // accuracy, so it runs as an FP32 GEMM (Z and X rounded to FP32 into the FP32 stage's
+  // buffers, the product into T2's storage) and is added to the FP64 Z.
+  float* P32 = (float*)T2;
+  auto add_product = [&](const double* X) -> cudaError_t {
+    cudaError_t e = convert_array<double, float>(dZ, Z32, nn, 1.0, s);
+    if (e == cudaSuccess) e = convert_array<double, float>(X, A32, nn, 1.0, s);
+    if (e == cudaSuccess) e = launch_gemm<float>(N32, N32, N32, Z32, N32, 0, A32, N32, P32, N32, s);
+    if (e == cudaSuccess) e = launch_add_f32(dZ, P32, nn, s);
+    return e;
+  };
   auto ns_step = [&]() -> cudaError_t {
-    // Z <- Z (1.5 I - 0.5 Z^T Z)
+    // Newton-Schulz: Z <- Z (1.5 I - 0.5 Z^T Z) = Z + Z E with E = (I - Z^T Z) / 2; Z^T Z in FP64
     cudaError_t e = gemm(N32, N32, N32, dZ, N32, 1, dZ, N32, T1, N32);
     if (e == cudaSuccess) e = launch_refine_elementwise(2, N32, nullptr, T1, 0.0, s);
-    if (e == cudaSuccess) e = gemm(N32, N32, N32, dZ, N32, 0, T1, N32, T2, N32);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dZ, T2, nn * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = add_product(T1);
     return e;
   };
   auto form_At = [&]() -> cudaError_t {
@@ -1085,9 +1221,9 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
     return e;
   };
   CK(convert_array<float, double>(Z32, dZ, nn, 1.0, s));
-  // two Newton-Schulz steps take the FP32 factor's orthogonality error (~1e-6) below eps
+  // one Newton-Schulz step takes the FP32 factor's orthogonality error e (~1e-6) to
+  // ~e^2; the step after the first correction (always taken, |S| ~ 1e-6) finishes it
   cudaError_t e = ns_step();
-  if (e == cudaSuccess) e = ns_step();
   if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "orthonormalisation: %s", cudaGetErrorString(e));
   // Convergence: the residual reaches the rounding level of forming Z^T A Z, or it stops
   // shrinking (Newton converges quadratically, so a step that gains less than 4x is at
@@ -1123,13 +1259,13 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
     for (int d = 0; d <= NB - 2 && e == cudaSuccess; ++d) e = launch_sylv_wave(N32, NB, d, T1, T2, W, Wt, dbs, dbz, floor, s);
     double wn[2] = {0.0, 0.0};
     if (e == cudaSuccess) e = launch_lower_norm(N32, W, dblk, nrm + 2, ctx->num_sms, s);
-    if (e == cudaSuccess) e = launch_refine_elementwise(0, N32, W, T3, 1.0, s);  // T3 = I + S
-    if (e == cudaSuccess) e = gemm(N32, N32, N32, dZ, N32, 0, T3, N32, T2, N32);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dZ, T2, nn * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = launch_refine_elementwise(0, N32, W, T3, 0.0, s);  // T3 = S
+    if (e == cudaSuccess) e = add_product(T3);                                     // Z <- Z (I + S)
     if (e == cudaSuccess) e = cudaMemcpyAsync(wn, nrm + 2, sizeof(wn), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    // Z (I + S) departs from orthogonality by |S|^2: re-orthonormalise unless that is below eps
-    if (e == cudaSuccess && !(std::sqrt(wn[1]) <= 1e-8)) e = ns_step();
+    // Z (I + S) departs from orthogonality by |S|^2: re-orthonormalise after the first
+    // correction and whenever |S|^2 is above eps
+    if (e == cudaSuccess && (its == 1 || !(std::sqrt(wn[1]) <= 1e-8))) e = ns_step();
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "refinement step: %s", cudaGetErrorString(e));
   }
   if (!conv) {

@@ -14,6 +14,8 @@
 // lanes split the two sums, lane 0 solves the (<= 4 x 4) Kronecker system of the pair.
 // Z is then updated to Z (I + S), which departs from orthogonality by O(|S|^2); a
 // Newton-Schulz step Z <- Z (3 I - Z^T Z) / 2 follows whenever |S| is above 1e-8.
+// Products with the small corrections S and (I - Z^T Z)/2 run in FP32 (their error is
+// second order); Z^T A Z and Z^T Z, whose small parts are the signal, run in FP64.
 #include "device_common.cuh"
 #include "gs_internal.h"
 
@@ -114,12 +116,18 @@ __global__ void k_exp2(int n, const double* __restrict__ S, double* __restrict__
   S2[idx] = (i == j ? 1.0 : 0.0) + S[idx] + 0.5 * S2[idx];
 }
 
-// Newton-Schulz factor: X <- 1.5 I - 0.5 X
+// Newton-Schulz correction: X <- (I - X) / 2  (X = Z^T Z on entry)
 __global__ void k_ns_factor(int n, double* X) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)n * n) return;
   const int i = idx % n, j = idx / n;
-  X[idx] = (i == j ? 1.5 : 0.0) - 0.5 * X[idx];
+  X[idx] = (i == j ? 0.5 : 0.0) - 0.5 * X[idx];
+}
+
+// Z += P (P an FP32 product)
+__global__ void k_add_f32(double* __restrict__ Z, const float* __restrict__ P, size_t cnt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
+    Z[i] += (double)P[i];
 }
 
 // transpose
@@ -249,6 +257,11 @@ cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b,
     case 2: k_ns_factor<<<g, 256, 0, s>>>(n, b); break;
     default: break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s) {
+  k_add_f32<<<1024, 256, 0, s>>>(Z, P, cnt);
   return cudaGetLastError();
 }
 

@@ -27,17 +27,7 @@ template <class T> __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x
 // Real reflector of length 2/3 in type T (householder.jl:12-54 semantics).
 template <class T>
 __device__ __forceinline__ T refl_t(T& a, T& x1, T& x2, int nr) {
-  if constexpr (sizeof(T) == 8) {
-    return reflector_fast(a, x1, x2, nr);
-  } else {
-    if (nr < 3) x2 = T(0);
-    const T xs = fmaf(x1, x1, x2 * x2);
-    if (xs == T(0)) return T(0);
-    double ad = a, x1d = x1, x2d = x2;  // float inputs: the scaled double path is exact enough
-    const double t = reflector_small(ad, x1d, x2d, nr);
-    a = (T)ad; x1 = (T)x1d; x2 = (T)x2d;
-    return (T)t;
-  }
+  return reflector_fast(a, x1, x2, nr);
 }
 
 }  // namespace

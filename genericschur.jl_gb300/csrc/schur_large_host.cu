@@ -74,11 +74,23 @@ cudaError_t copy2d(int m, int p, const S* src, int lds, D* dst, int ldd, cudaStr
 
 }  // namespace
 
-void large_tuning(int n, int* bulges, int* chunk) {
+void large_tuning(int n, int* bulges, int* chunk, int* aedw, size_t tsize) {
   const char* b = std::getenv("GS_LARGE_BULGES");
   const char* c = std::getenv("GS_LARGE_CHUNK");
+  const char* w = std::getenv("GS_LARGE_AEDW");
   *bulges = b ? std::max(1, std::min(kMaxBulges, std::atoi(b))) : (n >= 1024 ? 16 : 12);
   *chunk = c ? std::max(1, std::min(64, std::atoi(c))) : 16;
+  // The window's Schur form costs one small-matrix solve per deflation step; in FP64
+  // its latency limits the useful window to about two shifts' worth (measured on GB300:
+  // 32 at n <= 2048, 48 at n = 4096), in FP32 the solve is cheap and a wider window
+  // deflates more.
+  const int wdef = tsize == 4 ? 64 : (n >= 3072 ? 48 : 32);
+  *aedw = w ? std::max(0, std::min(kSmallMax, std::atoi(w))) : wdef;
+}
+
+int large_shift_fp32() {
+  const char* f = std::getenv("GS_LARGE_SHIFT32");
+  return f ? (std::atoi(f) != 0) : 0;
 }
 
 cudaError_t launch_absmax(const double* A, size_t cnt, unsigned long long* out, int num_sms, cudaStream_t s) {
@@ -95,6 +107,7 @@ size_t schur_large_ws_bytes(int n, size_t tsize) {
   b += tsize * 4 * kMaxBulges + 256;                                        // shifts
   b += 3 * sizeof(double) * nb * nb + 4 * sizeof(double) * nb + 1024;       // small solve blk, U, wr, wi, meta
   b += sizeof(int) * (nb + 3 * kNumBins + 8) + 256;                         // order/sched/status/scan
+  b += 2 * sizeof(double) * nb + sizeof(int) * 4 + 512;                      // AED eigenvalues, results
   b += tsize * (size_t)n * nb * 2 + tsize * nb * nb + 512;                  // GEMM temporaries, U in T
   return b + 16 * 256;
 }
@@ -120,8 +133,9 @@ int schur_large_run(LargeRun<T>& r) {
   T* logr = (T*)take(sizeof(T) * 64 * kMaxBulges * 5);
   T* dshift = (T*)take(sizeof(T) * 4 * kMaxBulges);
   const int nb = kSmallMax;
-  double* blk = (double*)take(sizeof(double) * nb * nb);
-  double* U = (double*)take(sizeof(double) * nb * nb);
+  T* blk = (T*)take(sizeof(T) * nb * nb);
+  T* U = (T*)take(sizeof(T) * nb * nb);
+  float* blk32 = (float*)take(sizeof(float) * nb * nb);
   double* bwr = (double*)take(sizeof(double) * nb);
   double* bwi = (double*)take(sizeof(double) * nb);
   long long* meta = (long long*)take(sizeof(long long) * 4);
@@ -131,8 +145,10 @@ int schur_large_run(LargeRun<T>& r) {
   int* dscan = (int*)take(sizeof(int) * 4);
   T* tmp = (T*)take(sizeof(T) * (size_t)n * nb);
   T* tmp2 = (T*)take(sizeof(T) * (size_t)n * nb);
-  T* Ut = (T*)take(sizeof(T) * nb * nb);
   unsigned long long* dmax = (unsigned long long*)take(sizeof(unsigned long long) * 2);
+  double* aewr = (double*)take(sizeof(double) * nb);
+  double* aewi = (double*)take(sizeof(double) * nb);
+  int* aout = (int*)take(sizeof(int) * 4);
   T* H = r.A;
   T* Z = r.Z;
   const size_t nn = (size_t)n * n;
@@ -147,7 +163,7 @@ int schur_large_run(LargeRun<T>& r) {
     CKL(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
     CKL(cudaStreamSynchronize(s));
     std::memcpy(&amax, &bits, sizeof(amax));
-    const double smlnum = std::sqrt(2.2250738585072014e-308) / 2.220446049250313e-16;
+    const double smlnum = std::sqrt((double)Prec<T>::fmin) / (double)Prec<T>::eps;
     const double bignum = 1.0 / smlnum;
     if (amax > 0.0 && amax < smlnum) { scaled = true; cscale = smlnum; }
     else if (amax > bignum) { scaled = true; cscale = bignum; }
@@ -163,14 +179,35 @@ int schur_large_run(LargeRun<T>& r) {
   CKL(cudaGetLastError());
 
   // ---- 3. QR
-  auto small_solve = [&](int lo, int hi, bool wantU, double* wr_out, double* wi_out) -> int {
+  // The small-matrix kernel in the working precision T on H[lo:hi, lo:hi] (copied to blk;
+  // T_blk back in blk, U in U), or -- eigenvalues only, fp32 set -- in FP32.
+  auto small_solve = [&](int lo, int hi, bool wantU, double* wr_out, double* wi_out, bool fp32) -> int {
     const int m = hi - lo + 1;
-    CKL(copy2d<T, double>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk, m, s));
     long long mh[4] = {0, 0, 0, 0};
     int m32 = m;
     CKL(cudaMemcpyAsync(meta, mh, sizeof(mh), cudaMemcpyHostToDevice, s));
     CKL(cudaMemcpyAsync(meta + 2, &m32, sizeof(int), cudaMemcpyHostToDevice, s));
-    RealBatch bt{};
+    if (fp32) {
+      CKL(copy2d<T, float>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk32, m, s));
+      RealBatchT<float> bt{};
+      bt.count = 1;
+      bt.ns = (const int*)(meta + 2);
+      bt.offs = meta;
+      bt.woffs = meta + 1;
+      bt.A = blk32;
+      bt.Z = nullptr;
+      bt.wr = wr_out;
+      bt.wi = wi_out;
+      bt.status = bstat;
+      bt.wantz = 0;
+      bt.scale = 0;
+      bt.maxiter_mult = 100;
+      CKL(launch_bin_sort(bt.ns, 1, order, sched, s));
+      CKL(launch_schur_batched_real<float, double>(bt, order, sched, r.num_sms, &s, 1));
+      return 0;
+    }
+    CKL(copy2d<T, T>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk, m, s));
+    RealBatchT<T> bt{};
     bt.count = 1;
     bt.ns = (const int*)(meta + 2);
     bt.offs = meta;
@@ -184,7 +221,28 @@ int schur_large_run(LargeRun<T>& r) {
     bt.scale = 0;
     bt.maxiter_mult = 100;
     CKL(launch_bin_sort(bt.ns, 1, order, sched, s));
-    CKL(launch_schur_batched_real(bt, order, sched, r.num_sms, &s, 1));
+    CKL(launch_schur_batched_real<T, double>(bt, order, sched, r.num_sms, &s, 1));
+    return 0;
+  };
+
+  // Apply the orthogonal factor U (m x m, in U) of the diagonal block [lo, hi] to the
+  // rest of H and to Z: H[lo:hi, hi+1:n] <- U^T H[lo:hi, hi+1:n], H[1:lo-1, lo:hi] <-
+  // H[1:lo-1, lo:hi] U, Z[:, lo:hi] <- Z[:, lo:hi] U.
+  auto apply_U = [&](int lo, int hi) -> int {
+    const int m = hi - lo + 1;
+    const int nr = n - hi;
+    if (nr > 0) {
+      CKL(copy2d<T, T>(m, nr, H + (size_t)hi * n + (lo - 1), n, tmp, m, s));
+      CKL(launch_gemm<T>(m, nr, m, U, m, 1, tmp, m, H + (size_t)hi * n + (lo - 1), n, s));
+    }
+    if (lo > 1) {
+      CKL(copy2d<T, T>(lo - 1, m, H + (size_t)(lo - 1) * n, n, tmp, lo - 1, s));
+      CKL(launch_gemm<T>(lo - 1, m, m, tmp, lo - 1, 0, U, m, H + (size_t)(lo - 1) * n, n, s));
+    }
+    if (Z) {
+      CKL(copy2d<T, T>(n, m, Z + (size_t)(lo - 1) * n, n, tmp, n, s));
+      CKL(launch_gemm<T>(n, m, m, tmp, n, 0, U, m, Z + (size_t)(lo - 1) * n, n, s));
+    }
     return 0;
   };
 
@@ -204,28 +262,12 @@ int schur_large_run(LargeRun<T>& r) {
     }
     const int ilo = kmax > 0 ? kmax : 1;
     if (kmax > 0) CKL(cudaMemsetAsync(H + (size_t)(ilo - 2) * n + (ilo - 1), 0, sizeof(T), s));
-    const int m = ihi - ilo + 1;
+    int m = ihi - ilo + 1;
     if (m <= NMIN) {
       // finish the block with the small-matrix kernel; eigenvalues straight into wr/wi
-      if (small_solve(ilo, ihi, true, r.wr + (ilo - 1), r.wi + (ilo - 1))) return -1;
-      CKL(copy2d<double, T>(m, m, blk, m, H + (size_t)(ilo - 1) * n + (ilo - 1), n, s));
-      CKL(copy2d<double, T>(m, m, U, m, Ut, m, s));
-      // H[lo:hi, hi+1:n] <- U^T H[lo:hi, hi+1:n]
-      const int nr = n - ihi;
-      if (nr > 0) {
-        CKL(copy2d<T, T>(m, nr, H + (size_t)ihi * n + (ilo - 1), n, tmp, m, s));
-        CKL(launch_gemm<T>(m, nr, m, Ut, m, 1, tmp, m, H + (size_t)ihi * n + (ilo - 1), n, s));
-      }
-      // H[1:lo-1, lo:hi] <- H[1:lo-1, lo:hi] U
-      if (ilo > 1) {
-        CKL(copy2d<T, T>(ilo - 1, m, H + (size_t)(ilo - 1) * n, n, tmp, ilo - 1, s));
-        CKL(launch_gemm<T>(ilo - 1, m, m, tmp, ilo - 1, 0, Ut, m, H + (size_t)(ilo - 1) * n, n, s));
-      }
-      // Z[:, lo:hi] <- Z[:, lo:hi] U
-      if (Z) {
-        CKL(copy2d<T, T>(n, m, Z + (size_t)(ilo - 1) * n, n, tmp, n, s));
-        CKL(launch_gemm<T>(n, m, m, tmp, n, 0, Ut, m, Z + (size_t)(ilo - 1) * n, n, s));
-      }
+      if (small_solve(ilo, ihi, true, r.wr + (ilo - 1), r.wi + (ilo - 1), false)) return -1;
+      CKL(copy2d<T, T>(m, m, blk, m, H + (size_t)(ilo - 1) * n + (ilo - 1), n, s));
+      if (apply_U(ilo, ihi)) return -1;
       int st = 0;
       CKL(cudaMemcpyAsync(&st, bstat, sizeof(int), cudaMemcpyDeviceToHost, s));
       CKL(cudaStreamSynchronize(s));
@@ -235,8 +277,44 @@ int schur_large_run(LargeRun<T>& r) {
       continue;
     }
     if (++sweeps > max_sweeps) return ST_UNCONVERGED;
-    // shifts: eigenvalues of the trailing 2B x 2B block
-    const int B = std::min(r.bulges > 0 ? r.bulges : kMaxBulges, std::max(1, (m - 8) / 6));
+    int B = std::min(r.bulges > 0 ? r.bulges : kMaxBulges, std::max(1, (m - 8) / 6));
+    std::vector<double> aed_wr, aed_wi;  // shift candidates from the deflation window
+    if (r.aedw > 0) {
+      // aggressive early deflation on the trailing window (aed.cu)
+      const int nw = std::min(r.aedw, m - 1);
+      const int kwtop = ihi - nw + 1;
+      if (small_solve(kwtop, ihi, true, aewr, aewi, false)) return -1;
+      AedArgs<T> ag{};
+      ag.H = H; ag.n = n; ag.ilo = ilo; ag.kwtop = kwtop; ag.nw = nw;
+      ag.Tw = blk; ag.V = U; ag.win_status = bstat;
+      ag.ewr = aewr; ag.ewi = aewi; ag.wr = r.wr; ag.wi = r.wi; ag.out = aout;
+      CKL(launch_aed<T>(ag, s));
+      int ao[3] = {0, 0, 0};
+      std::vector<double> ewr_w(nw), ewi_w(nw);
+      CKL(cudaMemcpyAsync(ao, aout, sizeof(ao), cudaMemcpyDeviceToHost, s));
+      CKL(cudaMemcpyAsync(ewr_w.data(), aewr, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+      CKL(cudaMemcpyAsync(ewi_w.data(), aewi, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+      CKL(cudaStreamSynchronize(s));
+      const int nsu = ao[0], nd = ao[1];
+      if (ao[2]) {
+        if (apply_U(kwtop, ihi)) return -1;
+      }
+      if (nd > 0) {
+        ihi = kwtop + nsu - 1;
+        since_defl = 0;
+        // deflated enough (LAPACK's nibble of 14%), or too little left for a sweep: AED again
+        if (nd * 100 >= 14 * nw || nsu < 2 || ihi - ilo + 1 <= NMIN) continue;
+      }
+      // candidate shifts: whole blocks from the bottom of the undeflated part
+      for (int q = nsu - 1; q >= 0 && (int)aed_wr.size() < 2 * B;) {
+        const int bs = (ewi_w[q] < 0.0 && q > 0) ? 2 : 1;
+        for (int t = q - bs + 1; t <= q; ++t) { aed_wr.push_back(ewr_w[t]); aed_wi.push_back(ewi_w[t]); }
+        q -= bs;
+      }
+      m = ihi - ilo + 1;
+      B = std::min(B, std::max(1, (m - 8) / 6));
+      if ((int)aed_wr.size() >= 2) B = std::min(B, (int)aed_wr.size() / 2);
+    }
     const int ns = 2 * B;
     std::vector<double> ewr(ns), ewi(ns);
     ++since_defl;
@@ -256,16 +334,21 @@ int schur_large_run(LargeRun<T>& r) {
         ewr[2 * b] = h11; ewi[2 * b] = sv * std::sqrt(7.0 / 16.0);
         ewr[2 * b + 1] = h11; ewi[2 * b + 1] = -ewi[2 * b];
       }
+    } else if ((int)aed_wr.size() >= 2) {
+      // the undeflated window eigenvalues (bottom-most first); fewer than 2B shorten the chain
+      ewr.assign(aed_wr.begin(), aed_wr.end());
+      ewi.assign(aed_wi.begin(), aed_wi.end());
     } else {
-      if (small_solve(ihi - ns + 1, ihi, false, bwr, bwi)) return -1;
+      if (small_solve(ihi - ns + 1, ihi, false, bwr, bwi, r.shift_fp32 != 0)) return -1;
       CKL(cudaMemcpyAsync(ewr.data(), bwr, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
       CKL(cudaMemcpyAsync(ewi.data(), bwi, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
       CKL(cudaStreamSynchronize(s));
     }
     // pair the shifts: conjugate pairs stay together, real shifts are paired in order
     std::vector<std::complex<double>> cpx, rl;
-    for (int q = 0; q < ns; ++q) {
-      if (ewi[q] > 0.0 && q + 1 < ns) { cpx.push_back({ewr[q], ewi[q]}); cpx.push_back({ewr[q + 1], ewi[q + 1]}); ++q; }
+    const int nc = (int)ewr.size();
+    for (int q = 0; q < nc; ++q) {
+      if (ewi[q] > 0.0 && q + 1 < nc) { cpx.push_back({ewr[q], ewi[q]}); cpx.push_back({ewr[q + 1], ewi[q + 1]}); ++q; }
       else if (ewi[q] == 0.0) rl.push_back({ewr[q], 0.0});
     }
     std::vector<std::complex<double>> sh(cpx);

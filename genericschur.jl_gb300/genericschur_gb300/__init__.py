@@ -75,8 +75,8 @@ def gschur_(A, wantZ=True, scale=True, maxiter=None, maxinner=None, ctx=None):
     is overwritten by T.  Returns Schur(T, Z, values), T being A itself."""
     n = _checksquare(A)
     ctx = ctx or get_context()
-    if not (A.flags.f_contiguous and A.dtype in (np.float64, np.complex128)):
-        raise ArgumentError("gschur_ needs a Fortran-ordered float64 or complex128 array")
+    if not (A.flags.f_contiguous and A.dtype in (np.float64, np.float32, np.complex128)):
+        raise ArgumentError("gschur_ needs a Fortran-ordered float64, float32 or complex128 array")
     flags = (GS_WANTZ if wantZ else 0) | (GS_SCALE if scale else 0)
     lib = ctx.lib
     if A.dtype == np.complex128:
@@ -87,14 +87,15 @@ def gschur_(A, wantZ=True, scale=True, maxiter=None, maxinner=None, ctx=None):
         if rc != GS_OK:
             _raise(rc, ctx, "gschur")
         return Schur(A, Z if wantZ else np.zeros((0, 0), dtype=np.complex128), w)
-    Z = np.zeros((n, n), dtype=np.float64, order="F") if wantZ else None
-    wr = np.zeros(n)
-    wi = np.zeros(n)
-    rc = lib.gs_schur_f64(ctx.handle, n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(wr), _ptr(wi), flags,
-                          int(maxiter or 0))
+    dt = A.dtype
+    Z = np.zeros((n, n), dtype=dt, order="F") if wantZ else None
+    wr = np.zeros(n, dtype=dt)
+    wi = np.zeros(n, dtype=dt)
+    fn = lib.gs_schur_f32 if dt == np.float32 else lib.gs_schur_f64
+    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), _ptr(Z), max(n, 1), _ptr(wr), _ptr(wi), flags, int(maxiter or 0))
     if rc != GS_OK:
         _raise(rc, ctx, "gschur")
-    return Schur(A, Z if wantZ else np.zeros((0, 0)), wr + 1j * wi)
+    return Schur(A, Z if wantZ else np.zeros((0, 0), dtype=dt), wr + 1j * wi)
 
 
 def gschur(A, **kw):
@@ -102,7 +103,10 @@ def gschur(A, **kw):
     A = np.asarray(A)
     if A.dtype.kind in "iub":
         raise TypeError("gschur is defined for floating-point element types only")
-    dt = np.complex128 if np.iscomplexobj(A) else np.float64
+    if np.iscomplexobj(A):
+        dt = np.complex128
+    else:
+        dt = np.float32 if A.dtype == np.float32 else np.float64  # Float32 stays Float32, as in the reference
     return gschur_(np.array(A, dtype=dt, order="F", copy=True), **kw)
 
 
@@ -165,9 +169,11 @@ def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ
         for m in mats:
             _checksquare(np.asarray(m))
         cplx = any(np.iscomplexobj(m) for m in mats)
-        packed, ns, offs, woffs = pack_batch(mats, np.complex128 if cplx else np.float64)
+        single = (not cplx) and all(np.asarray(m).dtype == np.float32 for m in mats) and len(mats) > 0
+        packed, ns, offs, woffs = pack_batch(mats, np.complex128 if cplx else (np.float32 if single else np.float64))
     else:
         cplx = np.iscomplexobj(packed)
+        single = (not cplx) and np.asarray(packed).dtype == np.float32
         packed = np.array(packed, copy=True)
     count = len(ns)
     ns = np.ascontiguousarray(ns, dtype=np.int32)
@@ -184,10 +190,12 @@ def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ
         rc = lib.gs_schur_batched_c64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), _ptr(packed), _ptr(Z),
                                       _ptr(w), _ptr(status), flags)
     else:
-        wr = np.zeros(nw)
-        wi = np.zeros(nw)
-        rc = lib.gs_schur_batched_f64(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), _ptr(packed), _ptr(Z),
-                                      _ptr(wr), _ptr(wi), _ptr(status), flags)
+        dt = np.float32 if single else np.float64
+        wr = np.zeros(nw, dtype=dt)
+        wi = np.zeros(nw, dtype=dt)
+        fn = lib.gs_schur_batched_f32 if single else lib.gs_schur_batched_f64
+        rc = fn(ctx.handle, count, _ptr(ns), _ptr(offs), _ptr(woffs), _ptr(packed), _ptr(Z), _ptr(wr), _ptr(wi),
+                _ptr(status), flags)
         w = wr + 1j * wi
     if rc not in (GS_OK, GS_UNCONVERGED) or (rc == GS_UNCONVERGED and raise_on_failure):
         _raise(rc, ctx, "gschur_batched")

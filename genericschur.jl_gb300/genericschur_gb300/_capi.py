@@ -39,8 +39,10 @@ SIGNATURES = {
     "gs_host_alloc": (_i, [_p, ctypes.POINTER(_p), ctypes.c_size_t]),
     "gs_host_free": (_i, [_p, _p]),
     "gs_schur_f64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
+    "gs_schur_f32": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
     "gs_schur_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _u, _i64, _i64]),
     "gs_schur_batched_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_schur_batched_f32": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_schur_batched_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_eigvecs_c64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
     "gs_eigvecs_f64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),

@@ -89,6 +89,12 @@ GS_API int gs_host_free(gs_context* ctx, void* ptr);
 GS_API int gs_schur_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz,
                  double* wr, double* wi, unsigned flags, int64_t maxiter);
 
+/* Float32 real Schur decomposition: gschur!(A::StridedMatrix{Float32}) computed in
+ * FP32 throughout (the reference's generic code in Float32 arithmetic); same layout
+ * and semantics as gs_schur_f64 with float arrays. */
+GS_API int gs_schur_f32(gs_context* ctx, int64_t n, float* A, int64_t lda, float* Z, int64_t ldz,
+                        float* wr, float* wi, unsigned flags, int64_t maxiter);
+
 /* Complex Schur decomposition of one n x n ComplexF64 matrix.
  * Replaces gschur!(A::StridedMatrix{Complex}) (GenericSchur.jl:350-372) with
  * gschur!(H::Hessenberg{Complex}, Z) (GenericSchur.jl:194-335).
@@ -110,6 +116,10 @@ GS_API int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, doub
 GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
                          int32_t* status, unsigned flags);
+
+GS_API int gs_schur_batched_f32(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                const int64_t* woffs, float* A, float* Z, float* wr, float* wi,
+                                int32_t* status, unsigned flags);
 
 GS_API int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* w, int32_t* status,
