@@ -200,10 +200,12 @@ inline std::vector<double> safescale_factors_host(double cfrom, double cto) {
 }
 
 // FP64 refinement kernels of the mixed-precision form (refine.cu).
-cudaError_t launch_sylv_wave(int n, int N, int d, const double* At, const double* Att, double* W, double* Wt,
-                             const int* bs, const int* bz, double floor, cudaStream_t s);
+// Tiles of the Sylvester solve: fills ts[0..nT], tbk[0..nT] (host arrays of n+1) from the
+// scalar-to-block map and returns nT.
+int sylv_tiles(int n, const int* blk_host, int* ts, int* tbk);
+cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const int* bs, const int* bz,
+                              const int* blk, const int* ts, const int* tbk, double floor, cudaStream_t s);
 cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s);
-cudaError_t launch_transpose(int n, const double* A, double* B, cudaStream_t s);
 cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s);
 cudaError_t launch_lower_norm(int n, const double* At, const int* blk, double* out, int num_sms, cudaStream_t s);
 cudaError_t launch_block_triu(int n, const double* At, const int* blk, double* T, cudaStream_t s);

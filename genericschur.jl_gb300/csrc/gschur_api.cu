@@ -1100,9 +1100,10 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   Arena ar;
   const size_t o_A0 = ar.take<double>(nn), o_A32 = ar.take<float>(nn), o_Z32 = ar.take<float>(nn);
   const size_t o_Z = ar.take<double>(nn), o_T1 = ar.take<double>(nn), o_T2 = ar.take<double>(nn);
-  const size_t o_T3 = ar.take<double>(nn), o_W = ar.take<double>(nn), o_Wt = ar.take<double>(nn);
+  const size_t o_T3 = ar.take<double>(nn), o_W = ar.take<double>(nn);
   const size_t o_wr = ar.take<double>(n), o_wi = ar.take<double>(n), o_sub = ar.take<float>(n);
   const size_t o_bs = ar.take<int>(n), o_bz = ar.take<int>(n), o_blk = ar.take<int>(n), o_cs = ar.take<double>(4 * n);
+  const size_t o_ts = ar.take<int>(n + 1), o_tbk = ar.take<int>(n + 1);
   const size_t o_nrm = ar.take<double>(4), o_max = ar.take<unsigned long long>(2);
   const size_t o_ws = ar.take<char>(schur_large_ws_bytes(N32, sizeof(float)));
   int rc = ensure_ws(ctx, ar.off);
@@ -1117,7 +1118,6 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   double* T2 = (double*)(base + o_T2);
   double* T3 = (double*)(base + o_T3);
   double* W = (double*)(base + o_W);
-  double* Wt = (double*)(base + o_Wt);
   double* dwr = (double*)(base + o_wr);
   double* dwi = (double*)(base + o_wi);
   double* nrm = (double*)(base + o_nrm);
@@ -1192,6 +1192,13 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   CK(cudaMemcpyAsync(dbs, bs.data(), sizeof(int) * NB, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dbz, bz.data(), sizeof(int) * NB, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dblk, blk.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  // tiles of the Sylvester solve (32 rows, never splitting a 2x2 block)
+  std::vector<int> ts(n + 1), tbk(n + 1);
+  const int nT = sylv_tiles(N32, blk.data(), ts.data(), tbk.data());
+  int* dts = (int*)(base + o_ts);
+  int* dtbk = (int*)(base + o_tbk);
+  CK(cudaMemcpyAsync(dts, ts.data(), sizeof(int) * (nT + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dtbk, tbk.data(), sizeof(int) * (nT + 1), cudaMemcpyHostToDevice, s));
   // ---- FP64 refinement
   auto gemm = [&](int m, int p, int q, const double* Am, int la, int tA, const double* Bm, int lb, double* Cm, int lc) {
     return launch_gemm<double>(m, p, q, Am, la, tA, Bm, lb, Cm, lc, s);
@@ -1252,11 +1259,9 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
     prev = res;
     ++its;
     // block Sylvester solve for W, then Z <- Z (I + S), S = W - W^T
-    e = launch_transpose(N32, T1, T2, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(W, 0, nn * sizeof(double), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(Wt, 0, nn * sizeof(double), s);
+    e = cudaMemsetAsync(W, 0, nn * sizeof(double), s);
     const double floor = 1e-3 * std::sqrt(hn[1]) * eps;
-    for (int d = 0; d <= NB - 2 && e == cudaSuccess; ++d) e = launch_sylv_wave(N32, NB, d, T1, T2, W, Wt, dbs, dbz, floor, s);
+    if (e == cudaSuccess) e = launch_sylv_tiled(N32, nT, T1, W, dbs, dbz, dblk, dts, dtbk, floor, s);
     double wn[2] = {0.0, 0.0};
     if (e == cudaSuccess) e = launch_lower_norm(N32, W, dblk, nrm + 2, ctx->num_sms, s);
     if (e == cudaSuccess) e = launch_refine_elementwise(0, N32, W, T3, 0.0, s);  // T3 = S

@@ -8,10 +8,8 @@
 // block rows p > q reads
 //     T_pp W_pq - W_pq T_qq = -L_pq - sum_{r>p} T_pr W_rq + sum_{r<q} W_pr T_rq,
 // a block triangular Sylvester equation (the iteration of Bujanovic, Kressner and
-// Schroeder, "Iterative refinement of Schur decompositions", Numer. Algorithms 2023).
-// It is solved by anti-diagonal waves over the block pairs: wave d holds the pairs
-// (p, q) = (N-1-d+q, q), which depend only on earlier waves.  One warp per pair: the
-// lanes split the two sums, lane 0 solves the (<= 4 x 4) Kronecker system of the pair.
+// Schroeder, "Iterative refinement of Schur decompositions", Numer. Algorithms 2023),
+// solved in 32-row tiles (k_sylv_tile).
 // Z is then updated to Z (I + S), which departs from orthogonality by O(|S|^2); a
 // Newton-Schulz step Z <- Z (3 I - Z^T Z) / 2 follows whenever |S| is above 1e-8.
 // Products with the small corrections S and (I - Z^T Z)/2 run in FP32 (their error is
@@ -47,57 +45,127 @@ __device__ void small_solve(int m, double M[4][4], double r[4], double floor) {
   }
 }
 
-// One wave of the block Sylvester solve.  T: At (n x n, ld n) whose block-upper part
-// is T and block-lower part is L; Tt = At^T; W, Wt: the solution and its transpose
-// (zero-initialised); bs/bz: block start (0-based) and size of the N blocks.
-__global__ void __launch_bounds__(256) k_sylv_wave(int n, int N, int d, const double* __restrict__ At,
-                                                   const double* __restrict__ Att, double* __restrict__ W,
-                                                   double* __restrict__ Wt, const int* __restrict__ bs,
-                                                   const int* __restrict__ bz, double floor) {
-  const int lane = threadIdx.x & 31;
-  const int q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (q > d) return;
-  const int p = N - 1 - d + q;
-  const int sp = bs[p], zp = bz[p], sq = bs[q], zq = bz[q];
-  const int kp = sp + zp;  // sum_{r>p}: scalar k >= kp
-  double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
-  // - sum_{k >= kp} T[i, k] W[k, j]   (T row i = Att column i)
-  for (int k = kp + lane; k < n; k += 32) {
-    for (int a = 0; a < zp; ++a) {
-      const double t = Att[(size_t)(sp + a) * n + k];
-      for (int b = 0; b < zq; ++b) acc[a][b] -= t * W[(size_t)(sq + b) * n + k];
+// Tiled block Sylvester solve.  The scalar index range is cut into tiles of at most
+// kSt rows that never split a 2x2 block (ts[t] = first row of tile t, tbk[t] = its first
+// block; ts[nT] = n, tbk[nT] = N).  Tile pair (P, Q), P >= Q, needs the tiles (R, Q),
+// R > P, and (P, R), R < Q, so the pairs go by levels D = P - Q from nT-1 down to 0,
+// one CTA per pair:
+//   1. rhs = -L_PQ - sum_{R>P} T_PR W_RQ + sum_{R<Q} W_PR T_RQ from tiles staged in
+//      shared memory (each level's pairs do the same number nT-1-D of tile products);
+//   2. the block pairs inside the tile pair by local anti-diagonal waves, warp per
+//      block pair: the in-tile sums over the lanes, then lane 0 solves the (<= 4x4)
+//      Kronecker system (I (x) T_pp - T_qq^T (x) I) vec(W_pq) = rhs.
+// At: Z^T A Z (block-upper part T, block-lower part L), W: the block-lower solution.
+constexpr int kSt = 32;
+
+__global__ void __launch_bounds__(256) k_sylv_tile(int n, int nT, int D, const double* __restrict__ At,
+                                                   double* __restrict__ W, const int* __restrict__ bs,
+                                                   const int* __restrict__ bz, const int* __restrict__ blk,
+                                                   const int* __restrict__ ts, const int* __restrict__ tbk,
+                                                   double floor) {
+  __shared__ double Ta[kSt][kSt + 1];
+  __shared__ double Tb[kSt][kSt + 1];
+  __shared__ double Wl[kSt][kSt + 1];
+  const int Q = blockIdx.x, P = Q + D;
+  if (P >= nT) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int p0 = ts[P], pw = ts[P + 1] - p0, q0 = ts[Q], qw = ts[Q + 1] - q0;
+  const int r = tid % kSt, cb = tid / kSt;  // 4 outputs per thread: (r, cb + 8 k)
+  double acc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = cb + 8 * k;
+    acc[k] = (r < pw && c < qw) ? -At[(size_t)(q0 + c) * n + p0 + r] : 0.0;
+  }
+  // - sum_{R > P} T_PR W_RQ
+  for (int R = P + 1; R < nT; ++R) {
+    const int r0 = ts[R], rw = ts[R + 1] - r0;
+    for (int idx = tid; idx < kSt * kSt; idx += 256) {
+      const int x = idx % kSt, y = idx / kSt;
+      Ta[x][y] = (x < pw && y < rw) ? At[(size_t)(r0 + y) * n + p0 + x] : 0.0;
+      Tb[x][y] = (x < rw && y < qw) ? W[(size_t)(q0 + y) * n + r0 + x] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < kSt; ++kk) {
+      const double t = Ta[r][kk];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[k] = fma(-t, Tb[kk][cb + 8 * k], acc[k]);
+    }
+    __syncthreads();
+  }
+  // + sum_{R < Q} W_PR T_RQ
+  for (int R = 0; R < Q; ++R) {
+    const int r0 = ts[R], rw = ts[R + 1] - r0;
+    for (int idx = tid; idx < kSt * kSt; idx += 256) {
+      const int x = idx % kSt, y = idx / kSt;
+      Ta[x][y] = (x < pw && y < rw) ? W[(size_t)(r0 + y) * n + p0 + x] : 0.0;
+      Tb[x][y] = (x < rw && y < qw) ? At[(size_t)(q0 + y) * n + r0 + x] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < kSt; ++kk) {
+      const double t = Ta[r][kk];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[k] = fma(t, Tb[kk][cb + 8 * k], acc[k]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) Wl[r][cb + 8 * k] = acc[k];
+  for (int idx = tid; idx < kSt * kSt; idx += 256) {
+    const int x = idx % kSt, y = idx / kSt;
+    Ta[x][y] = (x < pw && y < pw) ? At[(size_t)(p0 + y) * n + p0 + x] : 0.0;  // T_PP
+    Tb[x][y] = (x < qw && y < qw) ? At[(size_t)(q0 + y) * n + q0 + x] : 0.0;  // T_QQ
+  }
+  __syncthreads();
+  // local waves over the block pairs of the tile pair
+  const int pb0 = tbk[P], pb1 = tbk[P + 1], qb0 = tbk[Q], qb1 = tbk[Q + 1];
+  const int np = pb1 - pb0, nq = qb1 - qb0;
+  for (int d = 0; d < np + nq - 1; ++d) {
+    for (int i = warp; i < np; i += 8) {
+      const int j = d - i;
+      if (j < 0 || j >= nq) continue;
+      const int p = pb1 - 1 - i, q = qb0 + j;
+      if (P == Q && p <= q) continue;
+      const int sp = bs[p] - p0, zp = bz[p], sq = bs[q] - q0, zq = bz[q];
+      double s2[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+      for (int k = sp + zp + lane; k < pw; k += 32)
+        for (int a = 0; a < zp; ++a)
+          for (int b = 0; b < zq; ++b) s2[a][b] -= Ta[sp + a][k] * Wl[k][sq + b];
+      for (int k = lane; k < sq; k += 32)
+        for (int a = 0; a < zp; ++a)
+          for (int b = 0; b < zq; ++b) s2[a][b] += Wl[sp + a][k] * Tb[k][sq + b];
+      for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+          for (int o = 16; o > 0; o >>= 1) s2[a][b] += __shfl_xor_sync(0xffffffffu, s2[a][b], o);
+      if (lane == 0) {
+        const int m = zp * zq;
+        double M[4][4] = {{0}}, rr[4];
+        for (int b = 0; b < zq; ++b)
+          for (int a = 0; a < zp; ++a) rr[a + b * zp] = Wl[sp + a][sq + b] + s2[a][b];
+        for (int b = 0; b < zq; ++b)
+          for (int a = 0; a < zp; ++a) {
+            const int row = a + b * zp;
+            for (int a2 = 0; a2 < zp; ++a2) M[row][a2 + b * zp] += Ta[sp + a][sp + a2];
+            for (int b2 = 0; b2 < zq; ++b2) M[row][a + b2 * zp] -= Tb[sq + b2][sq + b];
+          }
+        small_solve(m, M, rr, floor);
+        for (int b = 0; b < zq; ++b)
+          for (int a = 0; a < zp; ++a) Wl[sp + a][sq + b] = rr[a + b * zp];
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  // write the tile back: block-lower entries only (the diagonal tile keeps zeros elsewhere)
+  for (int idx = tid; idx < kSt * kSt; idx += 256) {
+    const int x = idx % kSt, y = idx / kSt;
+    if (x < pw && y < qw) {
+      const bool lower = blk[p0 + x] > blk[q0 + y];
+      W[(size_t)(q0 + y) * n + p0 + x] = lower ? Wl[x][y] : 0.0;
     }
   }
-  // + sum_{k < sq} W[i, k] T[k, j]    (W row i = Wt column i)
-  for (int k = lane; k < sq; k += 32) {
-    for (int a = 0; a < zp; ++a) {
-      const double wv = Wt[(size_t)(sp + a) * n + k];
-      for (int b = 0; b < zq; ++b) acc[a][b] += wv * At[(size_t)(sq + b) * n + k];
-    }
-  }
-  for (int a = 0; a < 2; ++a)
-    for (int b = 0; b < 2; ++b)
-      for (int o = 16; o > 0; o >>= 1) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o);
-  if (lane != 0) return;
-  // r = -L_pq + sums;  unknowns x = vec(W_pq) (column-major, zp x zq)
-  const int m = zp * zq;
-  double M[4][4] = {{0}}, r[4];
-  for (int b = 0; b < zq; ++b)
-    for (int a = 0; a < zp; ++a) r[a + b * zp] = -At[(size_t)(sq + b) * n + sp + a] + acc[a][b];
-  // (I_zq (x) T_pp - T_qq^T (x) I_zp) x = r
-  for (int b = 0; b < zq; ++b)
-    for (int a = 0; a < zp; ++a) {
-      const int row = a + b * zp;
-      for (int a2 = 0; a2 < zp; ++a2) M[row][a2 + b * zp] += At[(size_t)(sp + a2) * n + sp + a];   // T_pp[a, a2]
-      for (int b2 = 0; b2 < zq; ++b2) M[row][a + b2 * zp] -= At[(size_t)(sq + b) * n + sq + b2];    // T_qq[b2, b]
-    }
-  small_solve(m, M, r, floor);
-  for (int b = 0; b < zq; ++b)
-    for (int a = 0; a < zp; ++a) {
-      const double x = r[a + b * zp];
-      W[(size_t)(sq + b) * n + sp + a] = x;
-      Wt[(size_t)(sp + a) * n + sq + b] = x;
-    }
 }
 
 // S = W - W^T (+ I when add_identity), and block-lower norm accumulation helpers.
@@ -128,21 +196,6 @@ __global__ void k_ns_factor(int n, double* X) {
 __global__ void k_add_f32(double* __restrict__ Z, const float* __restrict__ P, size_t cnt) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
     Z[i] += (double)P[i];
-}
-
-// transpose
-__global__ void k_transpose(int n, const double* __restrict__ A, double* __restrict__ B) {
-  __shared__ double t[32][33];
-  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-    const int r = bx + threadIdx.x, c = by + k;
-    if (r < n && c < n) t[k][threadIdx.x] = A[(size_t)c * n + r];
-  }
-  __syncthreads();
-  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-    const int r = by + threadIdx.x, c = bx + k;
-    if (r < n && c < n) B[(size_t)c * n + r] = t[threadIdx.x][k];
-  }
 }
 
 // sum of squares of the block-lower part (entries (i, j) with block(i) > block(j)) and of all
@@ -240,12 +293,29 @@ template cudaError_t convert_array<double, float>(const double*, float*, size_t,
 template cudaError_t convert_array<float, double>(const float*, double*, size_t, double, cudaStream_t);
 template cudaError_t convert_array<double, double>(const double*, double*, size_t, double, cudaStream_t);
 
-cudaError_t launch_sylv_wave(int n, int N, int d, const double* At, const double* Att, double* W, double* Wt,
-                             const int* bs, const int* bz, double floor, cudaStream_t s) {
-  const int pairs = d + 1;
-  const int wpb = 8;
-  k_sylv_wave<<<(pairs + wpb - 1) / wpb, 32 * wpb, 0, s>>>(n, N, d, At, Att, W, Wt, bs, bz, floor);
-  return cudaGetLastError();
+int sylv_tiles(int n, const int* blk_host, int* ts, int* tbk) {
+  int nT = 0, t = 0;
+  while (t < n) {
+    int e = t + kSt < n ? t + kSt : n;
+    if (e < n && blk_host[e] == blk_host[e - 1]) --e;  // never split a 2x2 block
+    ts[nT] = t;
+    tbk[nT] = blk_host[t];
+    ++nT;
+    t = e;
+  }
+  ts[nT] = n;
+  tbk[nT] = blk_host[n - 1] + 1;
+  return nT;
+}
+
+cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const int* bs, const int* bz,
+                              const int* blk, const int* ts, const int* tbk, double floor, cudaStream_t s) {
+  for (int D = nT - 1; D >= 0; --D) {
+    k_sylv_tile<<<nT - D, 256, 0, s>>>(n, nT, D, At, W, bs, bz, blk, ts, tbk, floor);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s) {
@@ -262,12 +332,6 @@ cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b,
 
 cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s) {
   k_add_f32<<<1024, 256, 0, s>>>(Z, P, cnt);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_transpose(int n, const double* A, double* B, cudaStream_t s) {
-  dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
-  k_transpose<<<g, b, 0, s>>>(n, A, B);
   return cudaGetLastError();
 }
 

@@ -14,6 +14,8 @@ from oracle import pyoracle as po
 pytestmark = pytest.mark.gpu
 
 SIZES = [1, 2, 3, 5, 8, 16, 33, 64, 65, 100, 128]
+# orders above 128 take the tiled back-substitution path (one matrix per call)
+LARGE_SIZES = [129, 161, 300]
 
 
 def _vectest(A, w, VR, VL, tol=20.0):
@@ -38,7 +40,7 @@ def _compare(V, Vref, s):
         assert np.max(np.abs(V[:, good] - Vref[:, good])) < 1e-9
 
 
-@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("n", SIZES + LARGE_SIZES)
 def test_eigvecs_complex(gs, n):
     rng = np.random.default_rng(3000 + n)
     A = randn_matrix(rng, n, cplx=True)
@@ -56,7 +58,7 @@ def test_eigvecs_complex(gs, n):
     _compare(VL, VLr, s)
 
 
-@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("n", SIZES + LARGE_SIZES)
 def test_eigvecs_real(gs, n):
     rng = np.random.default_rng(4000 + n)
     A = randn_matrix(rng, n)
@@ -88,9 +90,9 @@ def test_triangularize(gs, n):
 
 
 @pytest.mark.parametrize("cplx", [False, True])
-def test_eigen(gs, cplx):
+@pytest.mark.parametrize("n", [50, 260])
+def test_eigen(gs, cplx, n):
     rng = np.random.default_rng(6)
-    n = 50
     A = randn_matrix(rng, n, cplx)
     E = gs.eigen(A)
     assert np.all(np.diff(E.values.real) >= 0)
