@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="plain stream launches instead of the CUDA graph")
     ap.add_argument("--no-large", action="store_true", help="skip the n=4096 FP64 vs mixed-precision timing")
     ap.add_argument("--large-n", type=int, default=4096)
+    ap.add_argument("--large-only", action="store_true",
+                    help="only the large-matrix measurement (for profiling runs); prints its JSON object")
+    ap.add_argument("--large-mode", default="both", choices=["both", "fp64", "mixed"])
     return ap.parse_args()
 
 
@@ -295,7 +298,7 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def measure_large(ctx, torch, dev, n):
+def measure_large(ctx, torch, dev, n, mode="both"):
     """The second half of the metric: one n x n real Schur decomposition (iid N(0,1),
     seed 1 for n=4096) by the plain FP64 path and by the FP32 + FP64-refinement path,
     each through the C-ABI with host buffers (copies included), with its backward
@@ -316,18 +319,21 @@ def measure_large(ctx, torch, dev, n):
         return float(be) / (n * eps), float(oe) / (n * eps)
 
     out = {"n": n, "seed": LARGE_SEEDS.get(n, n), "entries": "iid N(0,1)"}
-    t = time.perf_counter()
-    S = gs.gschur(A, ctx=ctx)
-    out["fp64_s"] = time.perf_counter() - t
-    out["fp64_kernel_ms"] = ctx.last_kernel_ms()
-    out["fp64_backward_err_n_eps"], out["fp64_orth_err_n_eps"] = errors(S)
-    t = time.perf_counter()
-    S, info = gs.gschur_mixed(A, ctx=ctx, return_info=True)
-    out["mixed_s"] = time.perf_counter() - t
-    out["mixed_kernel_ms"] = ctx.last_kernel_ms()
-    out["mixed_backward_err_n_eps"], out["mixed_orth_err_n_eps"] = errors(S)
-    out["mixed_refinement"] = info
-    out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
+    if mode in ("both", "fp64"):
+        t = time.perf_counter()
+        S = gs.gschur(A, ctx=ctx)
+        out["fp64_s"] = time.perf_counter() - t
+        out["fp64_kernel_ms"] = ctx.last_kernel_ms()
+        out["fp64_backward_err_n_eps"], out["fp64_orth_err_n_eps"] = errors(S)
+    if mode in ("both", "mixed"):
+        t = time.perf_counter()
+        S, info = gs.gschur_mixed(A, ctx=ctx, return_info=True)
+        out["mixed_s"] = time.perf_counter() - t
+        out["mixed_kernel_ms"] = ctx.last_kernel_ms()
+        out["mixed_backward_err_n_eps"], out["mixed_orth_err_n_eps"] = errors(S)
+        out["mixed_refinement"] = info
+    if mode == "both":
+        out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
     out["flops_25n3"] = 25.0 * n ** 3
     return out
 
@@ -395,8 +401,22 @@ def measure_e2e(ctx, packed, ns, offs, woffs, steps):
             ctx.host_free(p)
 
 
+def run_large_only(args):
+    import torch
+    import build_lib
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    build_lib.build()
+    import genericschur_gb300 as gs
+    ctx = gs.Context(0)
+    print(json.dumps(measure_large(ctx, torch, dev, args.large_n, args.large_mode)))
+
+
 def main():
     args = parse()
+    if args.large_only:
+        run_large_only(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

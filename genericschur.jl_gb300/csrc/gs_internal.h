@@ -203,10 +203,14 @@ inline std::vector<double> safescale_factors_host(double cfrom, double cto) {
 // Tiles of the Sylvester solve: fills ts[0..nT], tbk[0..nT] (host arrays of n+1) from the
 // scalar-to-block map and returns nT.
 int sylv_tiles(int n, const int* blk_host, int* ts, int* tbk);
+size_t sylv_part_elems(int nT);  // partial right-hand sides of one level (doubles)
 cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const int* bs, const int* bz,
-                              const int* blk, const int* ts, const int* tbk, double floor, cudaStream_t s);
+                              const int* blk, const int* ts, const int* tbk, double* part, double floor,
+                              cudaStream_t s);
 cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s);
 cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s);
+cudaError_t launch_add_diff_f32(double* X, const float* P1, const float* P2, size_t cnt, cudaStream_t s);
+cudaError_t launch_sub_f32(double* X, const float* P, size_t cnt, cudaStream_t s);
 cudaError_t launch_lower_norm(int n, const double* At, const int* blk, double* out, int num_sms, cudaStream_t s);
 cudaError_t launch_block_triu(int n, const double* At, const int* blk, double* T, cudaStream_t s);
 cudaError_t launch_std_blocks(int n, int N, const int* bs, const int* bz, double* T, double* Z, double* cs_sn,

@@ -250,16 +250,26 @@ __global__ void __launch_bounds__(kHT) k_hess_update(int n, T* __restrict__ A, i
       const T ur = u[r];
       if (which == 0) w = fma(-tau * dot, ur, w);
       const T tw = tau * w, tu = tau * ur;
-      if (which == 0) {
-        for (int c = cb; c < ce; ++c) {
-          T* p = M + (size_t)c * ld + r;
-          *p = fma(-tw, u[c], fma(-tu, vs[c - cb], *p));
+      // four columns per round: the four loads are issued before any store
+      T* p = M + (size_t)cb * ld + r;
+      int c = cb;
+      for (; c + 3 < ce; c += 4, p += 4 * (size_t)ld) {
+        T a0 = p[0], a1 = p[ld], a2 = p[2 * (size_t)ld], a3 = p[3 * (size_t)ld];
+        if (which == 0) {
+          a0 = fma(-tu, vs[c - cb], a0);
+          a1 = fma(-tu, vs[c + 1 - cb], a1);
+          a2 = fma(-tu, vs[c + 2 - cb], a2);
+          a3 = fma(-tu, vs[c + 3 - cb], a3);
         }
-      } else {
-        for (int c = cb; c < ce; ++c) {
-          T* p = M + (size_t)c * ld + r;
-          *p = fma(-tw, u[c], *p);
-        }
+        p[0] = fma(-tw, u[c], a0);
+        p[ld] = fma(-tw, u[c + 1], a1);
+        p[2 * (size_t)ld] = fma(-tw, u[c + 2], a2);
+        p[3 * (size_t)ld] = fma(-tw, u[c + 3], a3);
+      }
+      for (; c < ce; ++c, p += ld) {
+        T a0 = *p;
+        if (which == 0) a0 = fma(-tu, vs[c - cb], a0);
+        *p = fma(-tw, u[c], a0);
       }
     }
   }

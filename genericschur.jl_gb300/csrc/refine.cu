@@ -49,77 +49,85 @@ __device__ void small_solve(int m, double M[4][4], double r[4], double floor) {
 // kSt rows that never split a 2x2 block (ts[t] = first row of tile t, tbk[t] = its first
 // block; ts[nT] = n, tbk[nT] = N).  Tile pair (P, Q), P >= Q, needs the tiles (R, Q),
 // R > P, and (P, R), R < Q, so the pairs go by levels D = P - Q from nT-1 down to 0,
-// one CTA per pair:
-//   1. rhs = -L_PQ - sum_{R>P} T_PR W_RQ + sum_{R<Q} W_PR T_RQ from tiles staged in
-//      shared memory (each level's pairs do the same number nT-1-D of tile products);
-//   2. the block pairs inside the tile pair by local anti-diagonal waves, warp per
-//      block pair: the in-tile sums over the lanes, then lane 0 solves the (<= 4x4)
-//      Kronecker system (I (x) T_pp - T_qq^T (x) I) vec(W_pq) = rhs.
+// one pair of launches per level:
+//   1. rhs = -L_PQ - sum_{R>P} T_PR W_RQ + sum_{R<Q} W_PR T_RQ: the nT-1-D tile
+//      products of every pair of the level are split over CTAs of kSplit products
+//      (k_sylv_rhs), whose partial tiles the solve step adds in a fixed order;
+//   2. the block pairs inside the tile pair by local anti-diagonal waves (k_sylv_solve).
 // At: Z^T A Z (block-upper part T, block-lower part L), W: the block-lower solution.
 constexpr int kSt = 32;
 
-__global__ void __launch_bounds__(256) k_sylv_tile(int n, int nT, int D, const double* __restrict__ At,
-                                                   double* __restrict__ W, const int* __restrict__ bs,
-                                                   const int* __restrict__ bz, const int* __restrict__ blk,
-                                                   const int* __restrict__ ts, const int* __restrict__ tbk,
-                                                   double floor) {
+// Level D, step 1: partial right-hand sides.  CTA (pair, chunk) adds the tile products
+// with indices [chunk * kSplit, ...) of the pair's list  R = P+1..nT-1 (minus T_PR W_RQ),
+// then R = 0..Q-1 (plus W_PR T_RQ), into part[pair][chunk] (32 x 32, column-major).
+constexpr int kSplit = 4;  // tile products per CTA
+
+__global__ void __launch_bounds__(256) k_sylv_rhs(int n, int nT, int D, const double* __restrict__ At,
+                                                  const double* __restrict__ W, const int* __restrict__ ts,
+                                                  double* __restrict__ part, int nchunk) {
+  __shared__ double Ta[kSt][kSt + 1];
+  __shared__ double Tb[kSt][kSt + 1];
+  const int Q = blockIdx.x, P = Q + D, chunk = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int p0 = ts[P], pw = ts[P + 1] - p0, q0 = ts[Q], qw = ts[Q + 1] - q0;
+  const int r = tid % kSt, cb = tid / kSt;
+  const int nprod = nT - 1 - D;  // (nT-1-P) + Q
+  const int n1 = nT - 1 - P;     // products of the first sum
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int t = chunk * kSplit; t < min(nprod, (chunk + 1) * kSplit); ++t) {
+    const bool first = t < n1;
+    const int R = first ? P + 1 + t : t - n1;
+    const int r0 = ts[R], rw = ts[R + 1] - r0;
+    for (int idx = tid; idx < kSt * kSt; idx += 256) {
+      const int x = idx % kSt, y = idx / kSt;
+      if (first) {
+        Ta[x][y] = (x < pw && y < rw) ? At[(size_t)(r0 + y) * n + p0 + x] : 0.0;  // T_PR
+        Tb[x][y] = (x < rw && y < qw) ? W[(size_t)(q0 + y) * n + r0 + x] : 0.0;   // W_RQ
+      } else {
+        Ta[x][y] = (x < pw && y < rw) ? W[(size_t)(r0 + y) * n + p0 + x] : 0.0;   // W_PR
+        Tb[x][y] = (x < rw && y < qw) ? At[(size_t)(q0 + y) * n + r0 + x] : 0.0;  // T_RQ
+      }
+    }
+    __syncthreads();
+    const double sg = first ? -1.0 : 1.0;
+#pragma unroll 8
+    for (int kk = 0; kk < kSt; ++kk) {
+      const double a = sg * Ta[r][kk];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[k] = fma(a, Tb[kk][cb + 8 * k], acc[k]);
+    }
+    __syncthreads();
+  }
+  double* out = part + ((size_t)Q * nchunk + chunk) * (kSt * kSt);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) out[(cb + 8 * k) * kSt + r] = acc[k];
+}
+
+// Level D, step 2: one CTA per tile pair sums its partials (fixed order) and -L_PQ,
+// then solves the block pairs inside the tile pair by local anti-diagonal waves, warp
+// per block pair (the in-tile sums over the lanes, lane 0 solves the <= 4x4 Kronecker
+// system (I (x) T_pp - T_qq^T (x) I) vec(W_pq) = rhs).
+__global__ void __launch_bounds__(256) k_sylv_solve(int n, int nT, int D, const double* __restrict__ At,
+                                                    double* __restrict__ W, const int* __restrict__ bs,
+                                                    const int* __restrict__ bz, const int* __restrict__ blk,
+                                                    const int* __restrict__ ts, const int* __restrict__ tbk,
+                                                    const double* __restrict__ part, int nchunk, double floor) {
   __shared__ double Ta[kSt][kSt + 1];
   __shared__ double Tb[kSt][kSt + 1];
   __shared__ double Wl[kSt][kSt + 1];
   const int Q = blockIdx.x, P = Q + D;
-  if (P >= nT) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int p0 = ts[P], pw = ts[P + 1] - p0, q0 = ts[Q], qw = ts[Q + 1] - q0;
-  const int r = tid % kSt, cb = tid / kSt;  // 4 outputs per thread: (r, cb + 8 k)
-  double acc[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int c = cb + 8 * k;
-    acc[k] = (r < pw && c < qw) ? -At[(size_t)(q0 + c) * n + p0 + r] : 0.0;
-  }
-  // - sum_{R > P} T_PR W_RQ
-  for (int R = P + 1; R < nT; ++R) {
-    const int r0 = ts[R], rw = ts[R + 1] - r0;
-    for (int idx = tid; idx < kSt * kSt; idx += 256) {
-      const int x = idx % kSt, y = idx / kSt;
-      Ta[x][y] = (x < pw && y < rw) ? At[(size_t)(r0 + y) * n + p0 + x] : 0.0;
-      Tb[x][y] = (x < rw && y < qw) ? W[(size_t)(q0 + y) * n + r0 + x] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < kSt; ++kk) {
-      const double t = Ta[r][kk];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[k] = fma(-t, Tb[kk][cb + 8 * k], acc[k]);
-    }
-    __syncthreads();
-  }
-  // + sum_{R < Q} W_PR T_RQ
-  for (int R = 0; R < Q; ++R) {
-    const int r0 = ts[R], rw = ts[R + 1] - r0;
-    for (int idx = tid; idx < kSt * kSt; idx += 256) {
-      const int x = idx % kSt, y = idx / kSt;
-      Ta[x][y] = (x < pw && y < rw) ? W[(size_t)(r0 + y) * n + p0 + x] : 0.0;
-      Tb[x][y] = (x < rw && y < qw) ? At[(size_t)(q0 + y) * n + r0 + x] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < kSt; ++kk) {
-      const double t = Ta[r][kk];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[k] = fma(t, Tb[kk][cb + 8 * k], acc[k]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int k = 0; k < 4; ++k) Wl[r][cb + 8 * k] = acc[k];
+  const int nused = (nT - 1 - D + kSplit - 1) / kSplit;
   for (int idx = tid; idx < kSt * kSt; idx += 256) {
     const int x = idx % kSt, y = idx / kSt;
+    double v = (x < pw && y < qw) ? -At[(size_t)(q0 + y) * n + p0 + x] : 0.0;
+    for (int c = 0; c < nused; ++c) v += part[((size_t)Q * nchunk + c) * (kSt * kSt) + y * kSt + x];
+    Wl[x][y] = v;
     Ta[x][y] = (x < pw && y < pw) ? At[(size_t)(p0 + y) * n + p0 + x] : 0.0;  // T_PP
     Tb[x][y] = (x < qw && y < qw) ? At[(size_t)(q0 + y) * n + q0 + x] : 0.0;  // T_QQ
   }
   __syncthreads();
-  // local waves over the block pairs of the tile pair
   const int pb0 = tbk[P], pb1 = tbk[P + 1], qb0 = tbk[Q], qb1 = tbk[Q + 1];
   const int np = pb1 - pb0, nq = qb1 - qb0;
   for (int d = 0; d < np + nq - 1; ++d) {
@@ -308,10 +316,22 @@ int sylv_tiles(int n, const int* blk_host, int* ts, int* tbk) {
   return nT;
 }
 
+size_t sylv_part_elems(int nT) {
+  const int nchunk = (nT + kSplit - 1) / kSplit;
+  return (size_t)nT * nchunk * kSt * kSt;
+}
+
 cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const int* bs, const int* bz,
-                              const int* blk, const int* ts, const int* tbk, double floor, cudaStream_t s) {
+                              const int* blk, const int* ts, const int* tbk, double* part, double floor,
+                              cudaStream_t s) {
+  const int nchunk = (nT + kSplit - 1) / kSplit;
   for (int D = nT - 1; D >= 0; --D) {
-    k_sylv_tile<<<nT - D, 256, 0, s>>>(n, nT, D, At, W, bs, bz, blk, ts, tbk, floor);
+    const int nprod = nT - 1 - D;
+    if (nprod > 0) {
+      dim3 g(nT - D, (nprod + kSplit - 1) / kSplit);
+      k_sylv_rhs<<<g, 256, 0, s>>>(n, nT, D, At, W, ts, part, nchunk);
+    }
+    k_sylv_solve<<<nT - D, 256, 0, s>>>(n, nT, D, At, W, bs, bz, blk, ts, tbk, part, nchunk, floor);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -327,6 +347,29 @@ cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b,
     case 2: k_ns_factor<<<g, 256, 0, s>>>(n, b); break;
     default: break;
   }
+  return cudaGetLastError();
+}
+
+// X += P1 - P2 (two FP32 products)
+__global__ void k_add_diff_f32(double* __restrict__ X, const float* __restrict__ P1, const float* __restrict__ P2,
+                               size_t cnt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
+    X[i] += (double)P1[i] - (double)P2[i];
+}
+
+cudaError_t launch_add_diff_f32(double* X, const float* P1, const float* P2, size_t cnt, cudaStream_t s) {
+  k_add_diff_f32<<<1024, 256, 0, s>>>(X, P1, P2, cnt);
+  return cudaGetLastError();
+}
+
+// X -= P (an FP32 product)
+__global__ void k_sub_f32(double* __restrict__ X, const float* __restrict__ P, size_t cnt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (size_t)gridDim.x * blockDim.x)
+    X[i] -= (double)P[i];
+}
+
+cudaError_t launch_sub_f32(double* X, const float* P, size_t cnt, cudaStream_t s) {
+  k_sub_f32<<<1024, 256, 0, s>>>(X, P, cnt);
   return cudaGetLastError();
 }
 

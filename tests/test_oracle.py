@@ -169,3 +169,17 @@ def test_oracle_golden_fixtures():
         np.testing.assert_array_equal(T, g["T_" + tag])
         np.testing.assert_array_equal(Z, g["Z_" + tag])
         np.testing.assert_array_equal(w, g["w_" + tag])
+
+
+def test_quad_fixture_pins_fp64_oracle():
+    """The 113-bit fixture of the n = 256 inputs: its own residuals are at quad level,
+    and the FP64 oracle's eigenvalues agree with it within the parity tolerance."""
+    import os
+    from common import eig_tolerances, match_eigenvalues
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "quad_256.npz"))
+    assert max(G["res_c256"]) < 1e-28 and max(G["res_cond256"]) < 1e-28
+    for key in ("c256", "cond256"):
+        A = G["A_" + key]
+        w, tol = eig_tolerances(A, po)
+        ok, worst = match_eigenvalues(w, G["w_" + key], tol)
+        assert ok, "%s: worst err/tol %.3g" % (key, worst)
