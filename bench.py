@@ -298,6 +298,7 @@ def run_ours(args):
             "kernel_ms": kernel_ms}
     cpu = None if args.no_cpu else cpu_baseline_sample(args.count, SEED)
     per_matrix = measure_per_matrix(ctx, packed, ns, offs)
+    secondary = measure_complex_and_adjoint(ctx, torch, dev, stream)
     large = None
     if not args.no_large:
         ctx.set_stream(None)
@@ -310,7 +311,7 @@ def run_ours(args):
                             "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
            "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
-           "large": large}
+           "large": large, **secondary}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -381,6 +382,77 @@ def measure_per_matrix(ctx, packed, ns, offs, sample=200):
     dt = time.perf_counter() - t
     return {"value": m / dt, "unit": UNIT, "sample": "first %d matrices of the batch, one gs_schur_f64 call each "
             "(device buffers)" % m}
+
+
+def measure_complex_and_adjoint(ctx, torch, dev, stream, steps=3):
+    """Secondary configs on device-resident inputs, CUDA events on the library's stream:
+    (a) gschur! over 5,000 ComplexF64 matrices, n ~ U{8..128}, seed 5 (one persistent
+    launch sequence); (b) the differentiation workload -- 4,096 complex 64 x 64 matrices,
+    seed 7: forward Schur + eigenvalue adjoint (eigenvectors recomputed from T, Z) per step."""
+    from genericschur_gb300 import _capi
+    from genericschur_gb300.workloads import adjoint_batch, batched_cplx, cplx_flops, logsumexp_loss
+    out = {}
+
+    def timed(fn, k):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    for name, (packed, ns, offs, woffs) in (("complex_batched", batched_cplx(5000, seed=5)),
+                                            ("adjoint", adjoint_batch(4096, 64, seed=7))):
+        cnt = len(ns)
+        A0 = torch.from_numpy(packed.view(np.float64)).to(dev)
+        A = torch.empty_like(A0)
+        Z = torch.empty_like(A0)
+        w = torch.empty(2 * int(ns.sum()), dtype=torch.float64, device=dev)
+        st = torch.empty(cnt, dtype=torch.int32, device=dev)
+        dns = torch.from_numpy(ns).to(dev)
+        doffs = torch.from_numpy(offs).to(dev)
+        dwoffs = torch.from_numpy(woffs).to(dev)
+        flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | _capi.GS_GRAPH
+
+        def fwd():
+            A.copy_(A0)
+            rc = ctx.lib.gs_schur_batched_c64(ctx.handle, cnt, dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
+                                              A.data_ptr(), Z.data_ptr(), w.data_ptr(), st.data_ptr(), flags)
+            if rc != 0:
+                raise RuntimeError(ctx.last_error())
+
+        if name == "complex_batched":
+            ms = timed(fwd, steps)
+            out[name] = {"value": cnt / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                         "workload": "5000 ComplexF64 matrices, n~U{8..128}, re/im N(0,1/2), seed 5",
+                         "tflops_100n3": cplx_flops(ns) / (ms * 1e-3) / 1e12}
+        else:
+            fwd()
+            torch.cuda.synchronize()
+            _, gbar = logsumexp_loss(torch.view_as_complex(w.view(-1, 2)).cpu().numpy(), woffs, 64)
+            dg = torch.from_numpy(gbar.view(np.float64)).to(dev)
+            G = torch.empty_like(A0)
+            plen, wlen = len(packed), int(ns.sum())
+
+            def step():
+                fwd()
+                rc = ctx.lib.gs_eig_adjoint_batched_c64(ctx.handle, cnt, dns.data_ptr(), doffs.data_ptr(),
+                                                        dwoffs.data_ptr(), plen, wlen, A.data_ptr(), Z.data_ptr(),
+                                                        dg.data_ptr(), G.data_ptr(), _capi.GS_DEVICE)
+                if rc != 0:
+                    raise RuntimeError(ctx.last_error())
+
+            ms = timed(step, steps)
+            out[name] = {"value": cnt / (ms * 1e-3), "unit": "matrices/s (forward Schur + eigenvalue adjoint)",
+                         "ms_per_step": ms,
+                         "workload": "4096 ComplexF64 64x64, entries complex N(0,1/2)/8, seed 7, "
+                                     "loss sum logsumexp(Re(l)/0.1)"}
+    return out
 
 
 def measure_e2e(ctx, packed, ns, offs, woffs, steps):

@@ -339,7 +339,169 @@ __device__ bool swap_blocks(const AedCtx<T>& a, int j1, int n1, int n2) {
   return true;
 }
 
+// dtrexc's move towards the top (GenericSchur's _trexchange!, rordschur.jl:54-166,
+// iold > inew branch): the block at iold moves to inew by adjacent swaps; a 2x2 block
+// that splits into two real eigenvalues on the way continues as two 1x1 blocks.
+// Returns the final position, or -position - 1 if a swap was rejected.  Collective.
+template <class T>
+__device__ int trexchange_up(const AedCtx<T>& a, int iold, int inew) {
+  const int n = a.nw;  // 1-based positions below
+#define T1(i, j) a.t[((i) - 1) + ((j) - 1) * a.ldt]
+  auto nbsize = [&](int j) { return (j < n && T1(j + 1, j) != T(0)) ? 2 : 1; };
+  if (iold > 1 && T1(iold, iold - 1) != T(0)) iold -= 1;
+  int nbold = nbsize(iold);
+  if (inew > 1 && T1(inew, inew - 1) != T(0)) inew -= 1;
+  if (iold == inew) return inew;
+  int here = iold;
+  while (here > inew) {
+    if (nbold == 1 || nbold == 2) {
+      const int nbnext = (here >= 3 && T1(here - 1, here - 2) != T(0)) ? 2 : 1;
+      if (!swap_blocks(a, here - nbnext - 1, nbnext, nbold)) return -here - 1;
+      here -= nbnext;
+      if (nbold == 2 && T1(here + 1, here) == T(0)) nbold = 3;
+    } else {
+      // two 1x1 blocks, each swapped on its own
+      int nbnext = (here >= 3 && T1(here - 1, here - 2) != T(0)) ? 2 : 1;
+      if (!swap_blocks(a, here - nbnext - 1, nbnext, 1)) return -here - 1;
+      if (nbnext == 1) {
+        swap_blocks(a, here - 1, nbnext, 1);
+        here -= 1;
+      } else {
+        if (T1(here, here - 1) == T(0)) nbnext = 1;
+        if (nbnext == 2) {
+          if (!swap_blocks(a, here - 2, 2, 1)) return -here - 1;
+          here -= 2;
+        } else {
+          swap_blocks(a, here - 1, 1, 1);
+          swap_blocks(a, here - 2, 1, 1);
+          here -= 2;
+        }
+      }
+    }
+  }
+#undef T1
+  return here;
+}
+
 }  // namespace
+
+// gordschur!(T, Z, select) for a real standard-form Schur pair (rordschur.jl:3-47):
+// selected eigenvalues (a 2x2 block is selected if either of its eigenvalues is) move
+// to the top in their order.  One CTA on T and Z in global memory (ld n).
+// st[0] = 0, or k (1-based) of the block whose swap was rejected.
+template <class T>
+__global__ void __launch_bounds__(kAedThreads) k_ordschur_real(T* Tm, T* Zm, int n, const int* __restrict__ select,
+                                                                double* wr, double* wi, int* st) {
+  __shared__ AedShared<T> sh;
+  AedCtx<T> a{Tm, n, Zm, n, &sh};
+  const int tid = threadIdx.x;
+  int ks = 0;
+  bool pair = false;
+  int err = 0;
+  for (int k = 1; k <= n; ++k) {
+    if (pair) { pair = false; continue; }
+    bool sw = select[k - 1] != 0;
+    if (k < n && Tm[(k - 1) * (size_t)n + k] != T(0)) {
+      pair = true;
+      sw = sw || select[k] != 0;
+    }
+    if (sw) {
+      ks += 1;
+      if (k != ks) {
+        const int r = trexchange_up(a, k, ks);
+        if (r < 0) { err = k; break; }
+        ks = r;
+      }
+      if (pair) ks += 1;
+    }
+  }
+  __syncthreads();
+  for (int j = tid; j < n; j += kAedThreads) {
+    const T d = Tm[(size_t)j * n + j];
+    double im = 0.0;
+    if (j + 1 < n && Tm[(size_t)j * n + j + 1] != T(0))
+      im = sqrt(fabs((double)Tm[(size_t)(j + 1) * n + j])) * sqrt(fabs((double)Tm[(size_t)j * n + j + 1]));
+    else if (j > 0 && Tm[(size_t)(j - 1) * n + j] != T(0))
+      im = -sqrt(fabs((double)Tm[(size_t)j * n + j - 1])) * sqrt(fabs((double)Tm[(size_t)(j - 1) * n + j]));
+    wr[j] = (double)d;
+    wi[j] = im;
+  }
+  if (tid == 0) st[0] = err;
+}
+
+// gordschur!(T, Z, select) for a complex triangular Schur pair (ordschur.jl:24-74):
+// selected eigenvalues move to the top in their order by adjacent swaps, each a plane
+// rotation G with G [T(k,k+1); T(k+1,k+1) - T(k,k)] = [r; 0] applied as T <- G T G^H,
+// Z <- Z G^H (Golub and Van Loan, Algorithm 7.6.1).  One CTA on T, Z in global memory.
+__global__ void __launch_bounds__(kAedThreads) k_ordschur_cplx(double2* Tm, double2* Zm, int n,
+                                                                const int* __restrict__ select, double2* w) {
+  __shared__ double c_s;
+  __shared__ double2 s_s;
+  const int tid = threadIdx.x;
+  int ks = 0;
+  for (int k = 1; k <= n; ++k) {
+    if (!select[k - 1]) continue;
+    ks += 1;
+    for (int kk = k - 1; kk >= ks; --kk) {
+      // swap the diagonal entries kk, kk+1 (1-based)
+      if (tid == 0) {
+        const double2 f = Tm[(size_t)kk * n + (kk - 1)];                        // T(kk, kk+1)
+        const double2 g = zsub(Tm[(size_t)kk * n + kk], Tm[(size_t)(kk - 1) * n + (kk - 1)]);
+        const double af = hypot(f.x, f.y), ag = hypot(g.x, g.y);
+        double c;
+        double2 sv;
+        if (ag == 0.0) { c = 1.0; sv = make_double2(0.0, 0.0); }
+        else if (af == 0.0) { c = 0.0; sv = zscal(zconj(g), 1.0 / ag); }
+        else {
+          const double rho = hypot(af, ag);
+          c = af / rho;
+          sv = zscal(zmul(zscal(f, 1.0 / af), zconj(g)), 1.0 / rho);
+        }
+        c_s = c;
+        s_s = sv;
+      }
+      __syncthreads();
+      const double c = c_s;
+      const double2 sv = s_s;
+      // rows kk, kk+1 of T (all columns): [x; y] <- [c x + s y; -conj(s) x + c y]
+      for (int j = tid; j < n; j += kAedThreads) {
+        double2* x = &Tm[(size_t)j * n + (kk - 1)];
+        double2* y = &Tm[(size_t)j * n + kk];
+        const double2 a0 = *x, b0 = *y;
+        *x = zadd(zscal(a0, c), zmul(sv, b0));
+        *y = zsub(zscal(b0, c), zmul(zconj(sv), a0));
+      }
+      __syncthreads();
+      // columns kk, kk+1 of T and Z (all rows): [u v] <- [c u + conj(s) v, -s u + c v]
+      for (int i = tid; i < 2 * n; i += kAedThreads) {
+        double2* M = i < n ? Tm : Zm;
+        const int r = i < n ? i : i - n;
+        double2* u = &M[(size_t)(kk - 1) * n + r];
+        double2* v = &M[(size_t)kk * n + r];
+        const double2 a0 = *u, b0 = *v;
+        *u = zadd(zscal(a0, c), zmul(zconj(sv), b0));
+        *v = zsub(zscal(b0, c), zmul(sv, a0));
+      }
+      __syncthreads();
+    }
+  }
+  // triu!(T); values = diag(T)
+  for (size_t idx = tid; idx < (size_t)n * n; idx += kAedThreads) {
+    const int i = idx % n, j = idx / n;
+    if (i > j) Tm[idx] = make_double2(0.0, 0.0);
+    if (i == j) w[i] = Tm[idx];
+  }
+}
+
+cudaError_t launch_ordschur_real(double* T, double* Z, int n, const int* select, double* wr, double* wi, int* st,
+                                 cudaStream_t s) {
+  k_ordschur_real<double><<<1, kAedThreads, 0, s>>>(T, Z, n, select, wr, wi, st);
+  return cudaGetLastError();
+}
+cudaError_t launch_ordschur_cplx(double2* T, double2* Z, int n, const int* select, double2* w, cudaStream_t s) {
+  k_ordschur_cplx<<<1, kAedThreads, 0, s>>>(T, Z, n, select, w);
+  return cudaGetLastError();
+}
 
 template <class T>
 __global__ void __launch_bounds__(kAedThreads) k_aed(AedArgs<T> g) {

@@ -17,8 +17,8 @@
 // right eigenvectors of W = P T^H P (P the index reversal, W upper triangular):
 // y = P x.  The xLATRS-style rescaling of _usolve!/_cusolve! is not carried out for
 // n > 128 (the systems are solved directly with the floored diagonal); a column
-// whose solution overflows is reported as GS_CUDA-free failure by the host (non-finite
-// entries), which the reference would have rescaled instead.
+// whose solution overflows (non-finite entries) makes the call return GS_UNCONVERGED,
+// where the reference would have rescaled it instead.
 #include "device_common.cuh"
 #include "gs_internal.h"
 
@@ -239,6 +239,12 @@ __global__ void k_ev_scatter(int n, const double2* __restrict__ src, double2* __
 }  // namespace
 
 size_t eigvecs_large_ws_elems(int n) { return 3 * (size_t)n * n; }
+
+cudaError_t launch_enormalize(int n, int m, double2* V, int normalize, int* bad, cudaStream_t s) {
+  // columns of V (n x m, ld n): 1 / max|v|_1, then _enormalize! when normalize
+  k_ev_normalize<<<(m + 7) / 8, 256, 0, s>>>(n, V, normalize, bad);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_eigvecs_large(int n, const double2* T, const double2* Z, double2* VR, double2* VL, int normalize,
                                  const int* cmap, double2* ws, int* bad, cudaStream_t s) {

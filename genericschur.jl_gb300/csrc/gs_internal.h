@@ -77,6 +77,19 @@ size_t eigvecs_smem_bytes(int nmax);
 size_t eigvecs_large_ws_elems(int n);
 cudaError_t launch_eigvecs_large(int n, const double2* T, const double2* Z, double2* VR, double2* VL, int normalize,
                                  const int* cmap, double2* ws, int* bad, cudaStream_t s);
+cudaError_t launch_enormalize(int n, int m, double2* V, int normalize, int* bad, cudaStream_t s);
+
+// Balancing (balance.cu).
+template <class S>
+cudaError_t launch_bal_mark(const S* A, int lda, int lo, int hi, int rows, int* flag, int num_sms, cudaStream_t s);
+cudaError_t launch_bal_pick(const int* flag, int lo, int hi, int rows, int* out, cudaStream_t s);
+template <class S>
+cudaError_t launch_bal_swap(S* A, int lda, int n, int p, int q, int rows, int c0, cudaStream_t s);
+template <class S>
+cudaError_t launch_bal_scale(S* A, int lda, int n, int ilo, int ihi, double* D, int* st, cudaStream_t s);
+cudaError_t launch_bal_apply(int n, int m, const double2* V, int ldv, double2* W, const int* src, const double* D,
+                             int scale, int inverse, int num_sms, cudaStream_t s);
+cudaError_t launch_rconde(int n, int m, const double2* VL, const double2* VR, double* out, cudaStream_t s);
 cudaError_t launch_eigvecs_batched(const EigBatch& eb, int nmax, int num_sms, cudaStream_t s);
 
 // Real quasi-triangular -> complex triangular Schur pairs (triang.jl:9-43).
@@ -149,6 +162,10 @@ struct AedArgs {
   int* out;               // [undeflated count, deflated count, H modified]
 };
 template <class T> cudaError_t launch_aed(const AedArgs<T>& g, cudaStream_t s);
+// Schur reordering (aed.cu): real standard form (st[0] = 0 or the rejected block) and complex.
+cudaError_t launch_ordschur_real(double* T, double* Z, int n, const int* select, double* wr, double* wi, int* st,
+                                 cudaStream_t s);
+cudaError_t launch_ordschur_cplx(double2* T, double2* Z, int n, const int* select, double2* w, cudaStream_t s);
 
 // One large real Schur decomposition (schur_large_host.cu).
 template <class T>

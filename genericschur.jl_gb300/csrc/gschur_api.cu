@@ -1356,3 +1356,284 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// balancing (balance!, balance.jl:33-185) and the Balancer on eigenvectors
+// ---------------------------------------------------------------------------
+template <class S>
+static int balance_impl(gs_context* ctx, int64_t n, S* A, int64_t lda, unsigned flags, int64_t* info, int64_t* sp,
+                        double* D) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (lda < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
+  if (!info || (n > 0 && (!A || !sp || !D))) return set_err(ctx, GS_BADARG, "null array argument");
+  for (int64_t i = 0; i < n; ++i) { sp[i] = 0; D[i] = 1.0; }
+  info[0] = 1; info[1] = n; info[2] = 1;
+  if (n == 0) return GS_OK;
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const bool permute = flags & GS_BAL_PERMUTE, scale = flags & GS_SCALE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_A = ar.take<S>(dev ? 1 : nn), o_flag = ar.take<int>(n + 2), o_pick = ar.take<int>(4),
+               o_D = ar.take<double>(n), o_st = ar.take<int>(4);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  S* dA = dev ? A : (S*)(base + o_A);
+  const int ld = dev ? (int)lda : (int)n;
+  if (!dev)
+    CK(cudaMemcpy2DAsync(dA, n * sizeof(S), A, lda * sizeof(S), n * sizeof(S), n, cudaMemcpyHostToDevice, s));
+  int* flag = (int*)(base + o_flag);
+  int* pick = (int*)(base + o_pick);
+  const int N = (int)n;
+  int ilo = 1, ihi = N;
+  bool trivial = true;
+  auto search = [&](int lo, int hi, int rows, int* out) -> int {
+    CK(cudaMemsetAsync(flag, 0, sizeof(int) * (n + 2), s));
+    CK(launch_bal_mark<S>(dA, ld, lo, hi, rows, flag, ctx->num_sms, s));
+    CK(launch_bal_pick(flag, lo, hi, rows, pick, s));
+    CK(cudaMemcpyAsync(out, pick, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return GS_OK;
+  };
+  if (permute) {
+    // rows whose off-diagonal part inside the block vanishes go to the bottom (balance.jl:62-95)
+    ihi = N + 1;
+    while (ihi > 1) {
+      ihi -= 1;
+      int js = 0;
+      if ((rc = search(1, ihi, 1, &js)) != GS_OK) return rc;
+      if (js == 0) break;
+      sp[ihi - 1] = js;
+      if (js != ihi) {
+        trivial = false;
+        CK(launch_bal_swap<S>(dA, ld, N, js, ihi, ihi, ilo, s));
+      }
+    }
+    // columns whose off-diagonal part vanishes go to the left (balance.jl:96-130)
+    if (ihi > 1) {
+      ilo = 0;
+      while (ilo < N) {
+        ilo += 1;
+        int js = 0;
+        if ((rc = search(ilo, ihi, 0, &js)) != GS_OK) return rc;
+        if (js == 0) break;
+        sp[ilo - 1] = js;
+        if (js != ilo) {
+          trivial = false;
+          CK(launch_bal_swap<S>(dA, ld, N, js, ilo, ihi, ilo, s));
+        }
+      }
+    }
+  }
+  if (scale) {
+    double* dD = (double*)(base + o_D);
+    int* st = (int*)(base + o_st);
+    std::vector<double> ones(n, 1.0);
+    CK(cudaMemcpyAsync(dD, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CK(launch_bal_scale<S>(dA, ld, N, ilo, ihi, dD, st, s));
+    int hst[2] = {0, 0};
+    CK(cudaMemcpyAsync(hst, st, sizeof(hst), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(D, dD, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (hst[0] == 2) return set_err(ctx, GS_BADARG, "NaN encountered while balancing");
+    if (hst[0] == 3) return set_err(ctx, GS_UNCONVERGED, "balancing did not settle within the sweep limit");
+    if (hst[1]) trivial = false;
+  }
+  if (!dev)
+    CK(cudaMemcpy2DAsync(A, lda * sizeof(S), dA, n * sizeof(S), n * sizeof(S), n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  info[0] = ilo;
+  info[1] = ihi;
+  info[2] = trivial ? 1 : 0;
+  return GS_OK;
+}
+
+extern "C" {
+
+int gs_balance_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, unsigned flags, int64_t* info, int64_t* sp,
+                   double* D) {
+  return balance_impl<double>(ctx, n, A, lda, flags, info, sp, D);
+}
+
+int gs_balance_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, unsigned flags, int64_t* info, int64_t* sp,
+                   double* D) {
+  return balance_impl<double2>(ctx, n, (double2*)A, lda, flags, info, sp, D);
+}
+
+int gs_balancer_apply_c64(gs_context* ctx, int64_t n, int64_t m, double* V, int64_t ldv, const int64_t* info,
+                          const int64_t* sp, const double* D, int inverse, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || m < 0 || ldv < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "bad dimensions");
+  if (!info || (n > 0 && m > 0 && (!V || !sp || !D))) return set_err(ctx, GS_BADARG, "null array argument");
+  const int64_t ilo = info[0], ihi = info[1], trivial = info[2];
+  if (n == 0 || m == 0 || trivial) return GS_OK;
+  if (ilo < 1 || ihi > n || ilo > ihi + 1) return set_err(ctx, GS_BADARG, "bad ilo/ihi");
+  // composed row permutation of the swaps (balance.jl:198-220), applied after the scaling
+  std::vector<int> src(n);
+  for (int64_t i = 0; i < n; ++i) src[i] = (int)i;
+  for (int64_t j = ilo - 1; j >= 1; --j) {
+    const int64_t mm = sp[j - 1];
+    if (mm < 1 || mm > n) return set_err(ctx, GS_BADARG, "bad permutation record");
+    if (mm != j) std::swap(src[j - 1], src[mm - 1]);
+  }
+  for (int64_t j = ihi + 1; j <= n; ++j) {
+    const int64_t mm = sp[j - 1];
+    if (mm < 1 || mm > n) return set_err(ctx, GS_BADARG, "bad permutation record");
+    if (mm != j) std::swap(src[j - 1], src[mm - 1]);
+  }
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nm = (size_t)n * m;
+  Arena ar;
+  const size_t o_V = ar.take<double2>(nm), o_W = ar.take<double2>(nm), o_src = ar.take<int>(n),
+               o_D = ar.take<double>(n);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double2* dV = (double2*)(base + o_V);
+  double2* dW = (double2*)(base + o_W);
+  int* dsrc = (int*)(base + o_src);
+  double* dD = (double*)(base + o_D);
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy2DAsync(dV, n * sizeof(double2), V, ldv * sizeof(double2), n * sizeof(double2), m, in, s));
+  CK(cudaMemcpyAsync(dsrc, src.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dD, D, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(launch_bal_apply((int)n, (int)m, dV, (int)n, dW, dsrc, dD, ilo != ihi, inverse, ctx->num_sms, s));
+  CK(cudaMemcpy2DAsync(V, ldv * sizeof(double2), dW, n * sizeof(double2), n * sizeof(double2), m, out, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+int gs_enormalize_c64(gs_context* ctx, int64_t n, int64_t m, double* V, int64_t ldv, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || m < 0 || ldv < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "bad dimensions");
+  if (n == 0 || m == 0) return GS_OK;
+  if (!V) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nm = (size_t)n * m;
+  Arena ar;
+  const size_t o_V = ar.take<double2>(nm), o_bad = ar.take<int>(4);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double2* dV = (double2*)(base + o_V);
+  int* bad = (int*)(base + o_bad);
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  CK(cudaMemcpy2DAsync(dV, n * sizeof(double2), V, ldv * sizeof(double2), n * sizeof(double2), m, in, s));
+  CK(launch_enormalize((int)n, (int)m, dV, !(flags & GS_RAW), bad, s));
+  CK(cudaMemcpy2DAsync(V, ldv * sizeof(double2), dV, n * sizeof(double2), n * sizeof(double2), m, out, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+int gs_rconde_c64(gs_context* ctx, int64_t n, const double* VL, const double* VR, double* rconde, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0) return set_err(ctx, GS_BADARG, "negative order");
+  if (n == 0) return GS_OK;
+  if (!VL || !VR || !rconde) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_L = ar.take<double2>(dev ? 1 : nn), o_R = ar.take<double2>(dev ? 1 : nn), o_o = ar.take<double>(n);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const double2* dL = (const double2*)VL;
+  const double2* dR = (const double2*)VR;
+  double* dout = dev ? rconde : (double*)(base + o_o);
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_L, VL, sizeof(double2) * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_R, VR, sizeof(double2) * nn, cudaMemcpyHostToDevice, s));
+    dL = (const double2*)(base + o_L);
+    dR = (const double2*)(base + o_R);
+  }
+  CK(launch_rconde((int)n, (int)n, dL, dR, dout, s));
+  if (!dev) CK(cudaMemcpyAsync(rconde, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+}  // extern "C"
+
+// gordschur!(T, Z, select): real standard form (rordschur.jl:3-47) or complex triangular
+// (ordschur.jl:24-74).  T, Z n x n, leading dimension n (in place); select n int32.
+static int ordschur_impl(gs_context* ctx, int64_t n, double* T, double* Z, const int32_t* select, double* wr,
+                         double* wi, unsigned flags, bool cplx) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (n == 0) return GS_OK;
+  if (!T || !Z || !select || !wr || (!cplx && !wi)) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n, es = cplx ? sizeof(double2) : sizeof(double);
+  Arena ar;
+  const size_t o_T = ar.take<char>(dev ? 1 : es * nn), o_Z = ar.take<char>(dev ? 1 : es * nn),
+               o_sel = ar.take<int>(n), o_w = ar.take<double>(2 * n), o_st = ar.take<int>(4);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  void* dT = dev ? (void*)T : (void*)(base + o_T);
+  void* dZ = dev ? (void*)Z : (void*)(base + o_Z);
+  int* dsel = (int*)(base + o_sel);
+  double* dw = (double*)(base + o_w);
+  int* dst = (int*)(base + o_st);
+  if (!dev) {
+    CK(cudaMemcpyAsync(dT, T, es * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dZ, Z, es * nn, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemcpyAsync(dsel, select, sizeof(int) * n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(dst, 0, sizeof(int), s));
+  CK(cudaEventRecord(ctx->t0, s));
+  if (cplx) CK(launch_ordschur_cplx((double2*)dT, (double2*)dZ, (int)n, dsel, (double2*)dw, s));
+  else CK(launch_ordschur_real((double*)dT, (double*)dZ, (int)n, dsel, dw, dw + n, dst, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (!dev) {
+    CK(cudaMemcpyAsync(T, dT, es * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Z, dZ, es * nn, cudaMemcpyDeviceToHost, s));
+  }
+  if (cplx) {
+    CK(cudaMemcpyAsync(wr, dw, sizeof(double2) * n, out, s));
+  } else {
+    CK(cudaMemcpyAsync(wr, dw, sizeof(double) * n, out, s));
+    CK(cudaMemcpyAsync(wi, dw + n, sizeof(double) * n, out, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (st) return set_err(ctx, GS_UNCONVERGED, "IllConditionException: block %d could not be swapped", st);
+  return GS_OK;
+}
+
+extern "C" {
+
+int gs_ordschur_f64(gs_context* ctx, int64_t n, double* T, double* Z, const int32_t* select, double* wr, double* wi,
+                    unsigned flags) {
+  return ordschur_impl(ctx, n, T, Z, select, wr, wi, flags, false);
+}
+
+int gs_ordschur_c64(gs_context* ctx, int64_t n, double* T, double* Z, const int32_t* select, double* w,
+                    unsigned flags) {
+  return ordschur_impl(ctx, n, T, Z, select, w, nullptr, flags, true);
+}
+
+}  // extern "C"
+

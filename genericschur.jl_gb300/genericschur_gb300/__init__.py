@@ -260,21 +260,164 @@ def triangularize(S, ctx=None):
     return Schur(Tc, Zc if Zc is not None else np.zeros((0, 0), dtype=np.complex128), w)
 
 
-def eigen(A, permute=False, scale=False, sortby="default", ctx=None):
-    """Eigen decomposition (pirates.jl:63-89): Schur form, triangularize for real
-    input, right eigenvectors, _enormalize!, sort.  Balancing (permute/scale,
-    balance.jl) is not part of this engine; asking for it raises ArgumentError."""
+Balancer = namedtuple("Balancer", ["ilo", "ihi", "prow_pcol", "D", "trivial"])
+
+
+def balance_(A, scale=True, permute=True, ctx=None):
+    """balance!(A; scale, permute) (balance.jl:33-185) on a Fortran-ordered float64 or
+    complex128 array, in place.  Returns (A, Balancer)."""
+    ctx = ctx or get_context()
+    n = _checksquare(A)
+    if not (A.flags.f_contiguous and A.dtype in (np.float64, np.complex128)):
+        raise ArgumentError("balance_ needs a Fortran-ordered float64 or complex128 array")
+    info = np.zeros(3, dtype=np.int64)
+    sp = np.zeros(max(n, 1), dtype=np.int64)
+    D = np.ones(max(n, 1))
+    flags = (GS_SCALE if scale else 0) | (_capi.GS_BAL_PERMUTE if permute else 0)
+    fn = ctx.lib.gs_balance_c64 if A.dtype == np.complex128 else ctx.lib.gs_balance_f64
+    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), flags, _ptr(info), _ptr(sp), _ptr(D))
+    if rc != GS_OK:
+        _raise(rc, ctx, "balance!")
+    return A, Balancer(int(info[0]), int(info[1]), sp[:n].copy(), D[:n].copy(), bool(info[2]))
+
+
+def balance(A, scale=True, permute=True, ctx=None):
+    """balance! on a copy of A."""
+    A = np.asarray(A)
+    dt = np.complex128 if np.iscomplexobj(A) else np.float64
+    return balance_(np.array(A, dtype=dt, order="F", copy=True), scale=scale, permute=permute, ctx=ctx)
+
+
+def _balancer_apply(B, V, inverse, ctx):
+    ctx = ctx or get_context()
+    V = np.array(V, dtype=np.complex128, order="F", copy=True)
+    n, m = V.shape
+    info = np.array([B.ilo, B.ihi, int(B.trivial)], dtype=np.int64)
+    sp = np.ascontiguousarray(B.prow_pcol, dtype=np.int64)
+    D = np.ascontiguousarray(B.D, dtype=np.float64)
+    rc = ctx.lib.gs_balancer_apply_c64(ctx.handle, n, m, _ptr(V), max(n, 1), _ptr(info), _ptr(sp), _ptr(D),
+                                       int(inverse), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "Balancer")
+    return V
+
+
+def balancer_lmul(B, V, ctx=None):
+    """lmul!(B, V): right eigenvectors of the balanced matrix -> of A (balance.jl:189-222)."""
+    return _balancer_apply(B, V, False, ctx)
+
+
+def balancer_ldiv(B, V, ctx=None):
+    """ldiv!(B, V): left eigenvectors of the balanced matrix -> of A (balance.jl:226-261)."""
+    return _balancer_apply(B, V, True, ctx)
+
+
+def enormalize(V, ctx=None):
+    """_enormalize! (util.jl:572-592) of the columns of V, on the GPU."""
+    ctx = ctx or get_context()
+    V = np.array(V, dtype=np.complex128, order="F", copy=True)
+    n, m = V.shape
+    rc = ctx.lib.gs_enormalize_c64(ctx.handle, n, m, _ptr(V), max(n, 1), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "_enormalize!")
+    return V
+
+
+def gordschur(S, select, ctx=None):
+    """gordschur!(S, select) / ordschur (ordschur.jl:12-74, rordschur.jl:3-47) on a copy:
+    the eigenvalues with select[k] true move to the leading positions, in their order.
+    Returns the reordered Schur(T, Z, values).  Raises UnconvergedException if a block
+    swap is rejected as ill-conditioned (the reference's IllConditionException)."""
+    ctx = ctx or get_context()
+    T = np.array(S.T, order="F", copy=True)
+    n = _checksquare(T)
+    sel = np.ascontiguousarray(np.asarray(select, dtype=bool).astype(np.int32))
+    if len(sel) != n:
+        raise DimensionMismatch("select must have length %d" % n)
+    cplx = np.iscomplexobj(T)
+    dt = np.complex128 if cplx else np.float64
+    T = np.array(T, dtype=dt, order="F")
+    Z = np.array(S.Z if (S.Z is not None and np.asarray(S.Z).size) else np.eye(n), dtype=dt, order="F", copy=True)
+    if cplx:
+        w = np.zeros(n, dtype=np.complex128)
+        rc = ctx.lib.gs_ordschur_c64(ctx.handle, n, _ptr(T), _ptr(Z), _ptr(sel), _ptr(w), 0)
+    else:
+        wr = np.zeros(n)
+        wi = np.zeros(n)
+        rc = ctx.lib.gs_ordschur_f64(ctx.handle, n, _ptr(T), _ptr(Z), _ptr(sel), _ptr(wr), _ptr(wi), 0)
+        w = wr + 1j * wi
+    if rc != GS_OK:
+        _raise(rc, ctx, "gordschur!")
+    return Schur(T, Z, w)
+
+
+ordschur = gordschur
+
+
+EigenFull = namedtuple("EigenFull", ["values", "vectors", "vectorsl", "rconde"])
+
+
+def rconde(VL, VR, ctx=None):
+    """Reciprocal eigenvalue condition numbers |vl_j^H vr_j| / (|vl_j| |vr_j|)
+    (pirates.jl:107-113), on the GPU."""
+    ctx = ctx or get_context()
+    VL = _fc(VL, np.complex128)
+    VR = _fc(VR, np.complex128)
+    n = _checksquare(VR)
+    out = np.zeros(n)
+    rc = ctx.lib.gs_rconde_c64(ctx.handle, n, _ptr(VL), _ptr(VR), _ptr(out), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "rconde")
+    return out
+
+
+def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, ctx=None):
+    """Eigen decomposition (pirates.jl:63-160): balance! (permute/scale, as the reference's
+    defaults), Schur form, triangularize for real input, right eigenvectors (and left
+    ones with jvl or jce), the Balancer's lmul!/ldiv!, _enormalize!, sort.  With jce the
+    reciprocal eigenvalue condition numbers are computed from the balanced form's
+    vectors, as the reference does.  Returns Eigen(values, vectors), or, when jvl or
+    jce is asked for, EigenFull(values, vectors, vectorsl, rconde)."""
+    A = np.asarray(A)
+    B = None
     if permute or scale:
-        raise ArgumentError("balancing is not implemented by the GB300 engine; call eigen(A, permute=False, scale=False)")
+        A, B = balance(A, scale=scale, permute=permute, ctx=ctx)
     S = gschur(A, ctx=ctx)
     if not np.iscomplexobj(S.T):
         S = triangularize(S, ctx=ctx)
-    V = geigvecs(S, ctx=ctx)
+    full = jvl or jce
     w = S.values
+    if not full:
+        if B is not None:
+            V = geigvecs(S, normalize=False, ctx=ctx)
+            V = balancer_lmul(B, V, ctx=ctx)
+            V = enormalize(V, ctx=ctx)
+        else:
+            V = geigvecs(S, ctx=ctx)
+        if sortby is None:
+            return Eigen(w, V)
+        p = _eigsortby(w) if sortby == "default" else np.argsort([sortby(x) for x in w], kind="stable")
+        return Eigen(w[p], V[:, p])
+    n = S.T.shape[0]
+    V = geigvecs(S, normalize=False, ctx=ctx) if (jvr or jce) else np.zeros((0, 0), dtype=np.complex128)
+    VL = geigvecs(S, left=True, normalize=False, ctx=ctx)
+    rce = rconde(VL, V, ctx=ctx) if jce else np.zeros(0)
+    if jvr:
+        if B is not None:
+            V = balancer_lmul(B, V, ctx=ctx)
+        V = enormalize(V, ctx=ctx)
+    else:
+        V = np.zeros((0, 0), dtype=np.complex128)
+    if jvl:
+        if B is not None:
+            VL = balancer_ldiv(B, VL, ctx=ctx)
+        VL = enormalize(VL, ctx=ctx)
+    else:
+        VL = np.zeros((0, 0), dtype=np.complex128)
     if sortby is None:
-        return Eigen(w, V)
+        return EigenFull(w, V, VL, rce)
     p = _eigsortby(w) if sortby == "default" else np.argsort([sortby(x) for x in w], kind="stable")
-    return Eigen(w[p], V[:, p])
+    return EigenFull(w[p], V[:, p] if V.size else V, VL[:, p] if VL.size else VL, rce[p] if rce.size else rce)
 
 
 def geigvecs_batched(T_packed, Z_packed, ns, offs, woffs=None, left=False, normalize=True, ctx=None):

@@ -22,6 +22,7 @@ GS_DEVICE = 4
 GS_GRAPH = 8
 GS_RAW = 16
 GS_NOFALLBACK = 32
+GS_BAL_PERMUTE = 64
 
 _i = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -52,6 +53,13 @@ SIGNATURES = {
     "gs_eig_adjoint_batched_c64": (_i, [_p, _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p, _u]),
     "gs_hessenberg_f64": (_i, [_p, _i64, _p, _i64, _p, _p, _i64, _u]),
     "gs_schur_mixed_f64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64, _p]),
+    "gs_balance_f64": (_i, [_p, _i64, _p, _i64, _u, _p, _p, _p]),
+    "gs_balance_c64": (_i, [_p, _i64, _p, _i64, _u, _p, _p, _p]),
+    "gs_balancer_apply_c64": (_i, [_p, _i64, _i64, _p, _i64, _p, _p, _p, _i, _u]),
+    "gs_enormalize_c64": (_i, [_p, _i64, _i64, _p, _i64, _u]),
+    "gs_rconde_c64": (_i, [_p, _i64, _p, _p, _p, _u]),
+    "gs_ordschur_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _u]),
+    "gs_ordschur_c64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
 }
 # allocation-free entry point (include/gschur_gb300_noalloc.h)
 SIGNATURES["gs_schur_batched_f64_noalloc"] = (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u])

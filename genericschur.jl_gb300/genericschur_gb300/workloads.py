@@ -54,7 +54,7 @@ def cplx_flops(ns):
 
 
 __all__ = ["batch_sizes", "batched_real", "batched_cplx", "real_flops", "cplx_flops", "pack_batch", "conditioned_matrix",
-           "large_real", "LARGE_SEEDS"]
+           "large_real", "LARGE_SEEDS", "adjoint_batch", "logsumexp_loss"]
 
 
 def conditioned_matrix(n=2048, seed=6, cond=1e3, lo=1e-3, hi=1e3):
@@ -81,3 +81,28 @@ def large_real(n=4096, seed=None):
         seed = LARGE_SEEDS.get(n, n)
     rng = np.random.default_rng(seed)
     return np.asfortranarray(rng.standard_normal((n, n)))
+
+
+def adjoint_batch(count=4096, n=64, seed=7):
+    """The differentiation workload: count complex n x n matrices, entries iid complex
+    N(0, 1/2) / sqrt(n) (real and imaginary parts N(0, 1/2), then scaled).
+    Returns (packed, ns, offs, woffs)."""
+    rng = np.random.default_rng(seed)
+    ns = np.full(count, n, dtype=np.int32)
+    offs = (np.arange(count, dtype=np.int64) * n * n)
+    woffs = (np.arange(count, dtype=np.int64) * n)
+    m = count * n * n
+    packed = (rng.standard_normal(m) + 1j * rng.standard_normal(m)) / np.sqrt(2.0) / np.sqrt(n)
+    return packed, ns, offs, woffs
+
+
+def logsumexp_loss(w_packed, woffs, n, tau=0.1):
+    """L = sum_b logsumexp(Re(l_b) / tau) and its cotangent dL/dRe(l) (as complex)."""
+    W = np.asarray(w_packed).reshape(-1, n)
+    x = W.real / tau
+    m = x.max(axis=1, keepdims=True)
+    e = np.exp(x - m)
+    s = e.sum(axis=1, keepdims=True)
+    L = float(np.sum(m[:, 0] + np.log(s[:, 0])))
+    gbar = (e / s / tau).astype(np.complex128).ravel()
+    return L, gbar

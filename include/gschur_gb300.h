@@ -47,6 +47,7 @@ extern "C" {
 #define GS_GRAPH 8u   /* batched calls: replay a cached CUDA graph of the launch sequence         */
 #define GS_RAW 16u    /* eigenvectors: skip _enormalize! (return the max-|re|+|im|-scaled vectors) */
 #define GS_NOFALLBACK 32u /* mixed precision: report GS_UNCONVERGED instead of recomputing in FP64   */
+#define GS_BAL_PERMUTE 64u /* balancing: search the row/column permutations (with GS_SCALE: scale too) */
 
 typedef struct gs_context gs_context;
 
@@ -200,6 +201,47 @@ GS_API int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda
  * A = Q H Q^T.  Any n. */
 GS_API int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* tau, double* Q, int64_t ldq,
                              unsigned flags);
+
+/* ---------------------------------------------------------------------------
+ * Balancing.  Replaces balance!(A; scale, permute) (balance.jl:33-185): with
+ * GS_BAL_PERMUTE, row/column permutations bring A to [T1 X Y; 0 C Z; 0 0 T2] (T1, T2
+ * upper triangular, C = A[ilo:ihi, ilo:ihi]); with GS_SCALE, powers of two balance the
+ * rows and columns of C (2-norms, the reference's "pr" variant).  A is overwritten
+ * by the balanced matrix; info receives {ilo, ihi, trivial}, sp (n) the permutation
+ * record (1-based, sp[j-1] for j < ilo and j > ihi), D (n) the scale factors.
+ * Returns GS_BADARG on NaN (the reference throws "NaN encountered while balancing").
+ * The complex form takes interleaved ComplexF64. */
+GS_API int gs_balance_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, unsigned flags, int64_t* info,
+                          int64_t* sp, double* D);
+GS_API int gs_balance_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, unsigned flags, int64_t* info,
+                          int64_t* sp, double* D);
+
+/* The Balancer on eigenvectors: lmul!(B, V) (inverse = 0, right eigenvectors of the
+ * balanced matrix -> of A) or ldiv!(B, V) (inverse = 1, left eigenvectors)
+ * (balance.jl:189-261).  V: n x m interleaved complex, leading dimension ldv. */
+GS_API int gs_balancer_apply_c64(gs_context* ctx, int64_t n, int64_t m, double* V, int64_t ldv, const int64_t* info,
+                                 const int64_t* sp, const double* D, int inverse, unsigned flags);
+
+/* Column normalisation of eigenvectors: each column scaled by 1 / max |v|_1, then (unless
+ * GS_RAW) _enormalize! (util.jl:572-592): unit 2-norm, largest-modulus entry real. */
+GS_API int gs_enormalize_c64(gs_context* ctx, int64_t n, int64_t m, double* V, int64_t ldv, unsigned flags);
+
+/* Reciprocal eigenvalue condition numbers from left/right eigenvector matrices
+ * (eigen!(A; jce = true), pirates.jl:107-113): rconde[j] = |vl_j^H vr_j| /
+ * (|vl_j|_2 |vr_j|_2).  VL, VR: n x n interleaved complex, ld n. */
+GS_API int gs_rconde_c64(gs_context* ctx, int64_t n, const double* VL, const double* VR, double* rconde, unsigned flags);
+
+/* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
+ * eigenvalues with select[k] != 0 move to the leading positions in their order.
+ * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if
+ * either of its eigenvalues is): T, Z n x n real, wr/wi the new eigenvalues.
+ * Complex (ordschur.jl:24-74): T, Z interleaved complex, w the new diagonal.
+ * T, Z in place, leading dimension n.  GS_UNCONVERGED if a block swap is rejected as
+ * ill-conditioned (the reference's IllConditionException). */
+GS_API int gs_ordschur_f64(gs_context* ctx, int64_t n, double* T, double* Z, const int32_t* select, double* wr,
+                           double* wi, unsigned flags);
+GS_API int gs_ordschur_c64(gs_context* ctx, int64_t n, double* T, double* Z, const int32_t* select, double* w,
+                           unsigned flags);
 
 #ifdef __cplusplus
 }

@@ -5,6 +5,7 @@
 #include <vector>
 #include "gschur_oracle.hpp"
 #include "eigvecs_oracle.hpp"
+#include "balance_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -163,6 +164,20 @@ int or_eigvecs_z(int n, const double* t, const double* z, double* v, int left, i
 
 int or_triangularize_d(int n, const double* t, const double* z, double* tc, double* zc_out, double* w) {
   triangularize<double>(n, t, n, z, n, (zc*)tc, (zc*)zc_out, (zc*)w);
+  return 0;
+}
+
+// balance! (balance.jl:33-185): out3 = {ilo, ihi, trivial}, sp / D of length n.
+int or_balance_d(int n, double* a, int lda, int scale, int permute, int* out3, int* sp, double* d) {
+  return balance<double, double>(n, a, lda, scale != 0, permute != 0, &out3[0], &out3[1], sp, d, &out3[2]);
+}
+int or_balance_z(int n, double* a, int lda, int scale, int permute, int* out3, int* sp, double* d) {
+  return balance<double, zc>(n, (zc*)a, lda, scale != 0, permute != 0, &out3[0], &out3[1], sp, d, &out3[2]);
+}
+// lmul!(B, V) / ldiv!(B, V) on complex V (n x m)
+int or_balancer_apply_z(int n, int m, double* v, int ldv, int ilo, int ihi, const int* sp, const double* d,
+                        int trivial, int inverse) {
+  balancer_apply<double, zc>(n, m, (zc*)v, ldv, ilo, ihi, sp, d, trivial != 0, inverse != 0);
   return 0;
 }
 

@@ -39,6 +39,9 @@ def lib():
             "or_reflector_d": [_p, _i, _p],
             "or_gschur_batched_d": [_i, _p, _p, _p, _p, _p, _p, _p, _p, _i],
             "or_gschur_batched_z": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
+            "or_balance_d": [_i, _p, _i, _i, _i, _p, _p, _p],
+            "or_balance_z": [_i, _p, _i, _i, _i, _p, _p, _p],
+            "or_balancer_apply_z": [_i, _i, _p, _i, _i, _i, _p, _p, _i, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -203,3 +206,29 @@ def gschur_batched_packed_real(count, offs, ns, a, z, wr, wi, woffs, status, nth
 def gschur_batched_packed_cplx(count, offs, ns, a, z, w, woffs, status, nthreads):
     return lib().or_gschur_batched_z(count, _ptr(offs), _ptr(ns), _ptr(a), _ptr(z), _ptr(w), _ptr(woffs),
                                      _ptr(status), nthreads)
+
+
+def balance(A, scale=True, permute=True):
+    """balance!(A; scale, permute) (balance.jl:33-185).  Returns (Abal, (ilo, ihi, sp, D,
+    trivial)) with sp the 1-based permutation record and D the scale factors."""
+    cplx = np.iscomplexobj(A)
+    A = _f(A, np.complex128 if cplx else np.float64)
+    n = A.shape[0]
+    out = np.zeros(3, dtype=np.int32)
+    sp = np.zeros(max(n, 1), dtype=np.int32)
+    D = np.ones(max(n, 1))
+    fn = lib().or_balance_z if cplx else lib().or_balance_d
+    rc = fn(n, _ptr(A), max(n, 1), int(scale), int(permute), _ptr(out), _ptr(sp), _ptr(D))
+    if rc:
+        raise ValueError("NaN encountered while balancing")
+    return A, (int(out[0]), int(out[1]), sp[:n].copy(), D[:n].copy(), bool(out[2]))
+
+
+def balancer_apply(V, B, inverse=False):
+    """lmul!(B, V) (right eigenvectors) or ldiv!(B, V) (left eigenvectors) on complex V."""
+    ilo, ihi, sp, D, trivial = B
+    V = _f(V, np.complex128)
+    n, m = V.shape
+    lib().or_balancer_apply_z(n, m, _ptr(V), max(n, 1), ilo, ihi, _ptr(np.ascontiguousarray(sp, dtype=np.int32)),
+                              _ptr(np.ascontiguousarray(D, dtype=np.float64)), int(trivial), int(inverse))
+    return V

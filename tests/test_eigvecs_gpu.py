@@ -98,8 +98,8 @@ def test_eigen(gs, cplx, n):
     assert np.all(np.diff(E.values.real) >= 0)
     _vectest(A, E.values, E.vectors, None)
     _normalized(E.vectors)
-    with pytest.raises(gs.ArgumentError):
-        gs.eigen(A, permute=True)
+    E2 = gs.eigen(A, permute=False, scale=False)
+    _vectest(A, E2.values, E2.vectors, None)
 
 
 def test_eigvecs_of_T_only(gs):

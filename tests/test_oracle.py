@@ -183,3 +183,22 @@ def test_quad_fixture_pins_fp64_oracle():
         w, tol = eig_tolerances(A, po)
         ok, worst = match_eigenvalues(w, G["w_" + key], tol)
         assert ok, "%s: worst err/tol %.3g" % (key, worst)
+
+
+def test_oracle_balance_restatement():
+    """balance! restated (balance.jl:33-185): eigenvalues are preserved, the block
+    structure [T1 X Y; 0 C Z; 0 0 T2] holds, and lmul!(B, V) maps eigenvectors of the
+    balanced matrix to eigenvectors of A."""
+    rng = np.random.default_rng(4700)
+    A = rng.standard_normal((10, 10))
+    A[7:, :7] = 0.0
+    A[8, 7] = 0.0
+    A[9, 7:9] = 0.0
+    d = 10.0 ** rng.integers(-4, 5, size=10)
+    A = (A * d[None, :]) / d[:, None]
+    Ab, B = po.balance(A)
+    ilo, ihi = B[0], B[1]
+    assert np.all(Ab[ihi:, :ihi] == 0) and np.all(Ab[ilo - 1:, :ilo - 1] == 0)
+    wb, Vb = np.linalg.eig(Ab)
+    V = po.balancer_apply(Vb, B)
+    assert np.linalg.norm(A @ V - V @ np.diag(wb)) <= 1e-10 * np.linalg.norm(A) * np.linalg.norm(V)
