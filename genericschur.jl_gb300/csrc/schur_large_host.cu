@@ -153,16 +153,20 @@ int schur_large_run(LargeRun<T>& r) {
   T* Z = r.Z;
   const size_t nn = (size_t)n * n;
 
-  // ---- 1. scale
+  // ---- 1. scale (the maximum is also the non-finite check: a NaN or Inf entry can only
+  // end in the iteration limit, so it is reported as such without iterating)
   double amax = 0.0, cscale = 1.0;
   bool scaled = false;
-  if (r.scale) {
+  {
     CKL(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
     k_absmax_bits<T><<<4 * r.num_sms, 256, 0, s>>>(H, nn, dmax);
     unsigned long long bits = 0;
     CKL(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
     CKL(cudaStreamSynchronize(s));
     std::memcpy(&amax, &bits, sizeof(amax));
+    if (!std::isfinite(amax)) return ST_UNCONVERGED;
+  }
+  if (r.scale) {
     const double smlnum = std::sqrt((double)Prec<T>::fmin) / (double)Prec<T>::eps;
     const double bignum = 1.0 / smlnum;
     if (amax > 0.0 && amax < smlnum) { scaled = true; cscale = smlnum; }

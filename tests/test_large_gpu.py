@@ -5,7 +5,7 @@ the oracle's within 1e2 n eps ||A||_F / s_i."""
 import numpy as np
 import pytest
 
-from common import EPS, assert_schur_real, eig_tolerances, match_eigenvalues, randn_matrix
+from common import EPS, assert_schur_real, checkblocks, eig_tolerances, match_eigenvalues, randn_matrix
 from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
@@ -76,3 +76,55 @@ def test_large_complex_schur(gs, n):
     w_ref, tol = eig_tolerances(A, po)
     ok, worst = match_eigenvalues(S.values, w_ref, tol)
     assert ok, "worst err/tol %.3g" % worst
+
+
+def _structured(n, kind, rng):
+    if kind == "zero":
+        return np.zeros((n, n))
+    if kind == "triangular":
+        return np.triu(rng.standard_normal((n, n)))
+    if kind == "blockdiag":
+        A = np.zeros((n, n))
+        cuts = [0, n // 3, n // 2, n]
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            A[a:b, a:b] = rng.standard_normal((b - a, b - a))
+        return A
+    if kind == "companion":
+        A = np.zeros((n, n))
+        A[1:, :-1] = np.eye(n - 1)
+        A[:, -1] = rng.standard_normal(n) / n
+        return A
+    if kind == "jordan":
+        # identity plus a nilpotent Jordan part: one eigenvalue of multiplicity n
+        return np.eye(n) + np.diag(np.ones(n - 1), 1)
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind", ["zero", "triangular", "blockdiag", "companion", "jordan"])
+def test_large_structured(gs, kind):
+    """Structured inputs of order > 128: the Schur form properties hold (the reference's
+    deflation handles the zero subdiagonals from the start)."""
+    n = 200
+    rng = np.random.default_rng(9900)
+    A = _structured(n, kind, rng)
+    S = gs.gschur(A)
+    assert np.all(np.tril(S.T, -2) == 0)
+    assert checkblocks(S.T)
+    nA = max(np.linalg.norm(A), 1.0)
+    assert np.linalg.norm(A - S.Z @ S.T @ S.Z.T) / nA <= 10 * n * EPS
+    assert np.linalg.norm(S.Z.T @ S.Z - np.eye(n)) <= 10 * n * EPS
+    if kind in ("zero", "triangular"):
+        np.testing.assert_allclose(np.sort(S.values.real), np.sort(np.diag(A)), atol=10 * n * EPS * nA)
+
+
+def test_large_nonfinite_input_terminates(gs):
+    """A NaN entry must end in an error or non-finite output, never in a hang (the
+    sweep limit bounds the iteration)."""
+    n = 150
+    A = np.random.default_rng(9901).standard_normal((n, n))
+    A[7, 3] = np.nan
+    try:
+        S = gs.gschur(A, maxiter=20 * n)
+    except (gs.UnconvergedException, gs.ArgumentError):
+        return
+    assert not np.all(np.isfinite(S.T))
