@@ -14,6 +14,7 @@
 // 2-norms c, r), the power-of-two search on thread 0, and the rescaling of row i
 // (columns ilo..n) and column i (rows 1..ihi) by all threads.  A sweep limit turns a
 // non-terminating case into an error status instead of a hang.
+#include <type_traits>
 #include "device_common.cuh"
 #include "gs_internal.h"
 
@@ -26,10 +27,13 @@ template <> __device__ __forceinline__ bool bz<double2>(double2 x) { return x.x 
 template <class S> __device__ __forceinline__ double babs(S x);
 template <> __device__ __forceinline__ double babs<double>(double x) { return fabs(x); }
 template <> __device__ __forceinline__ double babs<double2>(double2 x) { return hypot(x.x, x.y); }
-// _findamax (src/norm1est.jl:76-99): |x| for real, |x|^2 for complex
-template <class S> __device__ __forceinline__ double bamax(double a);
-template <> __device__ __forceinline__ double bamax<double>(double a) { return a; }
-template <> __device__ __forceinline__ double bamax<double2>(double a) { return a * a; }
+// _findamax (src/norm1est.jl:76-99) compares |x| for real entries and |x|^2 =
+// re*re + im*im (unfused) for complex ones, returning the square root of the largest.
+template <class S> __device__ __forceinline__ double babs2(S x);
+template <> __device__ __forceinline__ double babs2<double>(double x) { return fabs(x); }
+template <> __device__ __forceinline__ double babs2<double2>(double2 x) {
+  return __dadd_rn(__dmul_rn(x.x, x.x), __dmul_rn(x.y, x.y));
+}
 template <class S> __device__ __forceinline__ S bscale(S x, double f);
 template <> __device__ __forceinline__ double bscale<double>(double x, double f) { return x * f; }
 template <> __device__ __forceinline__ double2 bscale<double2>(double2 x, double f) { return make_double2(x.x * f, x.y * f); }
@@ -136,12 +140,17 @@ __global__ void __launch_bounds__(kBalT) k_bal_scale(S* A, int lda, int n, int i
     for (int i = ilo; i <= ihi; ++i) {
       const S* col = A + (size_t)(i - 1) * lda + (ilo - 1);
       const S* row = A + (size_t)(ilo - 1) * lda + (i - 1);
-      double mc = 0.0, mr = 0.0;
+      double mc = 0.0, mr = 0.0, qc = 0.0, qr = 0.0;
       for (int k = tid; k < m; k += kBalT) {
         mc = fmax(mc, babs(col[k]));
         mr = fmax(mr, babs(row[(size_t)k * lda]));
+        if constexpr (!std::is_same<S, double>::value) {
+          qc = fmax(qc, babs2(col[k]));
+          qr = fmax(qr, babs2(row[(size_t)k * lda]));
+        }
       }
       bmax2<kBalT>(mc, mr, red);
+      if constexpr (!std::is_same<S, double>::value) bmax2<kBalT>(qc, qr, red);
       double sc = 0.0, sr = 0.0;
       const double ic = mc > 0.0 ? 1.0 / mc : 0.0, ir = mr > 0.0 ? 1.0 / mr : 0.0;
       for (int k = tid; k < m; k += kBalT) {
@@ -152,7 +161,8 @@ __global__ void __launch_bounds__(kBalT) k_bal_scale(S* A, int lda, int n, int i
       bsum2<kBalT>(sc, sr, red);
       if (tid == 0) {
         double c = mc * sqrt(sc), r = mr * sqrt(sr);
-        double ca = bamax<S>(mc), ra = bamax<S>(mr);
+        double ca = mc, ra = mr;
+        if constexpr (!std::is_same<S, double>::value) { ca = sqrt(qc); ra = sqrt(qr); }
         int apply = 0;
         double f = 1.0;
         if (c != 0.0 && r != 0.0) {

@@ -90,6 +90,38 @@ cudaError_t launch_bal_scale(S* A, int lda, int n, int ilo, int ihi, double* D, 
 cudaError_t launch_bal_apply(int n, int m, const double2* V, int ldv, double2* W, const int* src, const double* D,
                              int scale, int inverse, int num_sms, cudaStream_t s);
 cudaError_t launch_rconde(int n, int m, const double2* VL, const double2* VR, double* out, cudaStream_t s);
+
+// Condition estimators (condition.cu): triangular Sylvester solves of sylvester.jl and
+// the vector steps of norm1est.jl.  S = double or double2.
+template <class S>
+struct SylvArgs {
+  const S* A;     // m x m, upper triangle read (the flipped conjugate transpose for adjoints)
+  int lda;
+  const S* B;     // p x p, upper triangle read
+  int ldb;
+  S* C;           // m x p right-hand side, overwritten by the solution
+  int ldc;
+  int m, p, mT, pT;
+  int flip;       // C(i, j) stored at C[(m-1-i) + (p-1-j) ldc] (adjoint solves)
+  int le;         // perturb |a11|_1 <= smin (trsylvester!) or < smin (adjtrsylvester!)
+  double smin, bignum;
+  int* flag;      // |= 1 perturbed, 2 the overflow rescaling is needed, 4 non-finite entry
+};
+enum { N1_FILL = 0, N1_UNIT = 1, N1_ALT = 2, N1_SIGN = 3 };
+template <class S>
+cudaError_t launch_cond_maxabs(const S* M, int ld, int rows, int cols, unsigned long long* out, int nsm, cudaStream_t s);
+template <class S>
+cudaError_t launch_adj_copy(const S* M, int ld, int m, S* Ap, int nsm, cudaStream_t s);
+template <class S>
+cudaError_t launch_trsyl_levels(const SylvArgs<S>& P, cudaStream_t s);
+template <class S>
+cudaError_t launch_trsyl_exact(const SylvArgs<S>& P, double* out, cudaStream_t s);
+template <class S>
+cudaError_t launch_n1_step(int op, S* x, long long N, double arg, int nsm, cudaStream_t s);
+template <class S>
+cudaError_t launch_n1_stats(const S* x, long long N, long long jlast, double* out, cudaStream_t s);
+template <class S>
+cudaError_t launch_cond_fro(const S* x, long long N, double* out, cudaStream_t s);
 cudaError_t launch_eigvecs_batched(const EigBatch& eb, int nmax, int num_sms, cudaStream_t s);
 
 // Real quasi-triangular -> complex triangular Schur pairs (triang.jl:9-43).

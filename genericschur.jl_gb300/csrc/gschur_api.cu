@@ -1637,3 +1637,306 @@ int gs_ordschur_c64(gs_context* ctx, int64_t n, double* T, double* Z, const int3
 
 }  // extern "C"
 
+
+// ---- condition estimators: eigvalscond / subspacesep (ordschur.jl:84-140) ----------
+namespace {
+
+// Julia's max / min propagate NaN
+inline double jmax(double a, double b) { return (a != a || b != b) ? NAN : std::max(a, b); }
+
+// Device workspace of one estimate for the leading m = nsub block of an n x n T.
+struct CondLayout {
+  size_t o_adjA, o_adjB, o_x, o_bak, o_flag, o_dbl, o_max, bytes;
+};
+template <class S> CondLayout cond_layout(int64_t n, int64_t m, size_t base) {
+  const int64_t p = n - m;
+  Arena ar;
+  ar.off = base;
+  CondLayout L;
+  L.o_adjA = ar.take<S>((size_t)m * m);
+  L.o_adjB = ar.take<S>((size_t)p * p);
+  L.o_x = ar.take<S>((size_t)std::max<int64_t>(m * p, 1));
+  L.o_bak = ar.take<S>((size_t)std::max<int64_t>(m * p, 1));
+  L.o_flag = ar.take<int>(4);
+  L.o_dbl = ar.take<double>(8);
+  L.o_max = ar.take<unsigned long long>(2);
+  L.bytes = ar.off;
+  return L;
+}
+
+template <class S> struct CondRun {
+  gs_context* ctx;
+  cudaStream_t s;
+  const S* T;     // device, leading dimension ldt
+  int ldt, m, p;
+  char* base;
+  CondLayout L;
+  double smin = 0, bignum = 0;
+
+  S* x() const { return (S*)(base + L.o_x); }
+  int* flag() const { return (int*)(base + L.o_flag); }
+  double* dbl() const { return (double*)(base + L.o_dbl); }
+
+  // smin and bignum of trsylvester! (sylvester.jl:37-41) for T11 = T[1:m,1:m], T22.
+  int prepare(bool adjoint) {
+    unsigned long long* dmax = (unsigned long long*)(base + L.o_max);
+    CK(cudaMemsetAsync(dmax, 0, 2 * sizeof(unsigned long long), s));
+    CK(launch_cond_maxabs<S>(T, ldt, m, m, dmax, ctx->num_sms, s));
+    CK(launch_cond_maxabs<S>(T + m + (size_t)m * ldt, ldt, p, p, dmax + 1, ctx->num_sms, s));
+    if (adjoint) {
+      CK(launch_adj_copy<S>(T, ldt, m, (S*)(base + L.o_adjA), ctx->num_sms, s));
+      CK(launch_adj_copy<S>(T + m + (size_t)m * ldt, ldt, p, (S*)(base + L.o_adjB), ctx->num_sms, s));
+    }
+    unsigned long long bits[2];
+    CK(cudaMemcpyAsync(bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    double na, nb;
+    std::memcpy(&na, &bits[0], sizeof(double));
+    std::memcpy(&nb, &bits[1], sizeof(double));
+    const double tiny = 2.220446049250313e-16;
+    const double small = 2.2250738585072014e-308 * m * p / tiny;
+    bignum = 1.0 / small;
+    smin = jmax(small, tiny * na * nb);
+    return GS_OK;
+  }
+
+  // trsylvester! (adj = false) / adjtrsylvester! (adj = true) on C = x (m x p, ld m);
+  // *scale receives sigma.
+  int solve(bool adj, double* scale) {
+    SylvArgs<S> P;
+    P.A = adj ? (const S*)(base + L.o_adjA) : T;
+    P.lda = adj ? m : ldt;
+    P.B = adj ? (const S*)(base + L.o_adjB) : T + m + (size_t)m * ldt;
+    P.ldb = adj ? p : ldt;
+    P.C = x();
+    P.ldc = m;
+    P.m = m;
+    P.p = p;
+    P.mT = (m + 31) / 32;
+    P.pT = (p + 31) / 32;
+    P.flip = adj ? 1 : 0;
+    P.le = adj ? 0 : 1;
+    P.smin = smin;
+    P.bignum = bignum;
+    P.flag = flag();
+    const size_t bytes = sizeof(S) * (size_t)m * p;
+    CK(cudaMemcpyAsync(base + L.o_bak, x(), bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(flag(), 0, sizeof(int), s));
+    CK(launch_trsyl_levels<S>(P, s));
+    int fl = 0;
+    CK(cudaMemcpyAsync(&fl, flag(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *scale = 1.0;
+    if (fl & 6) {
+      // the overflow rescaling (or a non-finite entry): the reference's element order
+      CK(cudaMemcpyAsync(x(), base + L.o_bak, bytes, cudaMemcpyDeviceToDevice, s));
+      CK(launch_trsyl_exact<S>(P, dbl() + 7, s));
+      CK(cudaMemcpyAsync(scale, dbl() + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    return GS_OK;
+  }
+
+  // stats of x: {sum |x|, _findamax value, its index, |x[jlast]|}
+  int stats(long long jlast, double out[4]) {
+    CK(launch_n1_stats<S>(x(), (long long)m * p, jlast, dbl(), s));
+    CK(cudaMemcpyAsync(out, dbl(), 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return GS_OK;
+  }
+
+  // eigvalscond (ordschur.jl:92-105)
+  int eigvalscond(double* out) {
+    if (m == 0 || p == 0) { *out = 1.0; return GS_OK; }
+    int rc = prepare(false);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(x(), sizeof(S) * m, T + (size_t)m * ldt, sizeof(S) * ldt, sizeof(S) * m, p,
+                         cudaMemcpyDeviceToDevice, s));
+    double scale;
+    rc = solve(false, &scale);
+    if (rc) return rc;
+    CK(launch_cond_fro<S>(x(), (long long)m * p, dbl() + 6, s));
+    double rnorm;
+    CK(cudaMemcpyAsync(&rnorm, dbl() + 6, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *out = rnorm > 0.0 ? scale / (std::sqrt(scale * scale / rnorm + rnorm) * std::sqrt(rnorm)) : 1.0;
+    return GS_OK;
+  }
+
+  // subspacesep (ordschur.jl:118-140) through norm1est! (norm1est.jl:21-74)
+  int subspacesep(double* out) {
+    if (m == 0 || p == 0) return set_err(ctx, GS_BADARG, "subspacesep needs 0 < nsub < n");
+    int rc = prepare(true);
+    if (rc) return rc;
+    const long long N = (long long)m * p;
+    const double tiny = 2.2250738585072014e-308;
+    double scale = 1.0, st[4];
+    auto step = [&](int op, double arg) -> int {
+      CK(launch_n1_step<S>(op, x(), N, arg, ctx->num_sms, s));
+      return GS_OK;
+    };
+#define COND_TRY(expr) do { int rc_ = (expr); if (rc_) return rc_; } while (0)
+    COND_TRY(step(N1_FILL, 1.0 / (double)N));
+    COND_TRY(solve(false, &scale));
+    COND_TRY(stats(-1, st));
+    double est;
+    if (N == 1) {
+      est = st[0];
+    } else {
+      double gamma = st[0];
+      COND_TRY(step(N1_SIGN, tiny));
+      COND_TRY(solve(true, &scale));
+      COND_TRY(stats(-1, st));
+      long long j0 = (long long)st[2];
+      for (int iter = 0; iter < 5; ++iter) {
+        COND_TRY(step(N1_UNIT, (double)j0));
+        COND_TRY(solve(false, &scale));
+        COND_TRY(stats(-1, st));
+        const double old = gamma;
+        gamma = st[0];
+        if (gamma <= old) break;
+        COND_TRY(step(N1_SIGN, tiny));
+        COND_TRY(solve(true, &scale));
+        const long long jlast = j0;
+        COND_TRY(stats(jlast, st));
+        j0 = (long long)st[2];
+        if (st[3] == st[1]) break;
+      }
+      COND_TRY(step(N1_ALT, 0.0));
+      COND_TRY(solve(false, &scale));
+      COND_TRY(stats(-1, st));
+      const double t = 2.0 * st[0] / (double)(3 * N);
+      est = jmax(t, gamma);
+    }
+#undef COND_TRY
+    *out = scale / est;
+    return GS_OK;
+  }
+};
+
+template <class S>
+int condition_impl(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* out, unsigned flags,
+                   bool sep) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || nsub < 0 || nsub > n || ldt < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "bad sizes");
+  if (!out || (n > 0 && !T)) return set_err(ctx, GS_BADARG, "null argument");
+  if (n > (1 << 16)) return set_err(ctx, GS_BADARG, "order too large");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  Arena ar;
+  const size_t o_T = ar.take<S>(dev ? 1 : (size_t)n * n);
+  CondLayout L = cond_layout<S>(n, nsub, ar.off);
+  int rc = ensure_ws(ctx, L.bytes);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  const S* dT = (const S*)T;
+  int64_t ld = ldt;
+  if (!dev && n > 0) {
+    CK(cudaMemcpy2DAsync(ctx->dws + o_T, sizeof(S) * n, T, sizeof(S) * ldt, sizeof(S) * n, n,
+                         cudaMemcpyHostToDevice, s));
+    dT = (const S*)(ctx->dws + o_T);
+    ld = n;
+  }
+  CondRun<S> r{ctx, s, dT, (int)ld, (int)nsub, (int)(n - nsub), ctx->dws, L};
+  CK(cudaEventRecord(ctx->t0, s));
+  rc = sep ? r.subspacesep(out) : r.eigvalscond(out);
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  return rc;
+}
+
+// eigen!(A; jcv = true) (pirates.jl:136-153): for each j, the eigenvalue moved to the
+// front of a copy of T by ordschur!, then eigvalscond(., 1) and subspacesep(., 1).
+template <class S>
+int rcondv_impl(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv, unsigned flags) {
+  constexpr bool cplx = sizeof(S) == sizeof(double2);
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16)) return set_err(ctx, GS_BADARG, "bad order");
+  if (n == 0) return GS_OK;
+  if (!T || (!rconde && !rcondv)) return set_err(ctx, GS_BADARG, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  Arena ar;
+  const size_t o_T = ar.take<S>(nn), o_Tt = ar.take<S>(nn), o_Z = ar.take<S>(nn), o_sel = ar.take<int>(n),
+               o_w = ar.take<double>(4 * n), o_st = ar.take<int>(4);
+  CondLayout L = cond_layout<S>(n, 1, ar.off);
+  int rc = ensure_ws(ctx, L.bytes);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  S* dT = (S*)(base + o_T);
+  S* dTt = (S*)(base + o_Tt);
+  S* dZ = (S*)(base + o_Z);
+  int* dsel = (int*)(base + o_sel);
+  double* dw = (double*)(base + o_w);
+  int* dst = (int*)(base + o_st);
+  CK(cudaMemcpyAsync(dT, T, sizeof(S) * nn, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(dZ, 0, sizeof(S) * nn, s));  // the reordering's Z is not wanted
+  std::vector<int> sel((size_t)n, 0);
+  std::vector<double> ec(rconde ? n : 0), vc(rcondv ? n : 0);
+  CK(cudaEventRecord(ctx->t0, s));
+  for (int64_t j = 0; j < n; ++j) {
+    CK(cudaMemcpyAsync(dTt, dT, sizeof(S) * nn, cudaMemcpyDeviceToDevice, s));
+    sel.assign((size_t)n, 0);
+    sel[j] = 1;
+    CK(cudaMemcpyAsync(dsel, sel.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(dst, 0, sizeof(int), s));
+    if (cplx) CK(launch_ordschur_cplx((double2*)dTt, (double2*)dZ, (int)n, dsel, (double2*)dw, s));
+    else CK(launch_ordschur_real((double*)dTt, (double*)dZ, (int)n, dsel, dw, dw + n, dst, s));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st) return set_err(ctx, GS_UNCONVERGED, "reordering rejected a block swap (eigenvalue %lld)", (long long)j + 1);
+    CondRun<S> r{ctx, s, dTt, (int)n, 1, (int)(n - 1), base, L};
+    if (rconde) {
+      rc = r.eigvalscond(&ec[j]);
+      if (rc) return rc;
+    }
+    if (rcondv) {
+      if (n == 1) {
+        return set_err(ctx, GS_BADARG, "subspacesep needs n > 1");
+      }
+      rc = r.subspacesep(&vc[j]);
+      if (rc) return rc;
+    }
+  }
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  const cudaMemcpyKind k = dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+  if (rconde) CK(cudaMemcpyAsync(rconde, ec.data(), sizeof(double) * n, k, s));
+  if (rcondv) CK(cudaMemcpyAsync(rcondv, vc.data(), sizeof(double) * n, k, s));
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs_eigvalscond_f64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* s,
+                       unsigned flags) {
+  return condition_impl<double>(ctx, n, T, ldt, nsub, s, flags, false);
+}
+int gs_eigvalscond_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* s,
+                       unsigned flags) {
+  return condition_impl<double2>(ctx, n, T, ldt, nsub, s, flags, false);
+}
+int gs_subspacesep_f64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
+                       unsigned flags) {
+  return condition_impl<double>(ctx, n, T, ldt, nsub, sep, flags, true);
+}
+int gs_subspacesep_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
+                       unsigned flags) {
+  return condition_impl<double2>(ctx, n, T, ldt, nsub, sep, flags, true);
+}
+int gs_eigen_rcond_f64(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv, unsigned flags) {
+  return rcondv_impl<double>(ctx, n, T, rconde, rcondv, flags);
+}
+int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv, unsigned flags) {
+  return rcondv_impl<double2>(ctx, n, T, rconde, rcondv, flags);
+}
+
+}  // extern "C"

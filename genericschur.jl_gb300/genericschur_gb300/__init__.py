@@ -29,8 +29,9 @@ from ._capi import (GS_BADARG, GS_CUDA, GS_DEVICE, GS_GRAPH, GS_OK, GS_SCALE, GS
 
 __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "ArgumentError", "gschur", "gschur_",
            "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
-           "eig_adjoint_batched", "hessenberg", "gschur_mixed",
-           "get_context", "Context", "pack_batch", "unpack_batch"]
+           "eig_adjoint_batched", "hessenberg", "gschur_mixed", "balance", "balance_", "Balancer", "balancer_lmul",
+           "balancer_ldiv", "enormalize", "gordschur", "ordschur", "rconde", "EigenFull", "eigvalscond",
+           "subspacesep", "eigen_rcond", "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
 Eigen = namedtuple("Eigen", ["values", "vectors"])
@@ -354,7 +355,62 @@ def gordschur(S, select, ctx=None):
 ordschur = gordschur
 
 
-EigenFull = namedtuple("EigenFull", ["values", "vectors", "vectorsl", "rconde"])
+EigenFull = namedtuple("EigenFull", ["values", "vectors", "vectorsl", "rconde", "rcondv"],
+                       defaults=(np.zeros(0),))
+
+
+def _cond_T(S):
+    T = S.T if hasattr(S, "T") and not isinstance(S, np.ndarray) else S
+    T = np.asarray(T)
+    cplx = np.iscomplexobj(T)
+    return np.array(T, dtype=np.complex128 if cplx else np.float64, order="F"), cplx
+
+
+def eigvalscond(S, nsub, ctx=None):
+    """eigvalscond(S, nsub) (ordschur.jl:84-105): reciprocal condition number of the
+    leading nsub eigenvalues of the Schur form S (a Schur tuple or its T), from one
+    triangular Sylvester solve on the GPU.  Use gordschur to bring the eigenvalues of
+    interest to the front first."""
+    ctx = ctx or get_context()
+    T, cplx = _cond_T(S)
+    n = _checksquare(T)
+    out = np.zeros(1)
+    fn = ctx.lib.gs_eigvalscond_c64 if cplx else ctx.lib.gs_eigvalscond_f64
+    rc = fn(ctx.handle, n, _ptr(T), max(n, 1), int(nsub), _ptr(out), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "eigvalscond")
+    return float(out[0])
+
+
+def subspacesep(S, nsub, ctx=None):
+    """subspacesep(S, nsub) (ordschur.jl:107-140): estimated reciprocal condition of the
+    invariant subspace of the leading nsub block (the separation of the two diagonal
+    blocks, by the one-norm estimator over GPU Sylvester solves).  0 < nsub < n."""
+    ctx = ctx or get_context()
+    T, cplx = _cond_T(S)
+    n = _checksquare(T)
+    out = np.zeros(1)
+    fn = ctx.lib.gs_subspacesep_c64 if cplx else ctx.lib.gs_subspacesep_f64
+    rc = fn(ctx.handle, n, _ptr(T), max(n, 1), int(nsub), _ptr(out), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "subspacesep")
+    return float(out[0])
+
+
+def eigen_rcond(S, want_rconde=True, want_rcondv=True, ctx=None):
+    """The per-eigenvalue loop of eigen!(A; jcv = true) (pirates.jl:136-153): for each j,
+    eigenvalue j moved to the front of a copy of T by ordschur!, then eigvalscond(., 1)
+    and subspacesep(., 1).  Returns (rconde, rcondv) (None for the ones not asked for)."""
+    ctx = ctx or get_context()
+    T, cplx = _cond_T(S)
+    n = _checksquare(T)
+    e = np.zeros(n) if want_rconde else None
+    v = np.zeros(n) if want_rcondv else None
+    fn = ctx.lib.gs_eigen_rcond_c64 if cplx else ctx.lib.gs_eigen_rcond_f64
+    rc = fn(ctx.handle, n, _ptr(T), _ptr(e), _ptr(v), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "eigen (jcv)")
+    return e, v
 
 
 def rconde(VL, VR, ctx=None):
@@ -371,13 +427,16 @@ def rconde(VL, VR, ctx=None):
     return out
 
 
-def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, ctx=None):
+def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, jcv=False, ctx=None):
     """Eigen decomposition (pirates.jl:63-160): balance! (permute/scale, as the reference's
     defaults), Schur form, triangularize for real input, right eigenvectors (and left
     ones with jvl or jce), the Balancer's lmul!/ldiv!, _enormalize!, sort.  With jce the
     reciprocal eigenvalue condition numbers are computed from the balanced form's
-    vectors, as the reference does.  Returns Eigen(values, vectors), or, when jvl or
-    jce is asked for, EigenFull(values, vectors, vectorsl, rconde)."""
+    vectors, as the reference does.  With jcv, every eigenvalue is moved to the front of
+    a copy of the Schur form and its subspacesep (and, with jce as well, its
+    eigvalscond, which then replaces the vector-based value) is computed, as the
+    reference's (expensive) loop does.  Returns Eigen(values, vectors), or, when jvl, jce
+    or jcv is asked for, EigenFull(values, vectors, vectorsl, rconde, rcondv)."""
     A = np.asarray(A)
     B = None
     if permute or scale:
@@ -385,7 +444,7 @@ def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jc
     S = gschur(A, ctx=ctx)
     if not np.iscomplexobj(S.T):
         S = triangularize(S, ctx=ctx)
-    full = jvl or jce
+    full = jvl or jce or jcv
     w = S.values
     if not full:
         if B is not None:
@@ -414,10 +473,16 @@ def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jc
         VL = enormalize(VL, ctx=ctx)
     else:
         VL = np.zeros((0, 0), dtype=np.complex128)
+    rcv = np.zeros(0)
+    if jcv:
+        e_j, rcv = eigen_rcond(S, want_rconde=jce, want_rcondv=True, ctx=ctx)
+        if jce:
+            rce = e_j
     if sortby is None:
-        return EigenFull(w, V, VL, rce)
+        return EigenFull(w, V, VL, rce, rcv)
     p = _eigsortby(w) if sortby == "default" else np.argsort([sortby(x) for x in w], kind="stable")
-    return EigenFull(w[p], V[:, p] if V.size else V, VL[:, p] if VL.size else VL, rce[p] if rce.size else rce)
+    return EigenFull(w[p], V[:, p] if V.size else V, VL[:, p] if VL.size else VL, rce[p] if rce.size else rce,
+                     rcv[p] if rcv.size else rcv)
 
 
 def geigvecs_batched(T_packed, Z_packed, ns, offs, woffs=None, left=False, normalize=True, ctx=None):

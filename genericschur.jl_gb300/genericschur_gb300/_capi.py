@@ -60,6 +60,12 @@ SIGNATURES = {
     "gs_rconde_c64": (_i, [_p, _i64, _p, _p, _p, _u]),
     "gs_ordschur_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _u]),
     "gs_ordschur_c64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
+    "gs_eigvalscond_f64": (_i, [_p, _i64, _p, _i64, _i64, _p, _u]),
+    "gs_eigvalscond_c64": (_i, [_p, _i64, _p, _i64, _i64, _p, _u]),
+    "gs_subspacesep_f64": (_i, [_p, _i64, _p, _i64, _i64, _p, _u]),
+    "gs_subspacesep_c64": (_i, [_p, _i64, _p, _i64, _i64, _p, _u]),
+    "gs_eigen_rcond_f64": (_i, [_p, _i64, _p, _p, _p, _u]),
+    "gs_eigen_rcond_c64": (_i, [_p, _i64, _p, _p, _p, _u]),
 }
 # allocation-free entry point (include/gschur_gb300_noalloc.h)
 SIGNATURES["gs_schur_batched_f64_noalloc"] = (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u])

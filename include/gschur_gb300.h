@@ -231,6 +231,32 @@ GS_API int gs_enormalize_c64(gs_context* ctx, int64_t n, int64_t m, double* V, i
  * (|vl_j|_2 |vr_j|_2).  VL, VR: n x n interleaved complex, ld n. */
 GS_API int gs_rconde_c64(gs_context* ctx, int64_t n, const double* VL, const double* VR, double* rconde, unsigned flags);
 
+/* eigvalscond(S, nsub) (ordschur.jl:84-105): reciprocal condition number of the leading
+ * nsub eigenvalues of the Schur factor T (n x n, leading dimension ldt; only the upper
+ * triangle of each diagonal block is read, as the reference's trsylvester! reads it).
+ * The result goes to the host scalar *s (with GS_DEVICE only T is a device pointer).
+ * nsub = 0 or n gives 1. */
+GS_API int gs_eigvalscond_f64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* s,
+                              unsigned flags);
+GS_API int gs_eigvalscond_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* s,
+                              unsigned flags);
+/* subspacesep(S, nsub) (ordschur.jl:107-140): estimated separation of the leading nsub
+ * block from the rest (norm1est! over trsylvester! / adjtrsylvester!, norm1est.jl:21-74).
+ * 0 < nsub < n (GS_BADARG otherwise: the reference fails on an empty block). */
+GS_API int gs_subspacesep_f64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
+                              unsigned flags);
+GS_API int gs_subspacesep_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
+                              unsigned flags);
+/* eigen!(A; jcv = true) (pirates.jl:136-153) on a Schur factor T (n x n, ld n): for each
+ * j, eigenvalue j moved to the front of a copy of T by ordschur!, then rconde[j] =
+ * eigvalscond(., 1) (skipped when rconde is NULL) and rcondv[j] = subspacesep(., 1)
+ * (skipped when rcondv is NULL).  With GS_DEVICE, T, rconde and rcondv are device
+ * pointers.  O(n^3) work, as the reference warns. */
+GS_API int gs_eigen_rcond_f64(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv,
+                              unsigned flags);
+GS_API int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv,
+                              unsigned flags);
+
 /* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
  * eigenvalues with select[k] != 0 move to the leading positions in their order.
  * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if

@@ -3,7 +3,7 @@
 // (src/balance.jl:33-261), used by eigen! (src/pirates.jl:63-89).  1-based index
 // macros so that the loops read against the reference line by line; column-major.
 // Kept as written there: the 2-norms of the "pr" variant with sf(c, r) = c + r, and
-// _findamax (src/norm1est.jl:76-99) returning |x|^2 for complex entries.
+// _findamax (src/norm1est.jl:76-99), which compares |x|^2 for complex entries.
 #pragma once
 #include <vector>
 #include "scalar.hpp"
@@ -16,6 +16,9 @@ template <class R> inline R bal_abs(R x) { return m_abs(x); }
 template <class R> inline R bal_abs(cx<R> x) { return cabs(x); }
 template <class R> inline R bal_amax(R x) { return m_abs(x); }
 template <class R> inline R bal_amax(cx<R> x) { return x.re * x.re + x.im * x.im; }
+// _findamax returns the largest |x|, found through |x|^2 for complex entries
+template <class R> inline R bal_amax_fin(R m, R) { return m; }
+template <class R> inline R bal_amax_fin(R m, cx<R>) { return m_sqrt(m); }
 
 // 2-norm of a strided vector (scaled sum of squares)
 template <class R, class S> R bal_norm2(const S* x, int n, long long inc) {
@@ -128,6 +131,8 @@ int balance(int n, S* a, int lda, bool do_scale, bool do_permute, int* ilo_out, 
           if (x > ca) ca = x;
           if (y > ra) ra = y;
         }
+        ca = bal_amax_fin<R>(ca, S());
+        ra = bal_amax_fin<R>(ra, S());
         if (c == R(0) || r == R(0)) continue;
         R g = r / beta;
         const R s = c + r;

@@ -6,6 +6,7 @@
 #include "gschur_oracle.hpp"
 #include "eigvecs_oracle.hpp"
 #include "balance_oracle.hpp"
+#include "condition_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -178,6 +179,34 @@ int or_balance_z(int n, double* a, int lda, int scale, int permute, int* out3, i
 int or_balancer_apply_z(int n, int m, double* v, int ldv, int ilo, int ihi, const int* sp, const double* d,
                         int trivial, int inverse) {
   balancer_apply<double, zc>(n, m, (zc*)v, ldv, ilo, ihi, sp, d, trivial != 0, inverse != 0);
+  return 0;
+}
+
+// trsylvester! / adjtrsylvester! (sylvester.jl:11-139) on C (m x p, in place);
+// out2 = {scale, perturbed}.
+int or_trsylv_d(int adj, int m, int p, const double* a, int lda, const double* b, int ldb, double* c, int ldc,
+                double* out2) {
+  bool pert = false;
+  out2[0] = trsylvester<double, double>(adj != 0, m, p, a, lda, b, ldb, c, ldc, &pert);
+  out2[1] = pert ? 1.0 : 0.0;
+  return 0;
+}
+int or_trsylv_z(int adj, int m, int p, const double* a, int lda, const double* b, int ldb, double* c, int ldc,
+                double* out2) {
+  bool pert = false;
+  out2[0] = trsylvester<double, zc>(adj != 0, m, p, (const zc*)a, lda, (const zc*)b, ldb, (zc*)c, ldc, &pert);
+  out2[1] = pert ? 1.0 : 0.0;
+  return 0;
+}
+// eigvalscond / subspacesep (ordschur.jl:84-140) of the leading nsub block of T (n x n).
+int or_econd_d(int n, const double* t, int ldt, int nsub, double* out2) {
+  out2[0] = eigvalscond<double, double>(n, t, ldt, nsub);
+  out2[1] = subspacesep<double, double>(n, t, ldt, nsub);
+  return 0;
+}
+int or_econd_z(int n, const double* t, int ldt, int nsub, double* out2) {
+  out2[0] = eigvalscond<double, zc>(n, (const zc*)t, ldt, nsub);
+  out2[1] = subspacesep<double, zc>(n, (const zc*)t, ldt, nsub);
   return 0;
 }
 

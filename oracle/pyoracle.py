@@ -42,6 +42,10 @@ def lib():
             "or_balance_d": [_i, _p, _i, _i, _i, _p, _p, _p],
             "or_balance_z": [_i, _p, _i, _i, _i, _p, _p, _p],
             "or_balancer_apply_z": [_i, _i, _p, _i, _i, _i, _p, _p, _i, _i],
+            "or_trsylv_d": [_i, _i, _i, _p, _i, _p, _i, _p, _i, _p],
+            "or_trsylv_z": [_i, _i, _i, _p, _i, _p, _i, _p, _i, _p],
+            "or_econd_d": [_i, _p, _i, _i, _p],
+            "or_econd_z": [_i, _p, _i, _i, _p],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -232,3 +236,28 @@ def balancer_apply(V, B, inverse=False):
     lib().or_balancer_apply_z(n, m, _ptr(V), max(n, 1), ilo, ihi, _ptr(np.ascontiguousarray(sp, dtype=np.int32)),
                               _ptr(np.ascontiguousarray(D, dtype=np.float64)), int(trivial), int(inverse))
     return V
+
+
+def trsylvester(A, B, C, adjoint=False):
+    """trsylvester!(A, B, C) (A X - X B = scale C) or adjtrsylvester!(A, B, C)
+    (A^H X - X B^H = scale C), sylvester.jl:11-139.  Returns (X, scale, perturbed)."""
+    cplx = np.iscomplexobj(A) or np.iscomplexobj(B) or np.iscomplexobj(C)
+    dt = np.complex128 if cplx else np.float64
+    A, B, X = _f(A, dt), _f(B, dt), _f(C, dt)
+    m, p = X.shape
+    out = np.zeros(2)
+    fn = lib().or_trsylv_z if cplx else lib().or_trsylv_d
+    fn(int(adjoint), m, p, _ptr(A), max(m, 1), _ptr(B), max(p, 1), _ptr(X), max(m, 1), _ptr(out))
+    return X, float(out[0]), bool(out[1])
+
+
+def condition(T, nsub):
+    """(eigvalscond(S, nsub), subspacesep(S, nsub)) of the Schur factor T
+    (ordschur.jl:84-140)."""
+    cplx = np.iscomplexobj(T)
+    T = _f(T, np.complex128 if cplx else np.float64)
+    n = T.shape[0]
+    out = np.zeros(2)
+    fn = lib().or_econd_z if cplx else lib().or_econd_d
+    fn(n, _ptr(T), max(n, 1), int(nsub), _ptr(out))
+    return float(out[0]), float(out[1])

@@ -32,6 +32,14 @@ def _cases():
     Cz = randn_matrix(rng, 40, cplx=True)
     dz = 2.0 ** rng.integers(-30, 31, size=40)
     out.append(("complex", (Cz * dz[None, :]) / dz[:, None]))
+    # the overflow / underflow guards of the scaling loop compare the largest |x| of a
+    # row or column (found through |x|^2 for complex entries) with the safe range:
+    # magnitudes near 1e+-150 (|x|^2 outside the range) and 1e-165 (|x|^2 underflows)
+    Cg = randn_matrix(rng, 24, cplx=True)
+    dg = 2.0 ** rng.integers(-20, 21, size=24)
+    Cg = (Cg * dg[None, :]) / dg[:, None]
+    for tag, mag in (("tiny", 1e-150), ("huge", 1e150), ("subtiny", 1e-165)):
+        out.append(("complex_" + tag, Cg * mag))
     return out
 
 

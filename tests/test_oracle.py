@@ -202,3 +202,52 @@ def test_oracle_balance_restatement():
     wb, Vb = np.linalg.eig(Ab)
     V = po.balancer_apply(Vb, B)
     assert np.linalg.norm(A @ V - V @ np.diag(wb)) <= 1e-10 * np.linalg.norm(A) * np.linalg.norm(V)
+
+
+@pytest.mark.parametrize("cplx", [True, False])
+def test_oracle_condition_vs_trsen(cplx):
+    """eigvalscond / subspacesep restated (ordschur.jl:84-140 over sylvester.jl and
+    norm1est.jl), pinned as the reference pins them (test/ordschur.jl:35-54): equal to
+    LAPACK's trsen s and sep for the same reordered Schur form.  Complex forms from
+    random matrices; real forms upper triangular (the reference's solver reads only the
+    upper triangle)."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    import scipy.linalg as sl
+    rng = np.random.default_rng(4900 + cplx)
+    for trial in range(4):
+        n = 32
+        sel = np.zeros(n, dtype=np.int32)
+        sel[rng.integers(0, n, 3)] = 1
+        if cplx:
+            T0, Z0 = sl.schur(rng.random((n, n)) + 1j * rng.random((n, n)), output="complex")
+            ts, _, _, m, s1, sep1, info = lapack.ztrsen(sel, T0, Z0, lwork=2 * n * n)
+        else:
+            T0 = np.triu(rng.standard_normal((n, n))) + 4 * np.diag(rng.standard_normal(n))
+            ts, _, _, _, m, s1, sep1, info = lapack.dtrsen(sel, T0, np.eye(n), lwork=2 * n * n, liwork=n * n)
+        assert info == 0
+        s2, sep2 = po.condition(ts, int(m))
+        assert abs(s1 - s2) <= 1e-8 * s1
+        assert abs(sep1 - sep2) <= 1e-8 * sep1
+
+
+def test_oracle_trsylvester_residual():
+    """trsylvester! / adjtrsylvester! restated (sylvester.jl:11-139): A X - X B = C and
+    A^H X - X B^H = C to working accuracy; a repeated eigenvalue is perturbed to smin."""
+    rng = np.random.default_rng(4950)
+    for cplx in (False, True):
+        m, p = 7, 11
+        A = np.triu(randn_matrix(rng, m, cplx))
+        B = np.triu(randn_matrix(rng, p, cplx))
+        C = randn_matrix(rng, m, cplx)[:, :1] @ randn_matrix(rng, p, cplx)[:1, :] + \
+            (rng.standard_normal((m, p)) if not cplx else rng.standard_normal((m, p)) * 1j)
+        X, scale, pert = po.trsylvester(A, B, C)
+        assert scale == 1.0 and not pert
+        assert np.linalg.norm(A @ X - X @ B - C) <= 100 * EPS * np.linalg.norm(X) * (np.linalg.norm(A) + np.linalg.norm(B))
+        Xh, scale, pert = po.trsylvester(A, B, C, adjoint=True)
+        Ah, Bh = A.conj().T, B.conj().T
+        assert np.linalg.norm(Ah @ Xh - Xh @ Bh - C) <= 100 * EPS * np.linalg.norm(Xh) * (np.linalg.norm(A) + np.linalg.norm(B))
+    A = np.triu(rng.standard_normal((3, 3)))
+    B = np.triu(rng.standard_normal((2, 2)))
+    B[1, 1] = A[0, 0]
+    _, _, pert = po.trsylvester(A, B, rng.standard_normal((3, 2)))
+    assert pert
