@@ -108,6 +108,27 @@ struct SylvArgs {
   int* flag;      // |= 1 perturbed, 2 the overflow rescaling is needed, 4 non-finite entry
 };
 enum { N1_FILL = 0, N1_UNIT = 1, N1_ALT = 2, N1_SIGN = 3 };
+// Hermitian path (hermitian.cu).  S = double or double2.
+struct HeCtlBuf {
+  alignas(16) unsigned char bytes[64];
+};
+template <class S>
+cudaError_t launch_he_tridiag(const S* A, long long lda, int n, int upper, S* B, S* W, S* partial, int npart,
+                              HeCtlBuf* ctl, S* tau, double* d, double* e, int num_sms, cudaStream_t s);
+template <class S>
+cudaError_t launch_he_formq(const S* B, int n, const S* tau, S* Q, int num_sms, cudaStream_t s);
+template <class S>
+cudaError_t launch_he_store(const S* B, int n, int upper, S* A, long long lda, cudaStream_t s);
+template <class S>
+cudaError_t launch_he_gather(const S* Z, int n, const int* p, int rev, S* V, long long ldv, cudaStream_t s);
+size_t steqr_ctl_bytes();
+// Tridiagonal QR with the rotations applied to Z (nz rows, ld ldz) when Z != NULL.  ctl:
+// steqr_ctl_bytes(); rot: 4 n doubles.  ctl holds {count, gen, err, done, status, ...}:
+// err != 0 (a barrier wait gave up) at byte 8, status (sweep limit) at byte 16.
+template <class S>
+cudaError_t launch_steqr(int n, double* d, double* e, S* Z, long long ldz, int nz, double* rot, void* ctl,
+                         long long maxsweeps, int num_sms, cudaStream_t s);
+
 template <class S>
 cudaError_t launch_cond_maxabs(const S* M, int ld, int rows, int cols, unsigned long long* out, int nsm, cudaStream_t s);
 template <class S>

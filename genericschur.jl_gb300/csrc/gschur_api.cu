@@ -1940,3 +1940,227 @@ int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rcon
 }
 
 }  // extern "C"
+
+// ---- Hermitian path: geigen! / geigvals!, hessenberg!(Hermitian), _gschur!(SymTridiagonal) ----
+namespace {
+
+struct HeLayout {
+  size_t o_A, o_B, o_W, o_part, o_ctl, o_tau, o_d, o_e, o_Q, o_rot, o_st, o_p, bytes;
+  int npart;
+};
+template <class S> HeLayout he_layout(int64_t n, bool host_a, bool wantq, int num_sms) {
+  HeLayout L;
+  Arena ar;
+  const size_t nn = (size_t)n * n;
+  L.npart = std::max(1, 4 * num_sms);
+  L.o_A = ar.take<S>(host_a ? nn : 1);
+  L.o_B = ar.take<S>(std::max<size_t>(nn, 1));
+  L.o_W = ar.take<S>(std::max<int64_t>(n, 1));
+  L.o_part = ar.take<S>(L.npart);
+  L.o_ctl = ar.take<HeCtlBuf>(1);
+  L.o_tau = ar.take<S>(std::max<int64_t>(n, 1));
+  L.o_d = ar.take<double>(std::max<int64_t>(n, 1));
+  L.o_e = ar.take<double>(std::max<int64_t>(n, 1));
+  L.o_Q = ar.take<S>(wantq ? nn : 1);
+  L.o_rot = ar.take<double>(4 * std::max<int64_t>(n, 1));
+  L.o_st = ar.take<char>(steqr_ctl_bytes());
+  L.o_p = ar.take<int>(std::max<int64_t>(n, 1));
+  L.bytes = ar.off;
+  return L;
+}
+
+// reads the sweep kernel's {err, status}
+int steqr_result(gs_context* ctx, const char* st_dev, cudaStream_t s) {
+  int words[5];
+  CK(cudaMemcpyAsync(words, st_dev, sizeof(words), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (words[2]) return set_err(ctx, GS_CUDA, "tridiagonal QR: a grid barrier wait gave up");
+  if (words[4]) return set_err(ctx, GS_UNCONVERGED, "tridiagonal QR: sweep limit reached");
+  return GS_OK;
+}
+
+template <class S>
+int heev_impl(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* w, double* V, int64_t ldv,
+              unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16) || lda < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "bad sizes");
+  if (uplo != 'L' && uplo != 'U') return set_err(ctx, GS_BADARG, "uplo must be 'L' or 'U'");
+  const bool wantz = flags & GS_WANTZ;
+  if (n == 0) return GS_OK;
+  if (!A || !w || (wantz && (!V || ldv < n))) return set_err(ctx, GS_BADARG, "null or short array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const HeLayout L = he_layout<S>(n, !dev, wantz, ctx->num_sms);
+  int rc = ensure_ws(ctx, L.bytes);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const S* dA = (const S*)A;
+  int64_t ld = lda;
+  if (!dev) {
+    CK(cudaMemcpy2DAsync(base + L.o_A, sizeof(S) * n, A, sizeof(S) * lda, sizeof(S) * n, n, cudaMemcpyHostToDevice, s));
+    dA = (const S*)(base + L.o_A);
+    ld = n;
+  }
+  S* B = (S*)(base + L.o_B);
+  S* tau = (S*)(base + L.o_tau);
+  double* d = (double*)(base + L.o_d);
+  double* e = (double*)(base + L.o_e);
+  S* Q = (S*)(base + L.o_Q);
+  const int upper = uplo == 'U';
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_he_tridiag<S>(dA, ld, (int)n, upper, B, (S*)(base + L.o_W), (S*)(base + L.o_part), L.npart,
+                          (HeCtlBuf*)(base + L.o_ctl), tau, d, e, ctx->num_sms, s));
+  if (wantz) CK(launch_he_formq<S>(B, (int)n, tau, Q, ctx->num_sms, s));
+  CK(launch_steqr<S>((int)n, d, e, wantz ? Q : nullptr, n, wantz ? (int)n : 0, (double*)(base + L.o_rot),
+                     base + L.o_st, 30LL * n, ctx->num_sms, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  rc = steqr_result(ctx, base + L.o_st, s);
+  if (rc == GS_CUDA) return rc;
+  // sorteig!(w, V, eigsortby): stable ascending order
+  std::vector<double> dh(n);
+  CK(cudaMemcpyAsync(dh.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  std::vector<int> p(n);
+  for (int64_t i = 0; i < n; ++i) p[i] = (int)i;
+  std::stable_sort(p.begin(), p.end(), [&](int a, int b) { return dh[a] < dh[b]; });
+  std::vector<double> ws(n);
+  for (int64_t j = 0; j < n; ++j) ws[j] = dh[p[j]];
+  CK(cudaMemcpyAsync(w, ws.data(), sizeof(double) * n, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost, s));
+  if (wantz) {
+    int* dp = (int*)(base + L.o_p);
+    CK(cudaMemcpyAsync(dp, p.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    if (dev) {
+      CK(launch_he_gather<S>(Q, (int)n, dp, upper, (S*)V, ldv, s));
+    } else {
+      CK(launch_he_gather<S>(Q, (int)n, dp, upper, B, n, s));
+      CK(cudaMemcpy2DAsync(V, sizeof(S) * ldv, B, sizeof(S) * n, sizeof(S) * n, n, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  CK(cudaStreamSynchronize(s));
+  return rc;
+}
+
+template <class S>
+int hetrd_impl(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e, double* tau,
+               unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16) || lda < std::max<int64_t>(n, 1)) return set_err(ctx, GS_BADARG, "bad sizes");
+  if (uplo != 'L' && uplo != 'U') return set_err(ctx, GS_BADARG, "uplo must be 'L' or 'U'");
+  if (n == 0) return GS_OK;
+  if (!A || !d || (n > 1 && (!e || !tau))) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const HeLayout L = he_layout<S>(n, true, false, ctx->num_sms);
+  int rc = ensure_ws(ctx, L.bytes);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  S* dA = (S*)(base + L.o_A);
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy2DAsync(dA, sizeof(S) * n, A, sizeof(S) * lda, sizeof(S) * n, n, in, s));
+  S* B = (S*)(base + L.o_B);
+  S* dtau = (S*)(base + L.o_tau);
+  double* dd = (double*)(base + L.o_d);
+  double* de = (double*)(base + L.o_e);
+  const int upper = uplo == 'U';
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_he_tridiag<S>(dA, n, (int)n, upper, B, (S*)(base + L.o_W), (S*)(base + L.o_part), L.npart,
+                          (HeCtlBuf*)(base + L.o_ctl), dtau, dd, de, ctx->num_sms, s));
+  CK(launch_he_store<S>(B, (int)n, upper, dA, n, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  CK(cudaMemcpy2DAsync(A, sizeof(S) * lda, dA, sizeof(S) * n, sizeof(S) * n, n, out, s));
+  // d, e, tau to the host (reversed for the upper form), then out
+  std::vector<double> hd(n), he(n > 1 ? n - 1 : 1);
+  std::vector<S> ht(n > 1 ? n - 1 : 1);
+  CK(cudaMemcpyAsync(hd.data(), dd, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (n > 1) {
+    CK(cudaMemcpyAsync(he.data(), de, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ht.data(), dtau, sizeof(S) * (n - 1), cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (upper) {
+    std::reverse(hd.begin(), hd.end());
+    if (n > 1) {
+      std::reverse(he.begin(), he.begin() + (n - 1));
+      std::reverse(ht.begin(), ht.begin() + (n - 1));
+    }
+  }
+  const cudaMemcpyKind hk = dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+  CK(cudaMemcpyAsync(d, hd.data(), sizeof(double) * n, hk, s));
+  if (n > 1) {
+    CK(cudaMemcpyAsync(e, he.data(), sizeof(double) * (n - 1), hk, s));
+    CK(cudaMemcpyAsync(tau, ht.data(), sizeof(S) * (n - 1), hk, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs_heev_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* w, double* V, int64_t ldv,
+                unsigned flags) {
+  return heev_impl<double>(ctx, n, A, lda, uplo, w, V, ldv, flags);
+}
+int gs_heev_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* w, double* V, int64_t ldv,
+                unsigned flags) {
+  return heev_impl<double2>(ctx, n, A, lda, uplo, w, V, ldv, flags);
+}
+int gs_hetrd_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e, double* tau,
+                 unsigned flags) {
+  return hetrd_impl<double>(ctx, n, A, lda, uplo, d, e, tau, flags);
+}
+int gs_hetrd_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e, double* tau,
+                 unsigned flags) {
+  return hetrd_impl<double2>(ctx, n, A, lda, uplo, d, e, tau, flags);
+}
+
+int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 16)) return set_err(ctx, GS_BADARG, "bad order");
+  if (n == 0) return GS_OK;
+  if (!d || (n > 1 && !e) || (Z && ldz < n)) return set_err(ctx, GS_BADARG, "null or short array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  Arena ar;
+  const size_t o_d = ar.take<double>(n), o_e = ar.take<double>(n), o_Z = ar.take<double>(Z && !dev ? (size_t)n * n : 1),
+               o_rot = ar.take<double>(4 * n), o_st = ar.take<char>(steqr_ctl_bytes());
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double* dd = (double*)(base + o_d);
+  double* de = (double*)(base + o_e);
+  double* dZ = Z ? (dev ? Z : (double*)(base + o_Z)) : nullptr;
+  const long long ldd = dev ? ldz : n;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpyAsync(dd, d, sizeof(double) * n, in, s));
+  CK(cudaMemsetAsync(de, 0, sizeof(double) * n, s));
+  if (n > 1) CK(cudaMemcpyAsync(de, e, sizeof(double) * (n - 1), in, s));
+  if (Z && !dev)
+    CK(cudaMemcpy2DAsync(dZ, sizeof(double) * n, Z, sizeof(double) * ldz, sizeof(double) * n, n, in, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_steqr<double>((int)n, dd, de, dZ, ldd, Z ? (int)n : 0, (double*)(base + o_rot), base + o_st, 30LL * n,
+                          ctx->num_sms, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  rc = steqr_result(ctx, base + o_st, s);
+  if (rc == GS_CUDA) return rc;
+  CK(cudaMemcpyAsync(d, dd, sizeof(double) * n, out, s));
+  if (n > 1) CK(cudaMemcpyAsync(e, de, sizeof(double) * (n - 1), out, s));
+  if (Z && !dev)
+    CK(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, dZ, sizeof(double) * n, sizeof(double) * n, n, out, s));
+  CK(cudaStreamSynchronize(s));
+  return rc;
+}
+
+}  // extern "C"

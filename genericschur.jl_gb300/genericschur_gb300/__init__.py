@@ -31,7 +31,8 @@ __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "Argum
            "schur", "eigvals", "eigvecs", "geigvecs", "eigen", "triangularize", "gschur_batched", "geigvecs_batched",
            "eig_adjoint_batched", "hessenberg", "gschur_mixed", "balance", "balance_", "Balancer", "balancer_lmul",
            "balancer_ldiv", "enormalize", "gordschur", "ordschur", "rconde", "EigenFull", "eigvalscond",
-           "subspacesep", "eigen_rcond", "get_context", "Context", "pack_batch", "unpack_batch"]
+           "subspacesep", "eigen_rcond", "Hermitian", "SymTridiagonal", "HermitianHessenberg", "geigen",
+           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
 Eigen = namedtuple("Eigen", ["values", "vectors"])
@@ -122,7 +123,12 @@ def _eigsortby(w):
 
 
 def eigvals(A, sortby="default", **kw):
-    """Eigenvalues via gschur!(A; wantZ=false) (pirates.jl:17-27)."""
+    """Eigenvalues via gschur!(A; wantZ=false) (pirates.jl:17-27); for a Hermitian or
+    SymTridiagonal argument, geigvals! (GenericSchur.jl:138-146, symtridiag.jl:51-57)."""
+    if isinstance(A, Hermitian):
+        return geigvals(A, sortby=sortby, **kw)
+    if isinstance(A, SymTridiagonal):
+        return _st_eig(A, False, sortby, kw.get("ctx"))[0]
     S = gschur(A, wantZ=False, **kw)
     w = S.values
     if sortby is None:
@@ -427,6 +433,102 @@ def rconde(VL, VR, ctx=None):
     return out
 
 
+# LinearAlgebra.Hermitian(data, uplo) / Symmetric: the triangle `uplo` of data is read.
+Hermitian = namedtuple("Hermitian", ["data", "uplo"], defaults=("U",))
+# LinearAlgebra.SymTridiagonal(dv, ev)
+SymTridiagonal = namedtuple("SymTridiagonal", ["dv", "ev"])
+# hessenberg!(Hermitian(A, uplo)): the tridiagonal and the reflectors (hessenberg.jl:26-96)
+HermitianHessenberg = namedtuple("HermitianHessenberg", ["factors", "tau", "dv", "ev", "uplo"])
+
+
+def _heev(H, wantv, ctx):
+    ctx = ctx or get_context()
+    A = np.asarray(H.data)
+    n = _checksquare(A)
+    cplx = np.iscomplexobj(A)
+    dt = np.complex128 if cplx else np.float64
+    A = np.array(A, dtype=dt, order="F")
+    w = np.zeros(max(n, 1))
+    V = np.zeros((n, n), dtype=dt, order="F") if wantv else None
+    fn = ctx.lib.gs_heev_c64 if cplx else ctx.lib.gs_heev_f64
+    uplo = str(H.uplo).upper()[:1]
+    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), ord(uplo), _ptr(w), _ptr(V), max(n, 1),
+            _capi.GS_WANTZ if wantv else 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "geigen!")
+    return w[:n], V
+
+
+def _sorted(w, V, sortby):
+    if sortby == "default" or sortby is None:
+        return w, V
+    p = np.argsort([sortby(x) for x in w], kind="stable")
+    return w[p], (V[:, p] if V is not None else None)
+
+
+def geigen(H, sortby="default", ctx=None):
+    """geigen!(Hermitian(A, uplo)) (GenericSchur.jl:126-136) with QRIteration, on the GPU:
+    Eigen(values ascending, orthonormal vectors)."""
+    if isinstance(H, SymTridiagonal):
+        w, V = _st_eig(H, True, sortby, ctx)
+        return Eigen(w, V)
+    w, V = _heev(H, True, ctx)
+    w, V = _sorted(w, V, sortby)
+    return Eigen(w, V)
+
+
+def geigvals(H, sortby="default", ctx=None):
+    """geigvals!(Hermitian(A, uplo)) (GenericSchur.jl:138-146) with QRIteration."""
+    if isinstance(H, SymTridiagonal):
+        return _st_eig(H, False, sortby, ctx)[0]
+    w, _ = _heev(H, False, ctx)
+    return _sorted(w, None, sortby)[0]
+
+
+def gschur_symtridiag(T, Z=None, ctx=None):
+    """_gschur!(SymTridiagonal(dv, ev), QRIteration(), Z) (symtridiag.jl:79-183): the
+    eigenvalues in the iteration's order, the rotations applied to Z (when given).
+    Returns (d, e, Z)."""
+    ctx = ctx or get_context()
+    d = np.array(T.dv, dtype=np.float64)
+    n = len(d)
+    e = np.zeros(max(n - 1, 1))
+    e[:max(n - 1, 0)] = np.asarray(T.ev, dtype=np.float64)[:max(n - 1, 0)]
+    Zc = np.array(Z, dtype=np.float64, order="F", copy=True) if Z is not None else None
+    rc = ctx.lib.gs_steqr_f64(ctx.handle, n, _ptr(d), _ptr(e), _ptr(Zc), max(n, 1), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "_gschur!(SymTridiagonal)")
+    return d, e[:max(n - 1, 0)], Zc
+
+
+def _st_eig(T, wantv, sortby, ctx):
+    n = len(T.dv)
+    d, _, Z = gschur_symtridiag(T, np.eye(n) if wantv else None, ctx=ctx)
+    p = np.argsort(d, kind="stable") if sortby == "default" else \
+        (np.arange(n) if sortby is None else np.argsort([sortby(x) for x in d], kind="stable"))
+    return d[p], (Z[:, p] if wantv else None)
+
+
+def hessenberg_hermitian(H, ctx=None):
+    """hessenberg!(Hermitian(A, uplo)) (pirates.jl:236-238 -> hessenberg.jl:26-96) on a
+    copy: HermitianHessenberg(factors, tau, dv, ev, uplo)."""
+    ctx = ctx or get_context()
+    A = np.asarray(H.data)
+    n = _checksquare(A)
+    cplx = np.iscomplexobj(A)
+    dt = np.complex128 if cplx else np.float64
+    A = np.array(A, dtype=dt, order="F", copy=True)
+    d = np.zeros(max(n, 1))
+    e = np.zeros(max(n - 1, 1))
+    tau = np.zeros(max(n - 1, 1), dtype=dt)
+    uplo = str(H.uplo).upper()[:1]
+    fn = ctx.lib.gs_hetrd_c64 if cplx else ctx.lib.gs_hetrd_f64
+    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), ord(uplo), _ptr(d), _ptr(e), _ptr(tau), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "hessenberg!(Hermitian)")
+    return HermitianHessenberg(A, tau[:max(n - 1, 0)], d[:n], e[:max(n - 1, 0)], uplo)
+
+
 def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, jcv=False, ctx=None):
     """Eigen decomposition (pirates.jl:63-160): balance! (permute/scale, as the reference's
     defaults), Schur form, triangularize for real input, right eigenvectors (and left
@@ -437,6 +539,9 @@ def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jc
     eigvalscond, which then replaces the vector-based value) is computed, as the
     reference's (expensive) loop does.  Returns Eigen(values, vectors), or, when jvl, jce
     or jcv is asked for, EigenFull(values, vectors, vectorsl, rconde, rcondv)."""
+    if isinstance(A, (Hermitian, SymTridiagonal)):
+        # eigen!(::Hermitian) / eigen!(::SymTridiagonal) (pirates.jl:162-184)
+        return geigen(A, sortby=sortby, ctx=ctx)
     A = np.asarray(A)
     B = None
     if permute or scale:

@@ -257,6 +257,30 @@ GS_API int gs_eigen_rcond_f64(gs_context* ctx, int64_t n, const double* T, doubl
 GS_API int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rconde, double* rcondv,
                               unsigned flags);
 
+/* geigen!(Hermitian(A, uplo)) / geigvals! (GenericSchur.jl:126-146) with the default
+ * QRIteration: Householder tridiagonalization (hessenberg.jl:26-96), Q (hessenberg.jl:
+ * 145-231) and the tridiagonal QL/QR iteration (symtridiag.jl:79-368).  uplo = 'L' or 'U'
+ * names the triangle of A (n x n, lda) that is read; A is not modified.  w (n) receives the
+ * eigenvalues in ascending order; with GS_WANTZ, V (n x n, ldv) the orthonormal
+ * eigenvectors in the same order.  _c64: A and V interleaved complex, w real. */
+GS_API int gs_heev_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* w, double* V,
+                       int64_t ldv, unsigned flags);
+GS_API int gs_heev_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* w, double* V,
+                       int64_t ldv, unsigned flags);
+/* hessenberg!(Hermitian(A, uplo)) (hessenberg.jl:26-96): the real symmetric tridiagonal
+ * (d: n, e: n-1), the reflector scalars tau (n-1; complex for _c64) and, in A's `uplo`
+ * triangle, the subdiagonal (superdiagonal) entries and reflector tails as the reference
+ * stores them.  A is overwritten in place. */
+GS_API int gs_hetrd_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e,
+                        double* tau, unsigned flags);
+GS_API int gs_hetrd_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e,
+                        double* tau, unsigned flags);
+/* _gschur!(SymTridiagonal(d, e), QRIteration(), Z) (symtridiag.jl:79-183): d (n) receives
+ * the eigenvalues in the iteration's order (unsorted), e (n-1) is overwritten; when Z
+ * (n x n, ldz) is not NULL every rotation is applied to it from the right.  Used by
+ * eigen!/eigvals!(::SymTridiagonal) (symtridiag.jl:43-57), which sort afterwards. */
+GS_API int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags);
+
 /* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
  * eigenvalues with select[k] != 0 move to the leading positions in their order.
  * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if

@@ -7,6 +7,7 @@
 #include "eigvecs_oracle.hpp"
 #include "balance_oracle.hpp"
 #include "condition_oracle.hpp"
+#include "hermitian_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -208,6 +209,31 @@ int or_econd_z(int n, const double* t, int ldt, int nsub, double* out2) {
   out2[0] = eigvalscond<double, zc>(n, (const zc*)t, ldt, nsub);
   out2[1] = subspacesep<double, zc>(n, (const zc*)t, ldt, nsub);
   return 0;
+}
+
+// geigen! / geigvals! of Hermitian(A, uplo) (GenericSchur.jl:126-146): w ascending, V
+// (when wantv) the eigenvectors; A overwritten.  Returns 1 if the sweep limit was hit.
+int or_heev_d(int n, double* a, int lda, int upper, int wantv, double* w, double* v) {
+  return heev<double, double>(n, a, lda, upper != 0, wantv != 0, w, v, n);
+}
+int or_heev_z(int n, double* a, int lda, int upper, int wantv, double* w, double* v) {
+  return heev<double, zc>(n, (zc*)a, lda, upper != 0, wantv != 0, w, (zc*)v, n);
+}
+// _hehessenberg! (hessenberg.jl:26-96): d (n), e (n-1), tau (n-1), A overwritten.
+int or_hetrd_d(int n, double* a, int lda, int upper, double* d, double* e, double* tau) {
+  if (upper) he_tridiag_U<double, double>(n, a, lda, tau, d, e);
+  else he_tridiag_L<double, double>(n, a, lda, tau, d, e);
+  return 0;
+}
+int or_hetrd_z(int n, double* a, int lda, int upper, double* d, double* e, double* tau) {
+  if (upper) he_tridiag_U<double, zc>(n, (zc*)a, lda, (zc*)tau, d, e);
+  else he_tridiag_L<double, zc>(n, (zc*)a, lda, (zc*)tau, d, e);
+  return 0;
+}
+// _gschur!(SymTridiagonal(d, e), QRIteration(), Z) (symtridiag.jl:79-183) with Z n x n
+// (wantz) or none.
+int or_steqr_d(int n, double* d, double* e, double* z, int wantz) {
+  return steqr<double, double>(n, d, e, wantz ? z : nullptr, n, wantz ? n : 0, 30LL * n);
 }
 
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {

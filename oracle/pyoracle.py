@@ -46,6 +46,11 @@ def lib():
             "or_trsylv_z": [_i, _i, _i, _p, _i, _p, _i, _p, _i, _p],
             "or_econd_d": [_i, _p, _i, _i, _p],
             "or_econd_z": [_i, _p, _i, _i, _p],
+            "or_heev_d": [_i, _p, _i, _i, _i, _p, _p],
+            "or_heev_z": [_i, _p, _i, _i, _i, _p, _p],
+            "or_hetrd_d": [_i, _p, _i, _i, _p, _p, _p],
+            "or_hetrd_z": [_i, _p, _i, _i, _p, _p, _p],
+            "or_steqr_d": [_i, _p, _p, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -261,3 +266,42 @@ def condition(T, nsub):
     fn = lib().or_econd_z if cplx else lib().or_econd_d
     fn(n, _ptr(T), max(n, 1), int(nsub), _ptr(out))
     return float(out[0]), float(out[1])
+
+
+def heev(A, uplo="U", wantv=True):
+    """geigen!(Hermitian(A, uplo)) / geigvals! (GenericSchur.jl:126-146) with the default
+    QRIteration: (w ascending, V or None, status)."""
+    cplx = np.iscomplexobj(A)
+    dt = np.complex128 if cplx else np.float64
+    A = _f(A, dt)
+    n = A.shape[0]
+    w = np.zeros(max(n, 1))
+    V = np.zeros((n, n), dtype=dt, order="F") if wantv else None
+    fn = lib().or_heev_z if cplx else lib().or_heev_d
+    st = fn(n, _ptr(A), max(n, 1), int(uplo == "U"), int(wantv), _ptr(w), _ptr(V))
+    return w[:n], V, st
+
+
+def hetrd(A, uplo="L"):
+    """_hehessenberg!(Hermitian(A, uplo)) (hessenberg.jl:26-96): (d, e, tau, factors)."""
+    cplx = np.iscomplexobj(A)
+    dt = np.complex128 if cplx else np.float64
+    A = _f(A, dt)
+    n = A.shape[0]
+    d = np.zeros(max(n, 1))
+    e = np.zeros(max(n - 1, 1))
+    tau = np.zeros(max(n - 1, 1), dtype=dt)
+    fn = lib().or_hetrd_z if cplx else lib().or_hetrd_d
+    fn(n, _ptr(A), max(n, 1), int(uplo == "U"), _ptr(d), _ptr(e), _ptr(tau))
+    return d[:n], e[:max(n - 1, 0)], tau[:max(n - 1, 0)], A
+
+
+def steqr(d, e, wantz=True):
+    """_gschur!(SymTridiagonal(d, e), QRIteration(), Z = I) (symtridiag.jl:79-183):
+    (eigenvalues in the iteration's order, Z, status)."""
+    d = np.array(d, dtype=np.float64)
+    n = len(d)
+    e = np.array(np.concatenate([e, [0.0]]) if n else [0.0], dtype=np.float64)
+    Z = np.asfortranarray(np.eye(n)) if wantz else None
+    st = lib().or_steqr_d(n, _ptr(d), _ptr(e), _ptr(Z), int(wantz))
+    return d, Z, st
