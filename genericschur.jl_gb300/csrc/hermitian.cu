@@ -397,6 +397,27 @@ __device__ void givens_alg(double f, double g, double& cs, double& sn, double& r
   r = rr;
 }
 
+// givensAlgorithm on its plain branch (2^-485 < max(|f|, |g|) < 2^485) from one Newton-
+// refined reciprocal square root: c = f / r, s = g / r, r = sqrt(f^2 + g^2) to ~1 ulp with
+// a third of the serial FP64 instructions of sqrt and two divisions.  The branch tests
+// run on the bit patterns (integer pipe).  Outside [2^-480, 2^480) the exact routine runs.
+__device__ __forceinline__ void givens_fast(double f, double g, double& cs, double& sn, double& r) {
+  const unsigned long long bf = (unsigned long long)__double_as_longlong(f) & 0x7fffffffffffffffULL;
+  const unsigned long long bg = (unsigned long long)__double_as_longlong(g) & 0x7fffffffffffffffULL;
+  if (bg == 0) { cs = 1.0; sn = 0.0; r = f; return; }
+  if (bf == 0) { cs = 0.0; sn = 1.0; r = g; return; }
+  const unsigned long long bm = bf > bg ? bf : bg;
+  if (bm >= 0x21F0000000000000ULL && bm < 0x5DF0000000000000ULL) {
+    const double ss = fma(f, f, g * g);
+    const double inv = rsqrt_nr(ss);
+    double c = f * inv, s = g * inv, rr = ss * inv;
+    if (bf > bg && __double_as_longlong(f) < 0) { c = -c; s = -s; rr = -rr; }
+    cs = c; sn = s; r = rr;
+    return;
+  }
+  givens_alg(f, g, cs, sn, r);
+}
+
 // _dgz_sym2x2 (symtridiag.jl:370-427)
 __device__ void dgz_sym2x2(double a, double b, double c, bool wantvec, double& rt1, double& rt2, double& cs1,
                            double& sn1) {
@@ -434,11 +455,13 @@ __device__ void dgz_sym2x2(double a, double b, double c, bool wantvec, double& r
   }
 }
 
-__device__ void safescale_vec(double* x, int len, double cfrom, double cto) {
+// safescale! of x[0..len) by the lanes of one warp (each element gets the factors in order).
+__device__ void safescale_vec(double* x, int len, double cfrom, double cto, int lane) {
   double mul[8];
   const int k = safescale_factors(cfrom, cto, mul);
-  for (int q = 0; q < k; ++q)
-    for (int i = 0; i < len; ++i) x[i] *= mul[q];
+  for (int i = lane; i < len; i += 32)
+    for (int q = 0; q < k; ++q) x[i] *= mul[q];
+  __syncwarp();
 }
 
 // State of the sweep machine (thread 0 only; persists across phases).
@@ -456,11 +479,17 @@ struct StPhase {
 };
 
 // Runs the state machine until it emits a phase of rotations (returns 1) or finishes
-// (returns 0).  d, e 1-based through the macros.
-__device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, double* sb, StPhase* ph, bool wantZ,
-                          long long maxsweeps) {
+// (returns 0).  Executed by all 32 lanes of one warp with identical values (an FP64
+// instruction costs the same for one lane or 32), so that the scans for splits and
+// negligible off-diagonals test 32 positions per instruction (ballot, first hit); every
+// lane stores the same values, so each lane reads back its own writes.  d, e 1-based
+// through the macros.
+__device__ int st_advance(StState& s, int n, double* __restrict__ d, double* __restrict__ e,
+                          double* __restrict__ cb, double* __restrict__ sb, StPhase* ph, bool wantZ,
+                          long long maxsweeps, int lane) {
 #define D(i) d[(i) - 1]
 #define E(i) e[(i) - 1]
+  const unsigned FULL = 0xffffffffu;
   const double epsT = Prec<double>::eps, eps2 = epsT * epsT;
   const double safmin = Prec<double>::fmin, safmax = 1.0 / safmin;
   const double ssfmax = sqrt(safmax) / 3.0, ssfmin = sqrt(safmin) / eps2;
@@ -468,11 +497,23 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
     if (s.mode == 0) {
       if (s.l1 > n) return 0;
       if (s.l1 > 1) E(s.l1 - 1) = 0.0;
+      // _st_findsplit_fwd!: first m >= l1 with e[m] == 0 or negligible
       int msplit = n;
-      for (int m = s.l1; m <= n - 1; ++m) {
-        const double tst = fabs(E(m));
-        if (tst == 0.0) { msplit = m; break; }
-        if (tst <= sqrt(fabs(D(m))) * sqrt(fabs(D(m + 1))) * epsT) { E(m) = 0.0; msplit = m; break; }
+      for (int base = s.l1; base <= n - 1; base += 32) {
+        const int m = base + lane;
+        int hit = 0;
+        if (m <= n - 1) {
+          const double tst = fabs(E(m));
+          if (tst == 0.0) hit = 1;
+          else if (tst <= sqrt(fabs(D(m))) * sqrt(fabs(D(m + 1))) * epsT) hit = 2;
+        }
+        const unsigned bal = __ballot_sync(FULL, hit != 0);
+        if (bal) {
+          const int first = __ffs(bal) - 1;
+          msplit = base + first;
+          if (__shfl_sync(FULL, hit, first) == 2) E(msplit) = 0.0;
+          break;
+        }
       }
       s.l = s.l1;
       s.lsave = s.l;
@@ -480,24 +521,29 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
       s.lendsave = s.lend;
       s.l1 = msplit + 1;
       if (s.lend == s.l) continue;
+      // opnorm(SymTridiagonal(d[l:lend], e[l:lend-1]), Inf)
       double an = 0.0;
-      for (int i = s.l; i <= s.lend; ++i) {
+      for (int i = s.l + lane; i <= s.lend; i += 32) {
         double t = fabs(D(i));
         if (i > s.l) t += fabs(E(i - 1));
         if (i < s.lend) t += fabs(E(i));
         if (t > an || t != t) an = t;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_xor_sync(FULL, an, o);
+        if (w > an || w != w) an = w;
       }
       s.anorm = an;
       s.iscale = 0;
       if (an == 0.0) continue;
       if (an > ssfmax) {
         s.iscale = 1;
-        safescale_vec(&D(s.l), s.lend - s.l + 1, an, ssfmax);
-        safescale_vec(&E(s.l), s.lend - s.l, an, ssfmax);
+        safescale_vec(&D(s.l), s.lend - s.l + 1, an, ssfmax, lane);
+        safescale_vec(&E(s.l), s.lend - s.l, an, ssfmax, lane);
       } else if (an < ssfmin) {
         s.iscale = 2;
-        safescale_vec(&D(s.l), s.lend - s.l + 1, an, ssfmin);
-        safescale_vec(&E(s.l), s.lend - s.l, an, ssfmin);
+        safescale_vec(&D(s.l), s.lend - s.l + 1, an, ssfmin, lane);
+        safescale_vec(&E(s.l), s.lend - s.l, an, ssfmin, lane);
       }
       if (fabs(D(s.lend)) < fabs(D(s.l))) { s.lend = s.lsave; s.l = s.lendsave; }
       s.mode = s.lend > s.l ? 1 : 2;
@@ -509,9 +555,18 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
         continue;
       }
       const int l = s.l, lend = s.lend;
+      // first m in [l, lend) with a negligible e[m]
       int ms = lend;
-      for (int m = l; m <= lend - 1; ++m)
-        if (E(m) * E(m) <= (eps2 * fabs(D(m))) * fabs(D(m + 1)) + safmin) { ms = m; break; }
+      for (int base = l; base <= lend - 1; base += 32) {
+        const int m = base + lane;
+        bool hit = false;
+        if (m <= lend - 1) {
+          const double em = E(m);
+          hit = em * em <= (eps2 * fabs(D(m))) * fabs(D(m + 1)) + safmin;
+        }
+        const unsigned bal = __ballot_sync(FULL, hit);
+        if (bal) { ms = base + __ffs(bal) - 1; break; }
+      }
       if (ms < lend) E(ms) = 0.0;
       double p = D(l);
       if (ms == l) {
@@ -534,15 +589,18 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
       double sn = 1.0, c = 1.0;
       p = 0.0;
       int q = 0;
+      double dn = D(ms);  // d[i+1] of the next step, carried
       for (int i = ms - 1; i >= l; --i, ++q) {
-        const double f = sn * E(i), b = c * E(i);
-        givens_alg(g, f, c, sn, r);
+        const double ei = E(i), di = D(i);
+        const double f = sn * ei, b = c * ei;
+        givens_fast(g, f, c, sn, r);
         if (i < ms - 1) E(i + 1) = r;
-        g = D(i + 1) - p;
-        r = (D(i) - g) * sn + 2.0 * c * b;
+        g = dn - p;
+        r = fma(di - g, sn, 2.0 * c * b);
         p = sn * r;
         D(i + 1) = g + p;
-        g = c * r - b;
+        g = fma(c, r, -b);
+        dn = di;
         if (wantZ) { cb[q] = c; sb[q] = -sn; }
       }
       D(l) -= p;
@@ -556,9 +614,18 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
         continue;
       }
       const int l = s.l, lend = s.lend;
+      // first m in (lend, l], descending, with a negligible e[m-1]
       int ms = lend;
-      for (int m = l; m >= lend + 1; --m)
-        if (E(m - 1) * E(m - 1) <= (eps2 * fabs(D(m))) * fabs(D(m - 1)) + safmin) { ms = m; break; }
+      for (int top = l; top >= lend + 1; top -= 32) {
+        const int m = top - lane;
+        bool hit = false;
+        if (m >= lend + 1) {
+          const double em = E(m - 1);
+          hit = em * em <= (eps2 * fabs(D(m))) * fabs(D(m - 1)) + safmin;
+        }
+        const unsigned bal = __ballot_sync(FULL, hit);
+        if (bal) { ms = top - (__ffs(bal) - 1); break; }
+      }
       if (ms > lend) E(ms - 1) = 0.0;
       double p = D(l);
       if (ms == l) {
@@ -581,15 +648,18 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
       double sn = 1.0, c = 1.0;
       p = 0.0;
       int q = 0;
+      double dc = D(ms);  // d[i] of the next step, carried
       for (int i = ms; i <= l - 1; ++i, ++q) {
-        const double f = sn * E(i), b = c * E(i);
-        givens_alg(g, f, c, sn, r);
+        const double ei = E(i), dn = D(i + 1);
+        const double f = sn * ei, b = c * ei;
+        givens_fast(g, f, c, sn, r);
         if (i != ms) E(i - 1) = r;
-        g = D(i) - p;
-        r = (D(i + 1) - g) * sn + 2.0 * c * b;
+        g = dc - p;
+        r = fma(dn - g, sn, 2.0 * c * b);
         p = sn * r;
         D(i) = g + p;
-        g = c * r - b;
+        g = fma(c, r, -b);
+        dc = dn;
         if (wantZ) { cb[q] = c; sb[q] = sn; }
       }
       D(l) -= p;
@@ -599,11 +669,11 @@ __device__ int st_advance(StState& s, int n, double* d, double* e, double* cb, d
     }
     // mode 3: the block is done; undo its scaling
     if (s.iscale == 1) {
-      safescale_vec(&D(s.lsave), s.lendsave - s.lsave + 1, ssfmax, s.anorm);
-      safescale_vec(&E(s.lsave), s.lendsave - s.lsave, ssfmax, s.anorm);
+      safescale_vec(&D(s.lsave), s.lendsave - s.lsave + 1, ssfmax, s.anorm, lane);
+      safescale_vec(&E(s.lsave), s.lendsave - s.lsave, ssfmax, s.anorm, lane);
     } else if (s.iscale == 2) {
-      safescale_vec(&D(s.lsave), s.lendsave - s.lsave + 1, ssfmin, s.anorm);
-      safescale_vec(&E(s.lsave), s.lendsave - s.lsave, ssfmin, s.anorm);
+      safescale_vec(&D(s.lsave), s.lendsave - s.lsave + 1, ssfmin, s.anorm, lane);
+      safescale_vec(&E(s.lsave), s.lendsave - s.lsave, ssfmin, s.anorm, lane);
     }
     s.mode = 0;
   }
@@ -678,15 +748,27 @@ __device__ __forceinline__ void apply_phase(S* Z, long long ldz, int r, const St
 }
 
 // The cooperative sweep kernel.  rot: 2 buffers x 2 x n doubles (c, s).
+// With smem_de (2 n doubles of dynamic shared memory), d and e live in shared memory
+// during the iteration: the recurrence reads them at every step.
 template <class S>
-__global__ void __launch_bounds__(kHeT) k_steqr(int n, double* d, double* e, S* Z, long long ldz, int nz,
-                                                 double* rot, StCtl* ctl, long long maxsweeps) {
+__global__ void __launch_bounds__(kHeT) k_steqr(int n, double* dg, double* eg, S* Z, long long ldz, int nz,
+                                                 double* rot, StCtl* ctl, long long maxsweeps, int smem_de) {
+  extern __shared__ double sde[];
   const bool wantZ = Z != nullptr && nz > 0;
-  const bool chain = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool chain = blockIdx.x == 0 && threadIdx.x < 32;  // warp 0 of block 0, lanes in lockstep
+  const int lane = threadIdx.x & 31;
+  double* d = dg;
+  double* e = eg;
   StState st;
   if (chain) {
     st.l1 = 1; st.l = 0; st.lend = 0; st.lsave = 0; st.lendsave = 0; st.iscale = 0; st.mode = 0;
     st.anorm = 0.0; st.sweeps = 0; st.status = 0;
+    if (smem_de) {
+      d = sde;
+      e = sde + n;
+      for (int i = lane; i < n; i += 32) { d[i] = dg[i]; e[i] = i < n - 1 ? eg[i] : 0.0; }
+      __syncwarp();
+    }
   }
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nzt = (long long)gridDim.x * blockDim.x - 32;  // warp 0 of block 0 runs the chain
@@ -697,8 +779,16 @@ __global__ void __launch_bounds__(kHeT) k_steqr(int n, double* d, double* e, S* 
       StPhase* ph = &ctl->ph[b];
       if (!finished) {
         const int emitted = st_advance(st, n, d, e, rot + (size_t)b * 2 * n, rot + (size_t)b * 2 * n + n, ph, wantZ,
-                                       maxsweeps);
-        if (!emitted) { finished = true; ph->count = 0; ctl->status = st.status; }
+                                       maxsweeps, lane);
+        if (!emitted) {
+          finished = true;
+          ph->count = 0;
+          ctl->status = st.status;
+          if (smem_de) {
+            __syncwarp();
+            for (int i = lane; i < n; i += 32) { dg[i] = d[i]; if (i < n - 1) eg[i] = e[i]; }
+          }
+        }
       } else {
         ph->count = 0;
       }
@@ -777,17 +867,26 @@ cudaError_t launch_steqr(int n, double* d, double* e, S* Z, long long ldz, int n
   cudaError_t err = cudaMemsetAsync(ctl, 0, sizeof(StCtl), s);
   if (err != cudaSuccess) return err;
   StCtl* c = reinterpret_cast<StCtl*>(ctl);
+  // d, e in shared memory when they fit
+  int smem_de = (size_t)2 * n * sizeof(double) <= 200 * 1024 ? 1 : 0;
+  const size_t smem = smem_de ? (size_t)2 * n * sizeof(double) : 0;
+  static size_t attr_set = 0;
+  if (smem > 48 * 1024 && attr_set < smem) {
+    err = cudaFuncSetAttribute(k_steqr<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (err != cudaSuccess) return err;
+    attr_set = 200 * 1024;
+  }
   if (Z == nullptr || nz == 0) {
-    k_steqr<S><<<1, 32, 0, s>>>(n, d, e, nullptr, 0, 0, rot, c, maxsweeps);
+    k_steqr<S><<<1, 32, smem, s>>>(n, d, e, nullptr, 0, 0, rot, c, maxsweeps, smem_de);
     return cudaGetLastError();
   }
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_steqr<S>, kHeT, 0);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_steqr<S>, kHeT, smem);
   if (err != cudaSuccess) return err;
   int blocks = (int)std::min<long long>(((long long)nz + 32 + kHeT - 1) / kHeT, (long long)num_sms * std::max(per_sm, 1));
   blocks = std::max(blocks, 1);
-  void* args[] = {&n, &d, &e, &Z, &ldz, &nz, &rot, &c, &maxsweeps};
-  return cudaLaunchCooperativeKernel((const void*)k_steqr<S>, dim3(blocks), dim3(kHeT), args, 0, s);
+  void* args[] = {&n, &d, &e, &Z, &ldz, &nz, &rot, &c, &maxsweeps, &smem_de};
+  return cudaLaunchCooperativeKernel((const void*)k_steqr<S>, dim3(blocks), dim3(kHeT), args, smem, s);
 }
 
 #define GS_HE_INST(S)                                                                                                 \
