@@ -387,4 +387,108 @@ template <> struct Prec<float> {
   static constexpr float eps = 1.1920929e-07f, fmin = 1.17549435e-38f;
   static constexpr float safe_lo = 1.0e-15f, safe_hi = 1.0e15f;
 };
+
+// ---- CTA-wide helpers: 2-norm and Householder reflector of a vector in global memory ----
+// Largest component magnitude (re and im separately) of x[0..m), over the CTA.
+template <class S> __device__ __forceinline__ double comp_max(S v);
+template <> __device__ __forceinline__ double comp_max<double>(double v) { return fabs(v); }
+template <> __device__ __forceinline__ double comp_max<double2>(double2 v) { return fmax(fabs(v.x), fabs(v.y)); }
+template <class S> __device__ __forceinline__ double comp_ssq(S v, double inv);
+template <> __device__ __forceinline__ double comp_ssq<double>(double v, double inv) { const double a = v * inv; return a * a; }
+template <> __device__ __forceinline__ double comp_ssq<double2>(double2 v, double inv) {
+  const double a = v.x * inv, b = v.y * inv;
+  return fma(a, a, b * b);
+}
+
+// 2-norm of x[0..m) without overflow (one CTA of NT threads).
+template <class S, int NT>
+__device__ double cta_norm2(const S* x, int m, double* red) {
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < m; k += NT) mx = fmax(mx, comp_max(x[k]));
+  mx = block_max<NT>(mx, red);
+  if (!(mx > 0.0) || !isfinite(mx)) return mx;
+  const double inv = 1.0 / mx;
+  double ss = 0.0;
+  for (int k = threadIdx.x; k < m; k += NT) ss += comp_ssq(x[k], inv);
+  ss = block_sum<NT>(ss, red);
+  return mx * sqrt(ss);
+}
+
+__device__ __forceinline__ double hypot3d(double a, double b, double c) {
+  const double m = fmax(fabs(a), fmax(fabs(b), fabs(c)));
+  if (!(m > 0.0) || !isfinite(m)) return m;
+  const double x = a / m, y = b / m, z = c / m;
+  return m * sqrt(fma(x, x, fma(y, y, z * z)));
+}
+
+// _reflector! (householder.jl:12-102) on x[0..m) by one CTA of NT threads: x[0] <- beta
+// (real), the tail scaled to the essential part; returns tau.  All threads call it.
+template <int NT>
+__device__ double cta_reflector(double* x, int m, double* red) {
+  if (m <= 1) return 0.0;
+  const double sfmin = 2.0 * Prec<double>::fmin / Prec<double>::eps;
+  double alpha = x[0];
+  double xnorm = cta_norm2<double, NT>(x + 1, m - 1, red);
+  if (xnorm == 0.0) return 0.0;
+  double beta = -copysign(hypot(alpha, xnorm), alpha);
+  int kount = 0;
+  if (fabs(beta) < sfmin) {
+    const double rs = 1.0 / sfmin;
+    bool smallb = true;
+    while (smallb) {
+      ++kount;
+      __syncthreads();
+      for (int k = 1 + threadIdx.x; k < m; k += NT) x[k] *= rs;
+      beta *= rs;
+      alpha *= rs;
+      smallb = fabs(beta) < sfmin && kount < 20;
+    }
+    __syncthreads();
+    xnorm = cta_norm2<double, NT>(x + 1, m - 1, red);
+    beta = -copysign(hypot(alpha, xnorm), alpha);
+  }
+  const double tau = (beta - alpha) / beta;
+  const double t = 1.0 / (alpha - beta);
+  __syncthreads();
+  for (int k = 1 + threadIdx.x; k < m; k += NT) x[k] *= t;
+  for (int j = 0; j < kount; ++j) beta *= sfmin;
+  __syncthreads();
+  if (threadIdx.x == 0) x[0] = beta;
+  return tau;
+}
+template <int NT>
+__device__ double2 cta_reflector(double2* x, int m, double* red) {
+  if (m < 1) return make_double2(0.0, 0.0);
+  const double sfmin = Prec<double>::fmin / Prec<double>::eps;
+  double ar = x[0].x, ai = x[0].y;
+  double xnorm = m > 1 ? cta_norm2<double2, NT>(x + 1, m - 1, red) : 0.0;
+  if (xnorm == 0.0 && ai == 0.0) return make_double2(0.0, 0.0);
+  double beta = -copysign(hypot3d(ar, ai, xnorm), ar);
+  int kount = 0;
+  if (fabs(beta) < sfmin) {
+    const double rs = 1.0 / sfmin;
+    bool smallb = true;
+    while (smallb) {
+      ++kount;
+      __syncthreads();
+      for (int k = 1 + threadIdx.x; k < m; k += NT) x[k] = make_double2(x[k].x * rs, x[k].y * rs);
+      beta *= rs;
+      ar *= rs;
+      ai *= rs;
+      smallb = fabs(beta) < sfmin && kount < 20;
+    }
+    __syncthreads();
+    xnorm = m > 1 ? cta_norm2<double2, NT>(x + 1, m - 1, red) : 0.0;
+    beta = -copysign(hypot3d(ar, ai, xnorm), ar);
+  }
+  const double2 tau = make_double2((beta - ar) / beta, -ai / beta);
+  const double2 t = zdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
+  __syncthreads();
+  for (int k = 1 + threadIdx.x; k < m; k += NT) x[k] = zmul(x[k], t);
+  for (int j = 0; j < kount; ++j) beta *= sfmin;
+  __syncthreads();
+  if (threadIdx.x == 0) x[0] = make_double2(beta, 0.0);
+  return tau;
+}
+
 }  // namespace gsk

@@ -108,6 +108,24 @@ struct SylvArgs {
   int* flag;      // |= 1 perturbed, 2 the overflow rescaling is needed, 4 non-finite entry
 };
 enum { N1_FILL = 0, N1_UNIT = 1, N1_ALT = 2, N1_SIGN = 3 };
+// Generalized Schur of complex pencils (qz.cu): one CTA per pencil of a ragged batch.
+struct QzBatch {
+  int count;
+  const int* ns;
+  const long long* offs;   // element (double2) offsets of A, B, Q, Z
+  const long long* woffs;  // offsets of alpha, beta
+  double2* A;              // in: A, out: S
+  double2* B;              // in: B, out: T
+  double2* Q;              // out (may be null)
+  double2* Z;              // out (may be null)
+  double2* alpha;
+  double2* beta;
+  int* status;             // per pencil: 0, or 1 when the iteration limit was reached
+  int scale;
+  int n1;                  // ns == null: one pencil of order n1 at offset 0
+};
+cudaError_t launch_ggschur(const QzBatch& bt, int num_sms, cudaStream_t s);
+
 // Hermitian path (hermitian.cu).  S = double or double2.
 struct HeCtlBuf {
   alignas(16) unsigned char bytes[64];

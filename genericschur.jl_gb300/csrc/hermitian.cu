@@ -71,111 +71,6 @@ template <class S> __device__ __forceinline__ S warp_sum(S v) {
   return v;
 }
 
-// Largest component magnitude (re and im separately) of x[0..m), over the CTA.
-template <class S> __device__ __forceinline__ double comp_max(S v);
-template <> __device__ __forceinline__ double comp_max<double>(double v) { return fabs(v); }
-template <> __device__ __forceinline__ double comp_max<double2>(double2 v) { return fmax(fabs(v.x), fabs(v.y)); }
-template <class S> __device__ __forceinline__ double comp_ssq(S v, double inv);
-template <> __device__ __forceinline__ double comp_ssq<double>(double v, double inv) { const double a = v * inv; return a * a; }
-template <> __device__ __forceinline__ double comp_ssq<double2>(double2 v, double inv) {
-  const double a = v.x * inv, b = v.y * inv;
-  return fma(a, a, b * b);
-}
-
-// 2-norm of x[0..m) without overflow (one CTA of NT threads).
-template <class S, int NT>
-__device__ double cta_norm2(const S* x, int m, double* red) {
-  double mx = 0.0;
-  for (int k = threadIdx.x; k < m; k += NT) mx = fmax(mx, comp_max(x[k]));
-  mx = block_max<NT>(mx, red);
-  if (!(mx > 0.0) || !isfinite(mx)) return mx;
-  const double inv = 1.0 / mx;
-  double ss = 0.0;
-  for (int k = threadIdx.x; k < m; k += NT) ss += comp_ssq(x[k], inv);
-  ss = block_sum<NT>(ss, red);
-  return mx * sqrt(ss);
-}
-
-__device__ __forceinline__ double hypot3d(double a, double b, double c) {
-  const double m = fmax(fabs(a), fmax(fabs(b), fabs(c)));
-  if (!(m > 0.0) || !isfinite(m)) return m;
-  const double x = a / m, y = b / m, z = c / m;
-  return m * sqrt(fma(x, x, fma(y, y, z * z)));
-}
-
-// _reflector! (householder.jl:12-102) on x[0..m), one CTA: x[0] <- beta (real), the
-// tail scaled to the essential part; returns tau.
-template <class S, int NT> __device__ S cta_reflector(S* x, int m, double* red, S* sh);
-template <>
-__device__ double cta_reflector<double, kHeT>(double* x, int m, double* red, double* sh) {
-  if (m <= 1) return 0.0;
-  const double sfmin = 2.0 * Prec<double>::fmin / Prec<double>::eps;
-  double alpha = x[0];
-  double xnorm = cta_norm2<double, kHeT>(x + 1, m - 1, red);
-  if (xnorm == 0.0) return 0.0;
-  double beta = -copysign(hypot(alpha, xnorm), alpha);
-  int kount = 0;
-  if (fabs(beta) < sfmin) {
-    const double rs = 1.0 / sfmin;
-    bool smallb = true;
-    while (smallb) {
-      ++kount;
-      __syncthreads();
-      for (int k = 1 + threadIdx.x; k < m; k += kHeT) x[k] *= rs;
-      beta *= rs;
-      alpha *= rs;
-      smallb = fabs(beta) < sfmin && kount < 20;
-    }
-    __syncthreads();
-    xnorm = cta_norm2<double, kHeT>(x + 1, m - 1, red);
-    beta = -copysign(hypot(alpha, xnorm), alpha);
-  }
-  const double tau = (beta - alpha) / beta;
-  const double t = 1.0 / (alpha - beta);
-  __syncthreads();
-  for (int k = 1 + threadIdx.x; k < m; k += kHeT) x[k] *= t;
-  for (int j = 0; j < kount; ++j) beta *= sfmin;
-  __syncthreads();
-  if (threadIdx.x == 0) x[0] = beta;
-  (void)sh;
-  return tau;
-}
-template <>
-__device__ double2 cta_reflector<double2, kHeT>(double2* x, int m, double* red, double2* sh) {
-  if (m < 1) return make_double2(0.0, 0.0);
-  const double sfmin = Prec<double>::fmin / Prec<double>::eps;
-  double ar = x[0].x, ai = x[0].y;
-  double xnorm = m > 1 ? cta_norm2<double2, kHeT>(x + 1, m - 1, red) : 0.0;
-  if (xnorm == 0.0 && ai == 0.0) return make_double2(0.0, 0.0);
-  double beta = -copysign(hypot3d(ar, ai, xnorm), ar);
-  int kount = 0;
-  if (fabs(beta) < sfmin) {
-    const double rs = 1.0 / sfmin;
-    bool smallb = true;
-    while (smallb) {
-      ++kount;
-      __syncthreads();
-      for (int k = 1 + threadIdx.x; k < m; k += kHeT) x[k] = make_double2(x[k].x * rs, x[k].y * rs);
-      beta *= rs;
-      ar *= rs;
-      ai *= rs;
-      smallb = fabs(beta) < sfmin && kount < 20;
-    }
-    __syncthreads();
-    xnorm = m > 1 ? cta_norm2<double2, kHeT>(x + 1, m - 1, red) : 0.0;
-    beta = -copysign(hypot3d(ar, ai, xnorm), ar);
-  }
-  const double2 tau = make_double2((beta - ar) / beta, -ai / beta);
-  const double2 t = zdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
-  __syncthreads();
-  for (int k = 1 + threadIdx.x; k < m; k += kHeT) x[k] = zmul(x[k], t);
-  for (int j = 0; j < kount; ++j) beta *= sfmin;
-  __syncthreads();
-  if (threadIdx.x == 0) x[0] = make_double2(beta, 0.0);
-  (void)sh;
-  return tau;
-}
-
 // Control block of the tridiagonalization (device memory).
 template <class S> struct HeCtl {
   S tau;          // reflector of the current step
@@ -201,11 +96,10 @@ __global__ void k_he_prep(const S* __restrict__ A, long long lda, int n, int upp
 // Reflector of column i (0-based) of B: x = B[i+1:n, i].  One CTA.  Writes tau, e[i],
 // d[i], sets B[i+1, i] = 1 (the head of v during the step).
 template <class S>
-__device__ void he_step_reflector(S* B, int n, int i, HeCtl<S>* ctl, S* tau, double* d, double* e, double* red,
-                                  S* sh) {
+__device__ void he_step_reflector(S* B, int n, int i, HeCtl<S>* ctl, S* tau, double* d, double* e, double* red) {
   S* x = B + (size_t)i * n + (i + 1);
   const int m = n - 1 - i;
-  const S t = cta_reflector<S, kHeT>(x, m, red, sh);
+  const S t = cta_reflector<kHeT>(x, m, red);
   __syncthreads();
   if (threadIdx.x == 0) {
     e[i] = Hs<S>::re(x[0]);
@@ -219,12 +113,11 @@ __device__ void he_step_reflector(S* B, int n, int i, HeCtl<S>* ctl, S* tau, dou
 template <class S>
 __global__ void __launch_bounds__(kHeT) k_he_first(S* B, int n, HeCtl<S>* ctl, S* tau, double* d, double* e) {
   __shared__ double red[kHeT / 32];
-  __shared__ S sh[2];
   if (n == 1) {
     if (threadIdx.x == 0) d[0] = Hs<S>::re(B[0]);
     return;
   }
-  he_step_reflector<S>(B, n, 0, ctl, tau, d, e, red, sh);
+  he_step_reflector<S>(B, n, 0, ctl, tau, d, e, red);
 }
 
 // w_j = tau sum_k conj(B[k, j]) v_k for j in [i+1, n); warp per column.  partial[cta] =
@@ -275,7 +168,6 @@ __global__ void __launch_bounds__(kHeT) k_he_update(S* B, int n, int i, const S*
                                                      S* tau, double* d, double* e) {
   using O = Hs<S>;
   __shared__ double red[kHeT / 32];
-  __shared__ S sh[2];
   __shared__ bool last;
   const int m = n - 1 - i;
   const S* v = B + (size_t)i * n + (i + 1);
@@ -308,7 +200,7 @@ __global__ void __launch_bounds__(kHeT) k_he_update(S* B, int n, int i, const S*
     ctl->t_up = 0;
   }
   if (i + 1 <= n - 2) {
-    he_step_reflector<S>(B, n, i + 1, ctl, tau, d, e, red, sh);
+    he_step_reflector<S>(B, n, i + 1, ctl, tau, d, e, red);
   } else if (threadIdx.x == 0) {
     d[n - 1] = O::re(B[(size_t)(n - 1) * n + (n - 1)]);
   }

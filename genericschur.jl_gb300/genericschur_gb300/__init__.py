@@ -32,7 +32,8 @@ __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "Argum
            "eig_adjoint_batched", "hessenberg", "gschur_mixed", "balance", "balance_", "Balancer", "balancer_lmul",
            "balancer_ldiv", "enormalize", "gordschur", "ordschur", "rconde", "EigenFull", "eigvalscond",
            "subspacesep", "eigen_rcond", "Hermitian", "SymTridiagonal", "HermitianHessenberg", "geigen",
-           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "get_context", "Context", "pack_batch", "unpack_batch"]
+           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "GeneralizedSchur", "ggschur", "ggschur_batched",
+           "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
 Eigen = namedtuple("Eigen", ["values", "vectors"])
@@ -112,7 +113,71 @@ def gschur(A, **kw):
     return gschur_(np.array(A, dtype=dt, order="F", copy=True), **kw)
 
 
-def schur(A, **kw):
+# LinearAlgebra.GeneralizedSchur(S, T, alpha, beta, Q, Z): A = Q S Z', B = Q T Z'
+GeneralizedSchur = namedtuple("GeneralizedSchur", ["S", "T", "alpha", "beta", "Q", "Z"])
+
+
+def ggschur(A, B, wantQ=True, wantZ=True, scale=True, ctx=None):
+    """ggschur!(A, B; wantQ, wantZ, scale) (generalized.jl:21-80) on copies, on the GPU:
+    the generalized Schur form of the pencil (A, B).  Real pencils are taken as complex
+    (the result is the complex generalized Schur form)."""
+    ctx = ctx or get_context()
+    S = np.array(A, dtype=np.complex128, order="F", copy=True)
+    T = np.array(B, dtype=np.complex128, order="F", copy=True)
+    n = _checksquare(S)
+    if _checksquare(T) != n:
+        raise ArgumentError("matrices must have the same sizes")
+    Q = np.zeros((n, n), dtype=np.complex128, order="F") if wantQ else None
+    Z = np.zeros((n, n), dtype=np.complex128, order="F") if wantZ else None
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1), dtype=np.complex128)
+    rc = ctx.lib.gs_ggschur_c64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(al), _ptr(be),
+                                _capi.GS_SCALE if scale else 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "ggschur!")
+    return GeneralizedSchur(S, T, al[:n], be[:n], Q, Z)
+
+
+def ggschur_batched(As, Bs, wantQ=True, wantZ=True, scale=True, ctx=None):
+    """ggschur! over a list of pencils in one launch (one CTA per pencil).  Returns a list
+    of GeneralizedSchur and the per-pencil status."""
+    ctx = ctx or get_context()
+    Ap, ns, offs, woffs = pack_batch(As, dtype=np.complex128)
+    Bp, ns2, _, _ = pack_batch(Bs, dtype=np.complex128)
+    if not np.array_equal(ns, ns2):
+        raise ArgumentError("matrices must have the same sizes")
+    plen = len(Ap)
+    wlen = int(ns.sum())
+    Qp = np.zeros(plen, dtype=np.complex128) if wantQ else None
+    Zp = np.zeros(plen, dtype=np.complex128) if wantZ else None
+    al = np.zeros(max(wlen, 1), dtype=np.complex128)
+    be = np.zeros(max(wlen, 1), dtype=np.complex128)
+    st = np.zeros(len(ns), dtype=np.int32)
+    rc = ctx.lib.gs_ggschur_batched_c64(ctx.handle, len(ns), _ptr(ns), _ptr(offs), plen, _ptr(Ap), _ptr(Bp), _ptr(Qp),
+                                        _ptr(Zp), _ptr(woffs), wlen, _ptr(al), _ptr(be), _ptr(st),
+                                        _capi.GS_SCALE if scale else 0)
+    if rc not in (GS_OK, GS_UNCONVERGED):
+        _raise(rc, ctx, "ggschur! (batched)")
+    out = []
+    for k, n in enumerate(ns):
+        n = int(n)
+        o, w = int(offs[k]), int(woffs[k])
+        sl = slice(o, o + n * n)
+        out.append(GeneralizedSchur(Ap[sl].reshape(n, n, order="F"), Bp[sl].reshape(n, n, order="F"),
+                                    al[w:w + n].copy(), be[w:w + n].copy(),
+                                    Qp[sl].reshape(n, n, order="F") if wantQ else None,
+                                    Zp[sl].reshape(n, n, order="F") if wantZ else None))
+    return out, st
+
+
+def schur(A, B=None, **kw):
+    """schur(A) (pirates.jl:8-10) or schur(A, B) -> ggschur (pirates.jl:11-15)."""
+    if B is not None:
+        return ggschur(A, B, **kw)
+    return _schur1(A, **kw)
+
+
+def _schur1(A, **kw):
     """LinearAlgebra.schur through the pirated schur! (pirates.jl:8-10)."""
     return gschur(A, **kw)
 
@@ -122,9 +187,14 @@ def _eigsortby(w):
     return np.lexsort((w.imag, w.real))
 
 
-def eigvals(A, sortby="default", **kw):
+def eigvals(A, B=None, sortby="default", **kw):
     """Eigenvalues via gschur!(A; wantZ=false) (pirates.jl:17-27); for a Hermitian or
-    SymTridiagonal argument, geigvals! (GenericSchur.jl:138-146, symtridiag.jl:51-57)."""
+    SymTridiagonal argument, geigvals! (GenericSchur.jl:138-146, symtridiag.jl:51-57); for a
+    pencil (A, B), alpha ./ beta of ggschur! in the Schur form's order."""
+    if B is not None:
+        G = ggschur(A, B, wantQ=False, wantZ=False, ctx=kw.get("ctx"))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return G.alpha / G.beta
     if isinstance(A, Hermitian):
         return geigvals(A, sortby=sortby, **kw)
     if isinstance(A, SymTridiagonal):

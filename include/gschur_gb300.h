@@ -281,6 +281,23 @@ GS_API int gs_hetrd_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int 
  * eigen!/eigvals!(::SymTridiagonal) (symtridiag.jl:43-57), which sort afterwards. */
 GS_API int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags);
 
+/* ggschur!(A, B; wantQ, wantZ, scale) (generalized.jl:21-80) for a complex pencil: qr!(B),
+ * Hessenberg-triangular reduction (_hessenberg!, 82-113) and the single-shift QZ
+ * iteration (_gqz!, 125-487).  A <- S, B <- T (both upper triangular, diag(T) real and
+ * non-negative), Q and Z (n x n; NULL when not wanted) unitary with A = Q S Z^H and
+ * B = Q T Z^H; alpha, beta (n) the generalized eigenvalues alpha ./ beta.  Interleaved
+ * complex, leading dimension n.  GS_SCALE applies _scale! to A and B as the reference's
+ * default scale = true does.  GS_UNCONVERGED at the reference's 100 n iteration limit. */
+GS_API int gs_ggschur_c64(gs_context* ctx, int64_t n, double* A, double* B, double* Q, double* Z, double* alpha,
+                          double* beta, unsigned flags);
+/* The same over a ragged batch: pencil b has order ns[b] at element offset offs[b] of the
+ * packed A, B, Q, Z (packed_len complex elements each) and its alpha, beta at woffs[b]
+ * (wlen elements).  One CTA per pencil.  status (count, may be NULL) receives 0 or
+ * GS_UNCONVERGED per pencil. */
+GS_API int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                  int64_t packed_len, double* A, double* B, double* Q, double* Z, const int64_t* woffs,
+                                  int64_t wlen, double* alpha, double* beta, int32_t* status, unsigned flags);
+
 /* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
  * eigenvalues with select[k] != 0 move to the leading positions in their order.
  * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if

@@ -8,6 +8,7 @@
 #include "balance_oracle.hpp"
 #include "condition_oracle.hpp"
 #include "hermitian_oracle.hpp"
+#include "qz_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -234,6 +235,12 @@ int or_hetrd_z(int n, double* a, int lda, int upper, double* d, double* e, doubl
 // (wantz) or none.
 int or_steqr_d(int n, double* d, double* e, double* z, int wantz) {
   return steqr<double, double>(n, d, e, wantz ? z : nullptr, n, wantz ? n : 0, 30LL * n);
+}
+
+// ggschur!(A, B) for complex pencils (generalized.jl:21-80): A <- S, B <- T, Q, Z (n x n
+// each, wanted when non-null), alpha, beta.  Returns 1 at the iteration limit.
+int or_ggschur_z(int n, double* a, double* b, double* q, double* z, double* alpha, double* beta, int scale) {
+  return ggschur_cplx<double>(n, (zc*)a, n, (zc*)b, n, (zc*)q, (zc*)z, (zc*)alpha, (zc*)beta, scale != 0, 100LL * n);
 }
 
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {

@@ -51,6 +51,7 @@ def lib():
             "or_hetrd_d": [_i, _p, _i, _i, _p, _p, _p],
             "or_hetrd_z": [_i, _p, _i, _i, _p, _p, _p],
             "or_steqr_d": [_i, _p, _p, _p, _i],
+            "or_ggschur_z": [_i, _p, _p, _p, _p, _p, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -305,3 +306,17 @@ def steqr(d, e, wantz=True):
     Z = np.asfortranarray(np.eye(n)) if wantz else None
     st = lib().or_steqr_d(n, _ptr(d), _ptr(e), _ptr(Z), int(wantz))
     return d, Z, st
+
+
+def ggschur(A, B, scale=True):
+    """ggschur!(A, B) for a complex pencil (generalized.jl:21-80): (S, T, alpha, beta, Q, Z,
+    status)."""
+    S = _f(A, np.complex128)
+    T = _f(B, np.complex128)
+    n = S.shape[0]
+    Q = np.zeros((n, n), dtype=np.complex128, order="F")
+    Z = np.zeros((n, n), dtype=np.complex128, order="F")
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1), dtype=np.complex128)
+    st = lib().or_ggschur_z(n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(al), _ptr(be), int(scale))
+    return S, T, al[:n], be[:n], Q, Z, st

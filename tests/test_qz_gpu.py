@@ -1,0 +1,120 @@
+"""GPU tests of the generalized Schur decomposition of complex pencils, ggschur!(A, B)
+(generalized.jl:21-80, _hessenberg! 82-113, _gqz! 125-487), restating the reference's
+gschurtest (test/generalized.jl:1-37): S and T upper triangular, A = Q S Z' and
+B = Q T Z' to 20 n eps |A|, Q and Z unitary to 20 n eps; on its "basic sanity" pencils
+(rand, n = 4 and 32) and its "challenging" ones (test/generalized.jl:98-121: triangular
+pencils with zero diagonal entries in A and in B, rotated by random unitaries), plus the
+oracle's restatement on the same inputs: the same generalized eigenvalues (optimal
+matching) and the same number of infinite ones (beta = 0)."""
+import numpy as np
+import pytest
+
+from common import EPS, randn_matrix
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def _gschurtest(A, B, G, tol=20.0):
+    n = A.shape[0]
+    nA = max(np.linalg.norm(A), np.finfo(float).tiny)
+    S, T, Q, Z = G.S, G.T, G.Q, G.Z
+    assert np.all(np.tril(S, -1) == 0) and np.all(np.tril(T, -1) == 0)
+    assert np.linalg.norm(A - Q @ S @ Z.conj().T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(B - Q @ T @ Z.conj().T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Z @ Z.conj().T) / (n * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Q @ Q.conj().T) / (n * EPS) < tol
+    assert np.all(np.diag(T).imag == 0) and np.all(np.diag(T).real >= 0)
+    assert np.array_equal(G.alpha, np.diag(S)) and np.array_equal(G.beta, np.diag(T))
+
+
+def _match(w1, w2):
+    from scipy.optimize import linear_sum_assignment
+    fin1, fin2 = np.isfinite(w1), np.isfinite(w2)
+    assert fin1.sum() == fin2.sum()
+    a, b = w1[fin1], w2[fin2]
+    if len(a) == 0:
+        return 0.0
+    C = np.abs(a[:, None] - b[None, :]) / np.maximum(1.0, np.abs(b[None, :]))
+    r, c = linear_sum_assignment(C)
+    return float(np.max(C[r, c]))
+
+
+def _ratio(G):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(G.beta != 0, G.alpha / np.where(G.beta != 0, G.beta, 1), np.inf)
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 32, 100])
+@pytest.mark.parametrize("kind", ["complex", "real"])
+def test_ggschur_random(gs, n, kind):
+    rng = np.random.default_rng(8000 + n)
+    if kind == "complex":
+        A = rng.random((n, n)) + 1j * rng.random((n, n))
+        B = rng.random((n, n)) + 1j * rng.random((n, n))
+    else:
+        A, B = rng.random((n, n)), rng.random((n, n))
+    G = gs.ggschur(A, B)
+    _gschurtest(A, B, G)
+    S, T, al, be, Q, Z, st = po.ggschur(A, B)
+    assert st == 0
+    assert _match(_ratio(G), np.where(be != 0, al / np.where(be != 0, be, 1), np.inf)) < 1e-8
+    w = gs.eigvals(A, B)
+    assert _match(w, _ratio(G)) == 0.0
+
+
+def _challenging(rng, n=32):
+    n1 = n >> 2
+    n2 = n - 2 * n1
+    A0 = np.triu(rng.random((n, n)) - 0.5 + 1j * (rng.random((n, n)) - 0.5))
+    B0 = np.triu(rng.random((n, n)) - 0.5 + 1j * (rng.random((n, n)) - 0.5))
+    for j in range(n1):
+        A0[j, j] = 0
+    for j in range(n1, n2):
+        B0[j, j] = 0
+    Qa, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    Qb, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    return Qa @ A0 @ Qa.conj().T, Qb @ B0 @ Qb.conj().T
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ggschur_challenging(gs, seed):
+    """Singular pencils: zero diagonal entries of B take the reference's zero-chasing
+    branches (split off the top, chase to the bottom, clear H[ilast, ilast-1])."""
+    rng = np.random.default_rng(8100 + seed)
+    A, B = _challenging(rng)
+    G = gs.ggschur(A, B)
+    _gschurtest(A, B, G)
+    S, T, al, be, Q, Z, st = po.ggschur(A, B)
+    assert st == 0
+    nb = np.sum(np.abs(G.beta) <= 1e-10 * np.linalg.norm(B))
+    nbo = np.sum(np.abs(be) <= 1e-10 * np.linalg.norm(B))
+    assert nb == nbo
+
+
+def test_ggschur_batched_matches_single(gs):
+    rng = np.random.default_rng(8200)
+    ns = [1, 3, 17, 40, 8, 64]
+    As = [randn_matrix(rng, n, True) for n in ns]
+    Bs = [randn_matrix(rng, n, True) for n in ns]
+    out, st = gs.ggschur_batched(As, Bs)
+    assert np.all(st == 0)
+    for A, B, Gb in zip(As, Bs, out):
+        G = gs.ggschur(A, B)
+        np.testing.assert_array_equal(Gb.S, G.S)
+        np.testing.assert_array_equal(Gb.T, G.T)
+        np.testing.assert_array_equal(Gb.Q, G.Q)
+        np.testing.assert_array_equal(Gb.Z, G.Z)
+        _gschurtest(A, B, Gb)
+
+
+@pytest.mark.parametrize("s", [1e-300, 1e300])
+def test_ggschur_scaled(gs, s):
+    """_scale! of A and B (generalized.jl:35-44): tiny and huge pencils."""
+    rng = np.random.default_rng(8300)
+    A0, B0 = randn_matrix(rng, 20, True), randn_matrix(rng, 20, True)
+    G = gs.ggschur(s * A0, s * B0)
+    assert np.all(np.isfinite(G.S)) and np.all(np.isfinite(G.T))
+    G0 = gs.ggschur(A0, B0)
+    assert _match(_ratio(G), _ratio(G0)) < 1e-10
+    _gschurtest(A0, B0, gs.GeneralizedSchur(G.S / s, G.T / s, G.alpha / s, G.beta / s, G.Q, G.Z))
