@@ -295,6 +295,14 @@ size_t sylv_part_elems(int nT);  // partial right-hand sides of one level (doubl
 cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const int* bs, const int* bz,
                               const int* blk, const int* ts, const int* tbk, double* part, double floor,
                               cudaStream_t s);
+// FP64 product on the BF16 tensor cores by exact splitting (gemm_f64_tc.cu):
+// C (m x p, ldc) = op(A) (m x q) B (q x p), column-major; ws of gemm_tc_ws_bytes bytes.
+// The error word (gemm_tc_err_word; the caller zeroes it) becomes nonzero when a launch's
+// pipeline waits time out; launches with the same (m, p, q) and ws share it.
+size_t gemm_tc_ws_bytes(int m, int p, int q);
+cudaError_t launch_gemm_tc(int m, int p, int q, const double* A, int lda, int transA, const double* B, int ldb,
+                           double* C, int ldc, void* ws, cudaStream_t s);
+int* gemm_tc_err_word(int m, int p, int q, void* ws);
 cudaError_t launch_refine_elementwise(int op, int n, const double* a, double* b, double x, cudaStream_t s);
 cudaError_t launch_add_f32(double* Z, const float* P, size_t cnt, cudaStream_t s);
 cudaError_t launch_add_diff_f32(double* X, const float* P1, const float* P2, size_t cnt, cudaStream_t s);

@@ -1084,6 +1084,64 @@ int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double
 }
 
 // ---------------------------------------------------------------------------
+// FP64 product on the BF16 tensor cores (gemm_f64_tc.cu)
+// ---------------------------------------------------------------------------
+int gs_gemm_f64_tc(gs_context* ctx, int64_t m, int64_t p, int64_t q, const double* A, int64_t lda, int transA,
+                   const double* B, int64_t ldb, double* C, int64_t ldc, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (m < 0 || p < 0 || q < 0 || m > (1 << 20) || p > (1 << 20) || q > (1 << 20))
+    return set_err(ctx, GS_BADARG, "bad dimensions");
+  const int64_t ar_rows = transA ? q : m;
+  if (lda < std::max<int64_t>(ar_rows, 1) || ldb < std::max<int64_t>(q, 1) || ldc < std::max<int64_t>(m, 1))
+    return set_err(ctx, GS_BADARG, "leading dimension too small");
+  if (m == 0 || p == 0) return GS_OK;
+  if (!C || (q > 0 && (!A || !B))) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const int M = (int)m, P = (int)p, Q = (int)q;
+  const int arows = (int)ar_rows, acols = transA ? M : Q;
+  Arena ar;
+  const size_t o_A = ar.take<double>(dev ? 1 : (size_t)arows * acols), o_B = ar.take<double>(dev ? 1 : (size_t)Q * P);
+  const size_t o_C = ar.take<double>(dev ? 1 : (size_t)M * P), o_ws = ar.take<char>(gemm_tc_ws_bytes(M, P, Q));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const double* dA = A;
+  const double* dB = B;
+  double* dC = C;
+  int la = (int)lda, lb = (int)ldb, lc = (int)ldc;
+  if (!dev) {
+    double* hA = (double*)(base + o_A);
+    double* hB = (double*)(base + o_B);
+    if (Q > 0) {
+      CK(cudaMemcpy2DAsync(hA, arows * sizeof(double), A, lda * sizeof(double), arows * sizeof(double), acols,
+                           cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpy2DAsync(hB, Q * sizeof(double), B, ldb * sizeof(double), Q * sizeof(double), P,
+                           cudaMemcpyHostToDevice, s));
+    }
+    dA = hA; dB = hB; la = std::max(arows, 1); lb = std::max(Q, 1);
+    dC = (double*)(base + o_C); lc = M;
+  }
+  void* ws = base + o_ws;
+  CK(cudaMemsetAsync(gemm_tc_err_word(M, P, Q, ws), 0, sizeof(int), s));
+  CK(cudaEventRecord(ctx->t0, s));
+  cudaError_t e = launch_gemm_tc(M, P, Q, dA, la, transA ? 1 : 0, dB, lb, dC, lc, ws, s);
+  if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "gemm_tc: %s", cudaGetErrorString(e));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, gemm_tc_err_word(M, P, Q, ws), sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!dev)
+    CK(cudaMemcpy2DAsync(C, ldc * sizeof(double), dC, M * sizeof(double), M * sizeof(double), P,
+                         cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (herr) return set_err(ctx, GS_CUDA, "gemm_tc: pipeline wait timed out (code %d)", herr);
+  return GS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // mixed precision: FP32 Schur on the GPU + FP64 refinement of the Schur pair
 // ---------------------------------------------------------------------------
 int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, int64_t ldz, double* wr,
@@ -1108,6 +1166,7 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   const size_t o_part = ar.take<double>(sylv_part_elems((int)((n + 30) / 31) + 1));
   const size_t o_nrm = ar.take<double>(4), o_max = ar.take<unsigned long long>(2);
   const size_t o_ws = ar.take<char>(schur_large_ws_bytes(N32, sizeof(float)));
+  const size_t o_tc = ar.take<char>(gemm_tc_ws_bytes(N32, N32, N32));
   int rc = ensure_ws(ctx, ar.off);
   if (rc) return rc;
   char* base = ctx->dws;
@@ -1202,8 +1261,14 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
   CK(cudaMemcpyAsync(dts, ts.data(), sizeof(int) * (nT + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dtbk, tbk.data(), sizeof(int) * (nT + 1), cudaMemcpyHostToDevice, s));
   // ---- FP64 refinement
+  // FP64 products (Z^T A Z, Z^T Z) on the BF16 tensor cores by exact splitting: FP64
+  // accuracy at tensor-core speed (gemm_f64_tc.cu).  Their timeout word is read at every
+  // host synchronisation of the loop below.
+  void* tcws = base + o_tc;
+  int* tc_err = gemm_tc_err_word(N32, N32, N32, tcws);
+  CK(cudaMemsetAsync(tc_err, 0, sizeof(int), s));
   auto gemm = [&](int m, int p, int q, const double* Am, int la, int tA, const double* Bm, int lb, double* Cm, int lc) {
-    return launch_gemm<double>(m, p, q, Am, la, tA, Bm, lb, Cm, lc, s);
+    return launch_gemm_tc(m, p, q, Am, la, tA, Bm, lb, Cm, lc, tcws, s);
   };
   // Z <- Z + Z X for a small correction X (|X| <= ~1e-6): the product only needs first-order
   // accuracy, so it runs as an FP32 GEMM (Z and X rounded to FP32 into the FP32 stage's
@@ -1257,9 +1322,12 @@ int gs_schur_mixed_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, doubl
     if (e == cudaSuccess) e = cudaMemsetAsync(nrm, 0, 4 * sizeof(double), s);
     if (e == cudaSuccess) e = launch_lower_norm(N32, T1, dblk, nrm, ctx->num_sms, s);
     double hn[2] = {0.0, 0.0};
+    int htc = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(hn, nrm, sizeof(hn), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&htc, tc_err, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "refinement residual: %s", cudaGetErrorString(e));
+    if (htc) return set_err(ctx, GS_CUDA, "refinement: tensor-core product timed out (code %d)", htc);
     res = std::sqrt(hn[0]) / std::max(std::sqrt(hn[1]), 1e-300);
     if (!(res == res)) break;
     if (res <= tol) { conv = true; break; }

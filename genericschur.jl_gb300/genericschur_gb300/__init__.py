@@ -728,6 +728,28 @@ def hessenberg(A, ctx=None):
     return A, tau[:max(n - 1, 0)], Q
 
 
+def gemm_f64_tc(A, B, transA=False, ctx=None):
+    """FP64 product op(A) @ B on the BF16 tensor cores by exact splitting (the product the
+    mixed-precision refinement uses for Z^T A Z and Z^T Z).  No counterpart in the
+    reference; accuracy at least that of an FP64 GEMM relative to the row maxima of op(A)
+    and column maxima of B."""
+    ctx = ctx or get_context()
+    A = np.asfortranarray(A, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    if A.ndim != 2 or B.ndim != 2:
+        raise DimensionMismatch("gemm_f64_tc: matrices expected")
+    m, q = (A.shape[1], A.shape[0]) if transA else A.shape
+    if B.shape[0] != q:
+        raise DimensionMismatch("gemm_f64_tc: inner dimensions %d and %d" % (q, B.shape[0]))
+    p = B.shape[1]
+    C = np.zeros((m, p), order="F")
+    rc = ctx.lib.gs_gemm_f64_tc(ctx.handle, m, p, q, _ptr(A), max(A.shape[0], 1), 1 if transA else 0, _ptr(B),
+                                max(q, 1), _ptr(C), max(m, 1), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "gemm_f64_tc")
+    return C
+
+
 def gschur_mixed(A, scale=True, maxiter=None, ctx=None, return_info=False, fallback=True):
     """Real Schur decomposition computed in FP32 on the GPU and refined to FP64
     accuracy (Newton refinement of the Schur pair).  Same outputs as gschur.

@@ -298,6 +298,18 @@ GS_API int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t*
                                   int64_t packed_len, double* A, double* B, double* Q, double* Z, const int64_t* woffs,
                                   int64_t wlen, double* alpha, double* beta, int32_t* status, unsigned flags);
 
+/* FP64 matrix product C (m x p, ldc) = op(A) (m x q) * B (q x p), op(A) = A (transA = 0)
+ * or A^T (transA = 1), column-major, computed on the BF16 tensor cores by exact splitting
+ * (Ozaki scheme: 10 slices of 6 bits per row of op(A) and column of B, exact FP32
+ * accumulation of each slice product, FP64 sum of the 55 leading slice products).  The
+ * error is below that of an FP64 dot product of the same length, measured against the
+ * row maxima of op(A) and column maxima of B; Inf/NaN in a row of op(A) (column of B)
+ * make that row (column) of C NaN.  No counterpart in the reference: the mixed-precision
+ * refinement (gs_schur_mixed_f64) forms Z^T A Z and Z^T Z with it.  Synchronous; host
+ * pointers, or device pointers with GS_DEVICE. */
+GS_API int gs_gemm_f64_tc(gs_context* ctx, int64_t m, int64_t p, int64_t q, const double* A, int64_t lda,
+                          int transA, const double* B, int64_t ldb, double* C, int64_t ldc, unsigned flags);
+
 /* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
  * eigenvalues with select[k] != 0 move to the leading positions in their order.
  * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if
