@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--large-only", action="store_true",
                     help="only the large-matrix measurement (for profiling runs); prints its JSON object")
     ap.add_argument("--large-mode", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--gemm-only", action="store_true",
+                    help="only the FP64 product on the BF16 tensor cores vs cuBLAS DGEMM; prints its JSON object")
+    ap.add_argument("--gemm-n", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -300,9 +303,11 @@ def run_ours(args):
     per_matrix = measure_per_matrix(ctx, packed, ns, offs)
     secondary = measure_complex_and_adjoint(ctx, torch, dev, stream)
     large = None
+    gemm_tc = None
     if not args.no_large:
         ctx.set_stream(None)
         large = measure_large(ctx, torch, dev, args.large_n)
+        gemm_tc = measure_gemm_tc(ctx, torch, dev, args.large_n)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -311,7 +316,7 @@ def run_ours(args):
                             "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
            "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
-           "large": large, **secondary}
+           "large": large, "gemm_f64_tc": gemm_tc, **secondary}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -491,6 +496,64 @@ def measure_e2e(ctx, packed, ns, offs, woffs, steps):
             ctx.host_free(p)
 
 
+def measure_gemm_tc(ctx, torch, dev, n, reps=5):
+    """The refinement's FP64 product on the BF16 tensor cores (gs_gemm_f64_tc, exact
+    splitting) against cuBLAS DGEMM on the FP64 pipe: C = A^T B, n x n x n, device
+    buffers, CUDA events around the library's launches (split + product).  Tensor work
+    per launch: 55 slice products x 2 n^3 BF16 FLOP."""
+    from genericschur_gb300 import _capi
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    A = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    B = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    C = torch.empty(n, n, dtype=torch.float64, device=dev)
+    ctx.set_stream(None)
+    ms = []
+    for i in range(3 + reps):
+        rc = ctx.lib.gs_gemm_f64_tc(ctx.handle, n, n, n, A.data_ptr(), n, 1, B.data_ptr(), n, C.data_ptr(), n,
+                                    _capi.GS_DEVICE)
+        if rc != 0:
+            raise RuntimeError(ctx.last_error())
+        if i >= 3:
+            ms.append(ctx.last_kernel_ms())
+    tc_ms = float(np.median(ms))
+    # column-major C = A_cm^T B_cm is, in torch's row-major view, C^T = A B^T
+    ref = A @ B.T
+    err = float((C.T - ref).norm() / ref.norm())
+    torch.cuda.synchronize()
+    dg = []
+    for i in range(3 + reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(A, B)
+        e1.record()
+        e1.synchronize()
+        if i >= 3:
+            dg.append(e0.elapsed_time(e1))
+    dgemm_ms = float(np.median(dg))
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+    except (OSError, KeyError, ValueError):
+        peak = None
+    tensor_tflops = 55 * 2.0 * n ** 3 / (tc_ms * 1e-3) / 1e12
+    return {"n": n, "tc_ms": tc_ms, "dgemm_ms": dgemm_ms, "speedup_vs_dgemm": dgemm_ms / tc_ms,
+            "fp64_equiv_tflops": 2.0 * n ** 3 / (tc_ms * 1e-3) / 1e12, "bf16_tensor_tflops": tensor_tflops,
+            "bf16_peak_tflops": peak, "frac_of_bf16_peak": (tensor_tflops / peak) if peak else None,
+            "rel_err_vs_dgemm": err}
+
+
+def run_gemm_only(args):
+    import torch
+    import build_lib
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    build_lib.build()
+    import genericschur_gb300 as gs
+    ctx = gs.Context(0)
+    print(json.dumps(measure_gemm_tc(ctx, torch, dev, args.gemm_n)))
+
+
 def run_large_only(args):
     import torch
     import build_lib
@@ -506,6 +569,9 @@ def main():
     args = parse()
     if args.large_only:
         run_large_only(args)
+        return
+    if args.gemm_only:
+        run_gemm_only(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -214,6 +214,16 @@ cudaError_t launch_gemm(int m, int p, int q, const T* A, int lda, int transA, co
                         cudaStream_t s);
 size_t hess_large_ws_elems(int n);
 template <class T> cudaError_t hessenberg_large(int n, T* A, int lda, T* Z, int ldz, T* tau_out, T* ws, cudaStream_t s);
+// Blocked (compact-WY panel) Hessenberg reduction (hessenberg_blocked.cu): the same
+// outputs as hessenberg_large; ws of hess_blocked_ws_elems(n) elements; *err_host (when
+// not null; the call then synchronises) is nonzero if a grid barrier timed out.
+size_t hess_blocked_ws_elems(int n);
+template <class T>
+cudaError_t hessenberg_blocked(int n, T* A, int lda, T* Z, int ldz, T* tau_out, T* ws, int num_sms, int* err_host,
+                               cudaStream_t s);
+// Orders from which the blocked reduction is used for element size tsize
+// (GS_HESS_BLOCKED_MIN overrides; default 256 for FP32, unused for FP64).
+int hess_blocked_min(size_t tsize);
 
 // Aggressive early deflation on the trailing window of the active block (aed.cu).
 template <class T>

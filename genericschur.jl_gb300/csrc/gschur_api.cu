@@ -1062,7 +1062,7 @@ int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double
   const size_t nn = (size_t)n * n;
   Arena ar;
   const size_t o_A = ar.take<double>(nn), o_Q = ar.take<double>(Q ? nn : 1), o_tau = ar.take<double>(n);
-  const size_t o_ws = ar.take<double>(hess_large_ws_elems((int)n));
+  const size_t o_ws = ar.take<double>(std::max(hess_large_ws_elems((int)n), hess_blocked_ws_elems((int)n)));
   int rc = ensure_ws(ctx, ar.off);
   if (rc) return rc;
   char* base = ctx->dws;
@@ -1074,8 +1074,16 @@ int gs_hessenberg_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, double
   double* dtau = (double*)(base + o_tau);
   CK(cudaMemsetAsync(dtau, 0, n * sizeof(double), s));
   CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, in, s));
-  cudaError_t e = hessenberg_large<double>((int)n, dA, (int)n, dQ, (int)n, dtau, (double*)(base + o_ws), s);
+  int herr = 0;
+  CK(cudaEventRecord(ctx->t0, s));
+  cudaError_t e = (n >= hess_blocked_min(sizeof(double)))
+                      ? hessenberg_blocked<double>((int)n, dA, (int)n, dQ, (int)n, dtau, (double*)(base + o_ws),
+                                                   ctx->num_sms, &herr, s)
+                      : hessenberg_large<double>((int)n, dA, (int)n, dQ, (int)n, dtau, (double*)(base + o_ws), s);
   if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "hessenberg: %s", cudaGetErrorString(e));
+  if (herr) return set_err(ctx, GS_CUDA, "hessenberg: grid barrier timed out");
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
   CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n, out, s));
   if (Q) CK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), dQ, n * sizeof(double), n * sizeof(double), n, out, s));
   if (n > 1) CK(cudaMemcpyAsync(tau, dtau, (n - 1) * sizeof(double), out, s));

@@ -102,7 +102,7 @@ cudaError_t launch_absmax(const double* A, size_t cnt, unsigned long long* out, 
 size_t schur_large_ws_bytes(int n, size_t tsize) {
   const size_t nb = kSmallMax;
   size_t b = 0;
-  b += tsize * hess_large_ws_elems(n) + 256;
+  b += tsize * std::max(hess_large_ws_elems(n), hess_blocked_ws_elems(n)) + 256;
   b += sizeof(int) * 64 * kMaxBulges + tsize * 64 * kMaxBulges * 5 + 512;  // chase log
   b += tsize * 4 * kMaxBulges + 256;                                        // shifts
   b += 3 * sizeof(double) * nb * nb + 4 * sizeof(double) * nb + 1024;       // small solve blk, U, wr, wi, meta
@@ -128,7 +128,7 @@ int schur_large_run(LargeRun<T>& r) {
   // ---- carve the workspace
   char* p = (char*)r.ws;
   auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~size_t(255); return (void*)q; };
-  T* hws = (T*)take(sizeof(T) * hess_large_ws_elems(n));
+  T* hws = (T*)take(sizeof(T) * std::max(hess_large_ws_elems(n), hess_blocked_ws_elems(n)));
   int* logk = (int*)take(sizeof(int) * 64 * kMaxBulges);
   T* logr = (T*)take(sizeof(T) * 64 * kMaxBulges * 5);
   T* dshift = (T*)take(sizeof(T) * 4 * kMaxBulges);
@@ -178,7 +178,16 @@ int schur_large_run(LargeRun<T>& r) {
   }
 
   // ---- 2. Hessenberg (+ Z)
-  CKL(hessenberg_large<T>(n, H, n, Z, n, nullptr, hws, s));
+  if (n >= hess_blocked_min(sizeof(T))) {
+    int herr = 0;
+    CKL(hessenberg_blocked<T>(n, H, n, Z, n, nullptr, hws, r.num_sms, &herr, s));
+    if (herr) {
+      r.cuda_error = cudaErrorLaunchTimeout;
+      return -1;
+    }
+  } else {
+    CKL(hessenberg_large<T>(n, H, n, Z, n, nullptr, hws, s));
+  }
   k_triu1<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(H, n);
   CKL(cudaGetLastError());
 

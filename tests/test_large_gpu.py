@@ -11,8 +11,20 @@ from oracle import pyoracle as po
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n", [3, 40, 150, 300])
-def test_hessenberg(gs, n):
+@pytest.fixture(params=["unblocked", "blocked"])
+def hess_variant(request, monkeypatch):
+    """Both FP64 Hessenberg reductions: the fused unblocked one (default for FP64) and
+    the compact-WY blocked one (default for FP32, selected for FP64 from order 256 on by
+    GS_HESS_BLOCKED_MIN, which the library reads at every call)."""
+    if request.param == "blocked":
+        monkeypatch.setenv("GS_HESS_BLOCKED_MIN", "256")
+    else:
+        monkeypatch.delenv("GS_HESS_BLOCKED_MIN", raising=False)
+    return request.param
+
+
+@pytest.mark.parametrize("n", [3, 40, 150, 257, 300, 515, 1030])
+def test_hessenberg(gs, n, hess_variant):
     rng = np.random.default_rng(9000 + n)
     A = rng.standard_normal((n, n))
     Hp, tau, Q = gs.hessenberg(A)
@@ -24,8 +36,25 @@ def test_hessenberg(gs, n):
     assert np.max(np.abs(tau - tauo)) < 1e-10
 
 
+@pytest.mark.parametrize("scale", [1e-300, 1e-155, 1e155, 1e300])
+def test_hessenberg_extreme_scale(gs, scale, hess_variant):
+    """Columns whose norms leave the range where squares are representable: the blocked
+    reduction's one-pass (scale, sum of squares) norms and the reflector's rescaling loop
+    (householder.jl:12-54) keep the reflectors equal to the oracle's."""
+    rng = np.random.default_rng(9050)
+    n = 300
+    A0 = rng.standard_normal((n, n))
+    A = A0 * scale
+    Hp, tau, Q = gs.hessenberg(A)
+    H = np.triu(Hp, -1)
+    assert np.all(np.isfinite(Hp)) and np.all(np.isfinite(Q))
+    assert np.linalg.norm(A0 - Q @ (H / scale) @ Q.T) / (n * np.linalg.norm(A0) * EPS) < 10
+    Ho, tauo, Qo = po.hessenberg(A)
+    assert np.max(np.abs(tau - tauo)) < 1e-10
+
+
 @pytest.mark.parametrize("n", [129, 160, 256, 400])
-def test_large_schur_random(gs, n):
+def test_large_schur_random(gs, n, hess_variant):
     rng = np.random.default_rng(9100 + n)
     A = randn_matrix(rng, n)
     S = gs.gschur(A)
