@@ -125,8 +125,30 @@ __global__ void k_exps(int R, const unsigned long long* __restrict__ amax, int* 
   ex[r] = e;
 }
 
+// |x| 2^(60 - e) truncated to an integer (|x| < 2^e, so below 2^60), from the IEEE bits:
+// the 53-bit significand shifted by its exponent.  The 6-bit groups of this integer are
+// exactly the successive truncations trunc(y 64^s) mod 64 of y = |x| 2^-e.
+__device__ __forceinline__ unsigned long long fixed60(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  const int be = (int)(b >> 52);
+  if (be == 0 && (b & 0xfffffffffffffull) == 0) return 0ull;
+  const unsigned long long m = (b & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull);
+  const int ex = be ? be - 1075 : -1074;  // x = m 2^ex
+  const int sh = ex + 60 - e;             // <= 7
+  if (sh >= 0) return m << sh;
+  return sh <= -64 ? 0ull : (m >> (-sh));
+}
+
+// BF16 bits of the integer q (|q| < 64) with the given sign.
+__device__ __forceinline__ unsigned short bf16_int(unsigned q, unsigned neg) {
+  if (q == 0u) return 0;
+  const int p = 31 - __clz(q);
+  return (unsigned short)((neg << 15) | ((unsigned)(127 + p) << 7) | ((q << (7 - p)) & 0x7fu));
+}
+
 // Slices of rows [128 rb, 128 rb + 128) x k [64 kb, 64 kb + 64): one CTA per tile, each
 // thread one (row, 8-k group) item at a time -> one 16-byte core-matrix row per slice.
+// Integer arithmetic only (the FP64 pipe is the scarce resource on this part).
 template <int TR>
 __global__ void __launch_bounds__(256) k_split(int R, int K, const double* __restrict__ X, int ld,
                                                const int* __restrict__ ex, int Rt, int Kt,
@@ -137,7 +159,8 @@ __global__ void __launch_bounds__(256) k_split(int R, int K, const double* __res
   for (int it = threadIdx.x; it < kTcBM * (kTcBK / 8); it += 256) {
     const int rl = it % kTcBM, kg = it / kTcBM;
     const int r = rb * kTcBM + rl, kbase = kb * kTcBK + kg * 8;
-    double y[8];
+    unsigned long long f[8];
+    unsigned neg[8];
     int e = kExpZero;
     if (r < R) e = ex[r];
     const bool live = (e != kExpZero && e != kExpBad);
@@ -146,20 +169,21 @@ __global__ void __launch_bounds__(256) k_split(int R, int K, const double* __res
       const int k = kbase + x;
       double v = 0.0;
       if (live && k < K) v = TR ? X[(size_t)r * ld + k] : X[(size_t)k * ld + r];
-      y[x] = live ? ldexp(v, -e) : 0.0;  // |y| < 1, exact
+      f[x] = live ? fixed60(v, e) : 0ull;
+      neg[x] = (unsigned)(((unsigned long long)__double_as_longlong(v)) >> 63);
     }
     const size_t off = (size_t)((rl >> 3) * 8 + kg) * 64 + (rl & 7) * 8;
 #pragma unroll 1
     for (int s = 0; s < kTcSlices; ++s) {
-      __align__(16) __nv_bfloat16 q[8];
+      const int sh = 60 - kTcBeta * (s + 1);
+      unsigned w[4];
 #pragma unroll
-      for (int x = 0; x < 8; ++x) {
-        const double t = y[x] * (double)(1 << kTcBeta);  // exact
-        const double qi = trunc(t);                       // |qi| <= 2^beta - 1
-        y[x] = t - qi;                                    // exact remainder
-        q[x] = __float2bfloat16_rn((float)qi);            // exact (|qi| < 256)
+      for (int x = 0; x < 4; ++x) {
+        const unsigned lo = bf16_int((unsigned)(f[2 * x] >> sh) & 63u, neg[2 * x]);
+        const unsigned hi = bf16_int((unsigned)(f[2 * x + 1] >> sh) & 63u, neg[2 * x + 1]);
+        w[x] = lo | (hi << 16);
       }
-      *reinterpret_cast<uint4*>(tile + s * slice_stride + off) = *reinterpret_cast<const uint4*>(q);
+      *reinterpret_cast<uint4*>(tile + s * slice_stride + off) = make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
 }
