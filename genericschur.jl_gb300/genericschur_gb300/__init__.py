@@ -32,7 +32,7 @@ __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "Argum
            "eig_adjoint_batched", "hessenberg", "gschur_mixed", "balance", "balance_", "Balancer", "balancer_lmul",
            "balancer_ldiv", "enormalize", "gordschur", "ordschur", "rconde", "EigenFull", "eigvalscond",
            "subspacesep", "eigen_rcond", "Hermitian", "SymTridiagonal", "HermitianHessenberg", "geigen",
-           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "GeneralizedSchur", "ggschur", "ggschur_batched",
+           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "GeneralizedSchur", "ggschur", "ggschur_batched", "ggeigvecs",
            "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
@@ -291,10 +291,33 @@ def _fc(a, dt):
     return np.array(a, dtype=dt, order="F", copy=True)
 
 
+def ggeigvecs(G, left=False, ctx=None):
+    """geigvecs(S::GeneralizedSchur; left) (vectors.jl:22-33) for a complex pencil: right
+    eigenvectors v_k with beta_k A v_k = alpha_k B v_k (back-transformed by G.Z), or left
+    eigenvectors (back-transformed by G.Q); columns scaled to max |re|+|im| = 1."""
+    ctx = ctx or get_context()
+    S = _fc(G.S, np.complex128)
+    T = _fc(G.T, np.complex128)
+    n = _checksquare(S)
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    if n == 0:
+        return V
+    M = G.Q if left else G.Z
+    M = _fc(M, np.complex128) if M is not None else None
+    Q, Z = (M, None) if left else (None, M)
+    outR, outL = (None, V) if left else (V, None)
+    rc = ctx.lib.gs_ggeigvecs_c64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(outR), _ptr(outL), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "geigvecs(GeneralizedSchur)")
+    return V
+
+
 def geigvecs(S, left=False, normalize=True, ctx=None):
     """Eigenvectors from a Schur decomposition (vectors.jl:12-20): right, or left
     with left=True; columns ordered like S.values, unit 2-norm with the
-    largest-modulus entry real."""
+    largest-modulus entry real.  A GeneralizedSchur goes to ggeigvecs (vectors.jl:22-33)."""
+    if isinstance(S, GeneralizedSchur):
+        return ggeigvecs(S, left=left, ctx=ctx)
     ctx = ctx or get_context()
     T = np.asarray(S.T)
     n = _checksquare(T)

@@ -310,6 +310,18 @@ GS_API int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t*
 GS_API int gs_gemm_f64_tc(gs_context* ctx, int64_t m, int64_t p, int64_t q, const double* A, int64_t lda,
                           int transA, const double* B, int64_t ldb, double* C, int64_t ldc, unsigned flags);
 
+/* Eigenvectors of the generalized Schur decomposition of a complex pencil (the output
+ * of gs_ggschur_c64: S, T upper triangular, A = Q S Z^H, B = Q T Z^H).  Replaces
+ * geigvecs(S::GeneralizedSchur; left) (vectors.jl:22-33): right eigenvectors
+ * (_geigvecs, vectors.jl:723-842) into VR, back-transformed by Z, with
+ * beta_k A v = alpha_k B v; left eigenvectors (_gleigvecs, vectors.jl:845-1038) into VL,
+ * back-transformed by Q, with conj(beta_k) A^H y = conj(alpha_k) B^H y.  Either output
+ * may be NULL; Q / Z NULL give the eigenvectors of the triangular pair.  Columns scaled
+ * to max |re| + |im| = 1; a singular pencil (S_kk = T_kk = 0) gives the unit vector e_k.
+ * Interleaved complex, leading dimension n; host pointers, or device with GS_DEVICE. */
+GS_API int gs_ggeigvecs_c64(gs_context* ctx, int64_t n, const double* S, const double* T, const double* Q,
+                            const double* Z, double* VR, double* VL, unsigned flags);
+
 /* Reordering a Schur decomposition.  Replaces gordschur!(T, Z, select) / ordschur!:
  * eigenvalues with select[k] != 0 move to the leading positions in their order.
  * Real (rordschur.jl:3-47, standard-form 2x2 blocks kept; a block is selected if

@@ -4,6 +4,7 @@ Compiles oracle_capi.cpp into oracle/_build/liboracle.so with g++.  FP contracti
 is disabled so that the restated algorithms round like the reference's Julia code
 (which does not fuse multiply-adds unless asked to).
 """
+import glob
 import os
 import platform
 import subprocess
@@ -12,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = ["oracle_capi.cpp"]
-HEADERS = ["scalar.hpp", "gschur_oracle.hpp", "eigvecs_oracle.hpp"]
+HEADERS = sorted(os.path.basename(h) for h in glob.glob(os.path.join(HERE, "*.hpp")))
 
 
 def _stale():

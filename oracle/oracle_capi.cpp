@@ -243,6 +243,16 @@ int or_ggschur_z(int n, double* a, double* b, double* q, double* z, double* alph
   return ggschur_cplx<double>(n, (zc*)a, n, (zc*)b, n, (zc*)q, (zc*)z, (zc*)alpha, (zc*)beta, scale != 0, 100LL * n);
 }
 
+// Eigenvectors of a complex generalized Schur pair (src/vectors.jl:723-1038): right (left
+// = 0, back-transformed by X = Z) or left (left = 1, X = Q); X may be null.  V n x n.
+int or_ggevc_z(int n, const double* s, const double* p, const double* x, double* v, int left) {
+  if (left)
+    ggevc_left<double>(n, (const zc*)s, (const zc*)p, (const zc*)x, (zc*)v);
+  else
+    ggevc_right<double>(n, (const zc*)s, (const zc*)p, (const zc*)x, (zc*)v);
+  return 0;
+}
+
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {
   gs2x2<double>(h, cs, sn, &w[0], &w[1], &w[2], &w[3]);
   return 0;

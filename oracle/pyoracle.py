@@ -52,6 +52,7 @@ def lib():
             "or_hetrd_z": [_i, _p, _i, _i, _p, _p, _p],
             "or_steqr_d": [_i, _p, _p, _p, _i],
             "or_ggschur_z": [_i, _p, _p, _p, _p, _p, _p, _i],
+            "or_ggevc_z": [_i, _p, _p, _p, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -320,3 +321,15 @@ def ggschur(A, B, scale=True):
     be = np.zeros(max(n, 1), dtype=np.complex128)
     st = lib().or_ggschur_z(n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(al), _ptr(be), int(scale))
     return S, T, al[:n], be[:n], Q, Z, st
+
+
+def ggeigvecs(S, T, X=None, left=False):
+    """Eigenvectors of a complex generalized Schur pair (vectors.jl:723-1038): right
+    (back-transformed by X = Z) or left (X = Q); columns scaled to max |re|+|im| = 1."""
+    Sf = _f(S, np.complex128)
+    Tf = _f(T, np.complex128)
+    n = Sf.shape[0]
+    Xf = _f(X, np.complex128) if X is not None else None
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    lib().or_ggevc_z(n, _ptr(Sf), _ptr(Tf), _ptr(Xf), _ptr(V), int(left))
+    return V

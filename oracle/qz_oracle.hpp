@@ -420,4 +420,226 @@ int ggschur_cplx(int n, cx<R>* a, int lda, cx<R>* b, int ldb, cx<R>* q, cx<R>* z
 #undef B_
 }
 
+
+// ---------------------------------------------------------------------------
+// Eigenvectors of a complex generalized Schur pair (S, P upper triangular):
+//   right  _geigvecs(S, P[, Z])   src/vectors.jl:723-842
+//   left   _gleigvecs(S, P[, Q])  src/vectors.jl:845-1038
+// Column idx of V is the eigenvector of (S[idx,idx], P[idx,idx]), back-transformed by
+// X (Z for right, Q for left) when X is non-null, scaled so that max |re|+|im| = 1.
+// Column-major, leading dimension n.  Same operation order as the reference.
+// ---------------------------------------------------------------------------
+template <class R>
+R gg_safemin() {
+  // safemin(T) (util.jl:5-12): floatmin unless 1/floatmax is larger
+  R sfmin = std::numeric_limits<R>::min();
+  R small = R(1) / std::numeric_limits<R>::max();
+  if (small >= sfmin) sfmin = small * (R(1) + std::numeric_limits<R>::epsilon());
+  return sfmin;
+}
+
+template <class R>
+void gg_norms(int n, const cx<R>* S, const cx<R>* P, std::vector<R>& sn, std::vector<R>& pn, R* anorm, R* bnorm) {
+  sn.assign(n, R(0));
+  pn.assign(n, R(0));
+  R an = abs1(S[0]), bn = abs1(P[0]);
+  for (int j = 2; j <= n; ++j) {
+    for (int i = 1; i <= j - 1; ++i) {
+      sn[j - 1] += abs1(S[(i - 1) + (size_t)(j - 1) * n]);
+      pn[j - 1] += abs1(P[(i - 1) + (size_t)(j - 1) * n]);
+    }
+    an = m_max(an, sn[j - 1] + abs1(S[(j - 1) + (size_t)(j - 1) * n]));
+    bn = m_max(bn, pn[j - 1] + abs1(P[(j - 1) + (size_t)(j - 1) * n]));
+  }
+  *anorm = an;
+  *bnorm = bn;
+}
+
+// coefficients a (real), b (complex) of (a S - b P) for diagonal entry k (1-based),
+// vectors.jl:775-812 / 930-967; returns false for the singular pencil case
+template <class R>
+bool gg_coeffs(int n, const cx<R>* S, const cx<R>* P, int k, R anorm, R bnorm, R ascale, R bscale, R* acoeff,
+               cx<R>* bcoeff) {
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = gg_safemin<R>();
+  const R smallnum = safmin * (R(n) / ulp);
+  const R bigx = R(1) / smallnum;
+  const cx<R> skk = S[(k - 1) + (size_t)(k - 1) * n];
+  const R pkk = P[(k - 1) + (size_t)(k - 1) * n].re;
+  if (abs1(skk) <= safmin && m_abs(pkk) <= safmin) return false;
+  const R t = R(1) / m_max(m_max(abs1(skk) * ascale, m_abs(pkk) * bscale), safmin);
+  const cx<R> salpha = (t * skk) * ascale;
+  const R sbeta = (t * pkk) * bscale;
+  R ac = sbeta * ascale;
+  cx<R> bc = salpha * bscale;
+  const bool lsa = m_abs(sbeta) >= safmin && m_abs(ac) < smallnum;
+  const bool lsb = abs1(salpha) >= safmin && abs1(bc) < smallnum;
+  R s = R(1);
+  if (lsa) s = (smallnum / m_abs(sbeta)) * m_min(anorm, bigx);
+  if (lsb) s = m_max(s, (smallnum / abs1(salpha)) * m_min(bnorm, bigx));
+  if (lsa || lsb) {
+    s = m_min(s, R(1) / (safmin * m_max(m_max(R(1), m_abs(ac)), abs1(bc))));
+    if (lsa) ac = ascale * (s * sbeta);
+    else ac = ac * s;
+    if (lsb) bc = bscale * (s * salpha);
+    else bc = bc * s;
+  }
+  *acoeff = ac;
+  *bcoeff = bc;
+  return true;
+}
+
+template <class R>
+void ggevc_right(int n, const cx<R>* S, const cx<R>* P, const cx<R>* Z, cx<R>* V) {
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = gg_safemin<R>();
+  const R bignum = R(1) / (R(n) * safmin);
+  std::vector<R> sn, pn;
+  R anorm, bnorm;
+  gg_norms(n, S, P, sn, pn, &anorm, &bnorm);
+  const R ascale = R(1) / m_max(anorm, safmin), bscale = R(1) / m_max(bnorm, safmin);
+  std::vector<cx<R>> v(n), v2(n);
+#define SS(i, j) S[((i) - 1) + (size_t)((j) - 1) * n]
+#define PP(i, j) P[((i) - 1) + (size_t)((j) - 1) * n]
+  for (int ki = n; ki >= 1; --ki) {
+    const int idx = ki;
+    cx<R>* col = V + (size_t)(idx - 1) * n;
+    R acoeff;
+    cx<R> bcoeff;
+    if (!gg_coeffs(n, S, P, ki, anorm, bnorm, ascale, bscale, &acoeff, &bcoeff)) {
+      for (int r = 0; r < n; ++r) col[r] = cx<R>(R(0));
+      col[idx - 1] = cx<R>(R(1));
+      continue;
+    }
+    const R aca = m_abs(acoeff), acb = abs1(bcoeff);
+    for (int r = 0; r < n; ++r) v[r] = cx<R>(R(0));
+    const R dmin = m_max(m_max(ulp * aca * anorm, ulp * acb * bnorm), safmin);
+    for (int i = 1; i <= ki - 1; ++i) v[i - 1] = acoeff * SS(i, ki) - bcoeff * PP(i, ki);
+    v[ki - 1] = cx<R>(R(1));
+    for (int j = ki - 1; j >= 1; --j) {
+      cx<R> d = acoeff * SS(j, j) - bcoeff * PP(j, j);
+      if (abs1(d) <= dmin) d = cx<R>(dmin);
+      if (abs1(d) < R(1)) {
+        if (abs1(v[j - 1]) >= bignum * abs1(d)) {
+          const R t = R(1) / abs1(v[j - 1]);
+          for (int r = 0; r < ki; ++r) v[r] = v[r] * t;
+        }
+      }
+      v[j - 1] = -v[j - 1] / d;
+      if (j > 1) {
+        if (abs1(v[j - 1]) > R(1)) {
+          const R t = R(1) / abs1(v[j - 1]);
+          if (aca * sn[j - 1] + acb * pn[j - 1] >= bignum * t)
+            for (int r = 0; r < ki; ++r) v[r] = v[r] * t;
+        }
+        const cx<R> ca = acoeff * v[j - 1];
+        const cx<R> cb = bcoeff * v[j - 1];
+        for (int i = 1; i <= j - 1; ++i) v[i - 1] = v[i - 1] + (ca * SS(i, j) - cb * PP(i, j));
+      }
+    }
+    int iend;
+    const cx<R>* src = v.data();
+    if (Z) {
+      for (int r = 0; r < n; ++r) {
+        cx<R> s(R(0));
+        for (int k = 0; k < n; ++k) s += Z[r + (size_t)k * n] * v[k];
+        v2[r] = s;
+      }
+      src = v2.data();
+      iend = n;
+    } else {
+      iend = ki;
+    }
+    R xmax = R(0);
+    for (int jr = 1; jr <= iend; ++jr) xmax = m_max(xmax, abs1(src[jr - 1]));
+    if (xmax > safmin) {
+      const R t = R(1) / xmax;
+      for (int jr = 1; jr <= iend; ++jr) col[jr - 1] = t * src[jr - 1];
+    } else {
+      iend = 0;
+    }
+    for (int jr = iend + 1; jr <= n; ++jr) col[jr - 1] = cx<R>(R(0));
+  }
+#undef SS
+#undef PP
+}
+
+template <class R>
+void ggevc_left(int n, const cx<R>* S, const cx<R>* P, const cx<R>* Q, cx<R>* V) {
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = gg_safemin<R>();
+  const R bignum = R(1) / (R(n) * safmin);
+  std::vector<R> sn, pn;
+  R anorm, bnorm;
+  gg_norms(n, S, P, sn, pn, &anorm, &bnorm);
+  const R ascale = R(1) / m_max(anorm, safmin), bscale = R(1) / m_max(bnorm, safmin);
+  std::vector<cx<R>> v(n), v2(n);
+#define SS(i, j) S[((i) - 1) + (size_t)((j) - 1) * n]
+#define PP(i, j) P[((i) - 1) + (size_t)((j) - 1) * n]
+  for (int je = 1; je <= n; ++je) {
+    const int idx = je;
+    cx<R>* col = V + (size_t)(idx - 1) * n;
+    R acoeff;
+    cx<R> bcoeff;
+    if (!gg_coeffs(n, S, P, je, anorm, bnorm, ascale, bscale, &acoeff, &bcoeff)) {
+      for (int r = 0; r < n; ++r) col[r] = cx<R>(R(0));
+      col[idx - 1] = cx<R>(R(1));
+      continue;
+    }
+    const R aca = m_abs(acoeff), acb = abs1(bcoeff);
+    R xmax = R(1);
+    for (int r = 0; r < n; ++r) v[r] = cx<R>(R(0));
+    const R dmin = m_max(m_max(ulp * aca * anorm, ulp * acb * bnorm), safmin);
+    v[je - 1] = cx<R>(R(1));
+    for (int j = je + 1; j <= n; ++j) {
+      R t = R(1) / xmax;
+      if (aca * sn[j - 1] + acb * pn[j - 1] > bignum * t) {
+        for (int r = je; r <= j - 1; ++r) v[r - 1] = v[r - 1] * t;
+        xmax = R(1);
+      }
+      cx<R> suma(R(0)), sumb(R(0));
+      for (int jr = je; jr <= j - 1; ++jr) {
+        suma += conj(SS(jr, j)) * v[jr - 1];
+        sumb += conj(PP(jr, j)) * v[jr - 1];
+      }
+      cx<R> sumx = acoeff * suma - conj(bcoeff) * sumb;
+      cx<R> d = conj(acoeff * SS(j, j) - bcoeff * PP(j, j));
+      if (abs1(d) <= dmin) d = cx<R>(dmin);
+      if (abs1(d) < R(1)) {
+        if (abs1(sumx) >= bignum * abs1(d)) {
+          t = R(1) / abs1(sumx);
+          for (int r = je; r <= j - 1; ++r) v[r - 1] = v[r - 1] * t;
+          xmax *= t;
+          sumx = sumx * t;
+        }
+      }
+      v[j - 1] = -sumx / d;
+      xmax = m_max(xmax, abs1(v[j - 1]));
+    }
+    int ibegin;
+    const cx<R>* src = v.data();
+    if (Q) {
+      for (int r = 0; r < n; ++r) {
+        cx<R> s(R(0));
+        for (int k = 0; k < n; ++k) s += Q[r + (size_t)k * n] * v[k];
+        v2[r] = s;
+      }
+      src = v2.data();
+      ibegin = 1;
+    } else {
+      ibegin = je;
+    }
+    xmax = R(0);
+    for (int jr = ibegin; jr <= n; ++jr) xmax = m_max(xmax, abs1(src[jr - 1]));
+    if (xmax > safmin) {
+      const R t = R(1) / xmax;
+      for (int jr = ibegin; jr <= n; ++jr) col[jr - 1] = t * src[jr - 1];
+    } else {
+      ibegin = n + 1;
+    }
+    for (int jr = 1; jr <= ibegin - 1; ++jr) col[jr - 1] = cx<R>(R(0));
+  }
+#undef SS
+#undef PP
+}
 }  // namespace orc

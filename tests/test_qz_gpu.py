@@ -118,3 +118,75 @@ def test_ggschur_scaled(gs, s):
     G0 = gs.ggschur(A0, B0)
     assert _match(_ratio(G), _ratio(G0)) < 1e-10
     _gschurtest(A0, B0, gs.GeneralizedSchur(G.S / s, G.T / s, G.alpha / s, G.beta / s, G.Q, G.Z))
+
+
+def _evcheck(gs, A, B, G, tol=20.0):
+    """The eigenvector half of the reference's gschurtest (test/generalized.jl:33-38):
+    ||(A VR) diag(beta) - (B VR) diag(alpha)|| and the same for the left vectors with
+    A', B' and conj(alpha), conj(beta), each below tol n ||A|| eps."""
+    n = A.shape[0]
+    nA = max(np.linalg.norm(A), np.finfo(float).tiny)
+    VR = gs.geigvecs(G)
+    VL = gs.geigvecs(G, left=True)
+    r = np.linalg.norm((A @ VR) @ np.diag(G.beta) - (B @ VR) @ np.diag(G.alpha))
+    assert r / (n * nA * EPS) < tol
+    Ah, Bh = A.conj().T, B.conj().T
+    r = np.linalg.norm((Ah @ VL) @ np.diag(G.beta.conj()) - (Bh @ VL) @ np.diag(G.alpha.conj()))
+    assert r / (n * nA * EPS) < tol
+    return VR, VL
+
+
+def _same_columns(V, Vo, tol):
+    """Column-by-column agreement with the oracle's vectors for the same Schur pair (both
+    scaled to max |re|+|im| = 1, so columns agree up to rounding)."""
+    err = np.max(np.abs(V - Vo)) if V.size else 0.0
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 32, 100])
+@pytest.mark.parametrize("kind", ["complex", "real"])
+def test_ggeigvecs_random(gs, n, kind):
+    rng = np.random.default_rng(8400 + n)
+    if kind == "complex":
+        A = rng.random((n, n)) + 1j * rng.random((n, n))
+        B = rng.random((n, n)) + 1j * rng.random((n, n))
+    else:
+        A, B = rng.random((n, n)), rng.random((n, n))
+    G = gs.ggschur(A, B)
+    VR, VL = _evcheck(gs, A, B, G)
+    _same_columns(VR, po.ggeigvecs(G.S, G.T, G.Z), 1e-9)
+    _same_columns(VL, po.ggeigvecs(G.S, G.T, G.Q, left=True), 1e-9)
+    # the triangular pair's own eigenvectors (no back-transform)
+    Gt = gs.GeneralizedSchur(G.S, G.T, G.alpha, G.beta, None, None)
+    _same_columns(gs.geigvecs(Gt), po.ggeigvecs(G.S, G.T), 1e-9)
+    _same_columns(gs.geigvecs(Gt, left=True), po.ggeigvecs(G.S, G.T, left=True), 1e-9)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ggeigvecs_challenging(gs, seed):
+    """Singular pencils (zero diagonal entries in A and in B): infinite and zero
+    eigenvalues, and the unit vectors of a singular pencil where S_kk = T_kk = 0."""
+    rng = np.random.default_rng(8100 + seed)
+    A, B = _challenging(rng)
+    G = gs.ggschur(A, B)
+    _evcheck(gs, A, B, G)
+    _same_columns(gs.geigvecs(G), po.ggeigvecs(G.S, G.T, G.Z), 1e-8)
+    _same_columns(gs.geigvecs(G, left=True), po.ggeigvecs(G.S, G.T, G.Q, left=True), 1e-8)
+
+
+def test_ggeigvecs_singular_unit_vectors(gs):
+    """A pencil with S_kk = T_kk = 0 (vectors.jl:769-772): unit eigenvector e_k."""
+    rng = np.random.default_rng(8500)
+    n = 12
+    S = np.triu(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    T = np.triu(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    T[np.diag_indices(n)] = np.abs(np.diag(T))
+    S[5, 5] = 0
+    T[5, 5] = 0
+    G = gs.GeneralizedSchur(S, T, np.diag(S), np.diag(T), None, None)
+    for left in (False, True):
+        V = gs.geigvecs(G, left=left)
+        e = np.zeros(n)
+        e[5] = 1
+        np.testing.assert_array_equal(V[:, 5], e)
+        _same_columns(V, po.ggeigvecs(S, T, left=left), 1e-9)
