@@ -490,7 +490,8 @@ def measure_e2e(ctx, packed, ns, offs, woffs, steps):
         h2d = nbytes + ns.nbytes + offs.nbytes + woffs.nbytes
         d2h = 2 * nbytes + 2 * nw * 8 + count * 4
         return {"value": count / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "seconds_per_step": dt}
+                "seconds_per_step": dt, "seconds_samples": [round(x, 4) for x in times],
+                "kernel_ms_last": ctx.last_kernel_ms()}
     finally:
         for p in hp + hw + [hs]:
             ctx.host_free(p)
