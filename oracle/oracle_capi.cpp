@@ -253,6 +253,12 @@ int or_ggevc_z(int n, const double* s, const double* p, const double* x, double*
   return 0;
 }
 
+// ggschur!(A, B) for real pencils (src/rgeneralized.jl:10-66): A <- S (quasi-triangular),
+// B <- T, Q, Z (when non-null), alpha = alr + i ali, beta.  Returns 1 at the iteration limit.
+int or_ggschur_d(int n, double* a, double* b, double* q, double* z, double* alr, double* ali, double* be, int scale) {
+  return ggschur_real<double>(n, a, n, b, n, q, z, alr, ali, be, scale != 0, 100LL * n);
+}
+
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {
   gs2x2<double>(h, cs, sn, &w[0], &w[1], &w[2], &w[3]);
   return 0;

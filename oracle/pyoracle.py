@@ -53,6 +53,7 @@ def lib():
             "or_steqr_d": [_i, _p, _p, _p, _i],
             "or_ggschur_z": [_i, _p, _p, _p, _p, _p, _p, _i],
             "or_ggevc_z": [_i, _p, _p, _p, _p, _i],
+            "or_ggschur_d": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -333,3 +334,18 @@ def ggeigvecs(S, T, X=None, left=False):
     V = np.zeros((n, n), dtype=np.complex128, order="F")
     lib().or_ggevc_z(n, _ptr(Sf), _ptr(Tf), _ptr(Xf), _ptr(V), int(left))
     return V
+
+
+def ggschur_real(A, B, scale=True):
+    """ggschur!(A, B) for a real pencil (rgeneralized.jl:10-66): (S quasi-triangular, T,
+    alpha (complex), beta (real), Q, Z, status)."""
+    S = _f(A, np.float64)
+    T = _f(B, np.float64)
+    n = S.shape[0]
+    Q = np.zeros((n, n), order="F")
+    Z = np.zeros((n, n), order="F")
+    alr = np.zeros(max(n, 1))
+    ali = np.zeros(max(n, 1))
+    be = np.zeros(max(n, 1))
+    st = lib().or_ggschur_d(n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(alr), _ptr(ali), _ptr(be), int(scale))
+    return S, T, (alr + 1j * ali)[:n], be[:n], Q, Z, st

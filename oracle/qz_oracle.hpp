@@ -9,6 +9,7 @@
 #pragma once
 #include <vector>
 #include "gschur_oracle.hpp"
+#include "hermitian_oracle.hpp"
 
 namespace orc {
 
@@ -642,4 +643,728 @@ void ggevc_left(int n, const cx<R>* S, const cx<R>* P, const cx<R>* Q, cx<R>* V)
 #undef SS
 #undef PP
 }
+
+// ---------------------------------------------------------------------------
+// Real pencils: ggschur!(A::Real, B) (src/rgeneralized.jl:10-66) with the real
+// _hessenberg! (src/generalized.jl:84-113), _gqz! (dhgeqz, src/rgeneralized.jl:68-808),
+// _ggs_2x2 (dlag2, 810-948) and _gsvd_2x2 (dlasv2, 950-1038).
+// Julia's Givens(i1, i2, c, s): lmul! [x; y] <- [c x + s y; c y - s x]; rmul!(M, G)
+// [a1 a2] <- [c a1 - s a2, s a1 + c a2]; rmul!(M, G') [a1 a2] <- [c a1 + s a2, c a2 - s a1].
+// givens(f, g, i1, i2) with i1 > i2 swaps the indices and negates s, which equals applying
+// the rotation with the indices in the given order (done below).
+// ---------------------------------------------------------------------------
+// Base.hypot(x, y, z) of Julia: the largest modulus times the 2-norm of the scaled triple.
+template <class R> inline R base_hypot3(R x, R y, R z) {
+  const R m = m_max(m_max(m_abs(x), m_abs(y)), m_abs(z));
+  if (m != m) return (m_abs(x) == std::numeric_limits<R>::infinity() || m_abs(y) == std::numeric_limits<R>::infinity() ||
+                      m_abs(z) == std::numeric_limits<R>::infinity()) ? std::numeric_limits<R>::infinity() : m;
+  if (m == R(0) || m == std::numeric_limits<R>::infinity()) return m;
+  const R a = x / m, b = y / m, c = z / m;
+  return m * m_sqrt(a * a + b * b + c * c);
+}
+template <class R> inline void gr_rows(R* m, int ld, int i1, int i2, R c, R s, int j0, int j1) {
+  for (int j = j0; j <= j1; ++j) {
+    R& a1 = m[(i1 - 1) + (long long)(j - 1) * ld];
+    R& a2 = m[(i2 - 1) + (long long)(j - 1) * ld];
+    const R x = a1, y = a2;
+    a1 = c * x + s * y;
+    a2 = c * y - s * x;
+  }
+}
+template <class R> inline void gr_cols(R* m, int ld, int i1, int i2, R c, R s, int r0, int r1) {
+  for (int r = r0; r <= r1; ++r) {
+    R& a1 = m[(r - 1) + (long long)(i1 - 1) * ld];
+    R& a2 = m[(r - 1) + (long long)(i2 - 1) * ld];
+    const R x = a1, y = a2;
+    a1 = x * c - y * s;
+    a2 = x * s + y * c;
+  }
+}
+template <class R> inline void gr_cols_adj(R* m, int ld, int i1, int i2, R c, R s, int r0, int r1) {
+  for (int r = r0; r <= r1; ++r) {
+    R& a1 = m[(r - 1) + (long long)(i1 - 1) * ld];
+    R& a2 = m[(r - 1) + (long long)(i2 - 1) * ld];
+    const R x = a1, y = a2;
+    a1 = x * c + y * s;
+    a2 = y * c - x * s;
+  }
+}
+
+template <class R> R fro_norm_real(const R* m, int ld, int n) {
+  R scale = 0, ssq = 1;
+  for (int j = 1; j <= n; ++j)
+    for (int i = 1; i <= n; ++i) {
+      const R a = m_abs(m[(i - 1) + (long long)(j - 1) * ld]);
+      if (a == R(0)) continue;
+      if (scale < a) { ssq = R(1) + ssq * (scale / a) * (scale / a); scale = a; }
+      else ssq += (a / scale) * (a / scale);
+    }
+  return scale * m_sqrt(ssq);
+}
+
+// dlag2: eigenvalues (wr1 + i wi)/scale1, (wr2 - i wi)/scale2 of the 2 x 2 pencil (A, B), B
+// upper triangular; a, b column-major 2 x 2 (ld 2 views passed as pointers + ld).
+template <class R>
+void ggs_2x2(const R* a, int lda, const R* b, int ldb, R safmin, R* scale1o, R* scale2o, R* wr1o, R* wr2o, R* wio) {
+  const R rtmin = m_sqrt(safmin), rtmax = R(1) / rtmin, safmax = R(1) / safmin;
+  const R fuzzy1 = R(1) + m_sqrt(m_sqrt(std::numeric_limits<R>::epsilon())) / R(10);
+#define GA(i, j) a[((i) - 1) + ((j) - 1) * lda]
+#define GB(i, j) b[((i) - 1) + ((j) - 1) * ldb]
+  const R anorm = m_max(m_max(m_abs(GA(1, 1)) + m_abs(GA(2, 1)), m_abs(GA(1, 2)) + m_abs(GA(2, 2))), safmin);
+  const R ascale = R(1) / anorm;
+  const R a11 = ascale * GA(1, 1), a12 = ascale * GA(1, 2), a21 = ascale * GA(2, 1), a22 = ascale * GA(2, 2);
+  R b11 = GB(1, 1), b12 = GB(1, 2), b22 = GB(2, 2);
+  const R bmin = rtmin * m_max(m_max(m_abs(b11), m_abs(b12)), m_max(m_abs(b22), rtmin));
+  if (m_abs(b11) < bmin) b11 = b11 < R(0) ? -bmin : bmin;
+  if (m_abs(b22) < bmin) b22 = b22 < R(0) ? -bmin : bmin;
+  const R bnorm = m_max(m_max(m_abs(b11), m_abs(b12) + m_abs(b22)), safmin);
+  const R bsize = m_max(m_abs(b11), m_abs(b22));
+  const R bscale = R(1) / bsize;
+  b11 *= bscale;
+  b12 *= bscale;
+  b22 *= bscale;
+  const R binv11 = R(1) / b11, binv22 = R(1) / b22;
+  const R s1 = a11 * binv11, s2 = a22 * binv22;
+  R as12, ss, abi22, pp, shift;
+  if (m_abs(s1) <= m_abs(s2)) {
+    as12 = a12 - s1 * b12;
+    const R as22 = a22 - s1 * b22;
+    ss = a21 * (binv11 * binv22);
+    abi22 = as22 * binv22 - ss * b12;
+    pp = abi22 / R(2);
+    shift = s1;
+  } else {
+    as12 = a12 - s2 * b12;
+    const R as11 = a11 - s2 * b11;
+    ss = a21 * (binv11 * binv22);
+    abi22 = -ss * b12;
+    pp = (as11 * binv11 + abi22) / R(2);
+    shift = s2;
+  }
+  const R qq = ss * as12;
+  R discr, r;
+  if (m_abs(pp * rtmin) >= R(1)) {
+    discr = (rtmin * pp) * (rtmin * pp) + qq * safmin;
+    r = m_sqrt(m_abs(discr)) * rtmax;
+  } else if (pp * pp + m_abs(qq) <= safmin) {
+    discr = (rtmax * pp) * (rtmax * pp) + qq * safmax;
+    r = m_sqrt(m_abs(discr)) * rtmin;
+  } else {
+    discr = pp * pp + qq;
+    r = m_sqrt(m_abs(discr));
+  }
+  R wr1, wr2, wi;
+  if (discr >= R(0) || r == R(0)) {
+    const R sm = pp + (pp < R(0) ? -r : r);
+    const R df = pp - (pp < R(0) ? -r : r);
+    const R wbig = shift + sm;
+    R wsmall = shift + df;
+    if (m_abs(wbig) / R(2) > m_max(m_abs(wsmall), safmin)) {
+      const R wdet = (a11 * a22 - a12 * a21) * (binv11 * binv22);
+      wsmall = wdet / wbig;
+    }
+    if (pp > abi22) {
+      wr1 = m_min(wbig, wsmall);
+      wr2 = m_max(wbig, wsmall);
+    } else {
+      wr2 = m_min(wbig, wsmall);
+      wr1 = m_max(wbig, wsmall);
+    }
+    wi = R(0);
+  } else {
+    wr1 = shift + pp;
+    wr2 = wr1;
+    wi = r;
+  }
+  const R c1 = bsize * (safmin * m_max(R(1), ascale));
+  const R c2 = safmin * m_max(R(1), bnorm);
+  const R c3 = bsize * safmin;
+  const R c4 = (ascale <= R(1) && bsize <= R(1)) ? m_min(R(1), (ascale / safmin) * bsize) : R(1);
+  const R c5 = (ascale <= R(1) || bsize <= R(1)) ? m_min(R(1), ascale * bsize) : R(1);
+  R scale1 = R(1), scale2 = R(1);
+  const R wabs = m_abs(wr1) + m_abs(wi);
+  R wsize = m_max(m_max(safmin, c1), m_max(fuzzy1 * (wabs * c2 + c3), m_min(c4, m_max(wabs, c5) / R(2))));
+  if (wsize != R(1)) {
+    const R wscale = R(1) / wsize;
+    if (wsize > R(1)) scale1 = (m_max(ascale, bsize) * wscale) * m_min(ascale, bsize);
+    else scale1 = (m_min(ascale, bsize) * wscale) * m_max(ascale, bsize);
+    wr1 *= wscale;
+    if (wi != R(0)) {
+      wi *= wscale;
+      wr2 = wr1;
+      scale2 = scale1;
+    }
+  } else {
+    scale1 = ascale * bsize;
+    scale2 = scale1;
+  }
+  if (wi == R(0)) {
+    wsize = m_max(m_max(safmin, c1), m_max(fuzzy1 * (m_abs(wr2) * c2 + c3), m_min(c4, m_max(m_abs(wr2), c5) / R(2))));
+    if (wsize != R(1)) {
+      const R wscale = R(1) / wsize;
+      if (wsize > R(1)) scale2 = (m_max(ascale, bsize) * wscale) * m_min(ascale, bsize);
+      else scale2 = (m_min(ascale, bsize) * wscale) * m_max(ascale, bsize);
+      wr2 *= wscale;
+    } else {
+      scale2 = ascale * bsize;
+    }
+  }
+  *scale1o = scale1; *scale2o = scale2; *wr1o = wr1; *wr2o = wr2; *wio = wi;
+#undef GA
+#undef GB
+}
+
+// dlasv2 on the upper triangular 2 x 2 [f g; 0 h]: returns ssmin, ssmax, snr, csr, snl, csl.
+template <class R>
+void gsvd_2x2(R f0, R g0, R h0, R* ssmino, R* ssmaxo, R* snro, R* csro, R* snlo, R* cslo) {
+  R ft = f0, gt = g0, ht = h0;
+  R fa = m_abs(ft), ha = m_abs(ht);
+  int pmax = 1;
+  const bool swap = ha > fa;
+  if (swap) {
+    pmax = 3;
+    R t = ft; ft = ht; ht = t;
+    t = fa; fa = ha; ha = t;
+  }
+  const R ga = m_abs(gt);
+  R ssmin, ssmax, clt, crt, slt, srt;
+  if (ga == R(0)) {
+    ssmin = ha; ssmax = fa; clt = R(1); crt = R(1); slt = R(0); srt = R(0);
+  } else {
+    bool ga_small = true;
+    if (ga > fa) {
+      pmax = 2;
+      if ((fa / ga) < std::numeric_limits<R>::epsilon()) {
+        ga_small = false;
+        ssmax = ga;
+        ssmin = (ha > R(1)) ? (fa / (ga / ha)) : ((fa / ha) * ha);
+        clt = R(1);
+        slt = ht / gt;
+        srt = R(1);
+        crt = ft / gt;
+      }
+    }
+    if (ga_small) {
+      const R d = fa - ha;
+      R l = (d == fa) ? R(1) : (d / fa);
+      const R m = gt / ft;
+      R t = R(2) - l;
+      const R mm = m * m, tt = t * t;
+      const R s = m_sqrt(tt + mm);
+      const R r = (l == R(0)) ? m_abs(m) : m_sqrt(l * l + mm);
+      const R a = (s + r) / R(2);
+      ssmin = ha / a;
+      ssmax = fa * a;
+      if (mm == R(0)) {
+        if (l == R(0)) t = m_copysign(R(2), ft) * m_copysign(R(1), gt);
+        else t = gt / m_copysign(d, ft) + m / t;
+      } else {
+        t = (m / (s + t) + m / (r + l)) * (R(1) + a);
+      }
+      l = m_sqrt(t * t + R(4));
+      crt = R(2) / l;
+      srt = t / l;
+      clt = (crt + srt * m) / a;
+      slt = (ht / ft) * srt / a;
+    }
+  }
+  R csl, snl, csr, snr;
+  if (swap) { csl = srt; snl = crt; csr = slt; snr = clt; }
+  else { csl = clt; snl = slt; csr = crt; snr = srt; }
+  R tsgn;
+  if (pmax == 1) tsgn = m_copysign(R(1), csr) * m_copysign(R(1), csl) * m_copysign(R(1), f0);
+  else if (pmax == 2) tsgn = m_copysign(R(1), snr) * m_copysign(R(1), csl) * m_copysign(R(1), g0);
+  else tsgn = m_copysign(R(1), snr) * m_copysign(R(1), snl) * m_copysign(R(1), h0);
+  ssmax = m_copysign(ssmax, tsgn);
+  ssmin = m_copysign(ssmin, tsgn * m_copysign(R(1), f0) * m_copysign(R(1), h0));
+  *ssmino = ssmin; *ssmaxo = ssmax; *snro = snr; *csro = csr; *snlo = snl; *cslo = csl;
+}
+
+// _gqz! for real H, B (src/rgeneralized.jl:68-808), ilo = 1, ihi = n, wantSchur = true.
+// alphar/alphai/beta: the generalized eigenvalues (alpha complex, beta real).
+// Returns 0, or 1 at the iteration limit.
+template <class R>
+int gqz_real(int n, R* h, int ldh, R* b, int ldb, R* q, int ldq, R* z, int ldz, R* alr, R* ali, R* be,
+             long long maxiter) {
+#define H_(i, j) h[((i) - 1) + (long long)((j) - 1) * ldh]
+#define B_(i, j) b[((i) - 1) + (long long)((j) - 1) * ldb]
+  const int ilo = 1, ihi = n;
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = std::numeric_limits<R>::min();
+  const R safmax = R(1) / safmin;
+  const R safety = R(100);
+  const R anorm = fro_norm_real(h, ldh, n), bnorm = fro_norm_real(b, ldb, n);
+  const R atol = m_max(safmin, ulp * anorm), btol = m_max(safmin, ulp * bnorm);
+  const R ascale = R(1) / m_max(safmin, anorm), bscale = R(1) / m_max(safmin, bnorm);
+  int ifirst = ilo, ilast = ihi;
+  const int ifirstm = 1, ilastm = n;
+  int shiftcount = 0;
+  R eshift = R(0);
+  R v[3] = {0, 0, 0};
+  enum { UNKNOWN, NONE, NORMAL, INF };
+  for (long long it = 1; it <= maxiter; ++it) {
+    int br = UNKNOWN;
+    if (ilast == ilo) br = NORMAL;
+    else if (m_abs(H_(ilast, ilast - 1)) < m_max(safmin, ulp * (m_abs(H_(ilast, ilast)) + m_abs(H_(ilast - 1, ilast - 1))))) {
+      H_(ilast, ilast - 1) = R(0);
+      br = NORMAL;
+    }
+    if (br == UNKNOWN) {
+      if (m_abs(B_(ilast, ilast)) <= btol) {
+        B_(ilast, ilast) = R(0);
+        br = INF;
+      } else {
+        for (int j = ilast - 1; j >= ilo; --j) {
+          bool have_H_0sd = false;
+          if (j == ilo) have_H_0sd = true;
+          else if (m_abs(H_(j, j - 1)) <= atol) {
+            H_(j, j - 1) = R(0);
+            have_H_0sd = true;
+          }
+          if (m_abs(B_(j, j)) < btol) {
+            B_(j, j) = R(0);
+            bool have2 = false;
+            if (!have_H_0sd) {
+              R t = m_abs(H_(j, j - 1)), t2 = m_abs(H_(j, j));
+              const R tr = m_max(t, t2);
+              if (tr < R(1) && tr != R(0)) { t = t / tr; t2 = t2 / tr; }
+              have2 = (t * (ascale * m_abs(H_(j + 1, j))) <= t2 * (ascale * atol));
+            }
+            if (have_H_0sd || have2) {
+              for (int jch = j; jch <= ilast - 1; ++jch) {
+                R c, s, r;
+                givens_alg(H_(jch, jch), H_(jch + 1, jch), &c, &s, &r);
+                H_(jch, jch) = r;
+                H_(jch + 1, jch) = R(0);
+                gr_rows(h, ldh, jch, jch + 1, c, s, jch + 1, ilastm);
+                gr_rows(b, ldb, jch, jch + 1, c, s, jch + 1, ilastm);
+                if (q) gr_cols_adj(q, ldq, jch, jch + 1, c, s, 1, n);
+                if (have2) H_(jch, jch - 1) *= c;
+                have2 = false;
+                if (m_abs(B_(jch + 1, jch + 1)) > btol) {
+                  if (jch + 1 >= ilast) br = NORMAL;
+                  else { ifirst = jch + 1; br = NONE; }
+                  break;
+                }
+                B_(jch + 1, jch + 1) = R(0);
+              }
+              if (br == UNKNOWN) br = INF;
+              break;
+            } else {
+              for (int jch = j; jch <= ilast - 1; ++jch) {
+                R c, s, r;
+                givens_alg(B_(jch, jch + 1), B_(jch + 1, jch + 1), &c, &s, &r);
+                B_(jch, jch + 1) = r;
+                B_(jch + 1, jch + 1) = R(0);
+                if (jch < ilastm - 1) gr_rows(b, ldb, jch, jch + 1, c, s, jch + 2, ilastm);
+                gr_rows(h, ldh, jch, jch + 1, c, s, jch - 1, ilastm);
+                if (q) gr_cols_adj(q, ldq, jch, jch + 1, c, s, 1, n);
+                givens_alg(H_(jch + 1, jch), H_(jch + 1, jch - 1), &c, &s, &r);
+                H_(jch + 1, jch) = r;
+                H_(jch + 1, jch - 1) = R(0);
+                gr_cols_adj(h, ldh, jch, jch - 1, c, s, ifirstm, jch);
+                gr_cols_adj(b, ldb, jch, jch - 1, c, s, ifirstm, jch - 1);
+                if (z) gr_cols_adj(z, ldz, jch, jch - 1, c, s, 1, n);
+              }
+              br = INF;
+              break;
+            }
+          } else if (have_H_0sd) {
+            ifirst = j;
+            br = NONE;
+            break;
+          }
+        }
+      }
+      if (br == INF) {
+        R c, s, r;
+        givens_alg(H_(ilast, ilast), H_(ilast, ilast - 1), &c, &s, &r);
+        H_(ilast, ilast) = r;
+        H_(ilast, ilast - 1) = R(0);
+        gr_cols_adj(h, ldh, ilast, ilast - 1, c, s, ifirstm, ilast - 1);
+        gr_cols_adj(b, ldb, ilast, ilast - 1, c, s, ifirstm, ilast - 1);
+        if (z) gr_cols_adj(z, ldz, ilast, ilast - 1, c, s, 1, n);
+        br = NORMAL;
+      }
+    }
+    if (br == NORMAL) {
+      if (B_(ilast, ilast) < R(0)) {
+        for (int i = ifirstm; i <= ilast; ++i) { H_(i, ilast) = -H_(i, ilast); B_(i, ilast) = -B_(i, ilast); }
+        if (z) for (int i = 1; i <= n; ++i) z[(i - 1) + (long long)(ilast - 1) * ldz] *= R(-1);
+      }
+      alr[ilast - 1] = H_(ilast, ilast);
+      ali[ilast - 1] = R(0);
+      be[ilast - 1] = B_(ilast, ilast);
+      ilast -= 1;
+      if (ilast < ilo) break;
+      shiftcount = 0;
+      eshift = R(0);
+      continue;
+    }
+    // QZ step on ifirst..ilast
+    ++shiftcount;
+    R s1, s2, wr, wr2, wi;
+    if (shiftcount % 10 != 0) {
+      ggs_2x2(&H_(ilast - 1, ilast - 1), ldh, &B_(ilast - 1, ilast - 1), ldb, safmin * safety, &s1, &s2, &wr, &wr2, &wi);
+      if (m_abs((wr / s1) * B_(ilast, ilast) - H_(ilast, ilast)) > m_abs((wr2 / s2) * B_(ilast, ilast) - H_(ilast, ilast))) {
+        R t = wr; wr = wr2; wr2 = t;
+        t = s1; s1 = s2; s2 = t;
+      }
+    } else {
+      if (R(maxiter) * safmin * m_abs(H_(ilast, ilast - 1)) < m_abs(B_(ilast - 1, ilast - 1)))
+        eshift = H_(ilast, ilast - 1) / B_(ilast - 1, ilast - 1);
+      else
+        eshift += R(1) / (safmin * R(maxiter));
+      s1 = R(1);
+      wr = eshift;
+      wi = R(0);
+    }
+    if (wi == R(0)) {
+      R t = m_min(ascale, R(1)) * (safmax / R(2));
+      R scale = s1 > t ? t / s1 : R(1);
+      t = m_min(bscale, R(1)) * (safmax / R(2));
+      if (m_abs(wr) > t) scale = m_min(scale, t / m_abs(wr));
+      s1 *= scale;
+      wr *= scale;
+      int istart = -1;
+      bool gotit = false;
+      for (int j = ilast - 1; j >= ifirst + 1; --j) {
+        istart = j;
+        R t1 = m_abs(s1 * H_(j, j - 1));
+        R t2 = m_abs(s1 * H_(j, j) - wr * B_(j, j));
+        const R tr = m_max(t1, t2);
+        if (tr < R(1) && tr != R(0)) { t1 /= tr; t2 /= tr; }
+        if (m_abs((ascale * H_(j + 1, j)) * t1) <= ascale * atol * t2) { gotit = true; break; }
+      }
+      if (!gotit) istart = ifirst;
+      const R f1 = s1 * H_(istart, istart) - wr * B_(istart, istart);
+      const R g2 = s1 * H_(istart + 1, istart);
+      R c, s, t3;
+      givens_alg(f1, g2, &c, &s, &t3);
+      for (int j = istart; j <= ilast - 1; ++j) {
+        if (j > istart) {
+          R r;
+          givens_alg(H_(j, j - 1), H_(j + 1, j - 1), &c, &s, &r);
+          H_(j, j - 1) = r;
+          H_(j + 1, j - 1) = R(0);
+        }
+        gr_rows(h, ldh, j, j + 1, c, s, j, ilastm);
+        gr_rows(b, ldb, j, j + 1, c, s, j, ilastm);
+        if (q) gr_cols_adj(q, ldq, j, j + 1, c, s, 1, n);
+        R r;
+        givens_alg(B_(j + 1, j + 1), B_(j + 1, j), &c, &s, &r);
+        B_(j + 1, j + 1) = r;
+        B_(j + 1, j) = R(0);
+        gr_cols(h, ldh, j, j + 1, c, s, ifirstm, m_min(j + 2, ilast));
+        gr_cols(b, ldb, j, j + 1, c, s, ifirstm, j);
+        if (z) gr_cols(z, ldz, j, j + 1, c, s, 1, n);
+      }
+    } else if (ilast == ifirst + 1) {
+      // 2 x 2 block with complex eigenvalues: diagonalise B, then alpha, beta
+      R b22, b11, sr, cr, sl, cl;
+      gsvd_2x2(B_(ifirst, ifirst), B_(ifirst, ilast), B_(ilast, ilast), &b22, &b11, &sr, &cr, &sl, &cl);
+      if (b11 < R(0)) { cr = -cr; sr = -sr; b11 = -b11; b22 = -b22; }
+      gr_rows(h, ldh, ifirst, ilast, cl, sl, ifirst, ilastm);
+      gr_cols_adj(h, ldh, ifirst, ilast, cr, sr, ifirstm, ilast);
+      if (ilast < ilastm) gr_rows(b, ldb, ifirst, ilast, cl, sl, ilast + 1, ilastm);
+      if (ifirstm < ifirst) gr_cols_adj(b, ldb, ifirst, ilast, cr, sr, ifirstm, ifirst - 1);
+      if (q) gr_cols_adj(q, ldq, ifirst, ilast, cl, sl, 1, n);
+      if (z) gr_cols_adj(z, ldz, ifirst, ilast, cr, sr, 1, n);
+      B_(ilast - 1, ilast - 1) = b11;
+      B_(ilast - 1, ilast) = R(0);
+      B_(ilast, ilast - 1) = R(0);
+      B_(ilast, ilast) = b22;
+      if (b22 < R(0)) {
+        for (int i = ifirstm; i <= ilast; ++i) { H_(i, ilast) = -H_(i, ilast); B_(i, ilast) = -B_(i, ilast); }
+        if (z) for (int i = 1; i <= n; ++i) z[(i - 1) + (long long)(ilast - 1) * ldz] *= R(-1);
+        b22 = -b22;
+      }
+      R d2, d3;
+      ggs_2x2(&H_(ilast - 1, ilast - 1), ldh, &B_(ilast - 1, ilast - 1), ldb, safmin * safety, &s1, &d2, &wr, &d3, &wi);
+      if (wi == R(0)) continue;  // back to a single shift
+      const R s1inv = R(1) / s1;
+      const R a11 = H_(ilast - 1, ilast - 1), a21 = H_(ilast, ilast - 1), a12 = H_(ilast - 1, ilast), a22 = H_(ilast, ilast);
+      const R c11r = s1 * a11 - wr * b11, c11i = -wi * b11, c12 = s1 * a12, c21 = s1 * a21;
+      const R c22r = s1 * a22 - wr * b22, c22i = -wi * b22;
+      R cz, szr, szi;
+      if (m_abs(c11r) + m_abs(c11i) + m_abs(c12) > m_abs(c21) + m_abs(c22r) + m_abs(c22i)) {
+        const R t1 = base_hypot3(c12, c11r, c11i);
+        cz = c12 / t1;
+        szr = -c11r / t1;
+        szi = -c11i / t1;
+      } else {
+        cz = m_hypot(c22r, c22i);
+        if (cz <= safmin) { cz = R(0); szr = R(1); szi = R(0); }
+        else {
+          const R tr = c22r / cz, ti = c22i / cz;
+          const R t1 = m_hypot(cz, c21);
+          cz /= t1;
+          szr = -c21 * tr / t1;
+          szi = c21 * ti / t1;
+        }
+      }
+      const R an = m_abs(a11) + m_abs(a12) + m_abs(a21) + m_abs(a22);
+      const R bn = m_abs(b11) + m_abs(b22);
+      const R wabs = m_abs(wr) + m_abs(wi);
+      R cq, sqr, sqi;
+      if (s1 * an > wabs * bn) {
+        cq = cz * b11;
+        sqr = szr * b22;
+        sqi = -szi * b22;
+      } else {
+        const R a1r = cz * a11 + szr * a12, a1i = szi * a12;
+        const R a2r = cz * a21 + szr * a22, a2i = szi * a22;
+        cq = m_hypot(a1r, a1i);
+        if (cq <= safmin) { cq = R(0); sqr = R(1); sqi = R(0); }
+        else {
+          const R tr = a1r / cq, ti = a1i / cq;
+          sqr = tr * a2r + ti * a2i;
+          sqi = ti * a2r - tr * a2i;
+        }
+      }
+      const R t1 = base_hypot3(cq, sqr, sqi);
+      cq /= t1;
+      sqr /= t1;
+      sqi /= t1;
+      const R tr = sqr * szr - sqi * szi, ti = sqr * szi + sqi * szr;
+      const R b1r = cq * cz * b11 + tr * b22, b1i = ti * b22;
+      const R b1a = m_hypot(b1r, b1i);
+      const R b2r = cq * cz * b22 + tr * b11, b2i = -ti * b11;
+      const R b2a = m_hypot(b2r, b2i);
+      be[ilast - 2] = b1a;
+      be[ilast - 1] = b2a;
+      alr[ilast - 2] = (wr * b1a) * s1inv;
+      ali[ilast - 2] = (wi * b1a) * s1inv;
+      alr[ilast - 1] = (wr * b2a) * s1inv;
+      ali[ilast - 1] = (-wi * b2a) * s1inv;
+      ilast = ifirst - 1;
+      if (ilast < ilo) break;
+      shiftcount = 0;
+      eshift = R(0);
+    } else {
+      // Francis implicit double shift on a block of order >= 3
+      const R ad11 = (ascale * H_(ilast - 1, ilast - 1)) / (bscale * B_(ilast - 1, ilast - 1));
+      const R ad21 = (ascale * H_(ilast, ilast - 1)) / (bscale * B_(ilast - 1, ilast - 1));
+      const R ad12 = (ascale * H_(ilast - 1, ilast)) / (bscale * B_(ilast, ilast));
+      const R ad22 = (ascale * H_(ilast, ilast)) / (bscale * B_(ilast, ilast));
+      const R u12 = B_(ilast - 1, ilast) / B_(ilast, ilast);
+      const R ad11l = (ascale * H_(ifirst, ifirst)) / (bscale * B_(ifirst, ifirst));
+      const R ad21l = (ascale * H_(ifirst + 1, ifirst)) / (bscale * B_(ifirst, ifirst));
+      const R ad12l = (ascale * H_(ifirst, ifirst + 1)) / (bscale * B_(ifirst + 1, ifirst + 1));
+      const R ad22l = (ascale * H_(ifirst + 1, ifirst + 1)) / (bscale * B_(ifirst + 1, ifirst + 1));
+      const R ad32l = (ascale * H_(ifirst + 2, ifirst + 1)) / (bscale * B_(ifirst + 1, ifirst + 1));
+      const R u12l = B_(ifirst, ifirst + 1) / B_(ifirst + 1, ifirst + 1);
+      v[0] = ((ad11 - ad11l) * (ad22 - ad11l) - ad12 * ad21 + ad21 * u12 * ad11l + (ad12l - ad11l * u12l) * ad21l);
+      v[1] = (((ad22l - ad11l) - ad21l * u12l - (ad11 - ad11l) - (ad22 - ad11l) + ad21 * u12)) * ad21l;
+      v[2] = ad32l * ad21l;
+      const int istart = ifirst;
+      R tau = reflector_real(v, 3);
+      v[0] = R(1);
+      for (int j = istart; j <= ilast - 2; ++j) {
+        if (j > istart) {
+          v[0] = H_(j, j - 1); v[1] = H_(j + 1, j - 1); v[2] = H_(j + 2, j - 1);
+          tau = reflector_real(v, 3);
+          H_(j, j - 1) = v[0];
+          v[0] = R(1);
+          H_(j + 1, j - 1) = R(0);
+          H_(j + 2, j - 1) = R(0);
+        }
+        R t2 = tau * v[1], t3 = tau * v[2];
+        for (int jc = j; jc <= ilastm; ++jc) {
+          R t1 = H_(j, jc) + v[1] * H_(j + 1, jc) + v[2] * H_(j + 2, jc);
+          H_(j, jc) -= t1 * tau;
+          H_(j + 1, jc) -= t1 * t2;
+          H_(j + 2, jc) -= t1 * t3;
+          t1 = B_(j, jc) + v[1] * B_(j + 1, jc) + v[2] * B_(j + 2, jc);
+          B_(j, jc) -= t1 * tau;
+          B_(j + 1, jc) -= t1 * t2;
+          B_(j + 2, jc) -= t1 * t3;
+        }
+        if (q)
+          for (int jr = 1; jr <= n; ++jr) {
+            R* qr = q + (jr - 1);
+            const R t1 = qr[(long long)(j - 1) * ldq] + v[1] * qr[(long long)j * ldq] + v[2] * qr[(long long)(j + 1) * ldq];
+            qr[(long long)(j - 1) * ldq] -= t1 * tau;
+            qr[(long long)j * ldq] -= t1 * t2;
+            qr[(long long)(j + 1) * ldq] -= t1 * t3;
+          }
+        // zero the j-th column of B: 2 x 2 solve with pivoting
+        bool pivot = false;
+        R scale, u1, u2;
+        {
+          R t1 = m_max(m_abs(B_(j + 1, j + 1)), m_abs(B_(j + 1, j + 2)));
+          R tt2 = m_max(m_abs(B_(j + 2, j + 1)), m_abs(B_(j + 2, j + 2)));
+          if (m_max(t1, tt2) < safmin) {
+            scale = R(0); u1 = R(1); u2 = R(0);
+          } else {
+            R w11, w21, w12, w22;
+            if (t1 >= tt2) {
+              w11 = B_(j + 1, j + 1); w21 = B_(j + 2, j + 1); w12 = B_(j + 1, j + 2); w22 = B_(j + 2, j + 2);
+              u1 = B_(j + 1, j); u2 = B_(j + 2, j);
+            } else {
+              w21 = B_(j + 1, j + 1); w11 = B_(j + 2, j + 1); w22 = B_(j + 1, j + 2); w12 = B_(j + 2, j + 2);
+              u2 = B_(j + 1, j); u1 = B_(j + 2, j);
+            }
+            if (m_abs(w12) > m_abs(w11)) {
+              pivot = true;
+              R t = w11; w11 = w12; w12 = t;
+              t = w21; w21 = w22; w22 = t;
+            }
+            t1 = w21 / w11;
+            u2 -= t1 * u1;
+            w22 -= t1 * w12;
+            scale = R(1);
+            if (m_abs(w22) < safmin) {
+              scale = R(0);
+            } else {
+              if (m_abs(w22) < m_abs(u2)) scale = m_abs(w22 / u2);
+              if (m_abs(w11) < m_abs(u1)) scale = m_min(scale, m_abs(w11 / u1));
+              u2 = (scale * u2) / w22;
+              u1 = (scale * u1 - w12 * u2) / w11;
+            }
+          }
+        }
+        if (pivot) { R t = u1; u1 = u2; u2 = t; }
+        {
+          const R t1 = base_hypot3(scale, u1, u2);
+          tau = R(1) + scale / t1;
+          const R vs = -R(1) / (scale + t1);
+          v[0] = R(1);
+          v[1] = vs * u1;
+          v[2] = vs * u2;
+        }
+        t2 = tau * v[1];
+        t3 = tau * v[2];
+        for (int jr = ifirstm; jr <= m_min(j + 3, ilast); ++jr) {
+          const R t1 = H_(jr, j) + v[1] * H_(jr, j + 1) + v[2] * H_(jr, j + 2);
+          H_(jr, j) -= t1 * tau;
+          H_(jr, j + 1) -= t2 * t1;
+          H_(jr, j + 2) -= t3 * t1;
+        }
+        for (int jr = ifirstm; jr <= j + 2; ++jr) {
+          const R t1 = B_(jr, j) + v[1] * B_(jr, j + 1) + v[2] * B_(jr, j + 2);
+          B_(jr, j) -= t1 * tau;
+          B_(jr, j + 1) -= t2 * t1;
+          B_(jr, j + 2) -= t3 * t1;
+        }
+        if (z)
+          for (int jr = 1; jr <= n; ++jr) {
+            R* zr = z + (jr - 1);
+            const R t1 = zr[(long long)(j - 1) * ldz] + v[1] * zr[(long long)j * ldz] + v[2] * zr[(long long)(j + 1) * ldz];
+            zr[(long long)(j - 1) * ldz] -= t1 * tau;
+            zr[(long long)j * ldz] -= t2 * t1;
+            zr[(long long)(j + 1) * ldz] -= t3 * t1;
+          }
+        B_(j + 1, j) = R(0);
+        B_(j + 2, j) = R(0);
+      }
+      // last two rotations
+      const int j = ilast - 1;
+      R c, s, r;
+      givens_alg(H_(j, j - 1), H_(j + 1, j - 1), &c, &s, &r);
+      H_(j, j - 1) = r;
+      H_(j + 1, j - 1) = R(0);
+      gr_rows(h, ldh, j, j + 1, c, s, j, ilastm);
+      gr_rows(b, ldb, j, j + 1, c, s, j, ilastm);
+      if (q) gr_cols_adj(q, ldq, j, j + 1, c, s, 1, n);
+      givens_alg(B_(j + 1, j + 1), B_(j + 1, j), &c, &s, &r);
+      B_(j + 1, j + 1) = r;
+      B_(j + 1, j) = R(0);
+      gr_cols_adj(h, ldh, j + 1, j, c, s, ifirstm, ilast);
+      gr_cols_adj(b, ldb, j + 1, j, c, s, ifirstm, ilast - 1);
+      if (z) gr_cols_adj(z, ldz, j + 1, j, c, s, 1, n);
+    }
+    if (it >= maxiter) return 1;
+  }
+  return 0;
+#undef H_
+#undef B_
+}
+
+// ggschur!(A, B) for real A, B (src/rgeneralized.jl:10-66).  A <- S (quasi-triangular), B <- T,
+// Q, Z (n x n, wanted when non-null); alphar + i alphai, beta the eigenvalues alpha ./ beta.
+template <class R>
+int ggschur_real(int n, R* a, int lda, R* b, int ldb, R* q, R* z, R* alr, R* ali, R* be, bool scale,
+                 long long maxiter) {
+#define A_(i, j) a[((i) - 1) + (long long)((j) - 1) * lda]
+#define B_(i, j) b[((i) - 1) + (long long)((j) - 1) * ldb]
+  R cscale = 1, anrm = 1, cscaleb = 1, bnrm = 1;
+  bool scaleA = false, scaleB = false;
+  if (scale) {
+    scaleA = scale_matrix<R, R>(n, a, lda, &cscale, &anrm);
+    scaleB = scale_matrix<R, R>(n, b, ldb, &cscaleb, &bnrm);
+  }
+  // qr!(B); A <- Q' A; Q = Matrix(Q)
+  std::vector<R> tau(n > 0 ? n : 1);
+  for (int j = 1; j <= n; ++j) {
+    const int m = n - j + 1;
+    const R t = reflector_real(&B_(j, j), m);
+    tau[j - 1] = t;
+    auto apply = [&](R* m0, int ld, int c0, int c1) {
+      for (int col = c0; col <= c1; ++col) {
+        R* x = m0 + (j - 1) + (long long)(col - 1) * ld;
+        R s = x[0];
+        for (int r = 1; r < m; ++r) s += B_(j + r, j) * x[r];
+        s = t * s;
+        x[0] -= s;
+        for (int r = 1; r < m; ++r) x[r] -= s * B_(j + r, j);
+      }
+    };
+    apply(b, ldb, j + 1, n);
+    apply(a, lda, 1, n);
+  }
+  if (q) {
+    for (int jj = 1; jj <= n; ++jj)
+      for (int ii = 1; ii <= n; ++ii) q[(ii - 1) + (long long)(jj - 1) * n] = R(ii == jj ? 1 : 0);
+    for (int j = n; j >= 1; --j) {
+      const int m = n - j + 1;
+      const R t = tau[j - 1];
+      for (int col = j; col <= n; ++col) {
+        R* x = q + (j - 1) + (long long)(col - 1) * n;
+        R s = x[0];
+        for (int r = 1; r < m; ++r) s += B_(j + r, j) * x[r];
+        s = t * s;
+        x[0] -= s;
+        for (int r = 1; r < m; ++r) x[r] -= s * B_(j + r, j);
+      }
+    }
+  }
+  for (int jj = 1; jj <= n; ++jj)
+    for (int ii = jj + 1; ii <= n; ++ii) B_(ii, jj) = R(0);
+  if (z)
+    for (int jj = 1; jj <= n; ++jj)
+      for (int ii = 1; ii <= n; ++ii) z[(ii - 1) + (long long)(jj - 1) * n] = R(ii == jj ? 1 : 0);
+  // _hessenberg!(A, B, Q, Z) (src/generalized.jl:84-113)
+  for (int jc = 1; jc <= n - 2; ++jc)
+    for (int jr = n; jr >= jc + 2; --jr) {
+      R c, s, r;
+      givens_alg(A_(jr - 1, jc), A_(jr, jc), &c, &s, &r);
+      gr_rows(a, lda, jr - 1, jr, c, s, 1, n);
+      gr_rows(b, ldb, jr - 1, jr, c, s, 1, n);
+      if (q) gr_cols_adj(q, n, jr - 1, jr, c, s, 1, n);
+      givens_alg(B_(jr, jr), B_(jr, jr - 1), &c, &s, &r);
+      gr_cols_adj(a, lda, jr, jr - 1, c, s, 1, n);
+      gr_cols_adj(b, ldb, jr, jr - 1, c, s, 1, n);
+      if (z) gr_cols_adj(z, n, jr, jr - 1, c, s, 1, n);
+    }
+  for (int jj = 1; jj <= n; ++jj)
+    for (int ii = 1; ii <= n; ++ii) {
+      if (ii > jj + 1) A_(ii, jj) = R(0);
+      if (ii > jj) B_(ii, jj) = R(0);
+    }
+  const int st = gqz_real<R>(n, a, lda, b, ldb, q, n, z, n, alr, ali, be, maxiter);
+  if (scaleA) {
+    for (int jj = 1; jj <= n; ++jj) safescale<R, R>(a + (long long)(jj - 1) * lda, n, cscale, anrm);
+    safescale<R, R>(alr, n, cscale, anrm);
+    safescale<R, R>(ali, n, cscale, anrm);
+  }
+  if (scaleB) {
+    for (int jj = 1; jj <= n; ++jj) safescale<R, R>(b + (long long)(jj - 1) * ldb, n, cscaleb, bnrm);
+    safescale<R, R>(be, n, cscaleb, bnrm);
+  }
+  return st;
+#undef A_
+#undef B_
+}
+
 }  // namespace orc
