@@ -203,6 +203,36 @@ __device__ inline void gs2x2(double& a, double& b, double& c, double& d, double&
 
 }  // namespace gsk
 
+namespace gsk {
+// LinearAlgebra.givensAlgorithm (LAPACK 3.x dlartg): safmn2 = 2^-485, safmx2 = 2^485.
+__device__ inline void givens_alg(double f, double g, double& cs, double& sn, double& r) {
+  const double mn2 = 0x1p-485, mx2 = 0x1p485;
+  if (g == 0.0) { cs = 1.0; sn = 0.0; r = f; return; }
+  if (f == 0.0) { cs = 0.0; sn = 1.0; r = g; return; }
+  double f1 = f, g1 = g, scale = fmax(fabs(f1), fabs(g1));
+  double rr;
+  if (scale >= mx2) {
+    int count = 0;
+    do { ++count; f1 *= mn2; g1 *= mn2; scale = fmax(fabs(f1), fabs(g1)); } while (!(scale < mx2 || count >= 20));
+    rr = sqrt(f1 * f1 + g1 * g1);
+    cs = f1 / rr; sn = g1 / rr;
+    for (int q = 0; q < count; ++q) rr *= mx2;
+  } else if (scale <= mn2) {
+    int count = 0;
+    do { ++count; f1 *= mx2; g1 *= mx2; scale = fmax(fabs(f1), fabs(g1)); } while (!(scale > mn2) && count < 40);
+    rr = sqrt(f1 * f1 + g1 * g1);
+    cs = f1 / rr; sn = g1 / rr;
+    for (int q = 0; q < count; ++q) rr *= mn2;
+  } else {
+    rr = sqrt(f1 * f1 + g1 * g1);
+    cs = f1 / rr; sn = g1 / rr;
+  }
+  if (fabs(f) > fabs(g) && cs < 0.0) { cs = -cs; sn = -sn; rr = -rr; }
+  r = rr;
+}
+
+}  // namespace gsk
+
 // ---- complex FP64 helpers (double2 = (re, im)) -------------------------------
 namespace gsk {
 __device__ __forceinline__ double2 zmk(double r, double i) { return make_double2(r, i); }

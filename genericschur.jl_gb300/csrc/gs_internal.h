@@ -125,6 +125,23 @@ struct QzBatch {
   int n1;                  // ns == null: one pencil of order n1 at offset 0
 };
 cudaError_t launch_ggschur(const QzBatch& bt, int num_sms, cudaStream_t s);
+// Real pencils (qz_real.cu): A, B, Q, Z real; alpha complex, beta real.
+struct QzrBatch {
+  int count;
+  const int* ns;
+  const long long* offs;   // element offsets of A, B, Q, Z
+  const long long* woffs;  // offsets of alpha, beta
+  double* A;               // in: A, out: S (quasi-triangular)
+  double* B;               // in: B, out: T
+  double* Q;               // out (may be null)
+  double* Z;               // out (may be null)
+  double2* alpha;
+  double* beta;
+  int* status;
+  int scale;
+  int n1;
+};
+cudaError_t launch_ggschur_real(const QzrBatch& bt, int num_sms, cudaStream_t s);
 
 // Hermitian path (hermitian.cu).  S = double or double2.
 struct HeCtlBuf {

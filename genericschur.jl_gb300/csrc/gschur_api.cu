@@ -2294,6 +2294,82 @@ int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, in
 namespace {
 
 // single > 0: one pencil of that order (ns, offs, woffs unused).
+int ggschur_real_impl(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs, int64_t plen, double* A,
+                      double* B, double* Q, double* Z, const int64_t* woffs, int64_t wlen, double* alpha, double* beta,
+                      int32_t* status, unsigned flags, int single = 0) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (count < 0 || plen < 0 || wlen < 0) return set_err(ctx, GS_BADARG, "negative size");
+  if (count == 0) return GS_OK;
+  if ((!single && (!ns || !offs || !woffs)) || !A || !B || !alpha || !beta)
+    return set_err(ctx, GS_BADARG, "null array argument");
+  const bool dev = flags & GS_DEVICE;
+  if (!dev && !single) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int64_t n = ns[b];
+      if (n < 0 || n > 4096 || offs[b] < 0 || offs[b] + n * n > plen || woffs[b] < 0 || woffs[b] + n > wlen)
+        return set_err(ctx, GS_BADARG, "pencil %lld: order or offsets out of range", (long long)b);
+    }
+  }
+  CK(cudaSetDevice(ctx->device));
+  Arena ar;
+  const size_t o_ns = ar.take<int>(dev ? 1 : count), o_off = ar.take<long long>(dev ? 1 : count),
+               o_woff = ar.take<long long>(dev ? 1 : count), o_A = ar.take<double>(dev ? 1 : plen),
+               o_B = ar.take<double>(dev ? 1 : plen), o_Q = ar.take<double>(dev || !Q ? 1 : plen),
+               o_Z = ar.take<double>(dev || !Z ? 1 : plen), o_al = ar.take<double2>(dev ? 1 : wlen),
+               o_be = ar.take<double>(dev ? 1 : wlen), o_st = ar.take<int>(count);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  QzrBatch bt;
+  bt.count = (int)count;
+  bt.scale = (flags & GS_SCALE) ? 1 : 0;
+  bt.n1 = single;
+  if (dev) {
+    bt.ns = single ? nullptr : ns;
+    bt.offs = (const long long*)offs;
+    bt.woffs = (const long long*)woffs;
+    bt.A = A; bt.B = B; bt.Q = Q; bt.Z = Z;
+    bt.alpha = (double2*)alpha; bt.beta = beta;
+    bt.status = status ? (int*)status : (int*)(base + o_st);
+  } else {
+    if (!single) {
+      CK(cudaMemcpyAsync(base + o_ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(base + o_off, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(base + o_woff, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(base + o_A, A, sizeof(double) * plen, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_B, B, sizeof(double) * plen, cudaMemcpyHostToDevice, s));
+    bt.ns = single ? nullptr : (const int*)(base + o_ns);
+    bt.offs = (const long long*)(base + o_off);
+    bt.woffs = (const long long*)(base + o_woff);
+    bt.A = (double*)(base + o_A); bt.B = (double*)(base + o_B);
+    bt.Q = Q ? (double*)(base + o_Q) : nullptr; bt.Z = Z ? (double*)(base + o_Z) : nullptr;
+    bt.alpha = (double2*)(base + o_al); bt.beta = (double*)(base + o_be);
+    bt.status = (int*)(base + o_st);
+  }
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_ggschur_real(bt, ctx->num_sms, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  std::vector<int> st(count);
+  CK(cudaMemcpyAsync(st.data(), bt.status, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+  if (!dev) {
+    CK(cudaMemcpyAsync(A, bt.A, sizeof(double) * plen, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(B, bt.B, sizeof(double) * plen, cudaMemcpyDeviceToHost, s));
+    if (Q) CK(cudaMemcpyAsync(Q, bt.Q, sizeof(double) * plen, cudaMemcpyDeviceToHost, s));
+    if (Z) CK(cudaMemcpyAsync(Z, bt.Z, sizeof(double) * plen, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(alpha, bt.alpha, sizeof(double2) * wlen, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(beta, bt.beta, sizeof(double) * wlen, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (status && !dev) std::memcpy(status, st.data(), sizeof(int) * count);
+  for (int64_t b = 0; b < count; ++b)
+    if (st[b]) return set_err(ctx, GS_UNCONVERGED, "pencil %lld: iteration limit reached", (long long)b);
+  return GS_OK;
+}
+
 int ggschur_batched_impl(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs, int64_t plen,
                          double* A, double* B, double* Q, double* Z, const int64_t* woffs, int64_t wlen, double* alpha,
                          double* beta, int32_t* status, unsigned flags, int single = 0) {
@@ -2379,6 +2455,23 @@ int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, co
                            double* A, double* B, double* Q, double* Z, const int64_t* woffs, int64_t wlen,
                            double* alpha, double* beta, int32_t* status, unsigned flags) {
   return ggschur_batched_impl(ctx, count, ns, offs, packed_len, A, B, Q, Z, woffs, wlen, alpha, beta, status, flags);
+}
+
+int gs_ggschur_f64(gs_context* ctx, int64_t n, double* A, double* B, double* Q, double* Z, double* alpha, double* beta,
+                   unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  if (n < 0 || n > 4096) return set_err(ctx, GS_BADARG, "bad order");
+  if (n == 0) return GS_OK;
+  return ggschur_real_impl(ctx, 1, nullptr, nullptr, n * n, A, B, Q, Z, nullptr, n, alpha, beta, nullptr, flags,
+                           (int)n);
+}
+
+int gs_ggschur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs, int64_t packed_len,
+                           double* A, double* B, double* Q, double* Z, const int64_t* woffs, int64_t wlen,
+                           double* alpha, double* beta, int32_t* status, unsigned flags) {
+  const int rc = ggschur_real_impl(ctx, count, ns, offs, packed_len, A, B, Q, Z, woffs, wlen, alpha, beta, status,
+                                   flags);
+  return rc;
 }
 
 int gs_ggschur_c64(gs_context* ctx, int64_t n, double* A, double* B, double* Q, double* Z, double* alpha, double* beta,

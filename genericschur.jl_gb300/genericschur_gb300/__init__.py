@@ -117,11 +117,31 @@ def gschur(A, **kw):
 GeneralizedSchur = namedtuple("GeneralizedSchur", ["S", "T", "alpha", "beta", "Q", "Z"])
 
 
+def _ggschur_real(A, B, wantQ, wantZ, scale, ctx):
+    S = np.array(A, dtype=np.float64, order="F", copy=True)
+    T = np.array(B, dtype=np.float64, order="F", copy=True)
+    n = _checksquare(S)
+    if _checksquare(T) != n:
+        raise ArgumentError("matrices must have the same sizes")
+    Q = np.zeros((n, n), order="F") if wantQ else None
+    Z = np.zeros((n, n), order="F") if wantZ else None
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1))
+    rc = ctx.lib.gs_ggschur_f64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(al), _ptr(be),
+                                _capi.GS_SCALE if scale else 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "ggschur!")
+    return GeneralizedSchur(S, T, al[:n], be[:n], Q, Z)
+
+
 def ggschur(A, B, wantQ=True, wantZ=True, scale=True, ctx=None):
-    """ggschur!(A, B; wantQ, wantZ, scale) (generalized.jl:21-80) on copies, on the GPU:
-    the generalized Schur form of the pencil (A, B).  Real pencils are taken as complex
-    (the result is the complex generalized Schur form)."""
+    """ggschur!(A, B; wantQ, wantZ, scale) on copies, on the GPU: the generalized Schur form
+    of the pencil (A, B).  Complex pencils (generalized.jl:21-80): S, T upper triangular.
+    Real pencils (rgeneralized.jl:10-66): S quasi-triangular with 2 x 2 blocks for complex
+    eigenvalue pairs, T upper triangular, alpha complex and beta real."""
     ctx = ctx or get_context()
+    if not (np.iscomplexobj(A) or np.iscomplexobj(B)):
+        return _ggschur_real(A, B, wantQ, wantZ, scale, ctx)
     S = np.array(A, dtype=np.complex128, order="F", copy=True)
     T = np.array(B, dtype=np.complex128, order="F", copy=True)
     n = _checksquare(S)
@@ -140,8 +160,10 @@ def ggschur(A, B, wantQ=True, wantZ=True, scale=True, ctx=None):
 
 def ggschur_batched(As, Bs, wantQ=True, wantZ=True, scale=True, ctx=None):
     """ggschur! over a list of pencils in one launch (one CTA per pencil).  Returns a list
-    of GeneralizedSchur and the per-pencil status."""
+    of GeneralizedSchur and the per-pencil status.  All-real lists take the real QZ."""
     ctx = ctx or get_context()
+    if not any(np.iscomplexobj(a) for a in list(As) + list(Bs)):
+        return _ggschur_batched_real(As, Bs, wantQ, wantZ, scale, ctx)
     Ap, ns, offs, woffs = pack_batch(As, dtype=np.complex128)
     Bp, ns2, _, _ = pack_batch(Bs, dtype=np.complex128)
     if not np.array_equal(ns, ns2):
@@ -154,6 +176,35 @@ def ggschur_batched(As, Bs, wantQ=True, wantZ=True, scale=True, ctx=None):
     be = np.zeros(max(wlen, 1), dtype=np.complex128)
     st = np.zeros(len(ns), dtype=np.int32)
     rc = ctx.lib.gs_ggschur_batched_c64(ctx.handle, len(ns), _ptr(ns), _ptr(offs), plen, _ptr(Ap), _ptr(Bp), _ptr(Qp),
+                                        _ptr(Zp), _ptr(woffs), wlen, _ptr(al), _ptr(be), _ptr(st),
+                                        _capi.GS_SCALE if scale else 0)
+    if rc not in (GS_OK, GS_UNCONVERGED):
+        _raise(rc, ctx, "ggschur! (batched)")
+    out = []
+    for k, n in enumerate(ns):
+        n = int(n)
+        o, w = int(offs[k]), int(woffs[k])
+        sl = slice(o, o + n * n)
+        out.append(GeneralizedSchur(Ap[sl].reshape(n, n, order="F"), Bp[sl].reshape(n, n, order="F"),
+                                    al[w:w + n].copy(), be[w:w + n].copy(),
+                                    Qp[sl].reshape(n, n, order="F") if wantQ else None,
+                                    Zp[sl].reshape(n, n, order="F") if wantZ else None))
+    return out, st
+
+
+def _ggschur_batched_real(As, Bs, wantQ, wantZ, scale, ctx):
+    Ap, ns, offs, woffs = pack_batch(As, dtype=np.float64)
+    Bp, ns2, _, _ = pack_batch(Bs, dtype=np.float64)
+    if not np.array_equal(ns, ns2):
+        raise ArgumentError("matrices must have the same sizes")
+    plen = len(Ap)
+    wlen = int(ns.sum())
+    Qp = np.zeros(plen) if wantQ else None
+    Zp = np.zeros(plen) if wantZ else None
+    al = np.zeros(max(wlen, 1), dtype=np.complex128)
+    be = np.zeros(max(wlen, 1))
+    st = np.zeros(len(ns), dtype=np.int32)
+    rc = ctx.lib.gs_ggschur_batched_f64(ctx.handle, len(ns), _ptr(ns), _ptr(offs), plen, _ptr(Ap), _ptr(Bp), _ptr(Qp),
                                         _ptr(Zp), _ptr(woffs), wlen, _ptr(al), _ptr(be), _ptr(st),
                                         _capi.GS_SCALE if scale else 0)
     if rc not in (GS_OK, GS_UNCONVERGED):
@@ -296,6 +347,9 @@ def ggeigvecs(G, left=False, ctx=None):
     eigenvectors v_k with beta_k A v_k = alpha_k B v_k (back-transformed by G.Z), or left
     eigenvectors (back-transformed by G.Q); columns scaled to max |re|+|im| = 1."""
     ctx = ctx or get_context()
+    if not (np.iscomplexobj(G.S) or np.iscomplexobj(G.T)):
+        raise ArgumentError("eigenvectors of a real generalized Schur form are not provided; "
+                            "use the complex form (ggschur of the pencil cast to complex)")
     S = _fc(G.S, np.complex128)
     T = _fc(G.T, np.complex128)
     n = _checksquare(S)

@@ -310,6 +310,22 @@ GS_API int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t*
 GS_API int gs_gemm_f64_tc(gs_context* ctx, int64_t m, int64_t p, int64_t q, const double* A, int64_t lda,
                           int transA, const double* B, int64_t ldb, double* C, int64_t ldc, unsigned flags);
 
+/* ggschur!(A, B; wantQ, wantZ, scale) for a real pencil (rgeneralized.jl:10-66): qr!(B),
+ * the Hessenberg-triangular reduction (_hessenberg!, generalized.jl:84-113) and the real QZ
+ * iteration (_gqz!, rgeneralized.jl:68-808; single and double shifts, 2 x 2 blocks of complex
+ * eigenvalues with B diagonal there).  A <- S (quasi-triangular), B <- T (upper triangular,
+ * non-negative diagonal), Q and Z (n x n real; NULL when not wanted) with A = Q S Z^T and
+ * B = Q T Z^T; alpha (n complex, interleaved) and beta (n real) the generalized eigenvalues
+ * alpha ./ beta.  Leading dimension n.  GS_SCALE applies _scale! to A and B.  GS_UNCONVERGED
+ * at the reference's 100 n iteration limit. */
+GS_API int gs_ggschur_f64(gs_context* ctx, int64_t n, double* A, double* B, double* Q, double* Z, double* alpha,
+                          double* beta, unsigned flags);
+/* The same over a ragged batch (layout as gs_ggschur_batched_c64 with real matrices, complex
+ * alpha, real beta). */
+GS_API int gs_ggschur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                  int64_t packed_len, double* A, double* B, double* Q, double* Z, const int64_t* woffs,
+                                  int64_t wlen, double* alpha, double* beta, int32_t* status, unsigned flags);
+
 /* Eigenvectors of the generalized Schur decomposition of a complex pencil (the output
  * of gs_ggschur_c64: S, T upper triangular, A = Q S Z^H, B = Q T Z^H).  Replaces
  * geigvecs(S::GeneralizedSchur; left) (vectors.jl:22-33): right eigenvectors

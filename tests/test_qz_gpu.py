@@ -46,14 +46,14 @@ def _ratio(G):
 
 
 @pytest.mark.parametrize("n", [1, 2, 4, 32, 100])
-@pytest.mark.parametrize("kind", ["complex", "real"])
+@pytest.mark.parametrize("kind", ["complex", "real-as-complex"])
 def test_ggschur_random(gs, n, kind):
     rng = np.random.default_rng(8000 + n)
     if kind == "complex":
         A = rng.random((n, n)) + 1j * rng.random((n, n))
         B = rng.random((n, n)) + 1j * rng.random((n, n))
     else:
-        A, B = rng.random((n, n)), rng.random((n, n))
+        A, B = rng.random((n, n)).astype(complex), rng.random((n, n)).astype(complex)
     G = gs.ggschur(A, B)
     _gschurtest(A, B, G)
     S, T, al, be, Q, Z, st = po.ggschur(A, B)
@@ -144,14 +144,14 @@ def _same_columns(V, Vo, tol):
 
 
 @pytest.mark.parametrize("n", [1, 2, 4, 32, 100])
-@pytest.mark.parametrize("kind", ["complex", "real"])
+@pytest.mark.parametrize("kind", ["complex", "real-as-complex"])
 def test_ggeigvecs_random(gs, n, kind):
     rng = np.random.default_rng(8400 + n)
     if kind == "complex":
         A = rng.random((n, n)) + 1j * rng.random((n, n))
         B = rng.random((n, n)) + 1j * rng.random((n, n))
     else:
-        A, B = rng.random((n, n)), rng.random((n, n))
+        A, B = rng.random((n, n)).astype(complex), rng.random((n, n)).astype(complex)
     G = gs.ggschur(A, B)
     VR, VL = _evcheck(gs, A, B, G)
     _same_columns(VR, po.ggeigvecs(G.S, G.T, G.Z), 1e-9)
@@ -190,3 +190,108 @@ def test_ggeigvecs_singular_unit_vectors(gs):
         e[5] = 1
         np.testing.assert_array_equal(V[:, 5], e)
         _same_columns(V, po.ggeigvecs(S, T, left=left), 1e-9)
+
+
+
+# ---------------------------------------------------------------------------
+# real pencils: ggschur!(A::Real, B) (rgeneralized.jl:10-808)
+# ---------------------------------------------------------------------------
+def _gschurtest_real(A, B, G, tol=20.0, exact=True):
+    """The reference's real gschurtest (test/generalized.jl:40-60): S quasi-triangular, T
+    upper triangular, A = Q S Z' and B = Q T Z' to tol n ||A|| eps, Q and Z orthogonal; plus
+    the form the real QZ leaves: diag(T) >= 0, B diagonal on each 2 x 2 block of S, whose
+    eigenvalues form a complex pair."""
+    n = A.shape[0]
+    nA = max(np.linalg.norm(A), np.finfo(float).tiny)
+    S, T, Q, Z = G.S, G.T, G.Q, G.Z
+    assert not np.iscomplexobj(S) and not np.iscomplexobj(T)
+    assert np.all(np.tril(S, -2) == 0) and np.all(np.tril(T, -1) == 0)
+    assert np.linalg.norm(A - Q @ S @ Z.T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(B - Q @ T @ Z.T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Z @ Z.T) / (n * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Q @ Q.T) / (n * EPS) < tol
+    assert np.all(np.diag(T) >= 0)
+    for k in range(n - 1):
+        if S[k + 1, k] != 0:
+            assert T[k, k + 1] == 0 and T[k + 1, k] == 0
+            w1, w2 = G.alpha[k] / G.beta[k], G.alpha[k + 1] / G.beta[k + 1]
+            assert w1.imag != 0 and abs(w2 - np.conj(w1)) <= 1e-12 * abs(w1)
+    one = [k for k in range(n) if (k == 0 or S[k, k - 1] == 0) and (k == n - 1 or S[k + 1, k] == 0)]
+    for k in one:
+        if exact:
+            assert G.alpha[k] == S[k, k] and G.beta[k] == T[k, k]
+        else:  # factors rescaled by the caller (complex vs real division)
+            assert abs(G.alpha[k] - S[k, k]) <= 4 * EPS * abs(S[k, k]) and abs(G.beta[k] - T[k, k]) <= 4 * EPS * abs(T[k, k])
+
+
+def _real_pencil_check(gs, A, B, oracle_tol=1e-8):
+    G = gs.ggschur(A, B)
+    _gschurtest_real(A, B, G)
+    S, T, al, be, Q, Z, st = po.ggschur_real(A, B)
+    assert st == 0
+    assert _match(_ratio(G), np.where(be != 0, al / np.where(be != 0, be, 1), np.inf)) < oracle_tol
+    return G
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 8, 32, 100])
+def test_ggschur_real_random(gs, n):
+    """The reference's basic sanity case for Float64 (test/generalized.jl:62-81: rand pencils
+    of order 4 and 32) and other orders: eigenvalues as the oracle's real QZ and LAPACK's."""
+    rng = np.random.default_rng(8600 + n)
+    A, B = rng.random((n, n)), rng.random((n, n))
+    G = _real_pencil_check(gs, A, B)
+    import scipy.linalg as sl
+    assert _match(_ratio(G), sl.eigvals(A, B)) < 1e-8
+    np.testing.assert_array_equal(gs.eigvals(A, B), _ratio(G))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ggschur_real_singular(gs, seed):
+    """Real pencils with zero diagonal entries in A and in B (rotated by random orthogonal
+    matrices): infinite and zero eigenvalues through the singular-B branches of the real
+    iteration (split off the top, chase the zero to the bottom)."""
+    rng = np.random.default_rng(8700 + seed)
+    n = 32
+    n1 = n >> 2
+    n2 = n - 2 * n1
+    A0 = np.triu(rng.random((n, n)) - 0.5)
+    B0 = np.triu(rng.random((n, n)) - 0.5)
+    A0[np.arange(n1), np.arange(n1)] = 0
+    B0[np.arange(n1, n2), np.arange(n1, n2)] = 0
+    Qa, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    Qb, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A, B = Qa @ A0 @ Qa.T, Qb @ B0 @ Qb.T
+    G = gs.ggschur(A, B)
+    _gschurtest_real(A, B, G)
+    S, T, al, be, Q, Z, st = po.ggschur_real(A, B)
+    assert st == 0
+    nb = np.sum(np.abs(G.beta) <= 1e-10 * np.linalg.norm(B))
+    assert nb == np.sum(np.abs(be) <= 1e-10 * np.linalg.norm(B))
+
+
+def test_ggschur_real_batched_matches_single(gs):
+    rng = np.random.default_rng(8800)
+    ns = [1, 2, 5, 17, 40, 64]
+    As = [rng.standard_normal((n, n)) for n in ns]
+    Bs = [rng.standard_normal((n, n)) for n in ns]
+    out, st = gs.ggschur_batched(As, Bs)
+    assert np.all(st == 0)
+    for A, B, Gb in zip(As, Bs, out):
+        G = gs.ggschur(A, B)
+        np.testing.assert_array_equal(Gb.S, G.S)
+        np.testing.assert_array_equal(Gb.T, G.T)
+        np.testing.assert_array_equal(Gb.Q, G.Q)
+        np.testing.assert_array_equal(Gb.Z, G.Z)
+        _gschurtest_real(A, B, Gb)
+
+
+@pytest.mark.parametrize("s", [1e-300, 1e300])
+def test_ggschur_real_scaled(gs, s):
+    """_scale! of A and B (rgeneralized.jl:25-33) and the unscaling of S, T, alpha, beta."""
+    rng = np.random.default_rng(8900)
+    A0, B0 = rng.standard_normal((20, 20)), rng.standard_normal((20, 20))
+    G = gs.ggschur(s * A0, s * B0)
+    assert np.all(np.isfinite(G.S)) and np.all(np.isfinite(G.T))
+    G0 = gs.ggschur(A0, B0)
+    assert _match(_ratio(G), _ratio(G0)) < 1e-10
+    _gschurtest_real(A0, B0, gs.GeneralizedSchur(G.S / s, G.T / s, G.alpha / s, G.beta / s, G.Q, G.Z), exact=False)
