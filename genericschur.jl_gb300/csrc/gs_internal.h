@@ -327,6 +327,11 @@ cudaError_t launch_sylv_tiled(int n, int nT, const double* At, double* W, const 
 size_t ggevc_ws_bytes(int n);
 cudaError_t launch_ggevc(int n, const double2* S, const double2* P, const double2* M, int left, double2* V, void* ws,
                          cudaStream_t s);
+// Eigenvectors of a real generalized Schur pair (rgevc.cu): complex V (n x n, ld n),
+// right (left = 0, M = Z) or left (left = 1, M = Q); M may be null; ws of rgevc_ws_bytes.
+size_t rgevc_ws_bytes(int n);
+cudaError_t launch_rgevc(int n, const double* S, const double* P, const double* M, int left, double2* V, void* ws,
+                         cudaStream_t s);
 // FP64 product on the BF16 tensor cores by exact splitting (gemm_f64_tc.cu):
 // C (m x p, ldc) = op(A) (m x q) B (q x p), column-major; ws of gemm_tc_ws_bytes bytes.
 // The error word (gemm_tc_err_word; the caller zeroes it) becomes nonzero when a launch's

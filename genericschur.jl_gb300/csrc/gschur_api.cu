@@ -1140,6 +1140,52 @@ int gs_ggeigvecs_c64(gs_context* ctx, int64_t n, const double* S, const double* 
   return GS_OK;
 }
 
+int gs_ggeigvecs_f64(gs_context* ctx, int64_t n, const double* S, const double* T, const double* Q, const double* Z,
+                     double* VR, double* VL, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 15)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (n == 0) return GS_OK;
+  if (!S || !T) return set_err(ctx, GS_BADARG, "null array argument");
+  if (!VR && !VL) return GS_OK;
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n;
+  const int N = (int)n;
+  Arena ar;
+  const size_t o_S = ar.take<double>(dev ? 1 : nn), o_T = ar.take<double>(dev ? 1 : nn);
+  const size_t o_Q = ar.take<double>(dev || !Q ? 1 : nn), o_Z = ar.take<double>(dev || !Z ? 1 : nn);
+  const size_t o_V = ar.take<double2>(dev ? 1 : nn), o_ws = ar.take<char>(rgevc_ws_bytes(N));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const double *dS = S, *dT = T, *dQ = Q, *dZ = Z;
+  if (!dev) {
+    CK(cudaMemcpyAsync(base + o_S, S, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_T, T, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (Q) CK(cudaMemcpyAsync(base + o_Q, Q, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (Z) CK(cudaMemcpyAsync(base + o_Z, Z, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    dS = (const double*)(base + o_S);
+    dT = (const double*)(base + o_T);
+    dQ = Q ? (const double*)(base + o_Q) : nullptr;
+    dZ = Z ? (const double*)(base + o_Z) : nullptr;
+  }
+  CK(cudaEventRecord(ctx->t0, s));
+  for (int left = 0; left < 2; ++left) {
+    double* out = left ? VL : VR;
+    if (!out) continue;
+    double2* dV = dev ? (double2*)out : (double2*)(base + o_V);
+    cudaError_t e = launch_rgevc(N, dS, dT, left ? dQ : dZ, left, dV, base + o_ws, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "generalized eigenvectors: %s", cudaGetErrorString(e));
+    if (!dev) CK(cudaMemcpyAsync(out, dV, nn * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  CK(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // FP64 product on the BF16 tensor cores (gemm_f64_tc.cu)
 // ---------------------------------------------------------------------------

@@ -348,8 +348,21 @@ def ggeigvecs(G, left=False, ctx=None):
     eigenvectors (back-transformed by G.Q); columns scaled to max |re|+|im| = 1."""
     ctx = ctx or get_context()
     if not (np.iscomplexobj(G.S) or np.iscomplexobj(G.T)):
-        raise ArgumentError("eigenvectors of a real generalized Schur form are not provided; "
-                            "use the complex form (ggschur of the pencil cast to complex)")
+        # real pencil (vectors.jl:1040-1513): complex vectors, conjugate columns for a pair
+        S = _fc(G.S, np.float64)
+        T = _fc(G.T, np.float64)
+        n = _checksquare(S)
+        V = np.zeros((n, n), dtype=np.complex128, order="F")
+        if n == 0:
+            return V
+        M = G.Q if left else G.Z
+        M = _fc(M, np.float64) if M is not None else None
+        Q, Z = (M, None) if left else (None, M)
+        outR, outL = (None, V) if left else (V, None)
+        rc = ctx.lib.gs_ggeigvecs_f64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(outR), _ptr(outL), 0)
+        if rc != GS_OK:
+            _raise(rc, ctx, "geigvecs(GeneralizedSchur)")
+        return V
     S = _fc(G.S, np.complex128)
     T = _fc(G.T, np.complex128)
     n = _checksquare(S)

@@ -298,6 +298,17 @@ GS_API int gs_ggschur_batched_c64(gs_context* ctx, int64_t count, const int32_t*
                                   int64_t packed_len, double* A, double* B, double* Q, double* Z, const int64_t* woffs,
                                   int64_t wlen, double* alpha, double* beta, int32_t* status, unsigned flags);
 
+/* Eigenvectors of the generalized Schur decomposition of a real pencil (the output of
+ * gs_ggschur_f64: S quasi-triangular, T upper triangular, A = Q S Z^T, B = Q T Z^T).
+ * Replaces geigvecs(S::GeneralizedSchur{<:Real}; left) (vectors.jl:22-33): right vectors
+ * (_geigvecs, vectors.jl:1040-1283) into VR, back-transformed by Z; left vectors
+ * (_gleigvecs, vectors.jl:1285-1513) into VL, back-transformed by Q.  VR, VL are complex
+ * n x n (interleaved); a complex pair's second column is the conjugate of the first.
+ * Either output may be NULL; Q / Z NULL give the eigenvectors of (S, T).  Columns scaled to
+ * max |re| + |im| = 1.  Host pointers, or device with GS_DEVICE. */
+GS_API int gs_ggeigvecs_f64(gs_context* ctx, int64_t n, const double* S, const double* T, const double* Q,
+                            const double* Z, double* VR, double* VL, unsigned flags);
+
 /* FP64 matrix product C (m x p, ldc) = op(A) (m x q) * B (q x p), op(A) = A (transA = 0)
  * or A^T (transA = 1), column-major, computed on the BF16 tensor cores by exact splitting
  * (Ozaki scheme: 10 slices of 6 bits per row of op(A) and column of B, exact FP32

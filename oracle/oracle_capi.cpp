@@ -259,6 +259,16 @@ int or_ggschur_d(int n, double* a, double* b, double* q, double* z, double* alr,
   return ggschur_real<double>(n, a, n, b, n, q, z, alr, ali, be, scale != 0, 100LL * n);
 }
 
+// Eigenvectors of a real generalized Schur pair (src/vectors.jl:1040-1513): right (left = 0,
+// back-transformed by X = Z) or left (left = 1, X = Q); X may be null.  V n x n complex.
+int or_rgevc_d(int n, const double* s, const double* p, const double* x, double* v, int left) {
+  if (left)
+    rgevc_left<double>(n, s, p, x, (zc*)v);
+  else
+    rgevc_right<double>(n, s, p, x, (zc*)v);
+  return 0;
+}
+
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {
   gs2x2<double>(h, cs, sn, &w[0], &w[1], &w[2], &w[3]);
   return 0;

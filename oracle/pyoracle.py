@@ -54,6 +54,7 @@ def lib():
             "or_ggschur_z": [_i, _p, _p, _p, _p, _p, _p, _i],
             "or_ggevc_z": [_i, _p, _p, _p, _p, _i],
             "or_ggschur_d": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
+            "or_rgevc_d": [_i, _p, _p, _p, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -349,3 +350,15 @@ def ggschur_real(A, B, scale=True):
     be = np.zeros(max(n, 1))
     st = lib().or_ggschur_d(n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(alr), _ptr(ali), _ptr(be), int(scale))
     return S, T, (alr + 1j * ali)[:n], be[:n], Q, Z, st
+
+
+def rgeigvecs(S, T, X=None, left=False):
+    """Eigenvectors of a real generalized Schur pair (vectors.jl:1040-1513), complex
+    columns (a complex pair's second column is the conjugate of the first)."""
+    Sf = _f(S, np.float64)
+    Tf = _f(T, np.float64)
+    n = Sf.shape[0]
+    Xf = _f(X, np.float64) if X is not None else None
+    V = np.zeros((n, n), dtype=np.complex128, order="F")
+    lib().or_rgevc_d(n, _ptr(Sf), _ptr(Tf), _ptr(Xf), _ptr(V), int(left))
+    return V

@@ -10,6 +10,7 @@
 #include <vector>
 #include "gschur_oracle.hpp"
 #include "hermitian_oracle.hpp"
+#include "eigvecs_oracle.hpp"
 
 namespace orc {
 
@@ -1365,6 +1366,370 @@ int ggschur_real(int n, R* a, int lda, R* b, int ldb, R* q, R* z, R* alr, R* ali
   return st;
 #undef A_
 #undef B_
+}
+
+
+// ---------------------------------------------------------------------------
+// Eigenvectors of a real generalized Schur pair (S quasi-triangular, P upper triangular),
+// the reference's dtgevc restatements in complex arithmetic:
+//   right _geigvecs(S, P[, Z])   src/vectors.jl:1040-1283
+//   left  _gleigvecs(S, P[, Q])  src/vectors.jl:1285-1513
+// with _xsolve (src/util.jl:698-751) for the 1 x 1 / 2 x 2 diagonal blocks.
+// ---------------------------------------------------------------------------
+
+// _xsolve(a, A, d, b, B, smin): (a A - b D) X = s B, A na x na real (column-major, ld na),
+// D = diag(d), b complex; B overwritten with X; returns s.
+template <class R>
+R xsolve_gen(R a, const R* A, int na, const R* d, cx<R> b, cx<R>* B, R smin, R* xnorm, bool* perturbed) {
+  typedef cx<R> C;
+  R s = 1;
+  const R small = R(2) * safemin<R>();
+  const R bignum = s / small;
+  smin = m_max(smin, small);
+  *perturbed = false;
+  if (na == 1) {
+    R csr = a * A[0] - b.re * d[0];
+    R csi = -b.im * d[0];
+    R cnorm = m_abs(csr) + m_abs(csi);
+    if (cnorm < smin) { *perturbed = true; csr = smin; csi = 0; cnorm = smin; }
+    const R bnorm = abs1(B[0]);
+    if (cnorm < R(1) && bnorm > R(1) && bnorm > bignum * cnorm) s = R(1) / bnorm;
+    const C x = (B[0] * s) / C(csr, csi);
+    *xnorm = abs1(x);
+    B[0] = x;
+    return s;
+  }
+  R cmax = 0;
+  C m[4];
+  for (int j = 1; j <= na; ++j)
+    for (int i = 1; i <= na; ++i) {
+      C zz = C(a * A[(i - 1) + (j - 1) * na]);
+      if (i == j) zz -= b * d[i - 1];
+      m[(i - 1) + (j - 1) * na] = zz;
+      cmax = m_max(cmax, abs1(zz));
+    }
+  if (cmax < smin) {
+    *perturbed = true;
+    R bnorm = 0;
+    for (int i = 0; i < na; ++i) bnorm = m_max(bnorm, abs1(B[i]));
+    if (smin < R(1) && bnorm > R(1) && bnorm > bignum * smin) s = R(1) / bnorm;
+    const R t1 = s / smin;
+    for (int i = 0; i < na; ++i) B[i] *= t1;
+  } else {
+    bool pert2 = false;
+    s = safe_lu_solve<R>(na, m, B, &pert2);
+  }
+  *xnorm = norm2_cplx(B, na);
+  return s;
+}
+
+// scaled coefficients of a real eigenvalue k (vectors.jl:1097-1139 / 1336-1378)
+template <class R>
+void rg_coeffs_real(const R* S, const R* P, int n, int k, R Anorm, R Bnorm, R ascale, R bscale, R* ao, R* bro) {
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = safemin<R>();
+  const R smallnum = safmin * (R(n) / ulp);
+  const R bigx = R(1) / smallnum;
+  const R skk = S[(k - 1) + (long long)(k - 1) * n], pkk = P[(k - 1) + (long long)(k - 1) * n];
+  const R t = R(1) / m_max(m_max(m_abs(skk) * ascale, m_abs(pkk) * bscale), safmin);
+  const R sar = (t * skk) * ascale;
+  const R sb = (t * pkk) * bscale;
+  R a = sb * ascale, br = sar * bscale;
+  const bool lsa = m_abs(sb) >= safmin && m_abs(a) < smallnum;
+  const bool lsb = m_abs(sar) >= safmin && m_abs(br) < smallnum;
+  R s = R(1);
+  if (lsa) s = (smallnum / m_abs(sb)) * m_min(Anorm, bigx);
+  if (lsb) s = m_max(s, (smallnum / m_abs(sar)) * m_min(Bnorm, bigx));
+  if (lsa || lsb) {
+    s = m_min(s, R(1) / (safmin * m_max(m_max(R(1), m_abs(a)), m_abs(br))));
+    a = lsa ? ascale * (s * sb) : a * s;
+    br = lsb ? bscale * (s * sar) : br * s;
+  }
+  *ao = a;
+  *bro = br;
+}
+
+// scaling of a complex pair's (a, br, bi) (vectors.jl:1163-1183 / 1401-1421)
+template <class R>
+void rg_scale_pair(R* a, R* br, R* bi, R ascale, R bscale) {
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = safemin<R>();
+  const R aa = m_abs(*a), ba = m_abs(*br) + m_abs(*bi);
+  R scale = R(1);
+  if (aa * ulp < safmin && aa >= safmin) scale = (safmin / ulp) / aa;
+  if (ba * ulp < safmin && ba >= safmin) scale = m_max(scale, (safmin / ulp) / ba);
+  if (safmin * aa > ascale) scale = ascale / (safmin * aa);
+  if (safmin * ba > bscale) scale = m_min(scale, bscale / (safmin * ba));
+  if (scale != R(1)) { *a *= scale; *br *= scale; *bi *= scale; }
+}
+
+template <class R>
+void rg_norms(int n, const R* S, const R* P, std::vector<R>& sn, std::vector<R>& pn, R* An, R* Bn) {
+  sn.assign(n, R(0));
+  pn.assign(n, R(0));
+  R a = m_abs(S[0]), b = m_abs(P[0]);
+  for (int j = 2; j <= n; ++j) {
+    for (int i = 1; i <= j - 1; ++i) {
+      sn[j - 1] += m_abs(S[(i - 1) + (long long)(j - 1) * n]);
+      pn[j - 1] += m_abs(P[(i - 1) + (long long)(j - 1) * n]);
+    }
+    a = m_max(a, sn[j - 1] + m_abs(S[(j - 1) + (long long)(j - 1) * n]));
+    b = m_max(b, pn[j - 1] + m_abs(P[(j - 1) + (long long)(j - 1) * n]));
+  }
+  *An = a;
+  *Bn = b;
+}
+
+template <class R>
+void rgevc_right(int n, const R* S, const R* P, const R* Z, cx<R>* V) {
+  typedef cx<R> C;
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = safemin<R>();
+  const R bignum = R(1) / (R(n) * safmin);
+  const R safety = R(100);
+  std::vector<R> sn, pn;
+  R Anorm, Bnorm;
+  rg_norms(n, S, P, sn, pn, &Anorm, &Bnorm);
+  const R ascale = R(1) / m_max(Anorm, safmin), bscale = R(1) / m_max(Bnorm, safmin);
+  std::vector<C> v(n);
+#define SS(i, j) S[((i) - 1) + (long long)((j) - 1) * n]
+#define PP(i, j) P[((i) - 1) + (long long)((j) - 1) * n]
+  int idx = n + 1;
+  bool inpair = false;
+  for (int je = n; je >= 1; --je) {
+    if (inpair) { inpair = false; continue; }
+    int nw = 1;
+    if (je > 1 && SS(je, je - 1) != R(0)) { inpair = true; nw = 2; }
+    R a, br, bi, aa, ba, xmax;
+    if (!inpair) {
+      if (m_abs(SS(je, je)) <= safmin && m_abs(PP(je, je)) <= safmin) {
+        idx -= 1;
+        cx<R>* col = V + (long long)(idx - 1) * n;
+        for (int r = 0; r < n; ++r) col[r] = C(R(0));
+        col[idx - 1] = C(R(1));
+        continue;
+      }
+      rg_coeffs_real(S, P, n, je, Anorm, Bnorm, ascale, bscale, &a, &br);
+      bi = R(0);
+      aa = m_abs(a);
+      ba = m_abs(br);
+      for (int r = 0; r < n; ++r) v[r] = C(R(0));
+      v[je - 1] = C(R(1));
+      xmax = R(1);
+      for (int jr = 1; jr <= je - 1; ++jr) v[jr - 1] = C(br * PP(jr, je) - a * SS(jr, je));
+    } else {
+      R s1, s2, wr1, wr2, wi;
+      ggs_2x2(&SS(je - 1, je - 1), n, &PP(je - 1, je - 1), n, safmin * safety, &s1, &s2, &wr1, &wr2, &wi);
+      a = s1;
+      br = wr1;
+      bi = wi;
+      rg_scale_pair(&a, &br, &bi, ascale, bscale);
+      aa = m_abs(a);
+      ba = m_abs(br) + m_abs(bi);
+      for (int r = 0; r < n; ++r) v[r] = C(R(0));
+      R t1 = a * SS(je, je - 1);
+      const R t2r = a * SS(je, je) - br * PP(je, je), t2i = -bi * PP(je, je);
+      if (m_abs(t1) > m_abs(t2r) + m_abs(t2i)) {
+        v[je - 1] = C(R(1));
+        v[je - 2] = -(C(t2r, t2i)) / C(t1);
+      } else {
+        v[je - 2] = C(R(1));
+        t1 = a * SS(je - 1, je);
+        v[je - 1] = C((br * PP(je - 1, je - 1) - a * SS(je - 1, je - 1)) / t1, bi * PP(je - 1, je - 1) / t1);
+      }
+      xmax = m_max(abs1(v[je - 1]), abs1(v[je - 2]));
+      const C bc(br, bi);
+      const C ca = a * v[je - 2], cb = bc * v[je - 2], c2a = a * v[je - 1], c2b = bc * v[je - 1];
+      for (int jr = 1; jr <= je - 2; ++jr)
+        v[jr - 1] = -ca * SS(jr, je - 1) + cb * PP(jr, je - 1) - c2a * SS(jr, je) + c2b * PP(jr, je);
+    }
+    const R dmin = m_max(m_max(ulp * aa * Anorm, ulp * ba * Bnorm), safmin);
+    const C bc(br, bi);
+    bool in2x2 = false;
+    for (int j = je - nw; j >= 1; --j) {
+      if (!in2x2 && j > 1 && SS(j, j - 1) != R(0)) { in2x2 = true; continue; }
+      const int na = in2x2 ? 2 : 1;
+      R dg[2] = {PP(j, j), na == 2 ? PP(j + 1, j + 1) : R(0)};
+      R blk[4];
+      for (int q = 0; q < na; ++q)
+        for (int p = 0; p < na; ++p) blk[p + q * na] = SS(j + p, j + q);
+      C x[2] = {v[j - 1], na == 2 ? v[j] : C(R(0))};
+      R t1;
+      bool pert;
+      const R scale = xsolve_gen<R>(a, blk, na, dg, bc, x, dmin, &t1, &pert);
+      // _xsolve overwrites its right-hand side, a view of v (vectors.jl:1229-1236), so the
+      // rescaling of v[1:je] that follows also applies to the new solution entries
+      for (int q = 0; q < na; ++q) v[j - 1 + q] = x[q];
+      if (scale < R(1))
+        for (int r = 0; r < je; ++r) v[r] = scale * v[r];
+      xmax = m_max(scale * xmax, t1);
+      if (j > 1) {
+        const R xscale = R(1) / m_max(R(1), xmax);
+        t1 = m_max(t1, aa * sn[j - 1] + ba * pn[j - 1]);
+        if (in2x2) t1 = m_max(t1, aa * sn[j] + ba * pn[j]);
+        t1 = m_max(m_max(t1, aa), ba);
+        if (t1 > bignum * xscale) {
+          for (int r = 0; r < je; ++r) v[r] = xscale * v[r];
+          xmax *= xscale;
+        }
+        for (int ja = 1; ja <= na; ++ja) {
+          const C ca = a * v[j + ja - 2], cb = bc * v[j + ja - 2];
+          for (int i = 1; i <= j - 1; ++i) v[i - 1] = v[i - 1] - ca * SS(i, j + ja - 1) + cb * PP(i, j + ja - 1);
+        }
+      }
+      in2x2 = false;
+    }
+    idx -= nw;
+    cx<R>* col = V + (long long)(idx - 1) * n;
+    int iend;
+    if (Z) {
+      for (int r = 0; r < n; ++r) {
+        C acc(R(0));
+        for (int k = 0; k < n; ++k) acc += Z[r + (long long)k * n] * v[k];
+        col[r] = acc;
+      }
+      iend = n;
+    } else {
+      for (int r = 0; r < n; ++r) col[r] = v[r];
+      iend = je;
+    }
+    for (int jr = 1; jr <= iend; ++jr) xmax = m_max(xmax, abs1(col[jr - 1]));
+    if (xmax > safmin) {
+      const R xs = R(1) / xmax;
+      for (int jr = 1; jr <= iend; ++jr) col[jr - 1] = xs * col[jr - 1];
+    }
+    if (inpair) {
+      cx<R>* col2 = V + (long long)idx * n;
+      for (int r = 0; r < n; ++r) col2[r] = conj(col[r]);
+    }
+  }
+#undef SS
+#undef PP
+}
+
+template <class R>
+void rgevc_left(int n, const R* S, const R* P, const R* Q, cx<R>* V) {
+  typedef cx<R> C;
+  const R ulp = std::numeric_limits<R>::epsilon();
+  const R safmin = safemin<R>();
+  const R bignum = R(1) / (R(n) * safmin);
+  const R safety = R(100);
+  std::vector<R> sn, pn;
+  R Anorm, Bnorm;
+  rg_norms(n, S, P, sn, pn, &Anorm, &Bnorm);
+  const R ascale = R(1) / m_max(Anorm, safmin), bscale = R(1) / m_max(Bnorm, safmin);
+  std::vector<C> v(n);
+#define SS(i, j) S[((i) - 1) + (long long)((j) - 1) * n]
+#define PP(i, j) P[((i) - 1) + (long long)((j) - 1) * n]
+  int idx = 0;
+  bool inpair = false;
+  for (int je = 1; je <= n; ++je) {
+    if (inpair) { inpair = false; continue; }
+    int nw = 1;
+    if (je < n && SS(je + 1, je) != R(0)) { inpair = true; nw = 2; }
+    R a, br, bi, aa, ba, xmax;
+    if (!inpair) {
+      if (m_abs(SS(je, je)) <= safmin && m_abs(PP(je, je)) <= safmin) {
+        idx += 1;
+        cx<R>* col = V + (long long)(idx - 1) * n;
+        for (int r = 0; r < n; ++r) col[r] = C(R(0));
+        col[idx - 1] = C(R(1));
+        continue;
+      }
+      rg_coeffs_real(S, P, n, je, Anorm, Bnorm, ascale, bscale, &a, &br);
+      bi = R(0);
+      aa = m_abs(a);
+      ba = m_abs(br);
+      for (int r = 0; r < n; ++r) v[r] = C(R(0));
+      v[je - 1] = C(R(1));
+      xmax = R(1);
+    } else {
+      R s1, s2, wr1, wr2, wi;
+      ggs_2x2(&SS(je, je), n, &PP(je, je), n, safmin * safety, &s1, &s2, &wr1, &wr2, &wi);
+      a = s1;
+      br = wr1;
+      bi = -wi;
+      rg_scale_pair(&a, &br, &bi, ascale, bscale);
+      aa = m_abs(a);
+      ba = m_abs(br) + m_abs(bi);
+      for (int r = 0; r < n; ++r) v[r] = C(R(0));
+      R t1 = a * SS(je + 1, je);
+      const R t2r = a * SS(je, je) - br * PP(je, je), t2i = -bi * PP(je, je);
+      if (m_abs(t1) > m_abs(t2r) + m_abs(t2i)) {
+        v[je - 1] = C(R(1));
+        v[je] = -(C(t2r, t2i)) / C(t1);
+      } else {
+        v[je] = C(R(1));
+        t1 = a * SS(je, je + 1);
+        v[je - 1] = C((br * PP(je + 1, je + 1) - a * SS(je + 1, je + 1)) / t1, bi * PP(je + 1, je + 1) / t1);
+      }
+      xmax = m_max(abs1(v[je - 1]), abs1(v[je]));
+    }
+    const R dmin = m_max(m_max(ulp * aa * Anorm, ulp * ba * Bnorm), safmin);
+    const C bc(br, bi);
+    bool in2x2 = false;
+    for (int j = je + nw; j <= n; ++j) {
+      if (in2x2) { in2x2 = false; continue; }
+      int na = 1;
+      if (j < n && SS(j + 1, j) != R(0)) { in2x2 = true; na = 2; }
+      R dg[2] = {PP(j, j), na == 2 ? PP(j + 1, j + 1) : R(0)};
+      const R xscale = R(1) / m_max(R(1), xmax);
+      R t1 = m_max(m_max(sn[j - 1], pn[j - 1]), aa * sn[j - 1] + ba * sn[j - 1]);
+      if (in2x2) t1 = m_max(m_max(t1, sn[j]), m_max(pn[j], aa * sn[j] + ba * sn[j]));
+      if (t1 > bignum * xscale) {
+        for (int r = je; r <= j - 1; ++r) v[r - 1] = v[r - 1] * xscale;
+        xmax *= xscale;
+      }
+      C sumS[2] = {C(R(0)), C(R(0))}, sumP[2] = {C(R(0)), C(R(0))};
+      const int jx = j + na - 1;
+      for (int jr = je; jr <= j - 1; ++jr)
+        for (int q = 0; q <= jx - j; ++q) {
+          sumS[q] = sumS[q] + SS(jr, j + q) * v[jr - 1];
+          sumP[q] = sumP[q] + PP(jr, j + q) * v[jr - 1];
+        }
+      C y[2];
+      for (int q = 0; q < na; ++q) y[q] = -a * sumS[q] + bc * sumP[q];
+      // the block of S', i.e. the transposed block of S
+      R blk[4];
+      for (int q = 0; q < na; ++q)
+        for (int p = 0; p < na; ++p) blk[p + q * na] = SS(j + q, j + p);
+      bool pert;
+      const R scale = xsolve_gen<R>(a, blk, na, dg, bc, y, dmin, &t1, &pert);
+      for (int q = 0; q < na; ++q) v[j - 1 + q] = y[q];
+      if (scale < R(1)) {
+        for (int r = je; r <= j - 1; ++r) v[r - 1] = scale * v[r - 1];
+        xmax *= scale;
+      }
+      xmax = m_max(xmax, t1);
+    }
+    idx += 1;
+    cx<R>* col = V + (long long)(idx - 1) * n;
+    int ibegin;
+    if (Q) {
+      for (int r = 0; r < n; ++r) {
+        C acc(R(0));
+        for (int k = 0; k < n; ++k) acc += Q[r + (long long)k * n] * v[k];
+        col[r] = acc;
+      }
+      ibegin = 1;
+    } else {
+      for (int r = 0; r < n; ++r) col[r] = v[r];
+      ibegin = je;
+    }
+    xmax = R(0);
+    for (int jr = ibegin; jr <= n; ++jr) xmax = m_max(xmax, abs1(col[jr - 1]));
+    if (xmax > safmin) {
+      const R xs = R(1) / xmax;
+      for (int jr = ibegin; jr <= n; ++jr) col[jr - 1] = xs * col[jr - 1];
+    }
+    if (inpair) {
+      cx<R>* col2 = V + (long long)idx * n;
+      for (int r = 0; r < n; ++r) col2[r] = conj(col[r]);
+    }
+    idx += nw - 1;
+  }
+#undef SS
+#undef PP
 }
 
 }  // namespace orc

@@ -295,3 +295,66 @@ def test_ggschur_real_scaled(gs, s):
     G0 = gs.ggschur(A0, B0)
     assert _match(_ratio(G), _ratio(G0)) < 1e-10
     _gschurtest_real(A0, B0, gs.GeneralizedSchur(G.S / s, G.T / s, G.alpha / s, G.beta / s, G.Q, G.Z), exact=False)
+
+
+
+def _evcheck_real(gs, A, B, G, tol=20.0):
+    """The eigenvector half of the reference's real gschurtest (test/generalized.jl:55-59):
+    ||(A VR) diag(beta) - (B VR) diag(alpha)|| and ||diag(beta) (VL' A) - diag(alpha) (VL' B)||
+    below tol n ||A|| eps."""
+    n = A.shape[0]
+    nA = max(np.linalg.norm(A), np.finfo(float).tiny)
+    VR = gs.geigvecs(G)
+    VL = gs.geigvecs(G, left=True)
+    r = np.linalg.norm((A @ VR) @ np.diag(G.beta) - (B @ VR) @ np.diag(G.alpha))
+    assert r / (n * nA * EPS) < tol
+    r = np.linalg.norm(np.diag(G.beta) @ (VL.conj().T @ A) - np.diag(G.alpha) @ (VL.conj().T @ B))
+    assert r / (n * nA * EPS) < tol
+    return VR, VL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 8, 32, 100])
+def test_ggeigvecs_real(gs, n):
+    """Real pencils: the reference's eigenvector check, and the same columns as the oracle's
+    restatement on the same Schur pair (with and without the back-transform)."""
+    rng = np.random.default_rng(9100 + n)
+    A, B = rng.random((n, n)), rng.random((n, n))
+    G = gs.ggschur(A, B)
+    VR, VL = _evcheck_real(gs, A, B, G)
+    _same_columns(VR, po.rgeigvecs(G.S, G.T, G.Z), 1e-9)
+    _same_columns(VL, po.rgeigvecs(G.S, G.T, G.Q, left=True), 1e-9)
+    Gt = gs.GeneralizedSchur(G.S, G.T, G.alpha, G.beta, None, None)
+    _same_columns(gs.geigvecs(Gt), po.rgeigvecs(G.S, G.T), 1e-9)
+    _same_columns(gs.geigvecs(Gt, left=True), po.rgeigvecs(G.S, G.T, left=True), 1e-9)
+    for k in range(n - 1):
+        if G.S[k + 1, k] != 0:
+            np.testing.assert_array_equal(VR[:, k + 1], VR[:, k].conj())
+            np.testing.assert_array_equal(VL[:, k + 1], VL[:, k].conj())
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_ggeigvecs_real_singular(gs, seed):
+    rng = np.random.default_rng(8700 + seed)
+    n = 32
+    n1 = n >> 2
+    n2 = n - 2 * n1
+    A0 = np.triu(rng.random((n, n)) - 0.5)
+    B0 = np.triu(rng.random((n, n)) - 0.5)
+    A0[np.arange(n1), np.arange(n1)] = 0
+    B0[np.arange(n1, n2), np.arange(n1, n2)] = 0
+    Qa, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    Qb, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A, B = Qa @ A0 @ Qa.T, Qb @ B0 @ Qb.T
+    G = gs.ggschur(A, B)
+    _evcheck_real(gs, A, B, G)
+    # eigenvectors of singular pencils can be ill-conditioned: the tolerance is ten times
+    # the change of the oracle's own vectors under 1-ulp relative perturbations of S and T
+    for left, M in ((False, G.Z), (True, G.Q)):
+        Vo = po.rgeigvecs(G.S, G.T, M, left=left)
+        sens = 0.0
+        for t in range(3):
+            r = np.random.default_rng(t)
+            Sp = G.S * (1 + EPS * r.standard_normal(G.S.shape))
+            Tp = G.T * (1 + EPS * r.standard_normal(G.T.shape))
+            sens = max(sens, float(np.max(np.abs(po.rgeigvecs(Sp, Tp, M, left=left) - Vo))))
+        _same_columns(gs.geigvecs(G, left=left), Vo, max(1e-9, 10 * sens))
