@@ -125,6 +125,9 @@ struct QzBatch {
   int n1;                  // ns == null: one pencil of order n1 at offset 0
 };
 cudaError_t launch_ggschur(const QzBatch& bt, int num_sms, cudaStream_t s);
+// gordschur! of a complex generalized Schur form (qz.cu); status 0 or 1 + j1 of a rejected swap.
+cudaError_t launch_ggordschur_cplx(int n, double2* S, double2* T, double2* Q, double2* Z, const int* select, int scale,
+                                   double2* alpha, double2* beta, int* status, cudaStream_t s);
 // Real pencils (qz_real.cu): A, B, Q, Z real; alpha complex, beta real.
 struct QzrBatch {
   int count;

@@ -1140,6 +1140,59 @@ int gs_ggeigvecs_c64(gs_context* ctx, int64_t n, const double* S, const double* 
   return GS_OK;
 }
 
+int gs_ggordschur_c64(gs_context* ctx, int64_t n, double* S, double* T, double* Q, double* Z, const int32_t* select,
+                      double* alpha, double* beta, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 15)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (n == 0) return GS_OK;
+  if (!S || !T || !Q || !Z || !select || !alpha || !beta) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n, zb = sizeof(double2);
+  Arena ar;
+  const size_t o_S = ar.take<double2>(dev ? 1 : nn), o_T = ar.take<double2>(dev ? 1 : nn),
+               o_Q = ar.take<double2>(dev ? 1 : nn), o_Z = ar.take<double2>(dev ? 1 : nn),
+               o_al = ar.take<double2>(dev ? 1 : n), o_be = ar.take<double2>(dev ? 1 : n), o_sel = ar.take<int>(n),
+               o_st = ar.take<int>(4);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double2* dS = dev ? (double2*)S : (double2*)(base + o_S);
+  double2* dT = dev ? (double2*)T : (double2*)(base + o_T);
+  double2* dQ = dev ? (double2*)Q : (double2*)(base + o_Q);
+  double2* dZ = dev ? (double2*)Z : (double2*)(base + o_Z);
+  double2* dal = dev ? (double2*)alpha : (double2*)(base + o_al);
+  double2* dbe = dev ? (double2*)beta : (double2*)(base + o_be);
+  int* dsel = (int*)(base + o_sel);
+  int* dst = (int*)(base + o_st);
+  if (!dev) {
+    CK(cudaMemcpyAsync(dS, S, zb * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dT, T, zb * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dQ, Q, zb * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dZ, Z, zb * nn, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemcpyAsync(dsel, select, sizeof(int) * n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_ggordschur_cplx((int)n, dS, dT, dQ, dZ, dsel, (flags & GS_SCALE) ? 1 : 0, dal, dbe, dst, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!dev) {
+    CK(cudaMemcpyAsync(S, dS, zb * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(T, dT, zb * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Q, dQ, zb * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(Z, dZ, zb * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(alpha, dal, zb * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(beta, dbe, zb * n, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (st) return set_err(ctx, GS_UNCONVERGED, "swap at %d rejected as ill-conditioned", st - 1);
+  return GS_OK;
+}
+
 int gs_ggeigvecs_f64(gs_context* ctx, int64_t n, const double* S, const double* T, const double* Q, const double* Z,
                      double* VR, double* VL, unsigned flags) {
   if (!ctx) return GS_BADARG;

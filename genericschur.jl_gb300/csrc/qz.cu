@@ -588,10 +588,168 @@ __global__ void __launch_bounds__(kQzT) k_ggschur(QzBatch bt) {
   }
 }
 
+// ---- gordschur!(S, T, Q, Z, select) for a complex generalized Schur form (ordschur.jl:
+// 147-305): selected eigenvalues move to the top in their order by adjacent swaps
+// (_trexch2!, ztgex2 with the weak and strong stability tests).  One CTA: every thread
+// computes the swap's 2 x 2 rotations from the same entries (identical decisions), the
+// rotations of rows and columns of S, T, Q, Z are split over the CTA.
+
+// _safe_fnorm of 8 complex numbers (util.jl:83-94, _ssq 466-505: the scale starts at 1).
+__device__ double safe_fnorm8(const double2* w) {
+  double scale = 1.0, sumsq = 0.0;
+  for (int i = 0; i < 8; ++i) {
+    const double parts[2] = {fabs(w[i].x), fabs(w[i].y)};
+    for (int q = 0; q < 2; ++q) {
+      const double t1 = parts[q];
+      if (t1 > 0.0 || t1 != t1) {
+        if (scale < t1) { const double r = scale / t1; sumsq = 1.0 + sumsq * r * r; scale = t1; }
+        else { const double r = t1 / scale; sumsq += r * r; }
+      }
+    }
+  }
+  return scale * sqrt(sumsq);
+}
+
+// rmul!(M2x2, Givens(1, 2, c, s)) / lmul!(Givens(1, 2, c, s), M2x2) on a column-major 2 x 2
+__device__ __forceinline__ void rz2(double2* M, double c, double2 sv) {
+  for (int r = 0; r < 2; ++r) {
+    const double2 m1 = M[r], m2 = M[r + 2];
+    M[r] = zsub(zmulr(m1, c), zmul(m2, zconj(sv)));
+    M[r + 2] = zadd(zmul(m1, sv), zmulr(m2, c));
+  }
+}
+__device__ __forceinline__ void lq2(double2* M, double c, double2 sv) {
+  for (int k = 0; k < 2; ++k) {
+    const double2 m1 = M[2 * k], m2 = M[2 * k + 1];
+    M[2 * k] = zadd(zmulr(m1, c), zmul(sv, m2));
+    M[2 * k + 1] = zsub(zmulr(m2, c), zmul(zconj(sv), m1));
+  }
+}
+
+// One adjacent swap at j1 (1-based); false if a stability test rejects it.  All threads
+// call it; the caller synchronises before (entries read) and it synchronises after.
+__device__ bool trexch2_cplx(const QzMats& m, int j1) {
+  const int n = m.n, tid = threadIdx.x;
+  double2 S[4] = {QA(j1, j1), QA(j1 + 1, j1), QA(j1, j1 + 1), QA(j1 + 1, j1 + 1)};
+  double2 T[4] = {QB(j1, j1), QB(j1 + 1, j1), QB(j1, j1 + 1), QB(j1 + 1, j1 + 1)};
+  const double2 orig[8] = {S[0], S[1], S[2], S[3], T[0], T[1], T[2], T[3]};
+  const double eps = Prec<double>::eps;
+  const double smlnum = Prec<double>::fmin / eps;
+  double sa = safe_fnorm8(orig);
+  const double thresh = fmax(20.0 * eps * sa, smlnum);
+  const double2 f = zsub(zmul(S[3], T[0]), zmul(T[3], S[0]));
+  const double2 g = zsub(zmul(S[3], T[2]), zmul(T[3], S[2]));
+  sa = zabs(S[3]) * zabs(T[0]);
+  const double sb = zabs(S[0]) * zabs(T[3]);
+  double cz;
+  double2 sz, r;
+  if (zis0(f) && zis0(g)) { cz = 0.0; sz = make_double2(1.0, 0.0); }
+  else zgivens(g, f, cz, sz, r);
+  rz2(S, cz, sz);
+  rz2(T, cz, sz);
+  double2 fq, gq;
+  if (sa >= sb) { fq = S[0]; gq = S[1]; } else { fq = T[0]; gq = T[1]; }
+  double cq;
+  double2 sq;
+  if (!zis0(sz) && zis0(fq) && zis0(gq)) { cq = 0.0; sq = make_double2(1.0, 0.0); }
+  else zgivens(fq, gq, cq, sq, r);
+  lq2(S, cq, sq);
+  lq2(T, cq, sq);
+  const double ws = zabs(S[1]) + zabs(T[1]);
+  if (!(ws <= thresh)) return false;
+  double2 Ss[4] = {S[0], S[1], S[2], S[3]}, Ts[4] = {T[0], T[1], T[2], T[3]};
+  rz2(Ss, cz, zneg(sz));
+  rz2(Ts, cz, zneg(sz));
+  lq2(Ss, cq, zneg(sq));
+  lq2(Ts, cq, zneg(sq));
+  double2 W[8];
+  for (int k = 0; k < 4; ++k) { W[k] = zsub(Ss[k], orig[k]); W[4 + k] = zsub(Ts[k], orig[4 + k]); }
+  if (!(safe_fnorm8(W) <= thresh)) return false;
+  __syncthreads();
+  // columns j1, j1+1 of A, B, Z (rmul! by Gz') and of Q (rmul! by Gq'), all rows
+  for (int i = tid; i < 4 * n; i += kQzT) {
+    const int which = i / n, rr = i % n;
+    double2* M = which == 0 ? m.A : which == 1 ? m.B : which == 2 ? m.Z : m.Q;
+    if (!M) continue;
+    double2* c1 = M + rr + (size_t)(j1 - 1) * n;
+    double2* c2 = M + rr + (size_t)j1 * n;
+    const double2 m1 = *c1, m2 = *c2;
+    if (which < 3) {
+      *c1 = zsub(zmulr(m1, cz), zmul(m2, zconj(sz)));
+      *c2 = zadd(zmul(m1, sz), zmulr(m2, cz));
+    } else {
+      *c1 = zadd(zmulr(m1, cq), zmul(m2, zconj(sq)));
+      *c2 = zsub(zmulr(m2, cq), zmul(m1, sq));
+    }
+  }
+  __syncthreads();
+  // rows j1, j1+1 of A and B (lmul! by Gq), all columns
+  for (int i = tid; i < 2 * n; i += kQzT) {
+    double2* M = i < n ? m.A : m.B;
+    const int cc = i % n;
+    double2* r1 = M + (j1 - 1) + (size_t)cc * n;
+    double2* r2 = M + j1 + (size_t)cc * n;
+    const double2 m1 = *r1, m2 = *r2;
+    *r1 = zadd(zmulr(m1, cq), zmul(sq, m2));
+    *r2 = zsub(zmulr(m2, cq), zmul(zconj(sq), m1));
+  }
+  __syncthreads();
+  if (tid == 0) {
+    QA(j1 + 1, j1) = make_double2(0.0, 0.0);
+    QB(j1 + 1, j1) = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  return true;
+}
+
+__global__ void __launch_bounds__(kQzT) k_ggordschur_cplx(QzMats m, const int* __restrict__ select, int scale,
+                                                          double2* alpha, double2* beta, int* status) {
+  __shared__ double red[kQzT / 32];
+  const int n = m.n, tid = threadIdx.x;
+  double cscale = 1.0, anrm = 1.0, cscaleb = 1.0, bnrm = 1.0;
+  bool scA = false, scB = false;
+  if (scale) {
+    scA = cta_scale(m.A, n, red, cscale, anrm);
+    scB = cta_scale(m.B, n, red, cscaleb, bnrm);
+  }
+  __syncthreads();
+  int st = 0;
+  int ks = 0;
+  for (int k = 1; k <= n && !st; ++k) {
+    if (!select[k - 1]) continue;
+    ks += 1;
+    if (k != ks)
+      for (int icur = k - 1; icur >= ks; --icur) {
+        __syncthreads();
+        if (!trexch2_cplx(m, icur)) { st = 1 + icur; break; }
+      }
+  }
+  __syncthreads();
+  if (scA) cta_safescale(m.A, n, cscale, anrm);
+  if (scB) cta_safescale(m.B, n, cscaleb, bnrm);
+  for (size_t e = tid; e < (size_t)n * n; e += kQzT) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    if (i > j) { m.A[e] = make_double2(0.0, 0.0); m.B[e] = make_double2(0.0, 0.0); }
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += kQzT) {
+    alpha[i] = m.A[i + (size_t)i * n];
+    beta[i] = m.B[i + (size_t)i * n];
+  }
+  if (tid == 0) *status = st;
+}
+
 #undef QA
 #undef QB
 
 }  // namespace
+
+cudaError_t launch_ggordschur_cplx(int n, double2* S, double2* T, double2* Q, double2* Z, const int* select, int scale,
+                                   double2* alpha, double2* beta, int* status, cudaStream_t s) {
+  QzMats m{S, T, Q, Z, n};
+  k_ggordschur_cplx<<<1, kQzT, 0, s>>>(m, select, scale, alpha, beta, status);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ggschur(const QzBatch& bt, int num_sms, cudaStream_t s) {
   if (bt.count <= 0) return cudaSuccess;

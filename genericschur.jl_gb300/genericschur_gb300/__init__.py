@@ -494,8 +494,11 @@ def gordschur(S, select, ctx=None):
     """gordschur!(S, select) / ordschur (ordschur.jl:12-74, rordschur.jl:3-47) on a copy:
     the eigenvalues with select[k] true move to the leading positions, in their order.
     Returns the reordered Schur(T, Z, values).  Raises UnconvergedException if a block
-    swap is rejected as ill-conditioned (the reference's IllConditionException)."""
+    swap is rejected as ill-conditioned (the reference's IllConditionException).
+    A complex GeneralizedSchur goes to gordschur! of the pencil (ordschur.jl:147-305)."""
     ctx = ctx or get_context()
+    if isinstance(S, GeneralizedSchur):
+        return _ggordschur(S, select, ctx)
     T = np.array(S.T, order="F", copy=True)
     n = _checksquare(T)
     sel = np.ascontiguousarray(np.asarray(select, dtype=bool).astype(np.int32))
@@ -516,6 +519,27 @@ def gordschur(S, select, ctx=None):
     if rc != GS_OK:
         _raise(rc, ctx, "gordschur!")
     return Schur(T, Z, w)
+
+
+def _ggordschur(G, select, ctx, scale=True):
+    if not (np.iscomplexobj(G.S) or np.iscomplexobj(G.T)):
+        raise ArgumentError("reordering of a real generalized Schur form is not provided; "
+                            "use the complex form (ggschur of the pencil cast to complex)")
+    S = _fc(G.S, np.complex128)
+    T = _fc(G.T, np.complex128)
+    n = _checksquare(S)
+    sel = np.ascontiguousarray(np.asarray(select, dtype=bool).astype(np.int32))
+    if len(sel) != n:
+        raise DimensionMismatch("select must have length %d" % n)
+    Q = _fc(G.Q if G.Q is not None else np.eye(n), np.complex128)
+    Z = _fc(G.Z if G.Z is not None else np.eye(n), np.complex128)
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1), dtype=np.complex128)
+    rc = ctx.lib.gs_ggordschur_c64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(sel), _ptr(al), _ptr(be),
+                                   _capi.GS_SCALE if scale else 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "gordschur!(GeneralizedSchur)")
+    return GeneralizedSchur(S, T, al[:n], be[:n], Q, Z)
 
 
 ordschur = gordschur

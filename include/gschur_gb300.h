@@ -337,6 +337,16 @@ GS_API int gs_ggschur_batched_f64(gs_context* ctx, int64_t count, const int32_t*
                                   int64_t packed_len, double* A, double* B, double* Q, double* Z, const int64_t* woffs,
                                   int64_t wlen, double* alpha, double* beta, int32_t* status, unsigned flags);
 
+/* gordschur!(S, T, Q, Z, select) / ordschur!(F::GeneralizedSchur, select) for a complex
+ * generalized Schur form (ordschur.jl:147-305): the eigenvalues with select[k] != 0 move to
+ * the leading positions in their order, by adjacent swaps (_trexch2!, ztgex2 with the weak
+ * and strong stability tests).  S, T, Q, Z (n x n, interleaved complex, leading dimension n)
+ * in place; alpha, beta (n) the new diagonals.  GS_SCALE applies the reference's default
+ * _scale! of S and T around the swaps.  GS_UNCONVERGED if a swap is rejected (the
+ * reference's IllConditionException); the form is then partly reordered. */
+GS_API int gs_ggordschur_c64(gs_context* ctx, int64_t n, double* S, double* T, double* Q, double* Z,
+                             const int32_t* select, double* alpha, double* beta, unsigned flags);
+
 /* Eigenvectors of the generalized Schur decomposition of a complex pencil (the output
  * of gs_ggschur_c64: S, T upper triangular, A = Q S Z^H, B = Q T Z^H).  Replaces
  * geigvecs(S::GeneralizedSchur; left) (vectors.jl:22-33): right eigenvectors

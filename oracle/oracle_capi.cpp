@@ -269,6 +269,13 @@ int or_rgevc_d(int n, const double* s, const double* p, const double* x, double*
   return 0;
 }
 
+// gordschur!(S, T, Q, Z, select) for a complex generalized Schur form (src/ordschur.jl:
+// 147-305), in place; alpha, beta the new diagonals.  Returns 0 or 1 + j1 of a rejected swap.
+int or_ggordschur_z(int n, double* s, double* t, double* q, double* z, const int* select, int scale, double* al,
+                    double* be) {
+  return gordschur_cplx<double>(n, (zc*)s, (zc*)t, (zc*)q, (zc*)z, select, scale != 0, (zc*)al, (zc*)be);
+}
+
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {
   gs2x2<double>(h, cs, sn, &w[0], &w[1], &w[2], &w[3]);
   return 0;

@@ -55,6 +55,7 @@ def lib():
             "or_ggevc_z": [_i, _p, _p, _p, _p, _i],
             "or_ggschur_d": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
             "or_rgevc_d": [_i, _p, _p, _p, _p, _i],
+            "or_ggordschur_z": [_i, _p, _p, _p, _p, _p, _i, _p, _p],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -362,3 +363,16 @@ def rgeigvecs(S, T, X=None, left=False):
     V = np.zeros((n, n), dtype=np.complex128, order="F")
     lib().or_rgevc_d(n, _ptr(Sf), _ptr(Tf), _ptr(Xf), _ptr(V), int(left))
     return V
+
+
+def ggordschur(S, T, Q, Z, select, scale=True):
+    """gordschur!(S, T, Q, Z, select) for a complex generalized Schur form (ordschur.jl:
+    147-305): (S, T, alpha, beta, Q, Z, status), status 1 + j1 for a rejected swap."""
+    Sf, Tf, Qf, Zf = (_f(x, np.complex128) for x in (S, T, Q, Z))
+    n = Sf.shape[0]
+    sel = np.ascontiguousarray(np.asarray(select, dtype=np.int32))
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1), dtype=np.complex128)
+    st = lib().or_ggordschur_z(n, _ptr(Sf), _ptr(Tf), _ptr(Qf), _ptr(Zf), sel.ctypes.data_as(ctypes.c_void_p),
+                               int(scale), _ptr(al), _ptr(be))
+    return Sf, Tf, al[:n], be[:n], Qf, Zf, st

@@ -1732,4 +1732,155 @@ void rgevc_left(int n, const R* S, const R* P, const R* Q, cx<R>* V) {
 #undef PP
 }
 
+
+// ---------------------------------------------------------------------------
+// Reordering a complex generalized Schur form: gordschur!(S, T, Q, Z, select)
+// (src/ordschur.jl:147-305): _trexchange! by adjacent swaps _trexch2! (ztgex2 with the
+// weak and strong stability tests).  Returns 0, or 1 + (1-based j1) of a rejected swap
+// (the reference's IllConditionException).
+// ---------------------------------------------------------------------------
+// _safe_fnorm(vec(W)) (util.jl:83-94 with _ssq 466-505): real and imaginary parts, the
+// running scale starting at 1.
+template <class R> R safe_fnorm_c(const cx<R>* w, int cnt) {
+  R scale = R(1), sumsq = R(0);
+  for (int i = 0; i < cnt; ++i) {
+    const R parts[2] = {m_abs(w[i].re), m_abs(w[i].im)};
+    for (R t1 : parts) {
+      if (t1 > R(0) || t1 != t1) {
+        if (scale < t1) { sumsq = R(1) + sumsq * (scale / t1) * (scale / t1); scale = t1; }
+        else sumsq += (t1 / scale) * (t1 / scale);
+      }
+    }
+  }
+  return scale * m_sqrt(sumsq);
+}
+
+template <class R>
+bool trexch2_cplx(int n, cx<R>* A, cx<R>* B, cx<R>* Q, cx<R>* Z, int j1) {
+  typedef cx<R> C;
+#define A_(i, j) A[((i) - 1) + (long long)((j) - 1) * n]
+#define B_(i, j) B[((i) - 1) + (long long)((j) - 1) * n]
+  C S[4] = {A_(j1, j1), A_(j1 + 1, j1), A_(j1, j1 + 1), A_(j1 + 1, j1 + 1)};  // column-major 2 x 2
+  C T[4] = {B_(j1, j1), B_(j1 + 1, j1), B_(j1, j1 + 1), B_(j1 + 1, j1 + 1)};
+  const R eps = std::numeric_limits<R>::epsilon();
+  const R smlnum = safemin<R>() / eps;
+  C W[8] = {S[0], S[1], S[2], S[3], T[0], T[1], T[2], T[3]};
+  R sa = safe_fnorm_c(W, 8);
+  const R thresh = m_max(R(20) * eps * sa, smlnum);
+  const C f = S[3] * T[0] - T[3] * S[0];
+  const C g = S[3] * T[2] - T[3] * S[2];
+  sa = cabs(S[3]) * cabs(T[0]);
+  const R sb = cabs(S[0]) * cabs(T[3]);
+  R cz;
+  C sz;
+  if (f == C(R(0)) && g == C(R(0))) { cz = R(0); sz = C(R(1)); }
+  else { C r; zgivens_alg(g, f, &cz, &sz, &r); }
+  // rmul!(M, Givens(1, 2, cz, sz)): [m1 m2] <- [m1 cz - m2 conj(sz), m1 sz + m2 cz]
+  auto rz = [&](C* M, R c, C sv) {
+    for (int r = 0; r < 2; ++r) {
+      const C m1 = M[r], m2 = M[r + 2];
+      M[r] = m1 * c - m2 * conj(sv);
+      M[r + 2] = m1 * sv + m2 * c;
+    }
+  };
+  // lmul!(Givens(1, 2, c, s), M): [m1; m2] <- [c m1 + s m2; -conj(s) m1 + c m2]
+  auto lq = [&](C* M, R c, C sv) {
+    for (int k = 0; k < 2; ++k) {
+      const C m1 = M[2 * k], m2 = M[2 * k + 1];
+      M[2 * k] = m1 * c + sv * m2;
+      M[2 * k + 1] = m2 * c - conj(sv) * m1;
+    }
+  };
+  rz(S, cz, sz);
+  rz(T, cz, sz);
+  C fq, gq;
+  if (sa >= sb) { fq = S[0]; gq = S[1]; } else { fq = T[0]; gq = T[1]; }
+  R cq;
+  C sq;
+  if (sz != C(R(0)) && fq == C(R(0)) && gq == C(R(0))) { cq = R(0); sq = C(R(1)); }
+  else { C r; zgivens_alg(fq, gq, &cq, &sq, &r); }
+  lq(S, cq, sq);
+  lq(T, cq, sq);
+  const R ws = cabs(S[1]) + cabs(T[1]);
+  if (!(ws <= thresh)) return false;
+  // strong test: undo the rotations on copies and compare with the original block
+  C Ss[4] = {S[0], S[1], S[2], S[3]}, Ts[4] = {T[0], T[1], T[2], T[3]};
+  rz(Ss, cz, -sz);
+  rz(Ts, cz, -sz);
+  lq(Ss, cq, -sq);
+  lq(Ts, cq, -sq);
+  const C orig[8] = {A_(j1, j1), A_(j1 + 1, j1), A_(j1, j1 + 1), A_(j1 + 1, j1 + 1),
+                     B_(j1, j1), B_(j1 + 1, j1), B_(j1, j1 + 1), B_(j1 + 1, j1 + 1)};
+  for (int k = 0; k < 4; ++k) { W[k] = Ss[k] - orig[k]; W[4 + k] = Ts[k] - orig[4 + k]; }
+  const R ss = safe_fnorm_c(W, 8);
+  if (!(ss <= thresh)) return false;
+  // apply: rmul!(A, Gz'), rmul!(B, Gz') on all rows; lmul!(Gq, A), lmul!(Gq, B) on all columns
+  for (int r = 1; r <= n; ++r) {
+    C m1 = A_(r, j1), m2 = A_(r, j1 + 1);
+    A_(r, j1) = m1 * cz - m2 * conj(sz);
+    A_(r, j1 + 1) = m1 * sz + m2 * cz;
+    m1 = B_(r, j1); m2 = B_(r, j1 + 1);
+    B_(r, j1) = m1 * cz - m2 * conj(sz);
+    B_(r, j1 + 1) = m1 * sz + m2 * cz;
+  }
+  for (int c = 1; c <= n; ++c) {
+    C m1 = A_(j1, c), m2 = A_(j1 + 1, c);
+    A_(j1, c) = m1 * cq + sq * m2;
+    A_(j1 + 1, c) = m2 * cq - conj(sq) * m1;
+    m1 = B_(j1, c); m2 = B_(j1 + 1, c);
+    B_(j1, c) = m1 * cq + sq * m2;
+    B_(j1 + 1, c) = m2 * cq - conj(sq) * m1;
+  }
+  A_(j1 + 1, j1) = C(R(0));
+  B_(j1 + 1, j1) = C(R(0));
+  // rmul!(Z, Gz') and rmul!(Q, Gq')
+  for (int r = 0; r < n; ++r) {
+    C* z1 = Z + r + (long long)(j1 - 1) * n;
+    C* z2 = Z + r + (long long)j1 * n;
+    C m1 = *z1, m2 = *z2;
+    *z1 = m1 * cz - m2 * conj(sz);
+    *z2 = m1 * sz + m2 * cz;
+    C* q1 = Q + r + (long long)(j1 - 1) * n;
+    C* q2 = Q + r + (long long)j1 * n;
+    m1 = *q1; m2 = *q2;
+    *q1 = m1 * cq + m2 * conj(sq);
+    *q2 = m2 * cq - m1 * sq;
+  }
+  return true;
+#undef A_
+#undef B_
+}
+
+template <class R>
+int gordschur_cplx(int n, cx<R>* S, cx<R>* T, cx<R>* Q, cx<R>* Z, const int* select, bool scale, cx<R>* alpha,
+                   cx<R>* beta) {
+  R cscale = 1, anrm = 1, cscaleb = 1, bnrm = 1;
+  bool scA = false, scB = false;
+  if (scale) {
+    scA = scale_matrix<R, cx<R>>(n, S, n, &cscale, &anrm);
+    scB = scale_matrix<R, cx<R>>(n, T, n, &cscaleb, &bnrm);
+  }
+  int status = 0;
+  int ks = 0;
+  for (int k = 1; k <= n && !status; ++k) {
+    if (!select[k - 1]) continue;
+    ks += 1;
+    if (k != ks)
+      for (int icur = k - 1; icur >= ks; --icur)
+        if (!trexch2_cplx<R>(n, S, T, Q, Z, icur)) { status = 1 + icur; break; }
+  }
+  if (scA) for (int j = 0; j < n; ++j) safescale<R, cx<R>>(S + (long long)j * n, n, cscale, anrm);
+  if (scB) for (int j = 0; j < n; ++j) safescale<R, cx<R>>(T + (long long)j * n, n, cscaleb, bnrm);
+  for (int j = 0; j < n; ++j)
+    for (int i = j + 1; i < n; ++i) {
+      S[i + (long long)j * n] = cx<R>(R(0));
+      T[i + (long long)j * n] = cx<R>(R(0));
+    }
+  for (int i = 0; i < n; ++i) {
+    alpha[i] = S[i + (long long)i * n];
+    beta[i] = T[i + (long long)i * n];
+  }
+  return status;
+}
+
 }  // namespace orc

@@ -358,3 +358,42 @@ def test_ggeigvecs_real_singular(gs, seed):
             Tp = G.T * (1 + EPS * r.standard_normal(G.T.shape))
             sens = max(sens, float(np.max(np.abs(po.rgeigvecs(Sp, Tp, M, left=left) - Vo))))
         _same_columns(gs.geigvecs(G, left=left), Vo, max(1e-9, 10 * sens))
+
+
+
+# ---------------------------------------------------------------------------
+# gordschur! of complex generalized Schur forms (ordschur.jl:147-305)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ggordschur_checkord(gs, seed):
+    """The reference's checkord for ComplexF64 (test/gordschur.jl:139-186): n = 16, B shifted
+    by I, the last half selected; S, T triangular, A = Q S Z', B = Q T Z' and Q, Z unitary to
+    10 n eps, the wanted eigenvalues in front; and the oracle's reordering of the same form."""
+    rng = np.random.default_rng(9200 + seed)
+    n = 16
+    A = rng.random((n, n)) + 1j * rng.random((n, n))
+    B = rng.random((n, n)) + 1j * rng.random((n, n)) - (0.5 + 0.5j) + np.eye(n)
+    G = gs.ggschur(A, B)
+    select = np.ones(n, dtype=bool)
+    select[: n >> 1] = False
+    G2 = gs.gordschur(G, select)
+    tol = 10
+    nA, nB = np.linalg.norm(A), np.linalg.norm(B)
+    assert np.linalg.norm(np.tril(G2.S, -1)) / (n * nA * EPS) < tol
+    assert np.linalg.norm(np.tril(G2.T, -1)) / (n * nA * EPS) < tol
+    assert np.linalg.norm(A - G2.Q @ G2.S @ G2.Z.conj().T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(B - G2.Q @ G2.T @ G2.Z.conj().T) / (n * nB * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - G2.Z @ G2.Z.conj().T) / (n * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - G2.Q @ G2.Q.conj().T) / (n * EPS) < tol
+    w = G.alpha / G.beta
+    wanted = list(w[select])
+    for i in range(int(select.sum())):
+        x = G2.alpha[i] / G2.beta[i]
+        d = np.abs(np.array(wanted) - x)
+        j = int(np.argmin(d))
+        assert d[j] / (EPS + abs(x)) < tol
+        wanted.pop(j)
+    S, T, al, be, Q, Z, st = po.ggordschur(G.S, G.T, G.Q, G.Z, select)
+    assert st == 0
+    np.testing.assert_allclose(G2.alpha / G2.beta, al / be, rtol=1e-10, atol=0)
+    assert np.max(np.abs(G2.S - S)) < 1e-10 * nA and np.max(np.abs(G2.T - T)) < 1e-10 * nB
