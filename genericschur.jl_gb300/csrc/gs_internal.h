@@ -128,6 +128,25 @@ cudaError_t launch_ggschur(const QzBatch& bt, int num_sms, cudaStream_t s);
 // gordschur! of a complex generalized Schur form (qz.cu); status 0 or 1 + j1 of a rejected swap.
 cudaError_t launch_ggordschur_cplx(int n, double2* S, double2* T, double2* Q, double2* Z, const int* select, int scale,
                                    double2* alpha, double2* beta, int* status, cudaStream_t s);
+// Generalized Sylvester solves of complex triangular A, D (m x m), B, E (n x n) on
+// C, F (m x n) (gcondition.cu).  mode 0 trsylvester!, 1 adjtrsylvester!, 2 the look-ahead
+// of _trgsep.  flag bits: 1 a perturbed pivot, 2 a rescaled right-hand side, 4 a singular
+// look-ahead system, 8 a grid barrier that timed out.
+struct GsylBar {
+  unsigned count, gen;
+  int err;
+};
+struct GsylArgs {
+  const double2 *A, *B, *D, *E;
+  int lda, ldb, ldd, lde;
+  double2 *C, *F;
+  int ldc, ldf;
+  int m, n, mode;
+  int* flag;
+  GsylBar* bar;
+};
+size_t gsyl_bar_bytes();
+cudaError_t launch_gsyl(const GsylArgs& P, int num_sms, cudaStream_t s);
 // Real pencils (qz_real.cu): A, B, Q, Z real; alpha complex, beta real.
 struct QzrBatch {
   int count;

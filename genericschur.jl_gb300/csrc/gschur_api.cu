@@ -1888,6 +1888,61 @@ template <class S> CondLayout cond_layout(int64_t n, int64_t m, size_t base) {
   return L;
 }
 
+// norm1est! (norm1est.jl:21-74) on the host over an operator applied in place to the
+// device vector x (N entries): apply(adjoint) runs the operator or its adjoint on x.
+// work holds at least four doubles of device memory.
+template <class S, class Apply>
+int norm1est_host(gs_context* ctx, cudaStream_t s, S* x, long long N, double* work, Apply apply, double* est_out) {
+  const double tiny = 2.2250738585072014e-308;
+  double st[4];
+  auto step = [&](int op, double arg) -> int {
+    CK(launch_n1_step<S>(op, x, N, arg, ctx->num_sms, s));
+    return GS_OK;
+  };
+  auto stats = [&](long long jlast) -> int {
+    CK(launch_n1_stats<S>(x, N, jlast, work, s));
+    CK(cudaMemcpyAsync(st, work, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return GS_OK;
+  };
+#define COND_TRY(expr) do { int rc_ = (expr); if (rc_) return rc_; } while (0)
+  COND_TRY(step(N1_FILL, 1.0 / (double)N));
+  COND_TRY(apply(false));
+  COND_TRY(stats(-1));
+  double est;
+  if (N == 1) {
+    est = st[0];
+  } else {
+    double gamma = st[0];
+    COND_TRY(step(N1_SIGN, tiny));
+    COND_TRY(apply(true));
+    COND_TRY(stats(-1));
+    long long j0 = (long long)st[2];
+    for (int iter = 0; iter < 5; ++iter) {
+      COND_TRY(step(N1_UNIT, (double)j0));
+      COND_TRY(apply(false));
+      COND_TRY(stats(-1));
+      const double old = gamma;
+      gamma = st[0];
+      if (gamma <= old) break;
+      COND_TRY(step(N1_SIGN, tiny));
+      COND_TRY(apply(true));
+      const long long jlast = j0;
+      COND_TRY(stats(jlast));
+      j0 = (long long)st[2];
+      if (st[3] == st[1]) break;
+    }
+    COND_TRY(step(N1_ALT, 0.0));
+    COND_TRY(apply(false));
+    COND_TRY(stats(-1));
+    const double t = 2.0 * st[0] / (double)(3 * N);
+    est = jmax(t, gamma);
+  }
+#undef COND_TRY
+  *est_out = est;
+  return GS_OK;
+}
+
 template <class S> struct CondRun {
   gs_context* ctx;
   cudaStream_t s;
@@ -1992,47 +2047,10 @@ template <class S> struct CondRun {
     if (m == 0 || p == 0) return set_err(ctx, GS_BADARG, "subspacesep needs 0 < nsub < n");
     int rc = prepare(true);
     if (rc) return rc;
-    const long long N = (long long)m * p;
-    const double tiny = 2.2250738585072014e-308;
-    double scale = 1.0, st[4];
-    auto step = [&](int op, double arg) -> int {
-      CK(launch_n1_step<S>(op, x(), N, arg, ctx->num_sms, s));
-      return GS_OK;
-    };
-#define COND_TRY(expr) do { int rc_ = (expr); if (rc_) return rc_; } while (0)
-    COND_TRY(step(N1_FILL, 1.0 / (double)N));
-    COND_TRY(solve(false, &scale));
-    COND_TRY(stats(-1, st));
-    double est;
-    if (N == 1) {
-      est = st[0];
-    } else {
-      double gamma = st[0];
-      COND_TRY(step(N1_SIGN, tiny));
-      COND_TRY(solve(true, &scale));
-      COND_TRY(stats(-1, st));
-      long long j0 = (long long)st[2];
-      for (int iter = 0; iter < 5; ++iter) {
-        COND_TRY(step(N1_UNIT, (double)j0));
-        COND_TRY(solve(false, &scale));
-        COND_TRY(stats(-1, st));
-        const double old = gamma;
-        gamma = st[0];
-        if (gamma <= old) break;
-        COND_TRY(step(N1_SIGN, tiny));
-        COND_TRY(solve(true, &scale));
-        const long long jlast = j0;
-        COND_TRY(stats(jlast, st));
-        j0 = (long long)st[2];
-        if (st[3] == st[1]) break;
-      }
-      COND_TRY(step(N1_ALT, 0.0));
-      COND_TRY(solve(false, &scale));
-      COND_TRY(stats(-1, st));
-      const double t = 2.0 * st[0] / (double)(3 * N);
-      est = jmax(t, gamma);
-    }
-#undef COND_TRY
+    double scale = 1.0, est = 0.0;
+    rc = norm1est_host<S>(
+        ctx, s, x(), (long long)m * p, dbl(), [&](bool adj) { return solve(adj, &scale); }, &est);
+    if (rc) return rc;
     *out = scale / est;
     return GS_OK;
   }
@@ -2136,6 +2154,212 @@ int rcondv_impl(gs_context* ctx, int64_t n, const double* T, double* rconde, dou
   return GS_OK;
 }
 
+// Generalized Sylvester solves and condition estimates of a complex generalized Schur form
+// (gsylvester.jl, gcondition.jl) over the wavefront solver of gcondition.cu.
+struct GsylRun {
+  gs_context* ctx;
+  cudaStream_t s;
+  int* flag;     // device, one int
+  GsylBar* bar;  // device
+  double* dbl;   // device, eight doubles
+
+  // one solve; *pert receives the perturbed-pivot flag of the reference
+  int run(int mode, int m, int n, const double2* A, int lda, const double2* B, int ldb, const double2* D, int ldd,
+          const double2* E, int lde, double2* C, int ldc, double2* F, int ldf, bool* pert = nullptr) {
+    if (pert) *pert = false;
+    if (m == 0 || n == 0) return GS_OK;
+    GsylArgs P{A, B, D, E, lda, ldb, ldd, lde, C, F, ldc, ldf, m, n, mode, flag, bar};
+    CK(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(bar, 0, gsyl_bar_bytes(), s));
+    CK(launch_gsyl(P, ctx->num_sms, s));
+    int fl = 0;
+    CK(cudaMemcpyAsync(&fl, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (fl & 8) return set_err(ctx, GS_CUDA, "generalized Sylvester solve: grid barrier timed out");
+    if (fl & 2)
+      return set_err(ctx, GS_BADARG,
+                     "generalized Sylvester solve: a 2 x 2 system needed rescaling against overflow, where "
+                     "the reference's trsylvester! calls lmul!(view, scale) and raises");
+    if (fl & 4)
+      return set_err(ctx, GS_BADARG, "singular 2 x 2 system in the separation estimate (lu raises SingularException)");
+    if (pert) *pert = (fl & 1) != 0;
+    return GS_OK;
+  }
+
+  double fro(const double2* x, long long N, int slot) {
+    if (N == 0) return 0.0;
+    if (launch_cond_fro<double2>(x, N, dbl + slot, s) != cudaSuccess) return -1.0;
+    double v = -1.0;
+    if (cudaMemcpyAsync(&v, dbl + slot, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1.0;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1.0;
+    return v;
+  }
+};
+
+struct GCondLayout {
+  size_t o_S, o_T, o_x, o_flag, o_bar, o_dbl, bytes;
+};
+GCondLayout gcond_layout(int64_t n, int64_t nsub, bool dev) {
+  Arena ar;
+  GCondLayout L;
+  L.o_S = ar.take<double2>(dev ? 1 : (size_t)n * n);
+  L.o_T = ar.take<double2>(dev ? 1 : (size_t)n * n);
+  L.o_x = ar.take<double2>((size_t)std::max<int64_t>(2 * nsub * (n - nsub), 1));
+  L.o_flag = ar.take<int>(4);
+  L.o_bar = ar.take<char>(std::max<size_t>(gsyl_bar_bytes(), 16));
+  L.o_dbl = ar.take<double>(8);
+  L.bytes = ar.off;
+  return L;
+}
+
+// eigvalscond (what = 0, gcondition.jl:121-165) and subspacesep (what = 1 with pnorm 0 for
+// :F, 1 for the one-norm estimate; gcondition.jl:169-260) of the pencil's leading nsub block.
+int gcond_impl(gs_context* ctx, int64_t n, const double* S, int64_t lds, const double* T, int64_t ldt, int64_t nsub,
+               int what, int pnorm, double* out, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || nsub < 0 || nsub > n || lds < std::max<int64_t>(n, 1) || ldt < std::max<int64_t>(n, 1))
+    return set_err(ctx, GS_BADARG, "bad sizes");
+  if (n > (1 << 16)) return set_err(ctx, GS_BADARG, "order too large");
+  if (!out || (n > 0 && (!S || !T))) return set_err(ctx, GS_BADARG, "null argument");
+  if (what == 1 && pnorm != 0 && pnorm != 1) return set_err(ctx, GS_BADARG, "pnorm must be :Frobenius or 1");
+  const int64_t n1 = nsub, n2 = n - nsub;
+  if (what == 0 && (n1 == 0 || n2 == 0)) {
+    out[0] = out[1] = 1.0;
+    return GS_OK;
+  }
+  if (what == 1 && pnorm == 0 && (n1 == 0 || n2 == 0)) {
+    out[0] = out[1] = 0.0;
+    return GS_OK;
+  }
+  if (what == 1 && (n1 == 0 || n2 == 0)) return set_err(ctx, GS_BADARG, "subspacesep with pnorm = 1 needs 0 < nsub < n");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const GCondLayout L = gcond_layout(n, nsub, dev);
+  int rc = ensure_ws(ctx, L.bytes);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const double2* dS = (const double2*)S;
+  const double2* dT = (const double2*)T;
+  int64_t ls = lds, lt = ldt;
+  if (!dev) {
+    CK(cudaMemcpy2DAsync(base + L.o_S, 16 * n, S, 16 * lds, 16 * n, n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpy2DAsync(base + L.o_T, 16 * n, T, 16 * ldt, 16 * n, n, cudaMemcpyHostToDevice, s));
+    dS = (const double2*)(base + L.o_S);
+    dT = (const double2*)(base + L.o_T);
+    ls = lt = n;
+  }
+  GsylRun g{ctx, s, (int*)(base + L.o_flag), (GsylBar*)(base + L.o_bar), (double*)(base + L.o_dbl)};
+  double2* x = (double2*)(base + L.o_x);
+  const long long N1 = (long long)n1 * n2;
+  const double2 *S11 = dS, *S22 = dS + n1 + (size_t)n1 * ls, *T11 = dT, *T22 = dT + n1 + (size_t)n1 * lt;
+  CK(cudaEventRecord(ctx->t0, s));
+  double res[2] = {0.0, 0.0};
+  if (what == 0) {
+    // S11 R - L S22 = s S12, T11 R - L T22 = s T12
+    CK(cudaMemcpy2DAsync(x, 16 * n1, dS + (size_t)n1 * ls, 16 * ls, 16 * n1, n2, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpy2DAsync(x + N1, 16 * n1, dT + (size_t)n1 * lt, 16 * lt, 16 * n1, n2, cudaMemcpyDeviceToDevice, s));
+    rc = g.run(0, (int)n1, (int)n2, S11, (int)ls, S22, (int)ls, T11, (int)lt, T22, (int)lt, x, (int)n1, x + N1, (int)n1);
+    if (rc) return rc;
+    for (int k = 0; k < 2; ++k) {
+      const double p = g.fro(x + k * N1, N1, k);
+      if (p < 0.0) return set_err(ctx, GS_CUDA, "CUDA error in the norm of the Sylvester solution");
+      res[k] = p == 0.0 ? 1.0 : 1.0 / (std::sqrt(1.0 / p + p) * std::sqrt(p));
+    }
+  } else {
+    for (int k = 0; k < 2; ++k) {
+      // k = 0: (S11, S22, T11, T22), m = n1; k = 1: the blocks exchanged, m = n2
+      const int m = (int)(k == 0 ? n1 : n2), q = (int)(k == 0 ? n2 : n1);
+      const double2 *A = k == 0 ? S11 : S22, *B = k == 0 ? S22 : S11, *D = k == 0 ? T11 : T22, *E = k == 0 ? T22 : T11;
+      if (pnorm == 0) {
+        CK(cudaMemsetAsync(x, 0, 16 * (size_t)(2 * N1), s));
+        rc = g.run(2, m, q, A, (int)ls, B, (int)ls, D, (int)lt, E, (int)lt, x, m, x + N1, m);
+        if (rc) return rc;
+        const double f = g.fro(x, 2 * N1, 2);
+        if (f < 0.0) return set_err(ctx, GS_CUDA, "CUDA error in the norm of the look-ahead solution");
+        res[k] = std::sqrt(2.0 * (double)m * (double)q) / f;
+      } else {
+        double est = 0.0;
+        rc = norm1est_host<double2>(
+            ctx, s, x, 2 * N1, g.dbl,
+            [&](bool adj) {
+              return g.run(adj ? 1 : 0, m, q, A, (int)ls, B, (int)ls, D, (int)lt, E, (int)lt, x, m, x + N1, m);
+            },
+            &est);
+        if (rc) return rc;
+        res[k] = 1.0 / est;
+      }
+    }
+  }
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  out[0] = res[0];
+  out[1] = res[1];
+  return GS_OK;
+}
+
+// trsylvester!(A, B, C, D, E, F) / adjtrsylvester! (gsylvester.jl:23-155), complex.
+int gtrsyl_impl(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B, int64_t ldb,
+                double* C, int64_t ldc, const double* D, int64_t ldd, const double* E, int64_t lde, double* F,
+                int64_t ldf, int adjoint, double* scale, int32_t* perturbed, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  const int64_t m1 = std::max<int64_t>(m, 1);
+  if (m < 0 || n < 0 || lda < m1 || ldd < m1 || ldc < m1 || ldf < m1 || ldb < std::max<int64_t>(n, 1) ||
+      lde < std::max<int64_t>(n, 1))
+    return set_err(ctx, GS_BADARG, "bad sizes");
+  if (m > (1 << 16) || n > (1 << 16)) return set_err(ctx, GS_BADARG, "order too large");
+  if (scale) *scale = 1.0;
+  if (perturbed) *perturbed = 0;
+  if (m == 0 || n == 0) return GS_OK;
+  if (!A || !B || !C || !D || !E || !F) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t mm = (size_t)m * m, nn = (size_t)n * n, mn = (size_t)m * n;
+  Arena ar;
+  const size_t o_A = ar.take<double2>(dev ? 1 : mm), o_D = ar.take<double2>(dev ? 1 : mm),
+               o_B = ar.take<double2>(dev ? 1 : nn), o_E = ar.take<double2>(dev ? 1 : nn),
+               o_C = ar.take<double2>(dev ? 1 : mn), o_F = ar.take<double2>(dev ? 1 : mn), o_flag = ar.take<int>(4),
+               o_bar = ar.take<char>(std::max<size_t>(gsyl_bar_bytes(), 16)), o_dbl = ar.take<double>(8);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const double2 *dA = (const double2*)A, *dB = (const double2*)B, *dD = (const double2*)D, *dE = (const double2*)E;
+  double2 *dC = (double2*)C, *dF = (double2*)F;
+  int64_t la = lda, lb = ldb, lc = ldc, ld = ldd, le = lde, lf = ldf;
+  if (!dev) {
+    auto up = [&](size_t off, const double* h, int64_t ldh, int64_t rows, int64_t cols) -> int {
+      CK(cudaMemcpy2DAsync(base + off, 16 * rows, h, 16 * ldh, 16 * rows, cols, cudaMemcpyHostToDevice, s));
+      return GS_OK;
+    };
+    if ((rc = up(o_A, A, lda, m, m)) || (rc = up(o_D, D, ldd, m, m)) || (rc = up(o_B, B, ldb, n, n)) ||
+        (rc = up(o_E, E, lde, n, n)) || (rc = up(o_C, C, ldc, m, n)) || (rc = up(o_F, F, ldf, m, n)))
+      return rc;
+    dA = (const double2*)(base + o_A); dD = (const double2*)(base + o_D);
+    dB = (const double2*)(base + o_B); dE = (const double2*)(base + o_E);
+    dC = (double2*)(base + o_C); dF = (double2*)(base + o_F);
+    la = ld = lc = lf = m;
+    lb = le = n;
+  }
+  GsylRun g{ctx, s, (int*)(base + o_flag), (GsylBar*)(base + o_bar), (double*)(base + o_dbl)};
+  CK(cudaEventRecord(ctx->t0, s));
+  bool pert = false;
+  rc = g.run(adjoint ? 1 : 0, (int)m, (int)n, dA, (int)la, dB, (int)lb, dD, (int)ld, dE, (int)le, dC, (int)lc, dF,
+             (int)lf, &pert);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  if (!dev) {
+    CK(cudaMemcpy2DAsync(C, 16 * ldc, dC, 16 * m, 16 * m, n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpy2DAsync(F, 16 * ldf, dF, 16 * m, 16 * m, n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  if (perturbed) *perturbed = pert ? 1 : 0;
+  return GS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -2163,6 +2387,20 @@ int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rcon
   return rcondv_impl<double2>(ctx, n, T, rconde, rcondv, flags);
 }
 
+int gs_gtrsylvester_c64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                        int64_t ldb, double* C, int64_t ldc, const double* D, int64_t ldd, const double* E,
+                        int64_t lde, double* F, int64_t ldf, int32_t adjoint, double* scale, int32_t* perturbed,
+                        unsigned flags) {
+  return gtrsyl_impl(ctx, m, n, A, lda, B, ldb, C, ldc, D, ldd, E, lde, F, ldf, adjoint, scale, perturbed, flags);
+}
+int gs_geigvalscond_c64(gs_context* ctx, int64_t n, const double* S, int64_t lds, const double* T, int64_t ldt,
+                        int64_t nsub, double* plpr, unsigned flags) {
+  return gcond_impl(ctx, n, S, lds, T, ldt, nsub, 0, 0, plpr, flags);
+}
+int gs_gsubspacesep_c64(gs_context* ctx, int64_t n, const double* S, int64_t lds, const double* T, int64_t ldt,
+                        int64_t nsub, int32_t pnorm, double* sep, unsigned flags) {
+  return gcond_impl(ctx, n, S, lds, T, ldt, nsub, 1, pnorm, sep, flags);
+}
 }  // extern "C"
 
 // ---- Hermitian path: geigen! / geigvals!, hessenberg!(Hermitian), _gschur!(SymTridiagonal) ----

@@ -32,7 +32,7 @@ __all__ = ["Schur", "Eigen", "UnconvergedException", "DimensionMismatch", "Argum
            "eig_adjoint_batched", "hessenberg", "gschur_mixed", "balance", "balance_", "Balancer", "balancer_lmul",
            "balancer_ldiv", "enormalize", "gordschur", "ordschur", "rconde", "EigenFull", "eigvalscond",
            "subspacesep", "eigen_rcond", "Hermitian", "SymTridiagonal", "HermitianHessenberg", "geigen",
-           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "GeneralizedSchur", "ggschur", "ggschur_batched", "ggeigvecs",
+           "geigvals", "gschur_symtridiag", "hessenberg_hermitian", "GeneralizedSchur", "ggschur", "ggschur_batched", "ggeigvecs", "trsylvester", "adjtrsylvester",
            "get_context", "Context", "pack_batch", "unpack_batch"]
 
 # LinearAlgebra.Eigen(values, vectors)
@@ -556,12 +556,36 @@ def _cond_T(S):
     return np.array(T, dtype=np.complex128 if cplx else np.float64, order="F"), cplx
 
 
+def _gpair(G):
+    """S and T of a GeneralizedSchur as complex Fortran arrays.  A real pair runs through the
+    complex path: on real triangular data every product, sum, quotient and modulus there has
+    a zero imaginary part, so the arithmetic is the reference's real arithmetic."""
+    S = np.array(G.S, dtype=np.complex128, order="F")
+    T = np.array(G.T, dtype=np.complex128, order="F")
+    n = _checksquare(S)
+    if T.shape != S.shape:
+        raise DimensionMismatch("S and T must have the same size")
+    return S, T, n
+
+
 def eigvalscond(S, nsub, ctx=None):
     """eigvalscond(S, nsub) (ordschur.jl:84-105): reciprocal condition number of the
     leading nsub eigenvalues of the Schur form S (a Schur tuple or its T), from one
     triangular Sylvester solve on the GPU.  Use gordschur to bring the eigenvalues of
-    interest to the front first."""
+    interest to the front first.
+
+    For a GeneralizedSchur (gcondition.jl:121-165) returns (pl, pr), the reciprocal norms of
+    the left and right projectors onto the deflating subspaces of the leading nsub block,
+    from one generalized Sylvester solve."""
     ctx = ctx or get_context()
+    if isinstance(S, GeneralizedSchur):
+        Sc, Tc, n = _gpair(S)
+        out = np.zeros(2)
+        rc = ctx.lib.gs_geigvalscond_c64(ctx.handle, n, _ptr(Sc), max(n, 1), _ptr(Tc), max(n, 1), int(nsub),
+                                         _ptr(out), 0)
+        if rc != GS_OK:
+            _raise(rc, ctx, "eigvalscond")
+        return float(out[0]), float(out[1])
     T, cplx = _cond_T(S)
     n = _checksquare(T)
     out = np.zeros(1)
@@ -572,11 +596,31 @@ def eigvalscond(S, nsub, ctx=None):
     return float(out[0])
 
 
-def subspacesep(S, nsub, ctx=None):
+def subspacesep(S, nsub, pnorm=None, ctx=None):
     """subspacesep(S, nsub) (ordschur.jl:107-140): estimated reciprocal condition of the
     invariant subspace of the leading nsub block (the separation of the two diagonal
-    blocks, by the one-norm estimator over GPU Sylvester solves).  0 < nsub < n."""
+    blocks, by the one-norm estimator over GPU Sylvester solves).  0 < nsub < n.
+
+    For a GeneralizedSchur (gcondition.jl:169-260) returns [Difu, Difl]: with pnorm "F"
+    (the default) the look-ahead estimates of _trgsep, with pnorm 1 the one-norm estimates
+    over the generalized Sylvester operator and its adjoint."""
     ctx = ctx or get_context()
+    if isinstance(S, GeneralizedSchur):
+        if pnorm is None or pnorm in ("F", "Frobenius"):
+            pn = 0
+        elif pnorm == 1:
+            pn = 1
+        else:
+            raise ArgumentError("pnorm must be :Frobenius or 1")
+        Sc, Tc, n = _gpair(S)
+        out = np.zeros(2)
+        rc = ctx.lib.gs_gsubspacesep_c64(ctx.handle, n, _ptr(Sc), max(n, 1), _ptr(Tc), max(n, 1), int(nsub), pn,
+                                         _ptr(out), 0)
+        if rc != GS_OK:
+            _raise(rc, ctx, "subspacesep")
+        return out
+    if pnorm is not None:
+        raise ArgumentError("subspacesep of a Schur form takes no pnorm")
     T, cplx = _cond_T(S)
     n = _checksquare(T)
     out = np.zeros(1)
@@ -585,6 +629,40 @@ def subspacesep(S, nsub, ctx=None):
     if rc != GS_OK:
         _raise(rc, ctx, "subspacesep")
     return float(out[0])
+
+
+def _gtrsyl(A, B, C, D, E, F, adjoint, ctx):
+    ctx = ctx or get_context()
+    A_, B_, D_, E_ = (np.array(x, dtype=np.complex128, order="F") for x in (A, B, D, E))
+    m, n = _checksquare(A_), _checksquare(B_)
+    if D_.shape != (m, m) or E_.shape != (n, n):
+        raise DimensionMismatch("dimensions of D and E must match A and B")
+    R = np.array(C, dtype=np.complex128, order="F")
+    L = np.array(F, dtype=np.complex128, order="F")
+    if R.shape != (m, n) or L.shape != (m, n):
+        raise DimensionMismatch("dimensions of C %s and F %s must match A, (%d,%d), and B, (%d,%d)"
+                                % (R.shape, L.shape, m, m, n, n))
+    sc = np.ones(1)
+    pert = np.zeros(1, dtype=np.int32)
+    rc = ctx.lib.gs_gtrsylvester_c64(ctx.handle, m, n, _ptr(A_), max(m, 1), _ptr(B_), max(n, 1), _ptr(R), max(m, 1),
+                                     _ptr(D_), max(m, 1), _ptr(E_), max(n, 1), _ptr(L), max(m, 1), int(adjoint),
+                                     _ptr(sc), _ptr(pert), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "adjtrsylvester" if adjoint else "trsylvester")
+    return R, L, float(sc[0]), bool(pert[0])
+
+
+def trsylvester(A, B, C, D, E, F, ctx=None):
+    """trsylvester!(A, B, C, D, E, F) (gsylvester.jl:23-99): solves A R - L B = s C,
+    D R - L E = s F for complex upper triangular A, D (m x m) and B, E (n x n) on the GPU.
+    Returns (R, L, s, perturbed); the inputs are not modified."""
+    return _gtrsyl(A, B, C, D, E, F, False, ctx)
+
+
+def adjtrsylvester(A, B, C, D, E, F, ctx=None):
+    """adjtrsylvester!(A, B, C, D, E, F) (gsylvester.jl:103-155): solves A^H R + D^H L = s C,
+    R B^H + L E^H = -s F.  Returns (R, L, s, perturbed)."""
+    return _gtrsyl(A, B, C, D, E, F, True, ctx)
 
 
 def eigen_rcond(S, want_rconde=True, want_rcondv=True, ctx=None):

@@ -76,6 +76,10 @@ SIGNATURES = {
     "gs_ggschur_batched_f64": (_i, [_p, _i64, _p, _p, _i64, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _u]),
     "gs_ggeigvecs_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _u]),
     "gs_ggordschur_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_gtrsylvester_c64": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i, _p,
+                                 _p, _u]),
+    "gs_geigvalscond_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _i64, _p, _u]),
+    "gs_gsubspacesep_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _i64, _i, _p, _u]),
     "gs_ggeigvecs_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _u]),
     "gs_gemm_f64_tc": (_i, [_p, _i64, _i64, _i64, _p, _i64, _i, _p, _i64, _p, _i64, _u]),
     "gs_ggschur_batched_c64": (_i, [_p, _i64, _p, _p, _i64, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _u]),

@@ -247,6 +247,33 @@ GS_API int gs_subspacesep_f64(gs_context* ctx, int64_t n, const double* T, int64
                               unsigned flags);
 GS_API int gs_subspacesep_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
                               unsigned flags);
+/* Generalized Sylvester equations of complex upper triangular A, D (m x m) and B, E
+ * (n x n), interleaved complex, C and F m x n overwritten with R and L:
+ *   adjoint = 0: trsylvester!(A, B, C, D, E, F) (gsylvester.jl:23-99)
+ *                A R - L B = scale C,  D R - L E = scale F
+ *   adjoint = 1: adjtrsylvester!(A, B, C, D, E, F) (gsylvester.jl:103-155)
+ *                A^H R + D^H L = scale C,  R B^H + L E^H = -scale F
+ * Only the upper triangles of A, B, D, E are read.  *scale is 1 on success; *perturbed is 1
+ * when a 2 x 2 pivot was raised to smin (the reference's fourth return value).  Where a
+ * 2 x 2 solve would need rescaling against overflow the call fails with GS_BADARG (the
+ * reference's rescaling branch raises there).  With GS_DEVICE all arrays are device
+ * pointers. */
+GS_API int gs_gtrsylvester_c64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                               int64_t ldb, double* C, int64_t ldc, const double* D, int64_t ldd, const double* E,
+                               int64_t lde, double* F, int64_t ldf, int32_t adjoint, double* scale,
+                               int32_t* perturbed, unsigned flags);
+/* eigvalscond(S::GeneralizedSchur, nsub) (gcondition.jl:121-165) of a complex generalized
+ * Schur pair (S, T), n x n: plpr[0] = pl, plpr[1] = pr, the reciprocal norms of the left
+ * and right projectors onto the deflating subspaces of the leading nsub block. */
+GS_API int gs_geigvalscond_c64(gs_context* ctx, int64_t n, const double* S, int64_t lds, const double* T,
+                               int64_t ldt, int64_t nsub, double* plpr, unsigned flags);
+/* subspacesep(S::GeneralizedSchur, nsub; pnorm) (gcondition.jl:169-260): sep[0], sep[1]
+ * the estimated separations (Difu, Difl) of the leading nsub block from the rest.
+ * pnorm = 0 (:Frobenius, the default there): the look-ahead estimate of _trgsep
+ * (gcondition.jl:8-115); pnorm = 1: the one-norm estimate of norm1est! over the generalized
+ * Sylvester operator and its adjoint, applied in place (0 < nsub < n). */
+GS_API int gs_gsubspacesep_c64(gs_context* ctx, int64_t n, const double* S, int64_t lds, const double* T,
+                               int64_t ldt, int64_t nsub, int32_t pnorm, double* sep, unsigned flags);
 /* eigen!(A; jcv = true) (pirates.jl:136-153) on a Schur factor T (n x n, ld n): for each
  * j, eigenvalue j moved to the front of a copy of T by ordschur!, then rconde[j] =
  * eigvalscond(., 1) (skipped when rconde is NULL) and rcondv[j] = subspacesep(., 1)

@@ -9,6 +9,7 @@
 #include "condition_oracle.hpp"
 #include "hermitian_oracle.hpp"
 #include "qz_oracle.hpp"
+#include "gcondition_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -274,6 +275,20 @@ int or_rgevc_d(int n, const double* s, const double* p, const double* x, double*
 int or_ggordschur_z(int n, double* s, double* t, double* q, double* z, const int* select, int scale, double* al,
                     double* be) {
   return gordschur_cplx<double>(n, (zc*)s, (zc*)t, (zc*)q, (zc*)z, select, scale != 0, (zc*)al, (zc*)be);
+}
+
+// trsylvester!(A, B, C, D, E, F) (adj = 0) / adjtrsylvester! (adj = 1) for complex triangular
+// A, D (m x m), B, E (n x n); C, F (m x n) overwritten; returns the reference's scale.
+double or_gtrsyl_z(int m, int n, const double* a, const double* b, double* c, const double* d, const double* e,
+                   double* f, int adj) {
+  if (adj) return gadjtrsyl<double>(m, n, (const zc*)a, (const zc*)b, (zc*)c, (const zc*)d, (const zc*)e, (zc*)f);
+  return gtrsyl<double>(m, n, (const zc*)a, (const zc*)b, (zc*)c, (const zc*)d, (const zc*)e, (zc*)f);
+}
+// eigvalscond / subspacesep (pnorm = :F) of a complex generalized Schur form (gcondition.jl)
+int or_gcond_z(int n, const double* s, const double* t, int nsub, double* out, int sep) {
+  if (sep) gsubspacesep<double>(n, (const zc*)s, (const zc*)t, nsub, out);
+  else geigvalscond<double>(n, (const zc*)s, (const zc*)t, nsub, &out[0], &out[1]);
+  return 0;
 }
 
 int or_gs2x2_d(double* h, double* cs, double* sn, double* w) {

@@ -56,6 +56,8 @@ def lib():
             "or_ggschur_d": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
             "or_rgevc_d": [_i, _p, _p, _p, _p, _i],
             "or_ggordschur_z": [_i, _p, _p, _p, _p, _p, _i, _p, _p],
+            "or_gtrsyl_z": [_i, _i, _p, _p, _p, _p, _p, _p, _i],
+            "or_gcond_z": [_i, _p, _p, _i, _p, _i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -376,3 +378,95 @@ def ggordschur(S, T, Q, Z, select, scale=True):
     st = lib().or_ggordschur_z(n, _ptr(Sf), _ptr(Tf), _ptr(Qf), _ptr(Zf), sel.ctypes.data_as(ctypes.c_void_p),
                                int(scale), _ptr(al), _ptr(be))
     return Sf, Tf, al[:n], be[:n], Qf, Zf, st
+
+
+def gtrsylvester(A, B, C, D, E, F, adjoint=False):
+    """trsylvester!(A, B, C, D, E, F) / adjtrsylvester! (gsylvester.jl:23-155) for complex
+    triangular matrices: (R, L, scale)."""
+    A_, B_, D_, E_ = (_f(x, np.complex128) for x in (A, B, D, E))
+    C_, F_ = _f(C, np.complex128), _f(F, np.complex128)
+    m, n = C_.shape
+    fn = lib().or_gtrsyl_z
+    fn.restype = ctypes.c_double
+    sc = fn(m, n, _ptr(A_), _ptr(B_), _ptr(C_), _ptr(D_), _ptr(E_), _ptr(F_), int(adjoint))
+    return C_, F_, sc
+
+
+def geigvalscond(S, T, nsub):
+    """eigvalscond(S::GeneralizedSchur, nsub) (gcondition.jl:121-165): (pl, pr)."""
+    Sf, Tf = _f(S, np.complex128), _f(T, np.complex128)
+    out = np.zeros(2)
+    lib().or_gcond_z(Sf.shape[0], _ptr(Sf), _ptr(Tf), int(nsub), _ptr(out), 0)
+    return out[0], out[1]
+
+
+def gsubspacesep(S, T, nsub):
+    """subspacesep(S::GeneralizedSchur, nsub) with pnorm = :F (gcondition.jl:169-260)."""
+    Sf, Tf = _f(S, np.complex128), _f(T, np.complex128)
+    out = np.zeros(2)
+    lib().or_gcond_z(Sf.shape[0], _ptr(Sf), _ptr(Tf), int(nsub), _ptr(out), 1)
+    return out
+
+
+def norm1est(apply, apply_h, N):
+    """norm1est! (norm1est.jl:21-74) with apply / apply_h returning the operator (its adjoint)
+    applied to a vector; _findamax (norm1est.jl:76-99) on abs2 for complex vectors."""
+    tiny = np.finfo(np.float64).tiny
+    x = apply(np.full(N, 1.0 / N, dtype=np.complex128))
+    if N == 1:
+        return abs(x[0])
+    gamma = float(np.sum(np.abs(x)))
+
+    def sign(v):
+        a = np.abs(v)
+        out = np.ones_like(v)
+        big = a > tiny
+        out[big] = v[big] / a[big]
+        return out
+
+    def findamax(v):
+        k = v.real * v.real + v.imag * v.imag
+        i0 = int(np.argmax(k))
+        return float(np.sqrt(k[i0])), i0
+
+    x = apply_h(sign(x))
+    ax0, j0 = findamax(x)
+    for _ in range(5):
+        e = np.zeros(N, dtype=np.complex128)
+        e[j0] = 1.0
+        x = apply(e)
+        old = gamma
+        gamma = float(np.sum(np.abs(x)))
+        if gamma <= old:
+            break
+        x = apply_h(sign(x))
+        jlast = j0
+        ax0, j0 = findamax(x)
+        if abs(x[jlast]) == ax0:
+            break
+    v = np.array([(1.0 if i % 2 == 0 else -1.0) * (1.0 + i / (N - 1)) for i in range(N)], dtype=np.complex128)
+    v = apply(v)
+    t = 2.0 * float(np.sum(np.abs(v))) / (3 * N)
+    return max(t, gamma)
+
+
+def gsubspacesep1(S, T, nsub):
+    """subspacesep(S::GeneralizedSchur, nsub; pnorm = 1) (gcondition.jl:169-260) with the
+    Sylvester solves applied in place, as in the standard-form subspacesep
+    (ordschur.jl:118-140): [1 / est_u, 1 / est_l]."""
+    S = np.asarray(S, dtype=np.complex128)
+    T = np.asarray(T, dtype=np.complex128)
+    n = S.shape[0]
+    n1, n2 = nsub, n - nsub
+    out = []
+    for A, B, D, E, m, q in ((S[:n1, :n1], S[n1:, n1:], T[:n1, :n1], T[n1:, n1:], n1, n2),
+                             (S[n1:, n1:], S[:n1, :n1], T[n1:, n1:], T[:n1, :n1], n2, n1)):
+        def op(adj, A=A, B=B, D=D, E=E, m=m, q=q):
+            def f(x):
+                R = x[:m * q].reshape((m, q), order="F")
+                L = x[m * q:].reshape((m, q), order="F")
+                R2, L2, _ = gtrsylvester(A, B, R, D, E, L, adjoint=adj)
+                return np.concatenate([R2.ravel(order="F"), L2.ravel(order="F")])
+            return f
+        out.append(1.0 / norm1est(op(False), op(True), 2 * m * q))
+    return np.array(out)

@@ -132,3 +132,90 @@ def godunov():
         [-287, -16, 1712, -128, 1968, -30, 2032],
         [-2176, -287, -1565, -512, -541, -1152, -289]], dtype=np.float64)
     return A, np.array([-4, -2, -1, 0, 1, 2, 4], dtype=np.float64), 7.0e16
+
+
+def kp_pencil(alpha=1.0, beta=1.0, x=1.0, y=1.0, dtype=2):
+    """The CHK4 pencils of Kagstrom and Poromaa (LAWN 87) as the reference's KPTest builds
+    them (test/gordschur.jl:203-225): A = YH \\ (Da / X), B = YH \\ (I / X), with known
+    eigenvalues atrue and eigenvector factors YH, X."""
+    n = 5
+    if dtype == 1:
+        Da = np.diag(np.array([1, 2, 3, 4, 5], dtype=complex)) + alpha * np.eye(n)
+        atrue = np.array([1, 2, 3, 4, 5], dtype=complex) + alpha
+    else:
+        Da = (np.diag(np.array([1, 1, 1, 1 + alpha, 1 + alpha], dtype=complex))
+              + np.diag(np.array([-1, 0, 0, 1 + beta], dtype=complex), 1)
+              + np.diag(np.array([1, 0, 0, -1 - beta], dtype=complex), -1))
+        atrue = np.array([1 - 1j, 1 + 1j, 1, 1 + alpha - (1 + beta) * 1j, 1 + alpha + (1 + beta) * 1j])
+    YH = (np.eye(n, dtype=complex) + np.diag([0, -y, 0, 0], 1) + np.diag([-y, y, 0], 2)
+          + np.diag([y, -y], 3) + np.diag([-y], 4))
+    X = (np.eye(n, dtype=complex) + np.diag([0, x, 0, 0], 1) + np.diag([-x, -x, 0], 2)
+         + np.diag([-x, -x], 3) + np.diag([x], 4))
+    A = np.linalg.solve(YH, Da @ np.linalg.inv(X))
+    B = np.linalg.solve(YH, np.linalg.inv(X))
+    return A, B, atrue, YH, X
+
+
+def kp_truth(A, B, YH, X, S2, T2, j, lam, dtype):
+    """The known reciprocal condition of eigenvalue j and Difl of the reordered pair
+    (S2, T2) with lam in front (test/gordschur.jl:238-268)."""
+    n = 5
+    if dtype == 1 or j == 2:
+        yv, xv = YH[j, :], X[:, j]
+    else:
+        rows = {0: (0, 1, 1), 1: (0, 1, -1), 3: (3, 4, -1), 4: (3, 4, 1)}[j]
+        a, b, sgn = rows
+        yv = YH[a, :] + sgn * 1j * YH[b, :]
+        xv = X[:, a] + sgn * 1j * X[:, b]
+    # dot(y, M x) conjugates y
+    rcond = (np.sqrt(abs(np.vdot(yv, A @ xv)) ** 2 + abs(np.vdot(yv, B @ xv)) ** 2)
+             / (np.linalg.norm(xv) * np.linalg.norm(yv))) / np.sqrt(3.0)
+    I4 = np.eye(n - 1)
+    Zl = np.block([[lam * I4, -S2[1:, 1:]], [I4, -T2[1:, 1:]]])
+    difl = np.linalg.svd(Zl, compute_uv=False).min()
+    return rcond, difl
+
+
+def gsyl_problem(rng, m, n, adjoint):
+    """checkgsyl / checkgasyl (test/gordschur.jl:6-74): triangular A, B, D, E with separated
+    spectra and right-hand sides made from known X, Y."""
+    r = 0.5 * (1 + 1j)
+    A = np.triu(rng.random((m, m)) + 1j * rng.random((m, m)) - r) + 2 * np.eye(m)
+    B = np.triu(rng.random((n, n)) + 1j * rng.random((n, n)) - r) + np.eye(n)
+    X = rng.random((m, n)) + 1j * rng.random((m, n))
+    D = np.triu(rng.random((m, m)) + 1j * rng.random((m, m)) - r) + 4 * np.eye(m)
+    E = np.triu(rng.random((n, n)) + 1j * rng.random((n, n)) - r) + np.eye(n)
+    Y = rng.random((m, n)) + 1j * rng.random((m, n))
+    if adjoint:
+        C = A.conj().T @ X + D.conj().T @ Y
+        F = -X @ B.conj().T - Y @ E.conj().T
+    else:
+        C = A @ X - Y @ B
+        F = D @ X - Y @ E
+    return A, B, C, D, E, F, X, Y
+
+
+def gsyl_errors(A, B, C, D, E, F, X, Y, X2, Y2, scale, adjoint):
+    fa = np.linalg.norm(scale * X - X2) / np.linalg.norm(X)
+    fb = np.linalg.norm(scale * Y - Y2) / np.linalg.norm(Y)
+    if adjoint:
+        ra = A.conj().T @ X2 + D.conj().T @ Y2 - scale * C
+        rb = X2 @ B.conj().T + Y2 @ E.conj().T + scale * F
+    else:
+        ra = A @ X2 - Y2 @ B - scale * C
+        rb = D @ X2 - Y2 @ E - scale * F
+    nx = np.linalg.norm(X)
+    ba = np.linalg.norm(ra) / ((np.linalg.norm(A) + np.linalg.norm(B)) * nx)
+    bb = np.linalg.norm(rb) / ((np.linalg.norm(D) + np.linalg.norm(E)) * nx)
+    return fa, fb, ba, bb
+
+
+def check_gsyl_errors(m, n, errs):
+    # the reference's bounds: tol = 2, forward errors only below order 10
+    fa, fb, ba, bb = errs
+    stol = 2 * max(m, n) * EPS
+    if max(m, n) < 10:
+        assert fa < np.sqrt(stol) and fb < np.sqrt(stol)
+    assert ba < 2 and bb < 2
+    # and the working accuracy actually reached
+    assert ba < 100 * EPS and bb < 100 * EPS

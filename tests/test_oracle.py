@@ -15,8 +15,8 @@ import os
 import numpy as np
 import pytest
 
-from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, checkblocks, godunov, orth_error,
-                    randn_matrix)
+from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, check_gsyl_errors, checkblocks, godunov,
+                    gsyl_errors, gsyl_problem, kp_pencil, kp_truth, orth_error, randn_matrix)
 from oracle import pyoracle as po
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -251,3 +251,82 @@ def test_oracle_trsylvester_residual():
     B[1, 1] = A[0, 0]
     _, _, pert = po.trsylvester(A, B, rng.standard_normal((3, 2)))
     assert pert
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+@pytest.mark.parametrize("m,n", [(2, 4), (4, 2), (24, 24)])
+def test_oracle_gsylvester(m, n, adjoint):
+    """trsylvester! / adjtrsylvester! for pencils restated (gsylvester.jl:23-155), on the
+    reference's checkgsyl / checkgasyl problems."""
+    rng = np.random.default_rng(1234 + 10 * m + n + adjoint)
+    A, B, C, D, E, F, X, Y = gsyl_problem(rng, m, n, adjoint)
+    X2, Y2, scale = po.gtrsylvester(A, B, C, D, E, F, adjoint=adjoint)
+    assert scale == 1.0
+    check_gsyl_errors(m, n, gsyl_errors(A, B, C, D, E, F, X, Y, X2, Y2, scale, adjoint))
+
+
+def test_oracle_geigvalscond_vs_tgsen():
+    """eigvalscond(S::GeneralizedSchur) restated (gcondition.jl:121-165): pl and pr equal
+    LAPACK ztgsen's (ijob = 4), which solves the same generalized Sylvester equation."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    rng = np.random.default_rng(4242)
+    for n, k in ((8, 3), (16, 1), (40, 20), (60, 59)):
+        A = randn_matrix(rng, n, True)
+        B = randn_matrix(rng, n, True)
+        S, T, al, be, Q, Z, st = po.ggschur(A, B)
+        assert st == 0
+        sel = np.zeros(n, np.int32)
+        sel[:k] = 1
+        r = lapack.ztgsen(sel, S, T, Q, Z, ijob=4, lwork=2 * n * n + 4, liwork=2 * n * n + 8)
+        assert r[-1] == 0
+        pl, pr = po.geigvalscond(S, T, k)
+        assert abs(pl - r[7]) <= 1e-12 * pl and abs(pr - r[8]) <= 1e-12 * pr
+        # the look-ahead separations estimate the same quantities as ztgsen's dif (whose
+        # 2 x 2 solves pivot completely where the reference's lu pivots by rows)
+        sep = po.gsubspacesep(S, T, k)
+        assert np.all(sep > 0) and np.all(np.abs(np.log10(sep / r[9])) < 1)
+
+
+@pytest.mark.parametrize("dtype", [2, 1])
+def test_oracle_gcondition_kptest(dtype):
+    """KPTest (test/gordschur.jl:193-295, alpha = beta = x = y = 1): every eigenvalue of the
+    CHK4 pencil moved to the front by gordschur!, then pl, pr within two orders of magnitude
+    of its known reciprocal condition and sep within two orders of Difl."""
+    A, B, atrue, YH, X = kp_pencil(dtype=dtype)
+    S, T, al, be, Q, Z, st = po.ggschur(A, B)
+    assert st == 0
+    est = al / be
+    for j in range(5):
+        idx = int(np.argmin(np.abs(est - atrue[j])))
+        sel = np.zeros(5, np.int32)
+        sel[idx] = 1
+        if idx == 0:
+            S2, T2 = S, T
+        else:
+            S2, T2, _, _, _, _, st = po.ggordschur(S, T, Q, Z, sel)
+            assert st == 0
+        pl, pr = po.geigvalscond(S2, T2, 1)
+        sep = po.gsubspacesep(S2, T2, 1)
+        rcond, difl = kp_truth(A, B, YH, X, S2, T2, j, atrue[j], dtype)
+        assert abs(np.log10(pl / rcond)) < 2 and abs(np.log10(pr / rcond)) < 2
+        assert abs(np.log10(sep[0] / difl)) < 2 and abs(np.log10(sep[1] / difl)) < 2
+
+
+def test_oracle_gsubspacesep_onenorm():
+    """subspacesep(.; pnorm = 1) with the solves applied in place: 1 / est is a lower
+    bound on the one-norm of the inverse generalized Sylvester operator (its Kronecker
+    form), and for these pencils within a factor of three of it."""
+    rng = np.random.default_rng(777)
+    for n, k in ((6, 2), (12, 5), (20, 19)):
+        A = randn_matrix(rng, n, True)
+        B = randn_matrix(rng, n, True)
+        S, T, *_ = po.ggschur(A, B)
+        sep = po.gsubspacesep1(S, T, k)
+        for (A_, B_, D_, E_), s in zip(((S[:k, :k], S[k:, k:], T[:k, :k], T[k:, k:]),
+                                        (S[k:, k:], S[:k, :k], T[k:, k:], T[:k, :k])), sep):
+            m, q = A_.shape[0], B_.shape[0]
+            Im, Iq = np.eye(m), np.eye(q)
+            Zk = np.block([[np.kron(Iq, A_), -np.kron(B_.T, Im)], [np.kron(Iq, D_), -np.kron(E_.T, Im)]])
+            inv1 = np.linalg.norm(np.linalg.inv(Zk), 1)
+            assert 1.0 / s <= inv1 * (1 + 1e-10)
+            assert 1.0 / s >= inv1 / 3
