@@ -185,6 +185,21 @@ size_t steqr_ctl_bytes();
 template <class S>
 cudaError_t launch_steqr(int n, double* d, double* e, S* Z, long long ldz, int nz, double* rot, void* ctl,
                          long long maxsweeps, int num_sms, cudaStream_t s);
+// The QR iteration on nprob independent small tridiagonals (problem b: entries off[b] ..
+// off[b] + msz[b] - 1 of d and e, msz[b] <= maxm <= 64), one warp each; with wantq the
+// problem's diagonal block of Q (ld ldq) is set to the identity and receives the rotations.
+// status |= 2 when a problem hit its iteration limit (30 msz).
+cudaError_t launch_steqr_leaves(int nprob, const int* off, const int* msz, int maxm, double* d, double* e, double* Q,
+                                long long ldq, int wantq, int* status, cudaStream_t s);
+// _gschur!(SymTridiagonal(d, e), DivideAndConquer(), Z) (symtri_dc.jl:6-104) on device
+// d (n), e (n - 1), Z (n x n, ld ldz; interleaved complex when zcplx; or NULL): d receives
+// the eigenvalues in the algorithm's order and Z is multiplied from the right by the
+// eigenvectors.  ws: stedc_ws_bytes(n, zcplx) bytes.  *status: 0, 1 (a secular equation did
+// not converge), 2 (a QR leaf hit its iteration limit), 4 (a wait in the tensor-core GEMM
+// timed out).  Synchronises the stream.
+size_t stedc_ws_bytes(int n, int zcplx);
+cudaError_t run_stedc(int n, double* d, double* e, double* Z, long long ldz, int zcplx, char* ws, int num_sms,
+                      cudaStream_t s, int* status);
 
 template <class S>
 cudaError_t launch_cond_maxabs(const S* M, int ld, int rows, int cols, unsigned long long* out, int nsm, cudaStream_t s);

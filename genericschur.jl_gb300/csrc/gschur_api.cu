@@ -2407,10 +2407,10 @@ int gs_gsubspacesep_c64(gs_context* ctx, int64_t n, const double* S, int64_t lds
 namespace {
 
 struct HeLayout {
-  size_t o_A, o_B, o_W, o_part, o_ctl, o_tau, o_d, o_e, o_Q, o_rot, o_st, o_p, bytes;
+  size_t o_A, o_B, o_W, o_part, o_ctl, o_tau, o_d, o_e, o_Q, o_rot, o_st, o_p, o_dc, bytes;
   int npart;
 };
-template <class S> HeLayout he_layout(int64_t n, bool host_a, bool wantq, int num_sms) {
+template <class S> HeLayout he_layout(int64_t n, bool host_a, bool wantq, int num_sms, bool dc = false) {
   HeLayout L;
   Arena ar;
   const size_t nn = (size_t)n * n;
@@ -2427,8 +2427,18 @@ template <class S> HeLayout he_layout(int64_t n, bool host_a, bool wantq, int nu
   L.o_rot = ar.take<double>(4 * std::max<int64_t>(n, 1));
   L.o_st = ar.take<char>(steqr_ctl_bytes());
   L.o_p = ar.take<int>(std::max<int64_t>(n, 1));
+  L.o_dc = ar.take<char>(dc ? stedc_ws_bytes((int)n, sizeof(S) == sizeof(double2) ? 1 : 0) : 1);
   L.bytes = ar.off;
   return L;
+}
+
+// run_stedc's status as the library's error codes (the reference throws
+// UnconvergedException when a secular equation fails, symtri_dc.jl:190-192)
+int stedc_result(gs_context* ctx, int st) {
+  if (st & 4) return set_err(ctx, GS_CUDA, "divide and conquer: a tensor-core GEMM wait timed out");
+  if (st & 1) return set_err(ctx, GS_UNCONVERGED, "unable to solve secular equation accurately");
+  if (st & 2) return set_err(ctx, GS_UNCONVERGED, "tridiagonal QR (divide-and-conquer leaf): sweep limit reached");
+  return GS_OK;
 }
 
 // reads the sweep kernel's {err, status}
@@ -2453,7 +2463,9 @@ int heev_impl(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, doub
   if (!A || !w || (wantz && (!V || ldv < n))) return set_err(ctx, GS_BADARG, "null or short array argument");
   CK(cudaSetDevice(ctx->device));
   const bool dev = flags & GS_DEVICE;
-  const HeLayout L = he_layout<S>(n, !dev, wantz, ctx->num_sms);
+  const bool dc = flags & GS_DC;
+  if (dc && n > (1 << 15)) return set_err(ctx, GS_BADARG, "order too large for divide and conquer");
+  const HeLayout L = he_layout<S>(n, !dev, wantz, ctx->num_sms, dc);
   int rc = ensure_ws(ctx, L.bytes);
   if (rc) return rc;
   char* base = ctx->dws;
@@ -2475,11 +2487,21 @@ int heev_impl(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, doub
   CK(launch_he_tridiag<S>(dA, ld, (int)n, upper, B, (S*)(base + L.o_W), (S*)(base + L.o_part), L.npart,
                           (HeCtlBuf*)(base + L.o_ctl), tau, d, e, ctx->num_sms, s));
   if (wantz) CK(launch_he_formq<S>(B, (int)n, tau, Q, ctx->num_sms, s));
-  CK(launch_steqr<S>((int)n, d, e, wantz ? Q : nullptr, n, wantz ? (int)n : 0, (double*)(base + L.o_rot),
-                     base + L.o_st, 30LL * n, ctx->num_sms, s));
-  CK(cudaEventRecord(ctx->t1, s));
-  ctx->timed = true;
-  rc = steqr_result(ctx, base + L.o_st, s);
+  if (dc) {
+    // gschur!(H, V, DivideAndConquer()) (GenericSchur.jl:126-136, symtri_dc.jl:6-104)
+    int st = 0;
+    CK(run_stedc((int)n, d, e, wantz ? (double*)Q : nullptr, n, sizeof(S) == sizeof(double2) ? 1 : 0, base + L.o_dc,
+                 ctx->num_sms, s, &st));
+    CK(cudaEventRecord(ctx->t1, s));
+    ctx->timed = true;
+    rc = stedc_result(ctx, st);
+  } else {
+    CK(launch_steqr<S>((int)n, d, e, wantz ? Q : nullptr, n, wantz ? (int)n : 0, (double*)(base + L.o_rot),
+                       base + L.o_st, 30LL * n, ctx->num_sms, s));
+    CK(cudaEventRecord(ctx->t1, s));
+    ctx->timed = true;
+    rc = steqr_result(ctx, base + L.o_st, s);
+  }
   if (rc == GS_CUDA) return rc;
   // sorteig!(w, V, eigsortby): stable ascending order
   std::vector<double> dh(n);
@@ -2582,6 +2604,47 @@ int gs_hetrd_f64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, d
 int gs_hetrd_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int uplo, double* d, double* e, double* tau,
                  unsigned flags) {
   return hetrd_impl<double2>(ctx, n, A, lda, uplo, d, e, tau, flags);
+}
+
+int gs_stedc_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 15)) return set_err(ctx, GS_BADARG, "bad order");
+  if (n == 0) return GS_OK;
+  if (!d || (n > 1 && !e) || (Z && ldz < n)) return set_err(ctx, GS_BADARG, "null or short array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  Arena ar;
+  const size_t o_d = ar.take<double>(n), o_e = ar.take<double>(n), o_Z = ar.take<double>(Z && !dev ? (size_t)n * n : 1),
+               o_dc = ar.take<char>(stedc_ws_bytes((int)n, 0));
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double* dd = (double*)(base + o_d);
+  double* de = (double*)(base + o_e);
+  double* dZ = Z ? (dev ? Z : (double*)(base + o_Z)) : nullptr;
+  const long long ldd = dev ? ldz : n;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpyAsync(dd, d, sizeof(double) * n, in, s));
+  CK(cudaMemsetAsync(de, 0, sizeof(double) * n, s));
+  if (n > 1) CK(cudaMemcpyAsync(de, e, sizeof(double) * (n - 1), in, s));
+  if (Z && !dev)
+    CK(cudaMemcpy2DAsync(dZ, sizeof(double) * n, Z, sizeof(double) * ldz, sizeof(double) * n, n, in, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  int st = 0;
+  CK(run_stedc((int)n, dd, de, dZ, ldd, 0, base + o_dc, ctx->num_sms, s, &st));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  rc = stedc_result(ctx, st);
+  if (rc == GS_CUDA) return rc;
+  CK(cudaMemcpyAsync(d, dd, sizeof(double) * n, out, s));
+  if (n > 1) CK(cudaMemcpyAsync(e, de, sizeof(double) * (n - 1), out, s));
+  if (Z && !dev)
+    CK(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, dZ, sizeof(double) * n, sizeof(double) * n, n, out, s));
+  CK(cudaStreamSynchronize(s));
+  return rc;
 }
 
 int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags) {

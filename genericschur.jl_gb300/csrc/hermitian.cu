@@ -679,6 +679,53 @@ __global__ void __launch_bounds__(kHeT) k_steqr(int n, double* dg, double* eg, S
   }
 }
 
+// The QR iteration on many small independent tridiagonals at once (the leaves of a
+// divide-and-conquer tree, symtri_dc.jl:145-168, and its small isolated blocks): one warp
+// per problem, d and e in shared memory, the rotations of each emitted phase applied to
+// the problem's diagonal block of Q (rows of the block = lanes) right away.  Q's block is
+// set to the identity first; the rest of Q is not touched.
+constexpr int kLeafMax = 64;
+constexpr int kLeafWarps = 4;
+__global__ void __launch_bounds__(32 * kLeafWarps) k_steqr_leaves(int nprob, const int* __restrict__ off,
+                                                                  const int* __restrict__ msz, double* dg, double* eg,
+                                                                  double* Q, long long ldq, int wantq, int* status) {
+  __shared__ double sd[kLeafWarps][kLeafMax + 1], se[kLeafWarps][kLeafMax + 1];
+  __shared__ double scb[kLeafWarps][kLeafMax], ssb[kLeafWarps][kLeafMax];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kLeafWarps + wid;
+  if (b >= nprob) return;
+  const int o = off[b], m = msz[b];
+  double* d = sd[wid];
+  double* e = se[wid];
+  for (int i = lane; i <= m; i += 32) {
+    d[i] = i < m ? dg[o + i] : 0.0;
+    e[i] = i < m - 1 ? eg[o + i] : 0.0;
+  }
+  double* Qb = wantq ? Q + o + (size_t)o * ldq : nullptr;
+  if (wantq)
+    for (int c = 0; c < m; ++c)
+      for (int r = lane; r < m; r += 32) Qb[r + (size_t)c * ldq] = r == c ? 1.0 : 0.0;
+  __syncwarp();
+  StState st;
+  st.l1 = 1; st.l = 0; st.lend = 0; st.lsave = 0; st.lendsave = 0; st.iscale = 0; st.mode = 0;
+  st.anorm = 0.0; st.sweeps = 0; st.status = 0;
+  StPhase ph;
+  ph.i0 = 0; ph.count = 0; ph.dir = 0; ph.done = 0;
+  const long long maxsweeps = 30LL * m;
+  for (;;) {
+    const int emitted = st_advance(st, m, d, e, scb[wid], ssb[wid], &ph, wantq != 0, maxsweeps, lane);
+    __syncwarp();
+    if (!emitted) break;
+    for (int r = lane; r < m; r += 32) apply_phase<double>(Qb, ldq, r, ph, scb[wid], ssb[wid]);
+    __syncwarp();
+  }
+  for (int i = lane; i < m; i += 32) {
+    dg[o + i] = d[i];
+    if (i < m - 1) eg[o + i] = e[i];
+  }
+  if (lane == 0 && st.status) atomicOr(status, 2);
+}
+
 int grid_of(size_t work) { return (int)std::min<size_t>((work + 255) / 256, 4096); }
 
 }  // namespace
@@ -725,6 +772,15 @@ cudaError_t launch_he_gather(const S* Z, int n, const int* p, int rev, S* V, lon
 }
 
 size_t steqr_ctl_bytes() { return sizeof(StCtl); }
+
+cudaError_t launch_steqr_leaves(int nprob, const int* off, const int* msz, int maxm, double* d, double* e, double* Q,
+                                long long ldq, int wantq, int* status, cudaStream_t s) {
+  if (nprob == 0) return cudaSuccess;
+  if (maxm > kLeafMax) return cudaErrorInvalidValue;
+  k_steqr_leaves<<<(nprob + kLeafWarps - 1) / kLeafWarps, 32 * kLeafWarps, 0, s>>>(nprob, off, msz, d, e, Q, ldq, wantq,
+                                                                                  status);
+  return cudaGetLastError();
+}
 
 template <class S>
 cudaError_t launch_steqr(int n, double* d, double* e, S* Z, long long ldz, int nz, double* rot, void* ctl,

@@ -703,7 +703,26 @@ SymTridiagonal = namedtuple("SymTridiagonal", ["dv", "ev"])
 HermitianHessenberg = namedtuple("HermitianHessenberg", ["factors", "tau", "dv", "ev", "uplo"])
 
 
-def _heev(H, wantv, ctx):
+_ALGS = {"QRIteration": "QR", "QR": "QR", "DivideAndConquer": "DC", "DC": "DC"}
+
+
+def _alg(alg):
+    """QRIteration() (the default) or DivideAndConquer() (GenericSchur.jl:119-136);
+    RobustRepresentations falls back to QRIteration with a warning (symtridiag.jl:12-26)."""
+    if alg is None:
+        return "QR"
+    name = alg if isinstance(alg, str) else type(alg).__name__
+    if name == "RobustRepresentations":
+        import warnings
+        warnings.warn("GenericSchur does not currently provide alg=RobustRepresentations (LinearAlgebra "
+                      "default); falling back to QRIteration.")
+        return "QR"
+    if name not in _ALGS:
+        raise ArgumentError("Unsupported algorithm %s" % (name,))
+    return _ALGS[name]
+
+
+def _heev(H, wantv, ctx, alg=None):
     ctx = ctx or get_context()
     A = np.asarray(H.data)
     n = _checksquare(A)
@@ -714,8 +733,8 @@ def _heev(H, wantv, ctx):
     V = np.zeros((n, n), dtype=dt, order="F") if wantv else None
     fn = ctx.lib.gs_heev_c64 if cplx else ctx.lib.gs_heev_f64
     uplo = str(H.uplo).upper()[:1]
-    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), ord(uplo), _ptr(w), _ptr(V), max(n, 1),
-            _capi.GS_WANTZ if wantv else 0)
+    flags = (_capi.GS_WANTZ if wantv else 0) | (_capi.GS_DC if _alg(alg) == "DC" else 0)
+    rc = fn(ctx.handle, n, _ptr(A), max(n, 1), ord(uplo), _ptr(w), _ptr(V), max(n, 1), flags)
     if rc != GS_OK:
         _raise(rc, ctx, "geigen!")
     return w[:n], V
@@ -728,44 +747,46 @@ def _sorted(w, V, sortby):
     return w[p], (V[:, p] if V is not None else None)
 
 
-def geigen(H, sortby="default", ctx=None):
-    """geigen!(Hermitian(A, uplo)) (GenericSchur.jl:126-136) with QRIteration, on the GPU:
-    Eigen(values ascending, orthonormal vectors)."""
+def geigen(H, alg=None, sortby="default", ctx=None):
+    """geigen!(Hermitian(A, uplo), alg) (GenericSchur.jl:126-136) and geigen!(::SymTridiagonal,
+    alg) (symtridiag.jl:43-49) on the GPU: Eigen(values ascending, orthonormal vectors).
+    alg: "QRIteration" (default) or "DivideAndConquer" (symtri_dc.jl)."""
     if isinstance(H, SymTridiagonal):
-        w, V = _st_eig(H, True, sortby, ctx)
+        w, V = _st_eig(H, True, sortby, ctx, alg)
         return Eigen(w, V)
-    w, V = _heev(H, True, ctx)
+    w, V = _heev(H, True, ctx, alg)
     w, V = _sorted(w, V, sortby)
     return Eigen(w, V)
 
 
-def geigvals(H, sortby="default", ctx=None):
-    """geigvals!(Hermitian(A, uplo)) (GenericSchur.jl:138-146) with QRIteration."""
+def geigvals(H, alg=None, sortby="default", ctx=None):
+    """geigvals!(Hermitian(A, uplo), alg) (GenericSchur.jl:138-146)."""
     if isinstance(H, SymTridiagonal):
-        return _st_eig(H, False, sortby, ctx)[0]
-    w, _ = _heev(H, False, ctx)
+        return _st_eig(H, False, sortby, ctx, alg)[0]
+    w, _ = _heev(H, False, ctx, alg)
     return _sorted(w, None, sortby)[0]
 
 
-def gschur_symtridiag(T, Z=None, ctx=None):
-    """_gschur!(SymTridiagonal(dv, ev), QRIteration(), Z) (symtridiag.jl:79-183): the
-    eigenvalues in the iteration's order, the rotations applied to Z (when given).
-    Returns (d, e, Z)."""
+def gschur_symtridiag(T, Z=None, alg=None, ctx=None):
+    """_gschur!(SymTridiagonal(dv, ev), alg, Z): with QRIteration (symtridiag.jl:79-183) or
+    DivideAndConquer (symtri_dc.jl:6-104); the eigenvalues in the algorithm's order, Z
+    multiplied from the right by the eigenvectors (when given).  Returns (d, e, Z)."""
     ctx = ctx or get_context()
     d = np.array(T.dv, dtype=np.float64)
     n = len(d)
     e = np.zeros(max(n - 1, 1))
     e[:max(n - 1, 0)] = np.asarray(T.ev, dtype=np.float64)[:max(n - 1, 0)]
     Zc = np.array(Z, dtype=np.float64, order="F", copy=True) if Z is not None else None
-    rc = ctx.lib.gs_steqr_f64(ctx.handle, n, _ptr(d), _ptr(e), _ptr(Zc), max(n, 1), 0)
+    fn = ctx.lib.gs_stedc_f64 if _alg(alg) == "DC" else ctx.lib.gs_steqr_f64
+    rc = fn(ctx.handle, n, _ptr(d), _ptr(e), _ptr(Zc), max(n, 1), 0)
     if rc != GS_OK:
         _raise(rc, ctx, "_gschur!(SymTridiagonal)")
     return d, e[:max(n - 1, 0)], Zc
 
 
-def _st_eig(T, wantv, sortby, ctx):
+def _st_eig(T, wantv, sortby, ctx, alg=None):
     n = len(T.dv)
-    d, _, Z = gschur_symtridiag(T, np.eye(n) if wantv else None, ctx=ctx)
+    d, _, Z = gschur_symtridiag(T, np.eye(n) if wantv else None, alg=alg, ctx=ctx)
     p = np.argsort(d, kind="stable") if sortby == "default" else \
         (np.arange(n) if sortby is None else np.argsort([sortby(x) for x in d], kind="stable"))
     return d[p], (Z[:, p] if wantv else None)

@@ -23,6 +23,7 @@ GS_GRAPH = 8
 GS_RAW = 16
 GS_NOFALLBACK = 32
 GS_BAL_PERMUTE = 64
+GS_DC = 128
 
 _i = ctypes.c_int
 _i64 = ctypes.c_int64
@@ -71,6 +72,7 @@ SIGNATURES = {
     "gs_hetrd_f64": (_i, [_p, _i64, _p, _i64, _i, _p, _p, _p, _u]),
     "gs_hetrd_c64": (_i, [_p, _i64, _p, _i64, _i, _p, _p, _p, _u]),
     "gs_steqr_f64": (_i, [_p, _i64, _p, _p, _p, _i64, _u]),
+    "gs_stedc_f64": (_i, [_p, _i64, _p, _p, _p, _i64, _u]),
     "gs_ggschur_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _u]),
     "gs_ggschur_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _u]),
     "gs_ggschur_batched_f64": (_i, [_p, _i64, _p, _p, _i64, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _u]),

@@ -48,6 +48,7 @@ extern "C" {
 #define GS_RAW 16u    /* eigenvectors: skip _enormalize! (return the max-|re|+|im|-scaled vectors) */
 #define GS_NOFALLBACK 32u /* mixed precision: report GS_UNCONVERGED instead of recomputing in FP64   */
 #define GS_BAL_PERMUTE 64u /* balancing: search the row/column permutations (with GS_SCALE: scale too) */
+#define GS_DC 128u         /* Hermitian eigensolver: DivideAndConquer() instead of QRIteration()       */
 
 typedef struct gs_context gs_context;
 
@@ -285,7 +286,7 @@ GS_API int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, doubl
                               unsigned flags);
 
 /* geigen!(Hermitian(A, uplo)) / geigvals! (GenericSchur.jl:126-146) with the default
- * QRIteration: Householder tridiagonalization (hessenberg.jl:26-96), Q (hessenberg.jl:
+ * QRIteration (with GS_DC: DivideAndConquer(), symtri_dc.jl:6-104, n <= 32768): Householder tridiagonalization (hessenberg.jl:26-96), Q (hessenberg.jl:
  * 145-231) and the tridiagonal QL/QR iteration (symtridiag.jl:79-368).  uplo = 'L' or 'U'
  * names the triangle of A (n x n, lda) that is read; A is not modified.  w (n) receives the
  * eigenvalues in ascending order; with GS_WANTZ, V (n x n, ldv) the orthonormal
@@ -307,6 +308,11 @@ GS_API int gs_hetrd_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, int 
  * (n x n, ldz) is not NULL every rotation is applied to it from the right.  Used by
  * eigen!/eigvals!(::SymTridiagonal) (symtridiag.jl:43-57), which sort afterwards. */
 GS_API int gs_steqr_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags);
+/* _gschur!(SymTridiagonal(d, e), DivideAndConquer(), Z) (symtri_dc.jl:6-104, after LAPACK's
+ * xSTEDC): the same contract as gs_steqr_f64 (d receives the eigenvalues in the algorithm's
+ * order; Z, when not NULL, is multiplied from the right by the eigenvectors).  n <= 32768.
+ * GS_UNCONVERGED when a secular equation fails (the reference's UnconvergedException). */
+GS_API int gs_stedc_f64(gs_context* ctx, int64_t n, double* d, double* e, double* Z, int64_t ldz, unsigned flags);
 
 /* ggschur!(A, B; wantQ, wantZ, scale) (generalized.jl:21-80) for a complex pencil: qr!(B),
  * Hessenberg-triangular reduction (_hessenberg!, 82-113) and the single-shift QZ

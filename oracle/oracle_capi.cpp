@@ -10,6 +10,7 @@
 #include "hermitian_oracle.hpp"
 #include "qz_oracle.hpp"
 #include "gcondition_oracle.hpp"
+#include "stedc_oracle.hpp"
 
 using namespace orc;
 typedef cx<double> zc;
@@ -234,6 +235,10 @@ int or_hetrd_z(int n, double* a, int lda, int upper, double* d, double* e, doubl
 }
 // _gschur!(SymTridiagonal(d, e), QRIteration(), Z) (symtridiag.jl:79-183) with Z n x n
 // (wantz) or none.
+// _gschur!(SymTridiagonal(d, e), DivideAndConquer(), Z) with Z (n x n) multiplied in
+// place when wantz; 1 when a secular equation did not converge.
+int or_stedc_d(int n, double* d, double* e, double* z, int wantz) { return stedc(n, d, e, wantz ? z : nullptr, n); }
+
 int or_steqr_d(int n, double* d, double* e, double* z, int wantz) {
   return steqr<double, double>(n, d, e, wantz ? z : nullptr, n, wantz ? n : 0, 30LL * n);
 }

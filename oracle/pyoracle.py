@@ -51,6 +51,7 @@ def lib():
             "or_hetrd_d": [_i, _p, _i, _i, _p, _p, _p],
             "or_hetrd_z": [_i, _p, _i, _i, _p, _p, _p],
             "or_steqr_d": [_i, _p, _p, _p, _i],
+            "or_stedc_d": [_i, _p, _p, _p, _i],
             "or_ggschur_z": [_i, _p, _p, _p, _p, _p, _p, _i],
             "or_ggevc_z": [_i, _p, _p, _p, _p, _i],
             "or_ggschur_d": [_i, _p, _p, _p, _p, _p, _p, _p, _i],
@@ -312,6 +313,23 @@ def steqr(d, e, wantz=True):
     Z = np.asfortranarray(np.eye(n)) if wantz else None
     st = lib().or_steqr_d(n, _ptr(d), _ptr(e), _ptr(Z), int(wantz))
     return d, Z, st
+
+
+def stedc(d, e, Z=None, wantz=True):
+    """_gschur!(SymTridiagonal(d, e), DivideAndConquer(), Z) (symtri_dc.jl:6-104): the
+    eigenvalues in the algorithm's order, Z times the eigenvectors (Z = I when not given),
+    and the status (1: a secular equation did not converge)."""
+    d = np.array(d, dtype=np.float64)
+    e = np.array(e, dtype=np.float64)
+    n = d.shape[0]
+    if Z is None:
+        Z = np.eye(n, order="F")
+    else:
+        Z = np.array(Z, dtype=np.float64, order="F")
+    ee = np.zeros(max(n, 1))
+    ee[:max(n - 1, 0)] = e[:max(n - 1, 0)]
+    st = lib().or_stedc_d(n, _ptr(d), _ptr(ee), _ptr(Z), int(wantz))
+    return d, (Z if wantz else None), st
 
 
 def ggschur(A, B, scale=True):

@@ -219,3 +219,99 @@ def check_gsyl_errors(m, n, errs):
     assert ba < 2 and bb < 2
     # and the working accuracy actually reached
     assert ba < 100 * EPS and bb < 100 * EPS
+
+
+# ---- symmetric tridiagonal test matrices (test/symtridiag.jl:9-176) ----------------------
+def _wilkinson(n):
+    if n % 2 == 1:
+        nh = (n - 1) // 2
+        D = np.concatenate([np.arange(nh, 0, -1), [0], np.arange(1, nh + 1)]).astype(float)
+    else:
+        D = np.abs(np.arange(-(n - 1), n, 2, dtype=float) / 2)
+    return D, np.ones(n - 1)
+
+
+def st_testmat1(n, itype, rng):
+    """LAPACK-style class 1 (test/symtridiag.jl:50-103): A = Q' diag(lam) Q for a random
+    orthogonal Q, reduced to tridiagonal form; returns (d, e)."""
+    ulp = np.finfo(float).eps
+    kpar = 1 / ulp
+    lam = np.zeros(n)
+    j = np.arange(1, n + 1)
+    if itype == 1:
+        lam = 1.0 / j
+    elif itype == 2:
+        lam[:] = 1.0
+        lam[-1] = 1.0 / n
+    elif itype == 3:
+        lam = 1.0 / kpar ** ((j - 1) / (n - 1))
+    elif itype == 4:
+        lam = 1.0 - ((j - 1) / (n - 1)) * (1 - 1 / kpar)
+    elif itype == 5:
+        lam = np.exp(-np.log(n) * rng.random(n))
+    elif itype == 6:
+        lam = rng.standard_normal(n)
+    elif itype == 7:
+        lam[:-1] = np.arange(1, n) * ulp
+        lam[-1] = 1.0
+    elif itype == 8:
+        lam[0] = ulp
+        lam[1:-1] = 1 + np.sqrt(ulp) * np.arange(2, n)
+        lam[-1] = 2.0
+    elif itype == 9:
+        lam[0] = 1.0
+        for k in range(1, n):
+            lam[k] = lam[k - 1] + 100 * ulp
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = Q.T @ np.diag(lam) @ Q
+    import scipy.linalg
+    H = scipy.linalg.hessenberg((A + A.T) / 2)
+    return np.diag(H).copy(), np.diag(H, -1).copy()
+
+
+def st_testmat2(n, itype):
+    """Class 2 (test/symtridiag.jl:107-155): constant, Wilkinson, Clement, Legendre, Laguerre,
+    Hermite, and three Wilkinson blocks at extreme scales glued with zero couplings."""
+    ulp = np.finfo(float).eps
+    i = np.arange(1, n)
+    if itype == 1:
+        return np.ones(n), np.zeros(n - 1)
+    if itype == 2:
+        return np.full(n, 2.0), np.ones(n - 1)
+    if itype == 3:
+        return _wilkinson(n)
+    if itype == 4:
+        return np.zeros(n), np.sqrt(i * (n + 1 - i).astype(float))
+    if itype == 5:
+        k = np.arange(2, n + 1)
+        return np.zeros(n), k / np.sqrt(((2 * k - 1) * (2 * k) + 1).astype(float))
+    if itype == 6:
+        return np.arange(3, 2 * n + 2, 2, dtype=float), np.arange(2, n + 1, dtype=float)
+    if itype == 7:
+        return np.zeros(n), np.sqrt(i.astype(float))
+    if itype == 8:
+        small = np.finfo(float).tiny / ulp
+        large = np.finfo(float).max * ulp
+        D1, E1 = _wilkinson(n)
+        D = np.concatenate([small * D1, D1, large * D1])
+        E = np.concatenate([small * E1, [0.0], E1, [0.0], large * E1])
+        return D, E
+    raise ValueError(itype)
+
+
+def st_errors(D, E, lam, V):
+    """runtest (test/symtridiag.jl:181-218): the scaled residual and orthogonality errors."""
+    n = len(D)
+    T = np.diag(D) + np.diag(E, 1) + np.diag(E, -1)
+    myeps = np.finfo(float).eps
+    ntol = n
+    resnorm = np.abs(V @ np.diag(lam) @ V.T - T).max()
+    Tnorm = max(np.abs(T).sum(axis=0).max(), np.finfo(float).tiny)
+    if resnorm < Tnorm:
+        d_err = (resnorm / Tnorm) / (myeps * ntol)
+    elif Tnorm < 1:
+        d_err = (min(resnorm, Tnorm * ntol) / Tnorm) / (myeps * ntol)
+    else:
+        d_err = min(resnorm / Tnorm, ntol) / (myeps * ntol)
+    v_err = np.abs(V @ V.T - np.eye(n)).max() / (myeps * ntol)
+    return d_err, v_err

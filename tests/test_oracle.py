@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, check_gsyl_errors, checkblocks, godunov,
+                    st_errors, st_testmat1, st_testmat2,
                     gsyl_errors, gsyl_problem, kp_pencil, kp_truth, orth_error, randn_matrix)
 from oracle import pyoracle as po
 
@@ -330,3 +331,21 @@ def test_oracle_gsubspacesep_onenorm():
             inv1 = np.linalg.norm(np.linalg.inv(Zk), 1)
             assert 1.0 / s <= inv1 * (1 + 1e-10)
             assert 1.0 / s >= inv1 / 3
+
+
+@pytest.mark.parametrize("n", [32, 100, 257])
+def test_oracle_stedc_batch(n):
+    """The reference's SymTridiagonal batch (test/symtridiag.jl:158-178, 221-225) with
+    DivideAndConquer(): both matrix classes, residual and orthogonality below 50 (scaled by
+    n eps); the reference runs it at n = 32 (one merge), the larger orders build deeper trees.
+    The eigenvalues also match LAPACK's (numpy eigvalsh) to 50 n eps |T|."""
+    rng = np.random.default_rng(2100 + n)
+    cases = [st_testmat1(n, it, rng) for it in range(1, 10)] + [st_testmat2(n, it) for it in range(1, 9)]
+    for D, E in cases:
+        lam, V, st = po.stedc(D, E)
+        assert st == 0
+        de, ve = st_errors(D, E, lam, V)
+        assert de < 50 and ve < 50, (de, ve)
+        T = np.diag(D) + np.diag(E, 1) + np.diag(E, -1)
+        ref = np.linalg.eigvalsh(T)
+        assert np.abs(np.sort(lam) - ref).max() <= 50 * len(D) * EPS * np.abs(T).max()
