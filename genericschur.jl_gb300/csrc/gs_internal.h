@@ -147,6 +147,10 @@ struct GsylArgs {
 };
 size_t gsyl_bar_bytes();
 cudaError_t launch_gsyl(const GsylArgs& P, int num_sms, cudaStream_t s);
+// gordschur! of a real generalized Schur pair (qz_real.cu); Q, Z may be NULL; status 0 or
+// 1 + k of the block that could not be moved.
+cudaError_t launch_ggordschur_real(int n, double* S, double* T, double* Q, double* Z, const int* select, int scale,
+                                   double2* alpha, double* beta, int* status, cudaStream_t s);
 // Real pencils (qz_real.cu): A, B, Q, Z real; alpha complex, beta real.
 struct QzrBatch {
   int count;

@@ -1193,6 +1193,59 @@ int gs_ggordschur_c64(gs_context* ctx, int64_t n, double* S, double* T, double* 
   return GS_OK;
 }
 
+int gs_ggordschur_f64(gs_context* ctx, int64_t n, double* S, double* T, double* Q, double* Z, const int32_t* select,
+                      double* alpha, double* beta, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (n < 0 || n > (1 << 15)) return set_err(ctx, GS_BADARG, "bad order %lld", (long long)n);
+  if (n == 0) return GS_OK;
+  if (!S || !T || !select || !alpha || !beta) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t nn = (size_t)n * n, db = sizeof(double);
+  Arena ar;
+  const size_t o_S = ar.take<double>(dev ? 1 : nn), o_T = ar.take<double>(dev ? 1 : nn),
+               o_Q = ar.take<double>(dev || !Q ? 1 : nn), o_Z = ar.take<double>(dev || !Z ? 1 : nn),
+               o_al = ar.take<double2>(dev ? 1 : n), o_be = ar.take<double>(dev ? 1 : n), o_sel = ar.take<int>(n),
+               o_st = ar.take<int>(4);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  double* dS = dev ? S : (double*)(base + o_S);
+  double* dT = dev ? T : (double*)(base + o_T);
+  double* dQ = Q ? (dev ? Q : (double*)(base + o_Q)) : nullptr;
+  double* dZ = Z ? (dev ? Z : (double*)(base + o_Z)) : nullptr;
+  double2* dal = dev ? (double2*)alpha : (double2*)(base + o_al);
+  double* dbe = dev ? beta : (double*)(base + o_be);
+  int* dsel = (int*)(base + o_sel);
+  int* dst = (int*)(base + o_st);
+  if (!dev) {
+    CK(cudaMemcpyAsync(dS, S, db * nn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dT, T, db * nn, cudaMemcpyHostToDevice, s));
+    if (Q) CK(cudaMemcpyAsync(dQ, Q, db * nn, cudaMemcpyHostToDevice, s));
+    if (Z) CK(cudaMemcpyAsync(dZ, Z, db * nn, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemcpyAsync(dsel, select, sizeof(int) * n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  CK(launch_ggordschur_real((int)n, dS, dT, dQ, dZ, dsel, (flags & GS_SCALE) ? 1 : 0, dal, dbe, dst, s));
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!dev) {
+    CK(cudaMemcpyAsync(S, dS, db * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(T, dT, db * nn, cudaMemcpyDeviceToHost, s));
+    if (Q) CK(cudaMemcpyAsync(Q, dQ, db * nn, cudaMemcpyDeviceToHost, s));
+    if (Z) CK(cudaMemcpyAsync(Z, dZ, db * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(alpha, dal, sizeof(double2) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(beta, dbe, db * n, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (st) return set_err(ctx, GS_UNCONVERGED, "the block at %d could not be moved (ill-conditioned swap)", st - 1);
+  return GS_OK;
+}
+
 int gs_ggeigvecs_f64(gs_context* ctx, int64_t n, const double* S, const double* T, const double* Q, const double* Z,
                      double* VR, double* VL, unsigned flags) {
   if (!ctx) return GS_BADARG;

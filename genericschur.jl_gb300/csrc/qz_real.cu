@@ -868,7 +868,648 @@ __global__ void __launch_bounds__(kQrT) k_ggschur_real(QzrBatch bt) {
 #undef BB
 #undef SYNC
 
+// ---- reordering of real generalized Schur forms (rordschur.jl:542-1178) -----------------
+// gordschur!(S, T, Q, Z, select) for a real pair in one CTA.  Thread 0 plans each swap of
+// adjacent blocks on copies of the (at most 4 x 4) diagonal blocks -- the Kronecker form
+// of the generalized Sylvester equation by _safe_lu_solve!, the QR and RQ factorizations
+// (LAPACK's reflector convention), the weak and strong stability tests and the
+// standardization of the new 2 x 2 blocks (_gqz_2x2!) -- and the CTA applies the accepted
+// transformation to the rest of S, T and to Q, Z.  Kept from the reference: `nbold == 3`
+// in _trexchange! (a block that splits stays nbold = 2), t2 from A in _gqz_2x2!, and its
+// singular-B1 branch rotating columns.
+
+// _safe_lu_solve! (util.jl:603-690) of a real nn x nn system (nn <= 8), in place on b
+__device__ double safe_lu_real(int nn, double* a, double* b) {
+#define LA(i, j) a[((i) - 1) + ((j) - 1) * nn]
+  const double eps = Prec<double>::eps, smallnum = Prec<double>::fmin / eps;
+  double smin = 0.0;
+  for (int e = 0; e < nn * nn; ++e) smin = fmax(smin, fabs(a[e]));
+  smin = fmax(eps * smin, smallnum);
+  int jpiv[8];
+  for (int i = 1; i <= nn - 1; ++i) {
+    double xmax = 0.0;
+    int ipsv = i, jpsv = i;
+    for (int ip = i; ip <= nn; ++ip)
+      for (int jp = i; jp <= nn; ++jp)
+        if (fabs(LA(ip, jp)) >= xmax) { xmax = fabs(LA(ip, jp)); ipsv = ip; jpsv = jp; }
+    if (ipsv != i) {
+      for (int j = 1; j <= nn; ++j) { const double t = LA(ipsv, j); LA(ipsv, j) = LA(i, j); LA(i, j) = t; }
+      const double t = b[i - 1]; b[i - 1] = b[ipsv - 1]; b[ipsv - 1] = t;
+    }
+    if (jpsv != i)
+      for (int j = 1; j <= nn; ++j) { const double t = LA(j, jpsv); LA(j, jpsv) = LA(j, i); LA(j, i) = t; }
+    jpiv[i - 1] = jpsv;
+    if (fabs(LA(i, i)) < smin) LA(i, i) = smin;
+    for (int j = i + 1; j <= nn; ++j) {
+      LA(j, i) = LA(j, i) / LA(i, i);
+      b[j - 1] -= LA(j, i) * b[i - 1];
+      for (int k = i + 1; k <= nn; ++k) LA(j, k) -= LA(j, i) * LA(i, k);
+    }
+  }
+  if (fabs(LA(nn, nn)) < smin) LA(nn, nn) = smin;
+  jpiv[nn - 1] = nn;
+  double scale = 1.0;
+  const double aa = 8.0 * smallnum;
+  bool needscl = false;
+  for (int i = 1; i <= nn; ++i)
+    if (aa * fabs(b[i - 1]) > fabs(LA(i, i))) { needscl = true; break; }
+  if (needscl) {
+    double bmax = 0.0;
+    for (int i = 0; i < nn; ++i) bmax = fmax(bmax, fabs(b[i]));
+    scale = (1.0 / 8.0) / bmax;
+    for (int i = 0; i < nn; ++i) b[i] *= scale;
+  }
+  for (int i = 1; i <= nn; ++i) {
+    const int k = nn + 1 - i;
+    const double t = 1.0 / LA(k, k);
+    b[k - 1] *= t;
+    for (int j = k + 1; j <= nn; ++j) b[k - 1] -= (t * LA(k, j)) * b[j - 1];
+  }
+  for (int i = 1; i <= nn - 1; ++i) {
+    const int jj = jpiv[nn - i - 1];
+    if (jj != nn - i) { const double t = b[nn - i - 1]; b[nn - i - 1] = b[jj - 1]; b[jj - 1] = t; }
+  }
+  return scale;
+#undef LA
+}
+
+// _safe_fnorm of a rows x cols block (columns in order, scale starting at 1)
+__device__ double safe_fnorm_blk(const double* m, int ld, int rows, int cols) {
+  double scale = 1.0, sumsq = 0.0;
+  for (int j = 0; j < cols; ++j)
+    for (int i = 0; i < rows; ++i) {
+      const double t1 = fabs(m[i + j * ld]);
+      if (t1 > 0.0 || t1 != t1) {
+        if (scale < t1) { sumsq = 1.0 + sumsq * (scale / t1) * (scale / t1); scale = t1; }
+        else sumsq += (t1 / scale) * (t1 / scale);
+      }
+    }
+  return scale * sqrt(sumsq);
+}
+
+// dlarfg on alpha and x (n - 1 entries, stride inc); returns tau
+__device__ double larfg_d(int n, double* alpha, double* x, int inc) {
+  if (n <= 1) return 0.0;
+  auto nrm2 = [&]() {
+    double sc = 0.0, sq = 1.0;
+    for (int i = 0; i < n - 1; ++i) {
+      const double a = fabs(x[i * inc]);
+      if (a > 0.0) {
+        if (sc < a) { sq = 1.0 + sq * (sc / a) * (sc / a); sc = a; }
+        else sq += (a / sc) * (a / sc);
+      }
+    }
+    return sc * sqrt(sq);
+  };
+  double xnorm = nrm2();
+  if (xnorm == 0.0) return 0.0;
+  double beta = -copysign(hypot(*alpha, xnorm), *alpha);
+  const double sfmin = Prec<double>::fmin / Prec<double>::eps;
+  int knt = 0;
+  if (fabs(beta) < sfmin) {
+    const double rsfmn = 1.0 / sfmin;
+    do {
+      ++knt;
+      for (int i = 0; i < n - 1; ++i) x[i * inc] *= rsfmn;
+      beta *= rsfmn;
+      *alpha *= rsfmn;
+    } while (fabs(beta) < sfmin && knt < 20);
+    xnorm = nrm2();
+    beta = -copysign(hypot(*alpha, xnorm), *alpha);
+  }
+  const double tau = (beta - *alpha) / beta;
+  const double sc = 1.0 / (*alpha - beta);
+  for (int i = 0; i < n - 1; ++i) x[i * inc] *= sc;
+  for (int j = 0; j < knt; ++j) beta *= sfmin;
+  *alpha = beta;
+  return tau;
+}
+
+// QR of a (m x k, ld m): R in the upper triangle, the full Q (m x m) in q
+__device__ void house_qr_d(int m, int k, double* a, double* q) {
+#define A_(i, j) a[((i) - 1) + ((j) - 1) * m]
+  double tau[4];
+  for (int i = 1; i <= k; ++i) {
+    tau[i - 1] = larfg_d(m - i + 1, &A_(i, i), i < m ? &A_(i + 1, i) : &A_(i, i), 1);
+    if (i < k && tau[i - 1] != 0.0) {
+      const double aii = A_(i, i);
+      A_(i, i) = 1.0;
+      for (int j = i + 1; j <= k; ++j) {
+        double t = 0.0;
+        for (int r = i; r <= m; ++r) t += A_(r, i) * A_(r, j);
+        for (int r = i; r <= m; ++r) A_(r, j) -= tau[i - 1] * A_(r, i) * t;
+      }
+      A_(i, i) = aii;
+    }
+  }
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) q[i + j * m] = i == j ? 1.0 : 0.0;
+  for (int i = k; i >= 1; --i) {
+    if (tau[i - 1] == 0.0) continue;
+    for (int j = 1; j <= m; ++j) {
+      double t = q[(i - 1) + (j - 1) * m];
+      for (int r = i + 1; r <= m; ++r) t += A_(r, i) * q[(r - 1) + (j - 1) * m];
+      t *= tau[i - 1];
+      q[(i - 1) + (j - 1) * m] -= t;
+      for (int r = i + 1; r <= m; ++r) q[(r - 1) + (j - 1) * m] -= A_(r, i) * t;
+    }
+  }
+  for (int j = 1; j <= k; ++j)
+    for (int i = j + 1; i <= m; ++i) A_(i, j) = 0.0;
+#undef A_
+}
+
+// RQ of a (mr x n, ld mr, mr <= n): a = R Q, the full Q (n x n) = H(1) ... H(k) in q
+__device__ void house_rq_d(int mr, int n, double* a, double* q) {
+#define A_(i, j) a[((i) - 1) + ((j) - 1) * mr]
+  const int k = mr < n ? mr : n;
+  double tau[4];
+  for (int i = k; i >= 1; --i) {
+    const int row = mr - k + i, col = n - k + i;
+    tau[i - 1] = larfg_d(col, &A_(row, col), &A_(row, 1), mr);
+    if (tau[i - 1] != 0.0 && row > 1) {
+      const double aii = A_(row, col);
+      A_(row, col) = 1.0;
+      for (int r = 1; r <= row - 1; ++r) {
+        double t = 0.0;
+        for (int c = 1; c <= col; ++c) t += A_(r, c) * A_(row, c);
+        for (int c = 1; c <= col; ++c) A_(r, c) -= tau[i - 1] * t * A_(row, c);
+      }
+      A_(row, col) = aii;
+    }
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) q[i + j * n] = i == j ? 1.0 : 0.0;
+  for (int i = k; i >= 1; --i) {
+    const int row = mr - k + i, col = n - k + i;
+    if (tau[i - 1] == 0.0) continue;
+    for (int j = 1; j <= n; ++j) {
+      double t = q[(col - 1) + (j - 1) * n];
+      for (int c = 1; c <= col - 1; ++c) t += A_(row, c) * q[(c - 1) + (j - 1) * n];
+      t *= tau[i - 1];
+      q[(col - 1) + (j - 1) * n] -= t;
+      for (int c = 1; c <= col - 1; ++c) q[(c - 1) + (j - 1) * n] -= A_(row, c) * t;
+    }
+  }
+  for (int i = 1; i <= mr; ++i)
+    for (int j = 1; j <= n; ++j)
+      if (j < n - mr + i) A_(i, j) = 0.0;
+#undef A_
+}
+
+// C = op(A) op(B), all m x m (m <= 4)
+__device__ void mm_d(int m, const double* A, bool ta, const double* B, bool tb, double* C) {
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) {
+      double t = 0.0;
+      for (int l = 0; l < m; ++l) t += (ta ? A[l + i * m] : A[i + l * m]) * (tb ? B[j + l * m] : B[l + j * m]);
+      C[i + j * m] = t;
+    }
+}
+
+// thread-local Julia Givens on a small matrix (ld): lmul!(G) rows, rmul!(., G) and
+// rmul!(., G') columns, over the given range
+__device__ void lrows(double* M, int ld, int i1, int i2, double c, double s, int j0, int j1) {
+  for (int j = j0; j <= j1; ++j) {
+    double* p1 = M + (i1 - 1) + (j - 1) * ld;
+    double* p2 = M + (i2 - 1) + (j - 1) * ld;
+    const double x = *p1, y = *p2;
+    *p1 = c * x + s * y;
+    *p2 = c * y - s * x;
+  }
+}
+__device__ void lcols(double* M, int ld, int i1, int i2, double c, double s, int r0, int r1) {
+  for (int r = r0; r <= r1; ++r) {
+    double* p1 = M + (r - 1) + (i1 - 1) * ld;
+    double* p2 = M + (r - 1) + (i2 - 1) * ld;
+    const double x = *p1, y = *p2;
+    *p1 = x * c - y * s;
+    *p2 = x * s + y * c;
+  }
+}
+__device__ void lcols_adj(double* M, int ld, int i1, int i2, double c, double s, int r0, int r1) {
+  for (int r = r0; r <= r1; ++r) {
+    double* p1 = M + (r - 1) + (i1 - 1) * ld;
+    double* p2 = M + (r - 1) + (i2 - 1) * ld;
+    const double x = *p1, y = *p2;
+    *p1 = x * c + y * s;
+    *p2 = y * c - x * s;
+  }
+}
+
+// _gqz_2x2!(A, B) on the 2 x 2 blocks at a, b (ld)
+__device__ void gqz_2x2_d(double* a, double* b, int ld, double& csl, double& snl, double& csr, double& snr) {
+#define GA(i, j) a[((i) - 1) + ((j) - 1) * ld]
+#define GB(i, j) b[((i) - 1) + ((j) - 1) * ld]
+  const double safmin = Prec<double>::fmin, ulp = Prec<double>::eps;
+  const double anorm = fmax(fmax(fabs(GA(1, 1)) + fabs(GA(2, 1)), fabs(GA(1, 2)) + fabs(GA(2, 2))), safmin);
+  const double ascale = 1.0 / anorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GA(i, j) *= ascale;
+  const double bnorm = fmax(fmax(fabs(GB(1, 1)), fabs(GB(1, 2)) + fabs(GB(2, 2))), safmin);
+  const double bscale = 1.0 / bnorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GB(i, j) *= bscale;
+  double rr;
+  if (fabs(GA(2, 1)) < ulp) {
+    csl = 1.0; snl = 0.0; csr = 1.0; snr = 0.0;
+    GA(2, 1) = 0.0;
+    GB(2, 1) = 0.0;
+  } else if (fabs(GB(1, 1)) < ulp) {
+    givens_alg(GA(1, 1), GA(2, 1), csl, snl, rr);
+    csr = 1.0; snr = 0.0;
+    lcols(a, ld, 1, 2, csl, snl, 1, 2);
+    lcols(b, ld, 1, 2, csl, snl, 1, 2);
+    GA(2, 1) = 0.0;
+    GB(1, 1) = 0.0;
+    GB(2, 1) = 0.0;
+  } else if (fabs(GB(2, 2)) < ulp) {
+    givens_alg(GA(2, 2), GA(2, 1), csr, snr, rr);
+    lrows(a, ld, 1, 2, csr, -snr, 1, 2);
+    lrows(b, ld, 1, 2, csr, -snr, 1, 2);
+    csl = 1.0; snl = 0.0;
+    GA(2, 1) = 0.0;
+    GB(2, 1) = 0.0;
+    GB(2, 2) = 0.0;
+  } else {
+    double scale1, scale2, wr1, wr2, wi;
+    ggs2x2(a, b, ld, 1, safmin, scale1, scale2, wr1, wr2, wi);
+    if (wi == 0.0) {
+      const double h1 = scale1 * GA(1, 1) - wr1 * GB(1, 1);
+      const double h2 = scale1 * GA(1, 2) - wr1 * GB(1, 2);
+      const double h3 = scale1 * GA(2, 2) - wr1 * GB(2, 2);
+      const double rr2 = hypot(h2, h1), qq = hypot(scale1 * GA(2, 1), h3);
+      if (rr2 > qq) givens_alg(h2, h1, csr, snr, rr);
+      else givens_alg(h3, scale1 * GA(2, 1), csr, snr, rr);
+      lcols(a, ld, 1, 2, csr, snr, 1, 2);
+      lcols(b, ld, 1, 2, csr, snr, 1, 2);
+      snr = -snr;
+      const double t1 = fmax(fabs(GA(1, 1)) + fabs(GA(1, 2)), fabs(GA(2, 1)) + fabs(GA(2, 2)));
+      const double t2 = t1;
+      if (scale1 * t1 >= fabs(wr1) * t2) givens_alg(GB(1, 1), GB(2, 1), csl, snl, rr);
+      else givens_alg(GA(1, 1), GA(2, 1), csl, snl, rr);
+      lrows(a, ld, 1, 2, csl, snl, 1, 2);
+      lrows(b, ld, 1, 2, csl, snl, 1, 2);
+      GA(2, 1) = 0.0;
+      GB(2, 1) = 0.0;
+    } else {
+      double ssmin, ssmax;
+      gsvd2x2(GB(1, 1), GB(1, 2), GB(2, 2), ssmin, ssmax, snr, csr, snl, csl);
+      lcols_adj(a, ld, 1, 2, csr, snr, 1, 2);
+      lcols_adj(b, ld, 1, 2, csr, snr, 1, 2);
+      lrows(a, ld, 1, 2, csl, snl, 1, 2);
+      lrows(b, ld, 1, 2, csl, snl, 1, 2);
+      GB(2, 1) = 0.0;
+      GB(1, 2) = 0.0;
+    }
+  }
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GA(i, j) *= anorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GB(i, j) *= bnorm;
+#undef GA
+#undef GB
+}
+
+// The plan of one swap, written by thread 0: for 1 x 1 pairs the four rotation
+// coefficients; otherwise the new m x m blocks of A and B and the transforms qf, zf.
+struct RordPlan {
+  int ok, m;
+  double cz, sz, cq, sq;
+  double SA[16], SB[16], qf[16], zf[16];
+};
+
+// _rtrexch2! (1096-1178): the rotations and the stability tests, on copies
+__device__ void plan_rtrexch2(const double* A, const double* B, int n, int j1, RordPlan& P) {
+  double S[4] = {A[(j1 - 1) + (size_t)(j1 - 1) * n], A[j1 + (size_t)(j1 - 1) * n], A[(j1 - 1) + (size_t)j1 * n],
+                 A[j1 + (size_t)j1 * n]};
+  double T[4] = {B[(j1 - 1) + (size_t)(j1 - 1) * n], B[j1 + (size_t)(j1 - 1) * n], B[(j1 - 1) + (size_t)j1 * n],
+                 B[j1 + (size_t)j1 * n]};
+  const double S0[4] = {S[0], S[1], S[2], S[3]}, T0[4] = {T[0], T[1], T[2], T[3]};
+  const double smlnum = Prec<double>::fmin / Prec<double>::eps;
+  double W[8] = {S[0], S[1], S[2], S[3], T[0], T[1], T[2], T[3]};
+  double sa = safe_fnorm_blk(W, 8, 8, 1);
+  const double thresh = fmax(20.0 * Prec<double>::eps * sa, smlnum);
+  const double f = S[3] * T[0] - T[3] * S[0];
+  const double g = S[3] * T[2] - T[3] * S[2];
+  sa = fabs(S[3]) * fabs(T[0]);
+  const double sb = fabs(S[0]) * fabs(T[3]);
+  double cz, sz, rr;
+  givens_alg(f, g, cz, sz, rr);
+  { const double t = sz; sz = cz; cz = t; }
+  lcols_adj(S, 2, 1, 2, cz, -sz, 1, 2);
+  lcols_adj(T, 2, 1, 2, cz, -sz, 1, 2);
+  const double fq = sa >= sb ? S[0] : T[0], gq = sa >= sb ? S[1] : T[1];
+  double cq, sq;
+  if (sz != 0.0 && fq == 0.0 && gq == 0.0) { cq = 0.0; sq = 1.0; }
+  else givens_alg(fq, gq, cq, sq, rr);
+  lrows(S, 2, 1, 2, cq, sq, 1, 2);
+  lrows(T, 2, 1, 2, cq, sq, 1, 2);
+  P.cz = cz; P.sz = sz; P.cq = cq; P.sq = sq; P.m = 2;
+  const double ws = fabs(S[1]) + fabs(T[1]);
+  if (!(ws <= thresh)) { P.ok = 0; return; }
+  double Ss[4] = {S[0], S[1], S[2], S[3]}, Ts[4] = {T[0], T[1], T[2], T[3]};
+  lcols_adj(Ss, 2, 1, 2, cz, sz, 1, 2);
+  lcols_adj(Ts, 2, 1, 2, cz, sz, 1, 2);
+  lrows(Ss, 2, 1, 2, cq, -sq, 1, 2);
+  lrows(Ts, 2, 1, 2, cq, -sq, 1, 2);
+  for (int e = 0; e < 4; ++e) { W[e] = Ss[e] - S0[e]; W[4 + e] = Ts[e] - T0[e]; }
+  const double ss = safe_fnorm_blk(W, 8, 8, 1);
+  P.ok = ss <= thresh ? 1 : 0;
+}
+
+// _swap1or2! (768-962) with at least one 2 x 2 block: the new blocks and transforms
+__device__ void plan_swap2(const double* A, const double* B, int n, int j1, int n1, int n2, RordPlan& P) {
+  const int m = n1 + n2;
+  P.m = m;
+  double S[16], T[16];
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) {
+      S[i + j * m] = A[(j1 - 1 + i) + (size_t)(j1 - 1 + j) * n];
+      T[i + j * m] = B[(j1 - 1 + i) + (size_t)(j1 - 1 + j) * n];
+    }
+  const double eps = Prec<double>::eps, smallnum = Prec<double>::fmin / eps;
+  double dnorm = 0.0, tnorm = 0.0;
+  for (int e = 0; e < m * m; ++e) { dnorm = fmax(dnorm, fabs(S[e])); tnorm = fmax(tnorm, fabs(T[e])); }
+  const double thresh = fmax(20.0 * eps * dnorm, smallnum), threshb = fmax(20.0 * eps * tnorm, smallnum);
+  // _syl1or2: the Kronecker system for [vec R; vec L]
+  const int nn = n1 * n2, kd = 2 * nn;
+  double K[64], rl[8];
+  for (int e = 0; e < kd * kd; ++e) K[e] = 0.0;
+  for (int q = 0; q < n2; ++q)
+    for (int p = 0; p < n1; ++p) {
+      const int row = p + q * n1;
+      for (int pp = 0; pp < n1; ++pp) {
+        K[row + (pp + q * n1) * kd] = S[p + pp * m];
+        K[(nn + row) + (pp + q * n1) * kd] = T[p + pp * m];
+      }
+      for (int qq = 0; qq < n2; ++qq) {
+        K[row + (nn + p + qq * n1) * kd] = -S[(n1 + qq) + (n1 + q) * m];
+        K[(nn + row) + (nn + p + qq * n1) * kd] = -T[(n1 + qq) + (n1 + q) * m];
+      }
+      rl[row] = S[p + (n1 + q) * m];
+      rl[nn + row] = T[p + (n1 + q) * m];
+    }
+  const double scale = safe_lu_real(kd, K, rl);
+  double LI[8], IR[8], qli[16], zir[16];
+  for (int j = 0; j < n2; ++j) {
+    for (int i = 0; i < n1; ++i) LI[i + j * m] = -rl[nn + i + j * n1];
+    for (int i = 0; i < n2; ++i) LI[n1 + i + j * m] = i == j ? scale : 0.0;
+  }
+  for (int i = 0; i < n1; ++i) {
+    for (int j = 0; j < n1; ++j) IR[i + j * n1] = i == j ? scale : 0.0;
+    for (int j = 0; j < n2; ++j) IR[i + (n1 + j) * n1] = rl[i + j * n1];
+  }
+  house_qr_d(m, n2, LI, qli);
+  house_rq_d(n1, m, IR, zir);
+  double tmp[16], s1[16], t1[16];
+  mm_d(m, qli, true, S, false, tmp);
+  mm_d(m, tmp, false, zir, true, s1);
+  mm_d(m, qli, true, T, false, tmp);
+  mm_d(m, tmp, false, zir, true, t1);
+  double t2a[16], zt1a[16], s2a[16], z2a[16], t2b[16], qt1b[16], s2b[16], q2b[16];
+  for (int e = 0; e < m * m; ++e) { t2a[e] = t1[e]; t2b[e] = t1[e]; }
+  house_rq_d(m, m, t2a, zt1a);
+  mm_d(m, s1, false, zt1a, true, s2a);
+  mm_d(m, zt1a, false, zir, false, z2a);
+  const double brq = safe_fnorm_blk(s2a + n2, m, m - n2, n2);
+  house_qr_d(m, m, t2b, qt1b);
+  mm_d(m, qt1b, true, s1, false, s2b);
+  mm_d(m, qli, false, qt1b, false, q2b);
+  const double bqr = safe_fnorm_blk(s2b + n2, m, m - n2, n2);
+  if (!(fmin(bqr, brq) <= thresh) || bqr != bqr || brq != brq) { P.ok = 0; return; }
+  const bool useb = bqr <= brq;
+  double* snew = useb ? s2b : s2a;
+  double* tnew = useb ? t2b : t2a;
+  const double* znew = useb ? zir : z2a;
+  const double* qnew = useb ? q2b : qli;
+  {
+    double r1[16], r2[16];
+    mm_d(m, qnew, false, snew, false, r1);
+    mm_d(m, r1, false, znew, false, r2);
+    for (int e = 0; e < m * m; ++e) r2[e] = S[e] - r2[e];
+    const double resa = safe_fnorm_blk(r2, m, m, m);
+    mm_d(m, qnew, false, tnew, false, r1);
+    mm_d(m, r1, false, znew, false, r2);
+    for (int e = 0; e < m * m; ++e) r2[e] = T[e] - r2[e];
+    const double resb = safe_fnorm_blk(r2, m, m, m);
+    if (!(resa <= thresh && resb <= threshb)) { P.ok = 0; return; }
+  }
+  for (int j = 0; j < n2; ++j)
+    for (int i = n2; i < m; ++i) snew[i + j * m] = 0.0;
+  double qtmp[16], ztmp[16];
+  for (int e = 0; e < m * m; ++e) { qtmp[e] = 0.0; ztmp[e] = 0.0; }
+  double csl, snl, csr, snr;
+  if (n2 > 1) {
+    gqz_2x2_d(snew, tnew, m, csl, snl, csr, snr);
+    qtmp[0] = csl; qtmp[1] = snl; qtmp[m] = -snl; qtmp[m + 1] = csl;
+    ztmp[0] = csr; ztmp[1] = snr; ztmp[m] = -snr; ztmp[m + 1] = csr;
+  } else {
+    ztmp[0] = 1.0;
+    qtmp[0] = 1.0;
+  }
+  if (n1 > 1) {
+    const int o = n2 + n2 * m;  // (j3, j3) within the block
+    gqz_2x2_d(snew + o, tnew + o, m, csl, snl, csr, snr);
+    qtmp[(m - 2) + (m - 2) * m] = csl; qtmp[(m - 1) + (m - 2) * m] = snl;
+    qtmp[(m - 2) + (m - 1) * m] = -snl; qtmp[(m - 1) + (m - 1) * m] = csl;
+    ztmp[(m - 2) + (m - 2) * m] = csr; ztmp[(m - 1) + (m - 2) * m] = snr;
+    ztmp[(m - 2) + (m - 1) * m] = -snr; ztmp[(m - 1) + (m - 1) * m] = csr;
+  } else {
+    qtmp[(m - 1) + (m - 1) * m] = 1.0;
+    ztmp[(m - 1) + (m - 1) * m] = 1.0;
+  }
+  // the off-diagonal block: qtmp[1:n2,1:n2]' X ztmp[n2+1:m, n2+1:m]
+  for (int w = 0; w < 2; ++w) {
+    double* M = w == 0 ? snew : tnew;
+    double X[4], ab[4];
+    for (int j = 0; j < n1; ++j) for (int i = 0; i < n2; ++i) X[i + j * n2] = M[i + (n2 + j) * m];
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n2; ++i) {
+        double t = 0.0;
+        for (int l = 0; l < n2; ++l) t += qtmp[l + i * m] * X[l + j * n2];
+        ab[i + j * n2] = t;
+      }
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n2; ++i) {
+        double t = 0.0;
+        for (int l = 0; l < n1; ++l) t += ab[i + l * n2] * ztmp[(n2 + l) + (n2 + j) * m];
+        M[i + (n2 + j) * m] = t;
+      }
+  }
+  mm_d(m, qnew, false, qtmp, false, P.qf);
+  mm_d(m, znew, true, ztmp, false, P.zf);
+  for (int e = 0; e < m * m; ++e) { P.SA[e] = snew[e]; P.SB[e] = tnew[e]; }
+  P.ok = 1;
+}
+
+// _swap1or2!(A, B, Q, Z, j1, n1, n2) on the CTA
+__device__ bool cta_swap1or2(double* A, double* B, double* Q, double* Z, int n, int j1, int n1, int n2, RordPlan& P) {
+  if (j1 + n1 > n) return true;
+  const int tid = threadIdx.x;
+  __syncthreads();
+  if (tid == 0) {
+    if (n1 == 1 && n2 == 1) plan_rtrexch2(A, B, n, j1, P);
+    else plan_swap2(A, B, n, j1, n1, n2, P);
+  }
+  __syncthreads();
+  if (!P.ok) return false;
+  if (n1 == 1 && n2 == 1) {
+    const double cz = P.cz, sz = P.sz, cq = P.cq, sq = P.sq;
+    ccols_adj(A, n, j1, j1 + 1, cz, -sz, 1, n);
+    ccols_adj(B, n, j1, j1 + 1, cz, -sz, 1, n);
+    __syncthreads();
+    crows(A, n, j1, j1 + 1, cq, sq, 1, n);
+    crows(B, n, j1, j1 + 1, cq, sq, 1, n);
+    __syncthreads();
+    if (tid == 0) {
+      A[j1 + (size_t)(j1 - 1) * n] = 0.0;
+      B[j1 + (size_t)(j1 - 1) * n] = 0.0;
+    }
+    if (Z) ccols_adj(Z, n, j1, j1 + 1, cz, -sz, 1, n);
+    if (Q) ccols_adj(Q, n, j1, j1 + 1, cq, sq, 1, n);
+    __syncthreads();
+    return true;
+  }
+  const int m = P.m, je = j1 + m - 1;
+  for (int e = tid; e < m * m; e += kQrT) {
+    const int i = e % m, j = e / m;
+    A[(j1 - 1 + i) + (size_t)(j1 - 1 + j) * n] = P.SA[e];
+    B[(j1 - 1 + i) + (size_t)(j1 - 1 + j) * n] = P.SB[e];
+  }
+  // Q[:, j1:je] qf, Z[:, j1:je] zf, A[1:j1-1, j1:je] zf (and B)
+  for (int r = tid; r < n; r += kQrT) {
+    double v[4];
+    if (Q) {
+      for (int j = 0; j < m; ++j) v[j] = Q[r + (size_t)(j1 - 1 + j) * n];
+      for (int j = 0; j < m; ++j) {
+        double t = 0.0;
+        for (int l = 0; l < m; ++l) t += v[l] * P.qf[l + j * m];
+        Q[r + (size_t)(j1 - 1 + j) * n] = t;
+      }
+    }
+    if (Z) {
+      for (int j = 0; j < m; ++j) v[j] = Z[r + (size_t)(j1 - 1 + j) * n];
+      for (int j = 0; j < m; ++j) {
+        double t = 0.0;
+        for (int l = 0; l < m; ++l) t += v[l] * P.zf[l + j * m];
+        Z[r + (size_t)(j1 - 1 + j) * n] = t;
+      }
+    }
+    if (r < j1 - 1)
+      for (int w = 0; w < 2; ++w) {
+        double* M = w == 0 ? A : B;
+        for (int j = 0; j < m; ++j) v[j] = M[r + (size_t)(j1 - 1 + j) * n];
+        for (int j = 0; j < m; ++j) {
+          double t = 0.0;
+          for (int l = 0; l < m; ++l) t += v[l] * P.zf[l + j * m];
+          M[r + (size_t)(j1 - 1 + j) * n] = t;
+        }
+      }
+  }
+  // A[j1:je, je+1:n] = qf' A[j1:je, je+1:n] (and B)
+  for (int c = je + 1 + tid; c <= n; c += kQrT)
+    for (int w = 0; w < 2; ++w) {
+      double* M = w == 0 ? A : B;
+      double v[4];
+      for (int i = 0; i < m; ++i) v[i] = M[(j1 - 1 + i) + (size_t)(c - 1) * n];
+      for (int i = 0; i < m; ++i) {
+        double t = 0.0;
+        for (int l = 0; l < m; ++l) t += P.qf[l + i * m] * v[l];
+        M[(j1 - 1 + i) + (size_t)(c - 1) * n] = t;
+      }
+    }
+  __syncthreads();
+  return true;
+}
+
+__global__ void __launch_bounds__(kQrT) k_ggordschur_real(double* S, double* T, double* Q, double* Z, int n,
+                                                          const int* __restrict__ select, int scale, double2* alpha,
+                                                          double* beta, int* status) {
+  __shared__ double red[kQrT / 32];
+  __shared__ RordPlan P;
+  const int tid = threadIdx.x;
+  double cscale = 1.0, anrm = 1.0, cscaleb = 1.0, bnrm = 1.0;
+  bool scA = false, scB = false;
+  if (scale) {
+    scA = cta_scale_real(S, n, red, cscale, anrm);
+    scB = cta_scale_real(T, n, red, cscaleb, bnrm);
+  }
+  __syncthreads();
+#define SM(i, j) S[((i) - 1) + (size_t)((j) - 1) * n]
+#define TM(i, j) T[((i) - 1) + (size_t)((j) - 1) * n]
+  int st = 0, ks = 0;
+  bool inpair = false;
+  for (int k = 1; k <= n && !st; ++k) {
+    if (inpair) { inpair = false; continue; }
+    __syncthreads();
+    bool doswap = select[k - 1] != 0;
+    if (k < n && SM(k + 1, k) != 0.0) {
+      inpair = true;
+      doswap = doswap || select[k] != 0;
+    }
+    if (!doswap) continue;
+    ks += 1;
+    if (k != ks) {
+      // _trexchange!(S, T, Q, Z, k, ks), the move-up branch
+      int iold = k, inew = ks;
+      if (iold > 1 && SM(iold, iold - 1) != 0.0) iold -= 1;
+      const int nbold = (iold < n && SM(iold + 1, iold) != 0.0) ? 2 : 1;
+      if (inew > 1 && SM(inew, inew - 1) != 0.0) inew -= 1;
+      int ihere = iold;
+      bool ok = iold >= inew;
+      while (ok && ihere > inew) {
+        __syncthreads();
+        const int nbnext = (ihere >= 3 && SM(ihere - 1, ihere - 2) != 0.0) ? 2 : 1;
+        ok = cta_swap1or2(S, T, Q, Z, n, ihere - nbnext, nbnext, nbold, P);
+        if (ok) ihere -= nbnext;
+      }
+      if (!ok) { st = 1 + k; break; }
+      ks = ihere;
+    }
+    if (inpair) ks += 1;
+  }
+  __syncthreads();
+  if (!st) {
+    if (scA) cta_safescale_real(S, (size_t)n * n, cscale, anrm);
+    if (scB) cta_safescale_real(T, (size_t)n * n, cscaleb, bnrm);
+    __syncthreads();
+    inpair = false;
+    for (int k = 1; k <= n; ++k) {
+      if (inpair) { inpair = false; continue; }
+      __syncthreads();
+      if (k < n && SM(k + 1, k) != 0.0) inpair = true;
+      if (inpair) {
+        if (tid == 0) {
+          double b1, b2, ar1, ar2, ai;
+          ggs2x2(&SM(k, k), &TM(k, k), n, 1, Prec<double>::fmin, b1, b2, ar1, ar2, ai);
+          alpha[k - 1] = make_double2(ar1, ai);
+          alpha[k] = make_double2(ar2, -ai);
+          beta[k - 1] = b1;
+          beta[k] = b2;
+        }
+      } else {
+        if (copysign(1.0, TM(k, k)) < 0.0) {
+          __syncthreads();
+          for (int j = 1 + tid; j <= n; j += kQrT) { SM(k, j) = -SM(k, j); TM(k, j) = -TM(k, j); }
+          if (Q) cnegcol(Q, n, k, 1, n);
+          __syncthreads();
+        }
+        if (tid == 0) {
+          alpha[k - 1] = make_double2(SM(k, k), 0.0);
+          beta[k - 1] = TM(k, k);
+        }
+      }
+    }
+  }
+#undef SM
+#undef TM
+  if (tid == 0) *status = st;
+}
+
 }  // namespace
+
+cudaError_t launch_ggordschur_real(int n, double* S, double* T, double* Q, double* Z, const int* select, int scale,
+                                   double2* alpha, double* beta, int* status, cudaStream_t s) {
+  k_ggordschur_real<<<1, kQrT, 0, s>>>(S, T, Q, Z, n, select, scale, alpha, beta, status);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ggschur_real(const QzrBatch& bt, int num_sms, cudaStream_t s) {
   if (bt.count <= 0) return cudaSuccess;

@@ -521,10 +521,27 @@ def gordschur(S, select, ctx=None):
     return Schur(T, Z, w)
 
 
+def _ggordschur_real(G, select, ctx, scale):
+    S = _fc(G.S, np.float64)
+    T = _fc(G.T, np.float64)
+    n = _checksquare(S)
+    sel = np.ascontiguousarray(np.asarray(select, dtype=bool).astype(np.int32))
+    if len(sel) != n:
+        raise DimensionMismatch("select must have length %d" % n)
+    Q = _fc(G.Q if G.Q is not None else np.eye(n), np.float64)
+    Z = _fc(G.Z if G.Z is not None else np.eye(n), np.float64)
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1))
+    rc = ctx.lib.gs_ggordschur_f64(ctx.handle, n, _ptr(S), _ptr(T), _ptr(Q), _ptr(Z), _ptr(sel), _ptr(al), _ptr(be),
+                                   _capi.GS_SCALE if scale else 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "gordschur!(GeneralizedSchur)")
+    return GeneralizedSchur(S, T, al[:n], be[:n], Q, Z)
+
+
 def _ggordschur(G, select, ctx, scale=True):
     if not (np.iscomplexobj(G.S) or np.iscomplexobj(G.T)):
-        raise ArgumentError("reordering of a real generalized Schur form is not provided; "
-                            "use the complex form (ggschur of the pencil cast to complex)")
+        return _ggordschur_real(G, select, ctx, scale)
     S = _fc(G.S, np.complex128)
     T = _fc(G.T, np.complex128)
     n = _checksquare(S)

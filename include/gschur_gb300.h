@@ -379,6 +379,16 @@ GS_API int gs_ggschur_batched_f64(gs_context* ctx, int64_t count, const int32_t*
  * reference's IllConditionException); the form is then partly reordered. */
 GS_API int gs_ggordschur_c64(gs_context* ctx, int64_t n, double* S, double* T, double* Q, double* Z,
                              const int32_t* select, double* alpha, double* beta, unsigned flags);
+/* gordschur!(S, T, Q, Z, select) for a real generalized Schur pair (rordschur.jl:542-627,
+ * _trexchange! 629-766, _swap1or2! 768-962 after LAPACK's dtgexc / dtgex2): the 1 x 1 and
+ * 2 x 2 blocks of the selected eigenvalues (a pair moves when either of its members is
+ * selected) are moved to the top by orthogonal equivalences accumulated into Q and Z (either
+ * may be NULL); S, T are overwritten with the reordered standardized pair, alpha (n,
+ * interleaved complex) and beta (n, real) with the generalized eigenvalues.  GS_SCALE scales
+ * as the reference's `scale = true` does.  GS_UNCONVERGED when a swap fails the stability
+ * tests (the reference's IllConditionException). */
+GS_API int gs_ggordschur_f64(gs_context* ctx, int64_t n, double* S, double* T, double* Q, double* Z,
+                             const int32_t* select, double* alpha, double* beta, unsigned flags);
 
 /* Eigenvectors of the generalized Schur decomposition of a complex pencil (the output
  * of gs_ggschur_c64: S, T upper triangular, A = Q S Z^H, B = Q T Z^H).  Replaces

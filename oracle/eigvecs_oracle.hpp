@@ -254,7 +254,7 @@ R safe_lu_solve(int nn, cx<R>* a, cx<R>* b, bool* perturbed) {
   for (int j = 1; j <= nn; ++j)
     for (int i = 1; i <= nn; ++i) smin = m_max(smin, cabs(A_(i, j)));
   smin = m_max(lim<R>::eps() * smin, smallnum);
-  int jpiv[2] = {0, 0};
+  int jpiv[16] = {0};  // nn <= 16
   for (int i = 1; i <= nn - 1; ++i) {
     R xmax = 0;
     int ipsv = i, jpsv = i;

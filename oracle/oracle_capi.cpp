@@ -282,6 +282,12 @@ int or_ggordschur_z(int n, double* s, double* t, double* q, double* z, const int
   return gordschur_cplx<double>(n, (zc*)s, (zc*)t, (zc*)q, (zc*)z, select, scale != 0, (zc*)al, (zc*)be);
 }
 
+// gordschur!(S, T, Q, Z, select) of a real generalized Schur pair; alpha interleaved complex
+int or_ggordschur_d(int n, double* s, double* t, double* q, double* z, const int* select, int scale, double* alpha,
+                    double* beta) {
+  return gordschur_real<double>(n, s, t, q, z, select, scale != 0, (zc*)alpha, beta);
+}
+
 // trsylvester!(A, B, C, D, E, F) (adj = 0) / adjtrsylvester! (adj = 1) for complex triangular
 // A, D (m x m), B, E (n x n); C, F (m x n) overwritten; returns the reference's scale.
 double or_gtrsyl_z(int m, int n, const double* a, const double* b, double* c, const double* d, const double* e,

@@ -58,6 +58,7 @@ def lib():
             "or_rgevc_d": [_i, _p, _p, _p, _p, _i],
             "or_ggordschur_z": [_i, _p, _p, _p, _p, _p, _i, _p, _p],
             "or_gtrsyl_z": [_i, _i, _p, _p, _p, _p, _p, _p, _i],
+            "or_ggordschur_d": [_i, _p, _p, _p, _p, _p, _i, _p, _p],
             "or_gcond_z": [_i, _p, _p, _i, _p, _i],
         }
         for name, args in sig.items():
@@ -394,6 +395,19 @@ def ggordschur(S, T, Q, Z, select, scale=True):
     al = np.zeros(max(n, 1), dtype=np.complex128)
     be = np.zeros(max(n, 1), dtype=np.complex128)
     st = lib().or_ggordschur_z(n, _ptr(Sf), _ptr(Tf), _ptr(Qf), _ptr(Zf), sel.ctypes.data_as(ctypes.c_void_p),
+                               int(scale), _ptr(al), _ptr(be))
+    return Sf, Tf, al[:n], be[:n], Qf, Zf, st
+
+
+def ggordschur_real(S, T, Q, Z, select, scale=True):
+    """gordschur!(S, T, Q, Z, select) for a real generalized Schur pair (rordschur.jl:542-627):
+    (S, T, alpha, beta, Q, Z, status), status 1 + k when the block at k could not be moved."""
+    Sf, Tf, Qf, Zf = (_f(x, np.float64) for x in (S, T, Q, Z))
+    n = Sf.shape[0]
+    sel = np.ascontiguousarray(np.asarray(select, dtype=np.int32))
+    al = np.zeros(max(n, 1), dtype=np.complex128)
+    be = np.zeros(max(n, 1))
+    st = lib().or_ggordschur_d(n, _ptr(Sf), _ptr(Tf), _ptr(Qf), _ptr(Zf), sel.ctypes.data_as(ctypes.c_void_p),
                                int(scale), _ptr(al), _ptr(be))
     return Sf, Tf, al[:n], be[:n], Qf, Zf, st
 

@@ -1883,4 +1883,516 @@ int gordschur_cplx(int n, cx<R>* S, cx<R>* T, cx<R>* Q, cx<R>* Z, const int* sel
   return status;
 }
 
+// ---------------------------------------------------------------------------
+// Reordering of real generalized Schur forms: gordschur!(S, T, Q, Z, select) for real
+// pencils (rordschur.jl:542-627), _trexchange! (629-766, its move-up branch: gordschur!
+// only moves blocks up), _swap1or2! (768-962), _gqz_2x2! (964-1063), _syl1or2 (1071-1091),
+// _rtrexch2! (1096-1178).  Kept from the reference: `nbold == 3` (a comparison, so a 2 x 2
+// block that splits keeps nbold = 2, 717-721), t2 computed from A as t1 is in _gqz_2x2!
+// (1023-1024), the singular-B1 branch rotating columns (991-993).  The QR and RQ
+// factorizations (LinearAlgebra.qr / MatrixFactorizations.rq, LAPACK geqrt / gerqf for
+// Float64) are restated with LAPACK's reflector convention (dlarfg) and formed explicitly.
+// ---------------------------------------------------------------------------
+// _safe_fnorm of a rows x cols block (columns in order; util.jl:83-94 with _ssq 466-505)
+template <class R> R safe_fnorm_r(const R* m, int ld, int rows, int cols) {
+  R scale = R(1), sumsq = R(0);
+  for (int j = 0; j < cols; ++j)
+    for (int i = 0; i < rows; ++i) {
+      const R t1 = m_abs(m[i + (long long)j * ld]);
+      if (t1 > R(0) || t1 != t1) {
+        if (scale < t1) { sumsq = R(1) + sumsq * (scale / t1) * (scale / t1); scale = t1; }
+        else sumsq += (t1 / scale) * (t1 / scale);
+      }
+    }
+  return scale * m_sqrt(sumsq);
+}
+
+// dlarfg: H (I - tau v v', v = [1; x]) with H [alpha; x] = [beta; 0]; x has n - 1 entries
+// at stride inc; alpha becomes beta, x becomes v's tail; returns tau.
+template <class R> R larfg_r(int n, R* alpha, R* x, int inc) {
+  if (n <= 1) return R(0);
+  auto nrm2 = [&]() {
+    R sc = R(0), sq = R(1);
+    for (int i = 0; i < n - 1; ++i) {
+      const R a = m_abs(x[i * inc]);
+      if (a > R(0)) {
+        if (sc < a) { sq = R(1) + sq * (sc / a) * (sc / a); sc = a; }
+        else sq += (a / sc) * (a / sc);
+      }
+    }
+    return sc * m_sqrt(sq);
+  };
+  R xnorm = nrm2();
+  if (xnorm == R(0)) return R(0);
+  R beta = -m_copysign(m_hypot(*alpha, xnorm), *alpha);
+  const R sfmin = lim<R>::fmin() / lim<R>::eps();
+  int knt = 0;
+  if (m_abs(beta) < sfmin) {
+    const R rsfmn = R(1) / sfmin;
+    do {
+      ++knt;
+      for (int i = 0; i < n - 1; ++i) x[i * inc] *= rsfmn;
+      beta *= rsfmn;
+      *alpha *= rsfmn;
+    } while (m_abs(beta) < sfmin && knt < 20);
+    xnorm = nrm2();
+    beta = -m_copysign(m_hypot(*alpha, xnorm), *alpha);
+  }
+  const R tau = (beta - *alpha) / beta;
+  const R sc = R(1) / (*alpha - beta);
+  for (int i = 0; i < n - 1; ++i) x[i * inc] *= sc;
+  for (int j = 0; j < knt; ++j) beta *= sfmin;
+  *alpha = beta;
+  return tau;
+}
+
+// QR of the m x k matrix a (ld m, k <= m): R in the upper triangle, Q (m x m) formed
+template <class R> void house_qr_r(int m, int k, R* a, R* q) {
+  std::vector<R> tau(k), w(m);
+#define A_(i, j) a[((i) - 1) + (long long)((j) - 1) * m]
+  for (int i = 1; i <= k; ++i) {
+    tau[i - 1] = larfg_r<R>(m - i + 1, &A_(i, i), i < m ? &A_(i + 1, i) : &A_(i, i), 1);
+    if (i < k && tau[i - 1] != R(0)) {
+      const R aii = A_(i, i);
+      A_(i, i) = R(1);
+      for (int j = i + 1; j <= k; ++j) {
+        R t = R(0);
+        for (int r = i; r <= m; ++r) t += A_(r, i) * A_(r, j);
+        for (int r = i; r <= m; ++r) A_(r, j) -= tau[i - 1] * A_(r, i) * t;
+      }
+      A_(i, i) = aii;
+    }
+  }
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) q[i + (long long)j * m] = i == j ? R(1) : R(0);
+  for (int i = k; i >= 1; --i) {
+    if (tau[i - 1] == R(0)) continue;
+    for (int j = 1; j <= m; ++j) {
+      R t = q[(i - 1) + (long long)(j - 1) * m];
+      for (int r = i + 1; r <= m; ++r) t += A_(r, i) * q[(r - 1) + (long long)(j - 1) * m];
+      t *= tau[i - 1];
+      q[(i - 1) + (long long)(j - 1) * m] -= t;
+      for (int r = i + 1; r <= m; ++r) q[(r - 1) + (long long)(j - 1) * m] -= A_(r, i) * t;
+    }
+  }
+  for (int j = 1; j <= k; ++j)
+    for (int i = j + 1; i <= m; ++i) A_(i, j) = R(0);
+#undef A_
+}
+
+// RQ of the mr x n matrix a (ld mr, mr <= n): a = R Q, R (mr x n) upper trapezoidal in the
+// last mr columns, Q (n x n) = H(1) ... H(k) formed
+template <class R> void house_rq_r(int mr, int n, R* a, R* q) {
+  const int k = mr < n ? mr : n;
+  std::vector<R> tau(k);
+#define A_(i, j) a[((i) - 1) + (long long)((j) - 1) * mr]
+  for (int i = k; i >= 1; --i) {
+    const int row = mr - k + i, col = n - k + i;
+    tau[i - 1] = larfg_r<R>(col, &A_(row, col), &A_(row, 1), mr);
+    if (tau[i - 1] != R(0) && row > 1) {
+      const R aii = A_(row, col);
+      A_(row, col) = R(1);
+      for (int r = 1; r <= row - 1; ++r) {
+        R t = R(0);
+        for (int c = 1; c <= col; ++c) t += A_(r, c) * A_(row, c);
+        for (int c = 1; c <= col; ++c) A_(r, c) -= tau[i - 1] * t * A_(row, c);
+      }
+      A_(row, col) = aii;
+    }
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) q[i + (long long)j * n] = i == j ? R(1) : R(0);
+  for (int i = k; i >= 1; --i) {
+    const int row = mr - k + i, col = n - k + i;
+    if (tau[i - 1] == R(0)) continue;
+    // Q = H(i) Q; v = [A(row, 1:col-1); 1]
+    for (int j = 1; j <= n; ++j) {
+      R t = q[(col - 1) + (long long)(j - 1) * n];
+      for (int c = 1; c <= col - 1; ++c) t += A_(row, c) * q[(c - 1) + (long long)(j - 1) * n];
+      t *= tau[i - 1];
+      q[(col - 1) + (long long)(j - 1) * n] -= t;
+      for (int c = 1; c <= col - 1; ++c) q[(c - 1) + (long long)(j - 1) * n] -= A_(row, c) * t;
+    }
+  }
+  // R: zero what lies left of the trapezoid's diagonal
+  for (int i = 1; i <= mr; ++i)
+    for (int j = 1; j <= n; ++j)
+      if (j < n - mr + i) A_(i, j) = R(0);
+#undef A_
+}
+
+// small dense products (column-major): C = op(A) op(B)
+template <class R> void mm_r(int m, int nn, int kk, const R* A, bool ta, const R* B, bool tb, R* C) {
+  for (int j = 0; j < nn; ++j)
+    for (int i = 0; i < m; ++i) {
+      R t = R(0);
+      for (int l = 0; l < kk; ++l) {
+        const R a = ta ? A[l + (long long)i * kk] : A[i + (long long)l * m];
+        const R b = tb ? B[j + (long long)l * nn] : B[l + (long long)j * kk];
+        t += a * b;
+      }
+      C[i + (long long)j * m] = t;
+    }
+}
+
+// _gqz_2x2!(A, B) on the 2 x 2 blocks at a, b (ld): standardizes in place, returns the
+// rotations (csl, snl, csr, snr)
+template <class R> void gqz_2x2_r(R* a, R* b, int ld, R* cslo, R* snlo, R* csro, R* snro) {
+#define GA(i, j) a[((i) - 1) + (long long)((j) - 1) * ld]
+#define GB(i, j) b[((i) - 1) + (long long)((j) - 1) * ld]
+  const R safmin = lim<R>::fmin(), ulp = lim<R>::eps();
+  const R anorm = m_max(m_max(m_abs(GA(1, 1)) + m_abs(GA(2, 1)), m_abs(GA(1, 2)) + m_abs(GA(2, 2))), safmin);
+  const R ascale = R(1) / anorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GA(i, j) *= ascale;
+  const R bnorm = m_max(m_max(m_abs(GB(1, 1)), m_abs(GB(1, 2)) + m_abs(GB(2, 2))), safmin);
+  const R bscale = R(1) / bnorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GB(i, j) *= bscale;
+  R csl, snl, csr, snr, rr;
+  if (m_abs(GA(2, 1)) < ulp) {
+    csl = 1; snl = 0; csr = 1; snr = 0;
+    GA(2, 1) = 0;
+    GB(2, 1) = 0;
+  } else if (m_abs(GB(1, 1)) < ulp) {
+    givens_alg<R>(GA(1, 1), GA(2, 1), &csl, &snl, &rr);
+    csr = 1; snr = 0;
+    gr_cols<R>(a, ld, 1, 2, csl, snl, 1, 2);
+    gr_cols<R>(b, ld, 1, 2, csl, snl, 1, 2);
+    GA(2, 1) = 0;
+    GB(1, 1) = 0;
+    GB(2, 1) = 0;
+  } else if (m_abs(GB(2, 2)) < ulp) {
+    givens_alg<R>(GA(2, 2), GA(2, 1), &csr, &snr, &rr);
+    gr_rows<R>(a, ld, 1, 2, csr, -snr, 1, 2);
+    gr_rows<R>(b, ld, 1, 2, csr, -snr, 1, 2);
+    csl = 1; snl = 0;
+    GA(2, 1) = 0;
+    GB(2, 1) = 0;
+    GB(2, 2) = 0;
+  } else {
+    R scale1, scale2, wr1, wr2, wi;
+    ggs_2x2<R>(a, ld, b, ld, safmin, &scale1, &scale2, &wr1, &wr2, &wi);
+    if (wi == R(0)) {
+      const R h1 = scale1 * GA(1, 1) - wr1 * GB(1, 1);
+      const R h2 = scale1 * GA(1, 2) - wr1 * GB(1, 2);
+      const R h3 = scale1 * GA(2, 2) - wr1 * GB(2, 2);
+      const R rr2 = m_hypot(h2, h1);
+      const R qq = m_hypot(scale1 * GA(2, 1), h3);
+      if (rr2 > qq) givens_alg<R>(h2, h1, &csr, &snr, &rr);
+      else givens_alg<R>(h3, scale1 * GA(2, 1), &csr, &snr, &rr);
+      gr_cols<R>(a, ld, 1, 2, csr, snr, 1, 2);
+      gr_cols<R>(b, ld, 1, 2, csr, snr, 1, 2);
+      snr = -snr;
+      const R t1 = m_max(m_abs(GA(1, 1)) + m_abs(GA(1, 2)), m_abs(GA(2, 1)) + m_abs(GA(2, 2)));
+      const R t2 = m_max(m_abs(GA(1, 1)) + m_abs(GA(1, 2)), m_abs(GA(2, 1)) + m_abs(GA(2, 2)));
+      if (scale1 * t1 >= m_abs(wr1) * t2) givens_alg<R>(GB(1, 1), GB(2, 1), &csl, &snl, &rr);
+      else givens_alg<R>(GA(1, 1), GA(2, 1), &csl, &snl, &rr);
+      gr_rows<R>(a, ld, 1, 2, csl, snl, 1, 2);
+      gr_rows<R>(b, ld, 1, 2, csl, snl, 1, 2);
+      GA(2, 1) = 0;
+      GB(2, 1) = 0;
+    } else {
+      R ssmin, ssmax;
+      gsvd_2x2<R>(GB(1, 1), GB(1, 2), GB(2, 2), &ssmin, &ssmax, &snr, &csr, &snl, &csl);
+      gr_cols_adj<R>(a, ld, 1, 2, csr, snr, 1, 2);
+      gr_cols_adj<R>(b, ld, 1, 2, csr, snr, 1, 2);
+      gr_rows<R>(a, ld, 1, 2, csl, snl, 1, 2);
+      gr_rows<R>(b, ld, 1, 2, csl, snl, 1, 2);
+      GB(2, 1) = 0;
+      GB(1, 2) = 0;
+    }
+  }
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GA(i, j) *= anorm;
+  for (int j = 1; j <= 2; ++j) for (int i = 1; i <= 2; ++i) GB(i, j) *= bnorm;
+  *cslo = csl; *snlo = snl; *csro = csr; *snro = snr;
+#undef GA
+#undef GB
+}
+
+// _rtrexch2!(A, B, Q, Z, j1): swap two 1 x 1 blocks of a real pair
+template <class R> bool rtrexch2_r(int n, R* A, R* B, R* Q, R* Z, int j1) {
+#define AM(i, j) A[((i) - 1) + (long long)((j) - 1) * n]
+#define BM(i, j) B[((i) - 1) + (long long)((j) - 1) * n]
+  R S[4] = {AM(j1, j1), AM(j1 + 1, j1), AM(j1, j1 + 1), AM(j1 + 1, j1 + 1)};
+  R T[4] = {BM(j1, j1), BM(j1 + 1, j1), BM(j1, j1 + 1), BM(j1 + 1, j1 + 1)};
+  const R S0[4] = {S[0], S[1], S[2], S[3]}, T0[4] = {T[0], T[1], T[2], T[3]};
+  const R smlnum = safemin<R>() / lim<R>::eps();
+  R W[8] = {S[0], S[1], S[2], S[3], T[0], T[1], T[2], T[3]};
+  R sa = safe_fnorm_r<R>(W, 8, 8, 1);
+  const R thresh = m_max(R(20) * lim<R>::eps() * sa, smlnum);
+  const R f = S[3] * T[0] - T[3] * S[0];
+  const R g = S[3] * T[2] - T[3] * S[2];
+  sa = m_abs(S[3]) * m_abs(T[0]);
+  const R sb = m_abs(S[0]) * m_abs(T[3]);
+  R cz, sz, rr;
+  givens_alg<R>(f, g, &cz, &sz, &rr);
+  { const R t = sz; sz = cz; cz = t; }
+  gr_cols_adj<R>(S, 2, 1, 2, cz, -sz, 1, 2);
+  gr_cols_adj<R>(T, 2, 1, 2, cz, -sz, 1, 2);
+  const R fq = sa >= sb ? S[0] : T[0], gq = sa >= sb ? S[1] : T[1];
+  R cq, sq;
+  if (sz != R(0) && fq == R(0) && gq == R(0)) { cq = 0; sq = 1; }
+  else givens_alg<R>(fq, gq, &cq, &sq, &rr);
+  gr_rows<R>(S, 2, 1, 2, cq, sq, 1, 2);
+  gr_rows<R>(T, 2, 1, 2, cq, sq, 1, 2);
+  const R ws = m_abs(S[1]) + m_abs(T[1]);
+  if (!(ws <= thresh)) return false;
+  R Ss[4] = {S[0], S[1], S[2], S[3]}, Ts[4] = {T[0], T[1], T[2], T[3]};
+  gr_cols_adj<R>(Ss, 2, 1, 2, cz, sz, 1, 2);
+  gr_cols_adj<R>(Ts, 2, 1, 2, cz, sz, 1, 2);
+  gr_rows<R>(Ss, 2, 1, 2, cq, -sq, 1, 2);
+  gr_rows<R>(Ts, 2, 1, 2, cq, -sq, 1, 2);
+  for (int e = 0; e < 4; ++e) { W[e] = Ss[e] - S0[e]; W[4 + e] = Ts[e] - T0[e]; }
+  const R ss = safe_fnorm_r<R>(W, 8, 8, 1);
+  if (!(ss <= thresh)) return false;
+  gr_cols_adj<R>(A, n, j1, j1 + 1, cz, -sz, 1, n);
+  gr_cols_adj<R>(B, n, j1, j1 + 1, cz, -sz, 1, n);
+  gr_rows<R>(A, n, j1, j1 + 1, cq, sq, 1, n);
+  gr_rows<R>(B, n, j1, j1 + 1, cq, sq, 1, n);
+  AM(j1 + 1, j1) = R(0);
+  BM(j1 + 1, j1) = R(0);
+  if (Z) gr_cols_adj<R>(Z, n, j1, j1 + 1, cz, -sz, 1, n);
+  if (Q) gr_cols_adj<R>(Q, n, j1, j1 + 1, cq, sq, 1, n);
+  return true;
+#undef AM
+#undef BM
+}
+
+// _swap1or2!(A, B, Q, Z, j1, n1, n2) (dtgex2)
+template <class R> bool swap1or2_r(int n, R* A, R* B, R* Q, R* Z, int j1, int n1, int n2) {
+  if (j1 + n1 > n) return true;
+  if (n1 == 1 && n2 == 1) return rtrexch2_r<R>(n, A, B, Q, Z, j1);
+#define AM(i, j) A[((i) - 1) + (long long)((j) - 1) * n]
+#define BM(i, j) B[((i) - 1) + (long long)((j) - 1) * n]
+  const int m = n1 + n2, je = j1 + m - 1;
+  R S[16], T[16];
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) { S[i + j * m] = AM(j1 + i, j1 + j); T[i + j * m] = BM(j1 + i, j1 + j); }
+  const R eps = lim<R>::eps(), smallnum = lim<R>::fmin() / eps;
+  R dnorm = 0, tnorm = 0;
+  for (int e = 0; e < m * m; ++e) { dnorm = m_max(dnorm, m_abs(S[e])); tnorm = m_max(tnorm, m_abs(T[e])); }
+  const R thresh = m_max(R(20) * eps * dnorm, smallnum);
+  const R threshb = m_max(R(20) * eps * tnorm, smallnum);
+  // _syl1or2: K [vec R; vec L] = [vec S12; vec T12], K = [I(n2)(x)S11, -S22'(x)I(n1); I(n2)(x)T11, -T22'(x)I(n1)]
+  const int nn = n1 * n2, kd = 2 * nn;
+  std::vector<cx<R>> K((size_t)kd * kd, cx<R>(R(0))), rl(kd);
+  auto Sb = [&](int i, int j) { return S[(i - 1) + (j - 1) * m]; };
+  auto Tb = [&](int i, int j) { return T[(i - 1) + (j - 1) * m]; };
+  for (int q = 0; q < n2; ++q)
+    for (int p = 0; p < n1; ++p) {
+      const int row = p + q * n1;  // (p, q) of an n1 x n2 block
+      for (int pp = 0; pp < n1; ++pp) {
+        K[row + (size_t)(pp + q * n1) * kd] = cx<R>(Sb(1 + p, 1 + pp));
+        K[(nn + row) + (size_t)(pp + q * n1) * kd] = cx<R>(Tb(1 + p, 1 + pp));
+      }
+      for (int qq = 0; qq < n2; ++qq) {
+        K[row + (size_t)(nn + p + qq * n1) * kd] = cx<R>(-Sb(n1 + 1 + qq, n1 + 1 + q));
+        K[(nn + row) + (size_t)(nn + p + qq * n1) * kd] = cx<R>(-Tb(n1 + 1 + qq, n1 + 1 + q));
+      }
+      rl[row] = cx<R>(Sb(1 + p, n1 + 1 + q));
+      rl[nn + row] = cx<R>(Tb(1 + p, n1 + 1 + q));
+    }
+  bool pert = false;
+  const R scale = safe_lu_solve<R>(kd, K.data(), rl.data(), &pert);
+  // LI = [-XL; scale I(n2)] (m x n2), IR = [scale I(n1) XR] (n1 x m)
+  R LI[8], IR[8], qli[16], zir[16];
+  for (int j = 0; j < n2; ++j) {
+    for (int i = 0; i < n1; ++i) LI[i + j * m] = -rl[nn + i + j * n1].re;
+    for (int i = 0; i < n2; ++i) LI[n1 + i + j * m] = i == j ? scale : R(0);
+  }
+  for (int i = 0; i < n1; ++i) {
+    for (int j = 0; j < n1; ++j) IR[i + j * n1] = i == j ? scale : R(0);
+    for (int j = 0; j < n2; ++j) IR[i + (n1 + j) * n1] = rl[i + j * n1].re;
+  }
+  house_qr_r<R>(m, n2, LI, qli);
+  house_rq_r<R>(n1, m, IR, zir);
+  R tmp[16], s1[16], t1[16];
+  mm_r<R>(m, m, m, qli, true, S, false, tmp);
+  mm_r<R>(m, m, m, tmp, false, zir, true, s1);
+  mm_r<R>(m, m, m, qli, true, T, false, tmp);
+  mm_r<R>(m, m, m, tmp, false, zir, true, t1);
+  // triangularize t1 by RQ (a) and by QR (b)
+  R t2a[16], zt1a[16], s2a[16], z2a[16], t2b[16], qt1b[16], s2b[16], q2b[16];
+  for (int e = 0; e < m * m; ++e) { t2a[e] = t1[e]; t2b[e] = t1[e]; }
+  house_rq_r<R>(m, m, t2a, zt1a);
+  mm_r<R>(m, m, m, s1, false, zt1a, true, s2a);
+  mm_r<R>(m, m, m, zt1a, false, zir, false, z2a);
+  const R brq = safe_fnorm_r<R>(s2a + n2, m, m - n2, n2);
+  house_qr_r<R>(m, m, t2b, qt1b);
+  mm_r<R>(m, m, m, qt1b, true, s1, false, s2b);
+  mm_r<R>(m, m, m, qli, false, qt1b, false, q2b);
+  const R bqr = safe_fnorm_r<R>(s2b + n2, m, m - n2, n2);
+  if (!(m_min(bqr, brq) <= thresh)) return false;
+  R *snew, *tnew, *znew, *qnew;
+  if (bqr <= brq) { snew = s2b; tnew = t2b; znew = zir; qnew = q2b; }
+  else { snew = s2a; tnew = t2a; znew = z2a; qnew = qli; }
+  {
+    R r1[16], r2[16];
+    mm_r<R>(m, m, m, qnew, false, snew, false, r1);
+    mm_r<R>(m, m, m, r1, false, znew, false, r2);
+    for (int e = 0; e < m * m; ++e) r2[e] = S[e] - r2[e];
+    const R resa = safe_fnorm_r<R>(r2, m, m, m);
+    mm_r<R>(m, m, m, qnew, false, tnew, false, r1);
+    mm_r<R>(m, m, m, r1, false, znew, false, r2);
+    for (int e = 0; e < m * m; ++e) r2[e] = T[e] - r2[e];
+    const R resb = safe_fnorm_r<R>(r2, m, m, m);
+    if (!(resa <= thresh && resb <= threshb)) return false;
+  }
+  for (int j = 0; j < n2; ++j)
+    for (int i = n2; i < m; ++i) snew[i + j * m] = R(0);
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) { AM(j1 + i, j1 + j) = snew[i + j * m]; BM(j1 + i, j1 + j) = tnew[i + j * m]; }
+  R qtmp[16], ztmp[16];
+  for (int e = 0; e < m * m; ++e) { qtmp[e] = R(0); ztmp[e] = R(0); }
+  R csl, snl, csr, snr;
+  if (n2 > 1) {
+    gqz_2x2_r<R>(&AM(j1, j1), &BM(j1, j1), n, &csl, &snl, &csr, &snr);
+    qtmp[0] = csl; qtmp[1] = snl; qtmp[m] = -snl; qtmp[m + 1] = csl;
+    ztmp[0] = csr; ztmp[1] = snr; ztmp[m] = -snr; ztmp[m + 1] = csr;
+  } else {
+    ztmp[0] = R(1);
+    qtmp[0] = R(1);
+  }
+  const int j3 = j1 + n2;
+  if (n1 > 1) {
+    gqz_2x2_r<R>(&AM(j3, j3), &BM(j3, j3), n, &csl, &snl, &csr, &snr);
+    qtmp[(m - 2) + (m - 2) * m] = csl; qtmp[(m - 1) + (m - 2) * m] = snl;
+    qtmp[(m - 2) + (m - 1) * m] = -snl; qtmp[(m - 1) + (m - 1) * m] = csl;
+    ztmp[(m - 2) + (m - 2) * m] = csr; ztmp[(m - 1) + (m - 2) * m] = snr;
+    ztmp[(m - 2) + (m - 1) * m] = -snr; ztmp[(m - 1) + (m - 1) * m] = csr;
+  } else {
+    qtmp[(m - 1) + (m - 1) * m] = R(1);
+    ztmp[(m - 1) + (m - 1) * m] = R(1);
+  }
+  // the off-diagonal block of the active region: qtmp[1:n2,1:n2]' X ztmp[n2+1:m, n2+1:m]
+  for (R* M : {A, B}) {
+    R X[4], ab[4];
+    for (int j = 0; j < n1; ++j) for (int i = 0; i < n2; ++i) X[i + j * n2] = M[(j1 - 1 + i) + (long long)(j3 - 1 + j) * n];
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n2; ++i) {
+        R t = R(0);
+        for (int l = 0; l < n2; ++l) t += qtmp[l + i * m] * X[l + j * n2];
+        ab[i + j * n2] = t;
+      }
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n2; ++i) {
+        R t = R(0);
+        for (int l = 0; l < n1; ++l) t += ab[i + l * n2] * ztmp[(n2 + l) + (n2 + j) * m];
+        M[(j1 - 1 + i) + (long long)(j3 - 1 + j) * n] = t;
+      }
+  }
+  R qf[16], zf[16];
+  mm_r<R>(m, m, m, qnew, false, qtmp, false, qf);
+  mm_r<R>(m, m, m, znew, true, ztmp, false, zf);
+  auto cols_times = [&](R* M, int rows, const R* X) {  // M[1:rows, j1:je] = M[1:rows, j1:je] X
+    for (int r = 1; r <= rows; ++r) {
+      R v[4];
+      for (int j = 0; j < m; ++j) v[j] = M[(r - 1) + (long long)(j1 - 1 + j) * n];
+      for (int j = 0; j < m; ++j) {
+        R t = R(0);
+        for (int l = 0; l < m; ++l) t += v[l] * X[l + j * m];
+        M[(r - 1) + (long long)(j1 - 1 + j) * n] = t;
+      }
+    }
+  };
+  if (Q) cols_times(Q, n, qf);
+  if (Z) cols_times(Z, n, zf);
+  if (je < n)
+    for (R* M : {A, B})
+      for (int c = je + 1; c <= n; ++c) {
+        R v[4];
+        for (int i = 0; i < m; ++i) v[i] = M[(j1 - 1 + i) + (long long)(c - 1) * n];
+        for (int i = 0; i < m; ++i) {
+          R t = R(0);
+          for (int l = 0; l < m; ++l) t += qf[l + i * m] * v[l];
+          M[(j1 - 1 + i) + (long long)(c - 1) * n] = t;
+        }
+      }
+  cols_times(A, j1 - 1, zf);
+  cols_times(B, j1 - 1, zf);
+  return true;
+#undef AM
+#undef BM
+}
+
+// _trexchange!(S, T, Q, Z, iold, inew) for inew <= iold; returns ok, *inew_out the final row
+template <class R> bool trexchange_r(int n, R* S, R* T, R* Q, R* Z, int iold, int inew, int* inew_out) {
+#define SM(i, j) S[((i) - 1) + (long long)((j) - 1) * n]
+  *inew_out = inew;
+  if (n <= 1) return true;
+  auto nbsize = [&](int j) { return (j < n && SM(j + 1, j) != R(0)) ? 2 : 1; };
+  if (iold > 1 && SM(iold, iold - 1) != R(0)) iold -= 1;
+  const int nbold = nbsize(iold);
+  if (inew > 1 && SM(inew, inew - 1) != R(0)) inew -= 1;
+  if (iold == inew) { *inew_out = inew; return true; }
+  if (iold < inew) return false;  // the move-down branch; gordschur! only moves blocks up
+  int ihere = iold;
+  while (ihere > inew) {
+    const int nbnext = (ihere >= 3 && SM(ihere - 1, ihere - 2) != R(0)) ? 2 : 1;
+    if (!swap1or2_r<R>(n, S, T, Q, Z, ihere - nbnext, nbnext, nbold)) { *inew_out = ihere; return false; }
+    ihere -= nbnext;
+  }
+  *inew_out = ihere;
+  return true;
+#undef SM
+}
+
+// gordschur!(S, T, Q, Z, select; scale) for a real pair; returns 0 or 1 + k of the block
+// that could not be moved (IllConditionException(k))
+template <class R>
+int gordschur_real(int n, R* S, R* T, R* Q, R* Z, const int* select, bool scale, cx<R>* alpha, R* beta) {
+  R cscale = 1, anrm = 1, cscaleb = 1, bnrm = 1;
+  bool scA = false, scB = false;
+  if (scale) {
+    scA = scale_matrix<R, R>(n, S, n, &cscale, &anrm);
+    scB = scale_matrix<R, R>(n, T, n, &cscaleb, &bnrm);
+  }
+#define SM(i, j) S[((i) - 1) + (long long)((j) - 1) * n]
+#define TM(i, j) T[((i) - 1) + (long long)((j) - 1) * n]
+  const R safmin = lim<R>::fmin();
+  int ks = 0;
+  bool inpair = false;
+  for (int k = 1; k <= n; ++k) {
+    if (inpair) { inpair = false; continue; }
+    bool doswap = select[k - 1] != 0;
+    if (k < n && SM(k + 1, k) != R(0)) {
+      inpair = true;
+      doswap = doswap || select[k] != 0;
+    }
+    if (doswap) {
+      ks += 1;
+      if (k != ks) {
+        int kn = ks;
+        if (!trexchange_r<R>(n, S, T, Q, Z, k, ks, &kn)) return 1 + k;
+        ks = kn;
+      }
+      if (inpair) ks += 1;
+    }
+  }
+  if (scA) for (int j = 0; j < n; ++j) safescale<R, R>(S + (long long)j * n, n, cscale, anrm);
+  if (scB) for (int j = 0; j < n; ++j) safescale<R, R>(T + (long long)j * n, n, cscaleb, bnrm);
+  inpair = false;
+  for (int k = 1; k <= n; ++k) {
+    if (inpair) { inpair = false; continue; }
+    if (k < n && SM(k + 1, k) != R(0)) inpair = true;
+    if (inpair) {
+      R b1, b2, ar1, ar2, ai;
+      ggs_2x2<R>(&SM(k, k), n, &TM(k, k), n, safmin, &b1, &b2, &ar1, &ar2, &ai);
+      alpha[k - 1] = cx<R>(ar1, ai);
+      alpha[k] = cx<R>(ar2, -ai);
+      beta[k - 1] = b1;
+      beta[k] = b2;
+    } else {
+      if (m_copysign(R(1), TM(k, k)) < R(0)) {
+        for (int j = 1; j <= n; ++j) { SM(k, j) = -SM(k, j); TM(k, j) = -TM(k, j); }
+        if (Q) for (int i = 0; i < n; ++i) Q[i + (long long)(k - 1) * n] = -Q[i + (long long)(k - 1) * n];
+      }
+      alpha[k - 1] = cx<R>(SM(k, k));
+      beta[k - 1] = TM(k, k);
+    }
+  }
+  return 0;
+#undef SM
+#undef TM
+}
+
 }  // namespace orc

@@ -315,3 +315,43 @@ def st_errors(D, E, lam, V):
         d_err = min(resnorm / Tnorm, ntol) / (myeps * ntol)
     v_err = np.abs(V @ V.T - np.eye(n)).max() / (myeps * ntol)
     return d_err, v_err
+
+
+def check_gordschur_real(A, B, vals, select, S2, T2, a, b, Q2, Z2, tol=10):
+    """The reference's real checkord criteria (test/gordschur.jl:90-137): quasi-triangular,
+    backward stable, orthogonal; and that the leading block holds exactly the selected
+    eigenvalues (a complex pair counts as selected when either member is)."""
+    n = A.shape[0]
+    nA, nB = np.linalg.norm(A), np.linalg.norm(B)
+    assert np.linalg.norm(np.tril(S2, -2)) / (n * nA * EPS) < tol
+    assert np.linalg.norm(np.tril(T2, -1)) / (n * nA * EPS) < tol
+    assert np.linalg.norm(A - Q2 @ S2 @ Z2.T) / (n * nA * EPS) < tol
+    assert np.linalg.norm(B - Q2 @ T2 @ Z2.T) / (n * nB * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Z2 @ Z2.T) / (n * EPS) < tol
+    assert np.linalg.norm(np.eye(n) - Q2 @ Q2.T) / (n * EPS) < tol
+    # the selected set, with pairs (the reference's own list, select[j] || (select[j + 1] &&
+    # imag(values[j]) != 0), also admits the second member of an unselected pair followed by a
+    # selected eigenvalue, so its matching can pair a leading eigenvalue with a wrong one)
+    sel = selected_with_pairs(vals, select)
+    k = int(sel.sum())
+    got = a[:k] / b[:k]
+    want = vals[sel]
+    from scipy.optimize import linear_sum_assignment
+    C = np.abs(got[:, None] - want[None, :]) / np.maximum(1.0, np.abs(want[None, :]))
+    r, c = linear_sum_assignment(C)
+    assert C[r, c].max() < 1e-8
+
+
+def selected_with_pairs(vals, select):
+    """select with each complex pair of a real generalized Schur form selected when either
+    member is (rordschur.jl:563-583)."""
+    n = len(vals)
+    sel = np.array(select, dtype=bool).copy()
+    j = 0
+    while j < n:
+        if vals[j].imag != 0 and j < n - 1:
+            sel[j] = sel[j + 1] = sel[j] or sel[j + 1]
+            j += 2
+        else:
+            j += 1
+    return sel

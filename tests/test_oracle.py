@@ -15,7 +15,8 @@ import os
 import numpy as np
 import pytest
 
-from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, check_gsyl_errors, checkblocks, godunov,
+from common import (EPS, assert_schur_cplx, assert_schur_real, backward_error, check_gordschur_real, check_gsyl_errors,
+                    checkblocks, godunov,
                     st_errors, st_testmat1, st_testmat2,
                     gsyl_errors, gsyl_problem, kp_pencil, kp_truth, orth_error, randn_matrix)
 from oracle import pyoracle as po
@@ -349,3 +350,25 @@ def test_oracle_stedc_batch(n):
         T = np.diag(D) + np.diag(E, 1) + np.diag(E, -1)
         ref = np.linalg.eigvalsh(T)
         assert np.abs(np.sort(lam) - ref).max() <= 50 * len(D) * EPS * np.abs(T).max()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_ggordschur_real_checkord(seed):
+    """gordschur! for real pencils restated (rordschur.jl:542-1178) on the reference's real
+    checkord problem (test/gordschur.jl:90-137: A = rand, B = rand - 1/2 + I, n = 16, the
+    second half selected) and on a random selection at n = 40: quasi-triangular, backward
+    stable, orthogonal, and exactly the selected eigenvalues (pairs travel together) lead."""
+    rng = np.random.default_rng(1600 + seed)
+    for n, half in ((16, True), (40, False)):
+        A = rng.random((n, n))
+        B = rng.random((n, n)) - 0.5 + np.eye(n)
+        S, T, al, be, Q, Z, st = po.ggschur_real(A, B)
+        assert st == 0
+        sel = np.ones(n, np.int32)
+        if half:
+            sel[: n >> 1] = 0
+        else:
+            sel = rng.integers(0, 2, n).astype(np.int32)
+        S2, T2, a, b, Q2, Z2, st = po.ggordschur_real(S, T, Q, Z, sel)
+        assert st == 0
+        check_gordschur_real(A, B, al / be, sel, S2, T2, a, b, Q2, Z2)

@@ -397,3 +397,59 @@ def test_ggordschur_checkord(gs, seed):
     assert st == 0
     np.testing.assert_allclose(G2.alpha / G2.beta, al / be, rtol=1e-10, atol=0)
     assert np.max(np.abs(G2.S - S)) < 1e-10 * nA and np.max(np.abs(G2.T - T)) < 1e-10 * nB
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_ggordschur_real(gs, seed):
+    """gordschur! of real generalized Schur forms (rordschur.jl:542-1178) on the GPU: the
+    reference's real checkord (test/gordschur.jl:90-137, n = 16, the second half selected)
+    and random selections at n = 16 and 40, through the GPU ggschur; against the oracle's
+    restatement on the same pair: the same eigenvalue order and the same leading deflating
+    subspaces.  Entry by entry the two differ by signs: each 2 x 2-block swap chooses
+    between re-triangularizing by RQ or by QR by comparing two residuals of order eps
+    (rordschur.jl:841-858), so the choice, and with it the signs of rows and columns,
+    follows rounding -- the oracle's own output changes so under 1-ulp perturbations."""
+    from common import check_gordschur_real, selected_with_pairs
+    rng = np.random.default_rng(4700 + seed)
+    for n, half in ((16, True), (16, False), (40, False)):
+        A = rng.random((n, n))
+        B = rng.random((n, n)) - 0.5 + np.eye(n)
+        G = gs.ggschur(A, B)
+        sel = np.ones(n, bool)
+        if half:
+            sel[: n >> 1] = False
+        else:
+            sel = rng.integers(0, 2, n).astype(bool)
+        G2 = gs.gordschur(G, sel)
+        check_gordschur_real(A, B, G.alpha / G.beta, sel, G2.S, G2.T, G2.alpha, G2.beta, G2.Q, G2.Z)
+        S, T, a, b, Q, Z, st = po.ggordschur_real(G.S, G.T, G.Q, G.Z, sel.astype(np.int32))
+        assert st == 0
+        np.testing.assert_allclose(G2.alpha / G2.beta, a / b, rtol=1e-9, atol=0)
+        k = int(selected_with_pairs(G.alpha / G.beta, sel).sum())
+        for M2, Mo in ((G2.Z, Z), (G2.Q, Q)):
+            P2 = M2[:, :k] @ M2[:, :k].T
+            Po = Mo[:, :k] @ Mo[:, :k].T
+            assert np.abs(P2 - Po).max() <= 1e-8, (k, np.abs(P2 - Po).max())
+
+
+def test_ggordschur_real_noop_and_pairs(gs):
+    """Nothing or everything selected leaves the eigenvalue order; selecting only one member
+    of a complex pair moves the pair."""
+    from common import check_gordschur_real
+    rng = np.random.default_rng(4800)
+    n = 20
+    A = rng.standard_normal((n, n))
+    B = rng.standard_normal((n, n))
+    G = gs.ggschur(A, B)
+    vals = G.alpha / G.beta
+    for sel in (np.zeros(n, bool), np.ones(n, bool)):
+        G2 = gs.gordschur(G, sel)
+        np.testing.assert_allclose(G2.alpha / G2.beta, vals, rtol=1e-12)
+    pairs = [j for j in range(n - 1) if vals[j].imag > 0]
+    assert pairs, "the pencil should have a complex pair"
+    sel = np.zeros(n, bool)
+    sel[pairs[-1] + 1] = True
+    G2 = gs.gordschur(G, sel)
+    check_gordschur_real(A, B, vals, sel, G2.S, G2.T, G2.alpha, G2.beta, G2.Q, G2.Z)
+    assert abs(G2.alpha[0] / G2.beta[0] - vals[pairs[-1]]) < 1e-8 * abs(vals[pairs[-1]]) or \
+        abs(G2.alpha[0] / G2.beta[0] - vals[pairs[-1] + 1]) < 1e-8 * abs(vals[pairs[-1]])
