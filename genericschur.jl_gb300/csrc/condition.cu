@@ -11,7 +11,8 @@
 //   2. the tile's own triangular system by element waves along its anti-diagonals (warp 0),
 //      with the reference's perturbation of small diagonal differences to smin.
 // The adjoint solve is the forward one on P A^H P, P B^H P and P C P (P the reversal
-// permutation): k_adj_copy builds the first two, the third is an index map.
+// permutation): k_adj_copy builds the first two, the third is an index map.  With possign
+// (A X + X B = scale C) the B terms change sign.
 // The reference rescales the whole right-hand side when an entry would overflow
 // (scaloc = 1 / |v|_1 when |a11|_1 < 1 < |v|_1 and |v|_1 > bignum |a11|_1).  The tiled
 // solve flags that case (and any non-finite entry) instead; the host then reruns the
@@ -141,11 +142,20 @@ __global__ void __launch_bounds__(kSyT) k_trsyl_level(SylvArgs<S> P, int d, int 
       Pb[i][j] = (j < ploc) ? P.B[(size_t)(jb + i) + (size_t)(c0 + j) * P.ldb] : O::zero();
     }
     __syncthreads();
+    if (P.pos) {
 #pragma unroll 4
-    for (int j = 0; j < kTs; ++j) {
-      const S b = Pb[j][cc];
+      for (int j = 0; j < kTs; ++j) {
+        const S b = Pb[j][cc];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[q] = O::fma(Pa[rb + q][j], b, acc[q]);
+        for (int q = 0; q < 4; ++q) acc[q] = O::fnma(Pa[rb + q][j], b, acc[q]);
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < kTs; ++j) {
+        const S b = Pb[j][cc];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = O::fma(Pa[rb + q][j], b, acc[q]);
+      }
     }
     __syncthreads();
   }
@@ -169,8 +179,8 @@ __global__ void __launch_bounds__(kSyT) k_trsyl_level(SylvArgs<S> P, int d, int 
         S suml = O::zero(), sumr = O::zero();
         for (int j = k + 1; j < mloc; ++j) suml = O::fma(Pa[k][j], R[j][l], suml);
         for (int j = 0; j < l; ++j) sumr = O::fma(R[k][j], Pb[j][l], sumr);
-        const S v = O::sub(R[k][l], O::sub(suml, sumr));
-        S a11 = O::sub(Pa[k][k], Pb[l][l]);
+        const S v = O::sub(R[k][l], P.pos ? O::add(suml, sumr) : O::sub(suml, sumr));
+        S a11 = P.pos ? O::add(Pa[k][k], Pb[l][l]) : O::sub(Pa[k][k], Pb[l][l]);
         double da11 = O::abs1(a11);
         if (P.le ? (da11 <= P.smin) : (da11 < P.smin)) {
           a11 = O::from(P.smin);
@@ -227,8 +237,9 @@ __global__ void __launch_bounds__(kSyT) k_trsyl_exact(SylvArgs<S> P, double* out
       suml = block_sum_s(suml, red);
       sumr = block_sum_s(sumr, red);
       if (t == 0) {
-        const S v = O::sub(*cptr(P, k, l), O::sub(suml, sumr));
-        S a11 = O::sub(P.A[(size_t)k + (size_t)k * P.lda], P.B[(size_t)l + (size_t)l * P.ldb]);
+        const S v = O::sub(*cptr(P, k, l), P.pos ? O::add(suml, sumr) : O::sub(suml, sumr));
+        S a11 = P.pos ? O::add(P.A[(size_t)k + (size_t)k * P.lda], P.B[(size_t)l + (size_t)l * P.ldb])
+                      : O::sub(P.A[(size_t)k + (size_t)k * P.lda], P.B[(size_t)l + (size_t)l * P.ldb]);
         double da11 = O::abs1(a11);
         if (P.le ? (da11 <= P.smin) : (da11 < P.smin)) {
           a11 = O::from(P.smin);

@@ -104,6 +104,7 @@ struct SylvArgs {
   int m, p, mT, pT;
   int flip;       // C(i, j) stored at C[(m-1-i) + (p-1-j) ldc] (adjoint solves)
   int le;         // perturb |a11|_1 <= smin (trsylvester!) or < smin (adjtrsylvester!)
+  int pos;        // possign: A X + X B = scale C (the B terms' sign is +)
   double smin, bignum;
   int* flag;      // |= 1 perturbed, 2 the overflow rescaling is needed, 4 non-finite entry
 };

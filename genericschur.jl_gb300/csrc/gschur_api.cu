@@ -2048,6 +2048,7 @@ template <class S> struct CondRun {
     P.pT = (p + 31) / 32;
     P.flip = adj ? 1 : 0;
     P.le = adj ? 0 : 1;
+    P.pos = 0;
     P.smin = smin;
     P.bignum = bignum;
     P.flag = flag();
@@ -2108,6 +2109,97 @@ template <class S> struct CondRun {
     return GS_OK;
   }
 };
+
+// trsylvester!(A, B, C; possign) / adjtrsylvester! (sylvester.jl:11-139) for upper
+// triangular A (m x m) and B (n x n) on C (m x n), through the tiled level solve of
+// condition.cu (and the reference's element order when a rescaling or a non-finite entry
+// is met).
+template <class S>
+int trsyl_std_impl(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B, int64_t ldb,
+                   double* C, int64_t ldc, int adjoint, int possign, double* scale, int32_t* perturbed,
+                   unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (m < 0 || n < 0 || lda < std::max<int64_t>(m, 1) || ldb < std::max<int64_t>(n, 1) ||
+      ldc < std::max<int64_t>(m, 1))
+    return set_err(ctx, GS_BADARG, "bad sizes");
+  if (m > (1 << 16) || n > (1 << 16)) return set_err(ctx, GS_BADARG, "order too large");
+  if (scale) *scale = 1.0;
+  if (perturbed) *perturbed = 0;
+  if (m == 0 || n == 0) return GS_OK;
+  if (!A || !B || !C) return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  const size_t mm = (size_t)m * m, nn = (size_t)n * n, mn = (size_t)m * n;
+  Arena ar;
+  const size_t o_A = ar.take<S>(mm), o_B = ar.take<S>(nn), o_C = ar.take<S>(mn), o_bak = ar.take<S>(mn),
+               o_scr = ar.take<S>(adjoint ? std::max(mm, nn) : 1), o_max = ar.take<unsigned long long>(2),
+               o_flag = ar.take<int>(4), o_dbl = ar.take<double>(2);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind in = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  S* dA = (S*)(base + o_A);
+  S* dB = (S*)(base + o_B);
+  S* dC = (S*)(base + o_C);
+  CK(cudaMemcpy2DAsync(dA, sizeof(S) * m, A, sizeof(S) * lda, sizeof(S) * m, m, in, s));
+  CK(cudaMemcpy2DAsync(dB, sizeof(S) * n, B, sizeof(S) * ldb, sizeof(S) * n, n, in, s));
+  CK(cudaMemcpy2DAsync(dC, sizeof(S) * m, C, sizeof(S) * ldc, sizeof(S) * m, n, in, s));
+  CK(cudaEventRecord(ctx->t0, s));
+  unsigned long long* dmax = (unsigned long long*)(base + o_max);
+  CK(cudaMemsetAsync(dmax, 0, 2 * sizeof(unsigned long long), s));
+  CK(launch_cond_maxabs<S>(dA, (int)m, (int)m, (int)m, dmax, ctx->num_sms, s));
+  CK(launch_cond_maxabs<S>(dB, (int)n, (int)n, (int)n, dmax + 1, ctx->num_sms, s));
+  unsigned long long bits[2];
+  CK(cudaMemcpyAsync(bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  double na, nb;
+  std::memcpy(&na, &bits[0], sizeof(double));
+  std::memcpy(&nb, &bits[1], sizeof(double));
+  const double tiny = 2.220446049250313e-16;
+  const double small = 2.2250738585072014e-308 * (double)m * (double)n / tiny;
+  SylvArgs<S> P;
+  if (adjoint) {
+    // the forward solve on the reversed conjugate transposes; C through the index map
+    S* Ap = (S*)(base + o_scr);
+    CK(launch_adj_copy<S>(dA, (int)m, (int)m, Ap, ctx->num_sms, s));
+    CK(cudaMemcpyAsync(dA, Ap, sizeof(S) * mm, cudaMemcpyDeviceToDevice, s));
+    CK(launch_adj_copy<S>(dB, (int)n, (int)n, Ap, ctx->num_sms, s));
+    CK(cudaMemcpyAsync(dB, Ap, sizeof(S) * nn, cudaMemcpyDeviceToDevice, s));
+  }
+  P.A = dA; P.lda = (int)m; P.B = dB; P.ldb = (int)n; P.C = dC; P.ldc = (int)m;
+  P.m = (int)m; P.p = (int)n; P.mT = (int)((m + 31) / 32); P.pT = (int)((n + 31) / 32);
+  P.flip = adjoint ? 1 : 0;
+  P.le = adjoint ? 0 : 1;
+  P.pos = possign ? 1 : 0;
+  P.bignum = 1.0 / small;
+  P.smin = jmax(small, tiny * na * nb);
+  P.flag = (int*)(base + o_flag);
+  CK(cudaMemcpyAsync(base + o_bak, dC, sizeof(S) * mn, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemsetAsync(P.flag, 0, sizeof(int), s));
+  CK(launch_trsyl_levels<S>(P, s));
+  int fl = 0;
+  CK(cudaMemcpyAsync(&fl, P.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  double sc = 1.0;
+  if (fl & 6) {
+    CK(cudaMemcpyAsync(dC, base + o_bak, sizeof(S) * mn, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(P.flag, 0, sizeof(int), s));
+    CK(launch_trsyl_exact<S>(P, (double*)(base + o_dbl), s));
+    CK(cudaMemcpyAsync(&sc, base + o_dbl, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&fl, P.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  CK(cudaEventRecord(ctx->t1, s));
+  ctx->timed = true;
+  CK(cudaMemcpy2DAsync(C, sizeof(S) * ldc, dC, sizeof(S) * m, sizeof(S) * m, n,
+                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (scale) *scale = sc;
+  if (perturbed) *perturbed = (fl & 1) ? 1 : 0;
+  return GS_OK;
+}
 
 template <class S>
 int condition_impl(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* out, unsigned flags,
@@ -2440,6 +2532,16 @@ int gs_eigen_rcond_c64(gs_context* ctx, int64_t n, const double* T, double* rcon
   return rcondv_impl<double2>(ctx, n, T, rconde, rcondv, flags);
 }
 
+int gs_trsylvester_f64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                       int64_t ldb, double* C, int64_t ldc, int32_t adjoint, int32_t possign, double* scale,
+                       int32_t* perturbed, unsigned flags) {
+  return trsyl_std_impl<double>(ctx, m, n, A, lda, B, ldb, C, ldc, adjoint, possign, scale, perturbed, flags);
+}
+int gs_trsylvester_c64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                       int64_t ldb, double* C, int64_t ldc, int32_t adjoint, int32_t possign, double* scale,
+                       int32_t* perturbed, unsigned flags) {
+  return trsyl_std_impl<double2>(ctx, m, n, A, lda, B, ldb, C, ldc, adjoint, possign, scale, perturbed, flags);
+}
 int gs_gtrsylvester_c64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
                         int64_t ldb, double* C, int64_t ldc, const double* D, int64_t ldd, const double* E,
                         int64_t lde, double* F, int64_t ldf, int32_t adjoint, double* scale, int32_t* perturbed,

@@ -669,16 +669,44 @@ def _gtrsyl(A, B, C, D, E, F, adjoint, ctx):
     return R, L, float(sc[0]), bool(pert[0])
 
 
-def trsylvester(A, B, C, D, E, F, ctx=None):
-    """trsylvester!(A, B, C, D, E, F) (gsylvester.jl:23-99): solves A R - L B = s C,
-    D R - L E = s F for complex upper triangular A, D (m x m) and B, E (n x n) on the GPU.
-    Returns (R, L, s, perturbed); the inputs are not modified."""
+def _trsyl(A, B, C, adjoint, possign, ctx):
+    ctx = ctx or get_context()
+    cplx = any(np.iscomplexobj(x) for x in (A, B, C))
+    dt = np.complex128 if cplx else np.float64
+    A_, B_ = np.array(A, dtype=dt, order="F"), np.array(B, dtype=dt, order="F")
+    m, n = _checksquare(A_), _checksquare(B_)
+    X = np.array(C, dtype=dt, order="F")
+    if X.ndim == 1:
+        X = X.reshape(-1, 1, order="F")
+    if X.shape != (m, n):
+        raise DimensionMismatch("dimensions of C %s must match A, (%d,%d), and B, (%d,%d)" % (X.shape, m, m, n, n))
+    sc = np.ones(1)
+    pert = np.zeros(1, dtype=np.int32)
+    fn = ctx.lib.gs_trsylvester_c64 if cplx else ctx.lib.gs_trsylvester_f64
+    rc = fn(ctx.handle, m, n, _ptr(A_), max(m, 1), _ptr(B_), max(n, 1), _ptr(X), max(m, 1), int(adjoint),
+            int(bool(possign)), _ptr(sc), _ptr(pert), 0)
+    if rc != GS_OK:
+        _raise(rc, ctx, "adjtrsylvester!" if adjoint else "trsylvester!")
+    return X, float(sc[0]), bool(pert[0])
+
+
+def trsylvester(A, B, C, D=None, E=None, F=None, possign=False, ctx=None):
+    """trsylvester!(A, B, C; possign) (sylvester.jl:11-75): A X - X B = s C (A X + X B with
+    possign) for upper triangular A, B; returns (X, s, perturbed).
+    trsylvester!(A, B, C, D, E, F) (gsylvester.jl:23-99): A R - L B = s C, D R - L E = s F for
+    complex upper triangular A, D (m x m) and B, E (n x n); returns (R, L, s, perturbed).
+    On the GPU; the inputs are not modified."""
+    if D is None and E is None and F is None:
+        return _trsyl(A, B, C, False, possign, ctx)
     return _gtrsyl(A, B, C, D, E, F, False, ctx)
 
 
-def adjtrsylvester(A, B, C, D, E, F, ctx=None):
-    """adjtrsylvester!(A, B, C, D, E, F) (gsylvester.jl:103-155): solves A^H R + D^H L = s C,
-    R B^H + L E^H = -s F.  Returns (R, L, s, perturbed)."""
+def adjtrsylvester(A, B, C, D=None, E=None, F=None, possign=False, ctx=None):
+    """adjtrsylvester!(A, B, C; possign) (sylvester.jl:80-139): A^H X - X B^H = s C;
+    adjtrsylvester!(A, B, C, D, E, F) (gsylvester.jl:103-155): A^H R + D^H L = s C,
+    R B^H + L E^H = -s F."""
+    if D is None and E is None and F is None:
+        return _trsyl(A, B, C, True, possign, ctx)
     return _gtrsyl(A, B, C, D, E, F, True, ctx)
 
 

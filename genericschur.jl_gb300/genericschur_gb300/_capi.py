@@ -79,6 +79,8 @@ SIGNATURES = {
     "gs_ggeigvecs_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _u]),
     "gs_ggordschur_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_ggordschur_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_trsylvester_f64": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i, _i, _p, _p, _u]),
+    "gs_trsylvester_c64": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i, _i, _p, _p, _u]),
     "gs_gtrsylvester_c64": (_i, [_p, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _i, _p,
                                  _p, _u]),
     "gs_geigvalscond_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _i64, _p, _u]),

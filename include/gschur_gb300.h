@@ -248,6 +248,18 @@ GS_API int gs_subspacesep_f64(gs_context* ctx, int64_t n, const double* T, int64
                               unsigned flags);
 GS_API int gs_subspacesep_c64(gs_context* ctx, int64_t n, const double* T, int64_t ldt, int64_t nsub, double* sep,
                               unsigned flags);
+/* trsylvester!(A, B, C; possign) (adjoint = 0) / adjtrsylvester!(A, B, C; possign)
+ * (adjoint = 1) (sylvester.jl:11-139): A X - X B = scale C, resp. A^H X - X B^H = scale C,
+ * with + for the B terms when possign; A (m x m) and B (n x n) upper triangular (only their
+ * upper triangles are read), C (m x n) overwritten with X; *scale the reference's scale
+ * (below one only when the solution would overflow), *perturbed whether a diagonal
+ * difference was raised to smin.  _c64: interleaved complex. */
+GS_API int gs_trsylvester_f64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                              int64_t ldb, double* C, int64_t ldc, int32_t adjoint, int32_t possign, double* scale,
+                              int32_t* perturbed, unsigned flags);
+GS_API int gs_trsylvester_c64(gs_context* ctx, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                              int64_t ldb, double* C, int64_t ldc, int32_t adjoint, int32_t possign, double* scale,
+                              int32_t* perturbed, unsigned flags);
 /* Generalized Sylvester equations of complex upper triangular A, D (m x m) and B, E
  * (n x n), interleaved complex, C and F m x n overwritten with R and L:
  *   adjoint = 0: trsylvester!(A, B, C, D, E, F) (gsylvester.jl:23-99)

@@ -29,10 +29,11 @@ template <class R, class S> R maxabs_block(const S* a, int lda, int rows, int co
 }
 
 // trsylvester! (adj = false): A X - X B = scale C;  adjtrsylvester! (adj = true):
-// A^H X - X B^H = scale C.  A m x m, B p x p upper triangular; C m x p overwritten by X.
+// A^H X - X B^H = scale C; with possign the signs of the B terms are +.  A m x m, B p x p upper triangular; C m x p overwritten by X.
 // Returns scale; *perturbed set when a diagonal difference was replaced by smin.
 template <class R, class S>
-R trsylvester(bool adj, int m, int p, const S* A, int lda, const S* B, int ldb, S* C, int ldc, bool* perturbed) {
+R trsylvester(bool adj, int m, int p, const S* A, int lda, const S* B, int ldb, S* C, int ldc, bool* perturbed,
+              bool possign = false) {
 #define SA(i, j) A[(i) + (long long)(j) * lda]
 #define SB(i, j) B[(i) + (long long)(j) * ldb]
 #define SC(i, j) C[(i) + (long long)(j) * ldc]
@@ -64,7 +65,8 @@ R trsylvester(bool adj, int m, int p, const S* A, int lda, const S* B, int ldb, 
         S suml = s_zero<S>(), sumr = s_zero<S>();
         for (int j = k + 1; j < m; ++j) suml += SA(k, j) * SC(j, l);
         for (int j = 0; j < l; ++j) sumr += SC(k, j) * SB(j, l);
-        step(k, l, SC(k, l) - (suml - sumr), SA(k, k) - SB(l, l));
+        if (possign) step(k, l, SC(k, l) - (suml + sumr), SA(k, k) + SB(l, l));
+        else step(k, l, SC(k, l) - (suml - sumr), SA(k, k) - SB(l, l));
       }
   } else {
     // sylvester.jl:110-136: l descending, k ascending
@@ -73,7 +75,8 @@ R trsylvester(bool adj, int m, int p, const S* A, int lda, const S* B, int ldb, 
         S suml = s_zero<S>(), sumr = s_zero<S>();
         for (int j = 0; j < k; ++j) suml += cj(SA(j, k)) * SC(j, l);
         for (int j = l + 1; j < p; ++j) sumr += cj(SC(k, j)) * SB(l, j);
-        step(k, l, SC(k, l) - (suml - cj(sumr)), cj(SA(k, k) - SB(l, l)));
+        if (possign) step(k, l, SC(k, l) - (suml + cj(sumr)), cj(SA(k, k) + SB(l, l)));
+        else step(k, l, SC(k, l) - (suml - cj(sumr)), cj(SA(k, k) - SB(l, l)));
       }
   }
   if (perturbed) *perturbed = pert;

@@ -191,14 +191,14 @@ int or_balancer_apply_z(int n, int m, double* v, int ldv, int ilo, int ihi, cons
 int or_trsylv_d(int adj, int m, int p, const double* a, int lda, const double* b, int ldb, double* c, int ldc,
                 double* out2) {
   bool pert = false;
-  out2[0] = trsylvester<double, double>(adj != 0, m, p, a, lda, b, ldb, c, ldc, &pert);
+  out2[0] = trsylvester<double, double>((adj & 1) != 0, m, p, a, lda, b, ldb, c, ldc, &pert, (adj & 2) != 0);
   out2[1] = pert ? 1.0 : 0.0;
   return 0;
 }
 int or_trsylv_z(int adj, int m, int p, const double* a, int lda, const double* b, int ldb, double* c, int ldc,
                 double* out2) {
   bool pert = false;
-  out2[0] = trsylvester<double, zc>(adj != 0, m, p, (const zc*)a, lda, (const zc*)b, ldb, (zc*)c, ldc, &pert);
+  out2[0] = trsylvester<double, zc>((adj & 1) != 0, m, p, (const zc*)a, lda, (const zc*)b, ldb, (zc*)c, ldc, &pert, (adj & 2) != 0);
   out2[1] = pert ? 1.0 : 0.0;
   return 0;
 }

@@ -252,16 +252,17 @@ def balancer_apply(V, B, inverse=False):
     return V
 
 
-def trsylvester(A, B, C, adjoint=False):
-    """trsylvester!(A, B, C) (A X - X B = scale C) or adjtrsylvester!(A, B, C)
-    (A^H X - X B^H = scale C), sylvester.jl:11-139.  Returns (X, scale, perturbed)."""
+def trsylvester(A, B, C, adjoint=False, possign=False):
+    """trsylvester!(A, B, C; possign) (A X -+ X B = scale C) or adjtrsylvester!(A, B, C;
+    possign) (A^H X -+ X B^H = scale C), sylvester.jl:11-139.  Returns (X, scale, perturbed)."""
     cplx = np.iscomplexobj(A) or np.iscomplexobj(B) or np.iscomplexobj(C)
     dt = np.complex128 if cplx else np.float64
     A, B, X = _f(A, dt), _f(B, dt), _f(C, dt)
     m, p = X.shape
     out = np.zeros(2)
     fn = lib().or_trsylv_z if cplx else lib().or_trsylv_d
-    fn(int(adjoint), m, p, _ptr(A), max(m, 1), _ptr(B), max(p, 1), _ptr(X), max(m, 1), _ptr(out))
+    fn(int(adjoint) | (2 if possign else 0), m, p, _ptr(A), max(m, 1), _ptr(B), max(p, 1), _ptr(X), max(m, 1),
+       _ptr(out))
     return X, float(out[0]), bool(out[1])
 
 

@@ -139,3 +139,42 @@ def test_eigen_jcv(gs):
         s_o, sep_o = po.condition(ts, 1)
         assert _close(E.rconde[j], s1, 1e-7) and _close(E.rconde[j], s_o, 1e-7)
         assert _close(E.rcondv[j], sep1, 1e-7) and _close(E.rcondv[j], sep_o, 1e-7)
+
+
+@pytest.mark.parametrize("possign", [False, True])
+@pytest.mark.parametrize("adjoint", [False, True])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("m,n", [(5, 7), (33, 65), (100, 40)])
+def test_trsylvester_std(gs, m, n, cplx, adjoint, possign):
+    """trsylvester!(A, B, C; possign) / adjtrsylvester! (sylvester.jl:11-139) through the
+    C-ABI: the oracle's solution (the tiled GPU solve sums in another order) and the
+    residual of the equation."""
+    rng = np.random.default_rng(5200 + m + n + 2 * cplx + 4 * adjoint + 8 * possign)
+    A = np.triu(randn_matrix(rng, m, cplx)) + 3 * np.eye(m)
+    B = np.triu(randn_matrix(rng, n, cplx)) - 3 * np.eye(n)
+    if possign:
+        B = B + 6 * np.eye(n)
+    C = randn_matrix(rng, max(m, n), cplx)[:m, :n]
+    fn = gs.adjtrsylvester if adjoint else gs.trsylvester
+    X, sc, pert = fn(A, B, C, possign=possign)
+    Xo, so, po_ = po.trsylvester(A, B, C, adjoint=adjoint, possign=possign)
+    assert sc == so == 1.0 and pert == po_
+    assert np.abs(X - Xo).max() <= 1e-10 * np.abs(Xo).max()
+    sg = 1.0 if possign else -1.0
+    Ah, Bh = (A.conj().T, B.conj().T) if adjoint else (A, B)
+    res = Ah @ X + sg * X @ Bh - C
+    assert np.abs(res).max() <= 1e-12 * (np.abs(A).max() + np.abs(B).max()) * np.abs(X).max()
+
+
+def test_trsylvester_std_rescale(gs):
+    """A solution past the overflow threshold: the reference's rescaling (scale < 1), in its
+    element order, to the oracle's scale and solution; and a shared eigenvalue perturbed."""
+    A, B, C = np.array([[1e-200]]), np.array([[-1e-200]]), np.array([[1e100]])
+    X, sc, pert = gs.trsylvester(A, B, C)
+    Xo, so, _ = po.trsylvester(A, B, C)
+    assert sc == so and sc < 1.0 and X[0, 0] == Xo[0, 0]
+    A = np.triu(np.ones((3, 3)))
+    B = np.triu(np.ones((2, 2)))
+    X, sc, pert = gs.trsylvester(A, B, np.ones((3, 2)))
+    _, _, po_ = po.trsylvester(A, B, np.ones((3, 2)))
+    assert pert and po_
