@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--gemm-only", action="store_true",
                     help="only the FP64 product on the BF16 tensor cores vs cuBLAS DGEMM; prints its JSON object")
     ap.add_argument("--gemm-n", type=int, default=4096)
+    ap.add_argument("--dc-only", action="store_true",
+                    help="only the divide-and-conquer tridiagonal eigensolver (n = --dc-n); prints its JSON object")
+    ap.add_argument("--dc-n", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -304,10 +307,12 @@ def run_ours(args):
     secondary = measure_complex_and_adjoint(ctx, torch, dev, stream)
     large = None
     gemm_tc = None
+    stedc = None
     if not args.no_large:
         ctx.set_stream(None)
         large = measure_large(ctx, torch, dev, args.large_n)
         gemm_tc = measure_gemm_tc(ctx, torch, dev, args.large_n)
+        stedc = measure_stedc(ctx, args.dc_n)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -316,7 +321,7 @@ def run_ours(args):
                             "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
            "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
-           "large": large, "gemm_f64_tc": gemm_tc, **secondary}
+           "large": large, "gemm_f64_tc": gemm_tc, "stedc": stedc, **secondary}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -544,6 +549,40 @@ def measure_gemm_tc(ctx, torch, dev, n, reps=5):
             "rel_err_vs_dgemm": err}
 
 
+def measure_stedc(ctx, n, reps=3):
+    """_gschur!(SymTridiagonal(d, e), DivideAndConquer(), Z = I) through the C-ABI on a
+    seeded random tridiagonal of order n (N(0,1) diagonal and off-diagonal): device time of
+    the call (its events bracket the whole tree, host-side index work included), the
+    eigenvalue error against LAPACK's tridiagonal solver and the orthogonality of Z."""
+    import scipy.linalg
+    import genericschur_gb300 as gs
+    rng = np.random.default_rng(21)
+    D, E = rng.standard_normal(n), rng.standard_normal(n - 1)
+    times = []
+    for _ in range(reps + 1):
+        d, _, Z = gs.gschur_symtridiag(gs.SymTridiagonal(D.copy(), E.copy()), np.eye(n), alg="DivideAndConquer",
+                                       ctx=ctx)
+        times.append(ctx.last_kernel_ms())
+    times = times[1:]
+    ref = scipy.linalg.eigh_tridiagonal(D, E, eigvals_only=True)
+    nT = max(np.abs(D).max(), np.abs(E).max()) * 3
+    eps = np.finfo(float).eps
+    ev_err = float(np.abs(np.sort(d) - ref).max() / (n * eps * nT))
+    orth = float(np.abs(Z.T @ Z - np.eye(n)).max() / (n * eps))
+    return {"n": n, "seed": 21, "entries": "d, e iid N(0,1)", "ms_min": float(min(times)),
+            "ms_median": float(np.median(times)), "eigenvalue_err_n_eps_T": ev_err, "orth_err_n_eps": orth}
+
+
+def run_dc_only(args):
+    import torch
+    import build_lib
+    torch.cuda.set_device(0)
+    build_lib.build()
+    import genericschur_gb300 as gs
+    ctx = gs.Context(0)
+    print(json.dumps(measure_stedc(ctx, args.dc_n)))
+
+
 def run_gemm_only(args):
     import torch
     import build_lib
@@ -573,6 +612,9 @@ def main():
         return
     if args.gemm_only:
         run_gemm_only(args)
+        return
+    if args.dc_only:
+        run_dc_only(args)
         return
     if args.impl == "reference":
         run_reference(args)

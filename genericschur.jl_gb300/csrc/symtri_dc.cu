@@ -11,10 +11,13 @@
 //     level's merges at once:
 //       k_dc_prep     z (last row of Q1, first row of Q2), lambda = d[indexq], the tolerance
 //       k_dc_rank     sortperm of lambda (stable, by counting ranks)
-//       k_dc_deflate  _dcdeflate! (221-425): one CTA per merge; thread 0 runs the reference's
-//                     scan (small z, close pairs, the sorted insertion of deflated entries)
-//                     and records the Givens rotations, which the CTA then applies to Q row
-//                     by row; the gathers of Q2 by column type
+//       k_dc_deflate  _dcdeflate! (221-425): one CTA per merge; the small-z and close-pair
+//                     tests evaluated for all positions in parallel, then thread 0 walks the
+//                     reference's scan (re-testing a pair only after a rotation) and records
+//                     the Givens rotations, which the CTA applies to Q row by row; the
+//                     column-type counts and partition by ballot scans
+//       k_dc_gather / k_dc_place  the gathers of Q2 by column type and the deflated columns
+//                     to the end, one warp per column over all the level's merges
 //       k_dc_secular  the roots of the secular equation, one thread per root (_dcroot!,
 //                     777-927, with _dcroot2!, _dcnewton and the i = n / i < n helpers)
 //       k_dc_lowner / k_dc_vecs   the eigenvectors of the rank-one problem (_dcsecular!,
@@ -550,10 +553,11 @@ __global__ void __launch_bounds__(kDcT) k_dc_deflate(const DcMerge* __restrict__
                                                      double* Q, long long ld, int* indexqg, double* zg,
                                                      double* lamg, double* wg, int* indexcg, int* indexg,
                                                      int* indexpg, int* coltypeg, int* rpg, int* rng_,
-                                                     double* rcg, double* rsg, double* Q2) {
+                                                     double* rcg, double* rsg, double* Q2, int* sfg, int* sprevg,
+                                                     double* scg, double* ssg, double* stg) {
   __shared__ int sh[8];
   const DcMerge M = mg[blockIdx.x];
-  const int o = M.off, n = M.n, n1 = M.n1, n2 = n - n1, tid = threadIdx.x;
+  const int o = M.off, n = M.n, n1 = M.n1, tid = threadIdx.x;
   double* Qb = Q + o + (size_t)o * ld;
   double* d = dg + o;
   double* z = zg + o;
@@ -568,7 +572,12 @@ __global__ void __launch_bounds__(kDcT) k_dc_deflate(const DcMerge* __restrict__
   int* rn = rng_ + o;
   double* rc = rcg + o;
   double* rs = rsg + o;
-  double* W2 = Q2 + M.qoff;
+  int* sf = sfg + o;        // per sorted position: bit 0 small z, bit 1 close pair with the previous candidate
+  int* sprev = sprevg + o;  // inclusive max-scan of the positions whose z is not small
+  double* sc = scg + o;     // the close-pair test's c, s, tau on the unrotated values
+  double* ss = ssg + o;
+  double* st = stg + o;
+  (void)Q2;
   DcInfo I = info[blockIdx.x];
   for (int j = tid; j < n; j += kDcT) {
     index[j] = clamp1(indexq[clamp1(indexc[j], n) - 1], n);
@@ -578,17 +587,9 @@ __global__ void __launch_bounds__(kDcT) k_dc_deflate(const DcMerge* __restrict__
   }
   __syncthreads();
   if (I.trivial) {
-    // reorganize Q so that its columns follow the sorted d (233-243)
-    for (size_t x = tid; x < (size_t)n * n; x += kDcT) {
-      const int r = (int)(x % n), j = (int)(x / n);
-      W2[x] = Qb[r + (size_t)(clamp1(index[j], n) - 1) * ld];
-    }
+    // d follows its sorted order; k_dc_gather / k_dc_place reorganize Q's columns (233-243)
     for (int j = tid; j < n; j += kDcT) lam[j] = d[clamp1(index[j], n) - 1];
     __syncthreads();
-    for (size_t x = tid; x < (size_t)n * n; x += kDcT) {
-      const int r = (int)(x % n), j = (int)(x / n);
-      Qb[r + (size_t)j * ld] = W2[x];
-    }
     for (int j = tid; j < n; j += kDcT) {
       d[j] = lam[j];
       indexq[j] = j + 1;
@@ -600,117 +601,225 @@ __global__ void __launch_bounds__(kDcT) k_dc_deflate(const DcMerge* __restrict__
     }
     return;
   }
+  // The reference's scan (244-367) decides, in sorted order, whether each z is small and
+  // whether each remaining candidate forms a close pair with the previous one.  Only the
+  // rotations of close pairs change z and d (of those two columns), so the tests can be
+  // evaluated first for every position in parallel on the values before any rotation; the
+  // sequential walk (thread 0) then re-evaluates a pair only right after a rotation, with
+  // the same expressions in the same order.
+  const double rho = I.rho, tol = I.tol;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = tid & 31, wid = tid >> 5;
+  __shared__ int s_red[kDcT / 32];
+  __shared__ int s_carry;
+  // pass 1: small-z flags and the inclusive max-scan of the positions whose z is not small
+  if (tid == 0) s_carry = -1;
+  __syncthreads();
+  for (int t0 = 0; t0 < n; t0 += kDcT) {
+    const int j = t0 + tid;
+    int v = -1;
+    if (j < n) {
+      const bool sm = rho * fabs(z[clamp1(index[j], n) - 1]) <= tol;
+      sf[j] = sm ? 1 : 0;
+      v = sm ? -1 : j;
+    }
+    int x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(FULL, x, off);
+      if (lane >= off) x = max(x, y);
+    }
+    if (lane == 31) s_red[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int wv = lane < kDcT / 32 ? s_red[lane] : -1;
+      for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(FULL, wv, off);
+        if (lane >= off) wv = max(wv, y);
+      }
+      if (lane < kDcT / 32) s_red[lane] = wv;
+    }
+    __syncthreads();
+    const int incl = max(max(x, wid > 0 ? s_red[wid - 1] : -1), s_carry);
+    if (j < n) sprev[j] = incl;
+    __syncthreads();
+    if (tid == kDcT - 1) s_carry = incl;
+    __syncthreads();
+  }
+  // pass 2: the close-pair test of (previous candidate, j) on the unrotated values
+  for (int j = tid; j < n; j += kDcT) {
+    if (sf[j] & 1) continue;
+    const int p = j > 0 ? sprev[j - 1] : -1;
+    if (p < 0) continue;
+    const int nj = clamp1(index[j], n), pjv = clamp1(index[p], n);
+    double sv = z[pjv - 1], c = z[nj - 1];
+    const double tau = hypot(c, sv);
+    const double t = d[nj - 1] - d[pjv - 1];
+    c /= tau;
+    sv = -sv / tau;
+    sc[j] = c;
+    ss[j] = sv;
+    st[j] = tau;
+    if (fabs(t * c * sv) <= tol) sf[j] |= 2;
+  }
+  __syncthreads();
+  // pass 3: the reference's walk
   if (tid == 0) {
-    // 1-based views
-    double* D = d - 1;
+    double* D = d - 1;  // 1-based views
     double* Z = z - 1;
     double* L = lam - 1;
     double* Wv = w - 1;
     int* IX = index - 1;
     int* IP = indexp - 1;
     int* CT = coltype - 1;
-    const double rho = I.rho, tol = I.tol;
-    int k = 0, k2 = n + 1, jj = 0, pj = 0, nrot = 0;
-    bool bdone = false;
-    for (int j = 1; j <= n; ++j) {
-      jj = j;
-      const int nj = IX[j];
-      if (rho * fabs(Z[nj]) <= tol) {
+    int k = 0, k2 = n + 1, jj = 1, pj = 0, nrot = 0;
+    for (; jj <= n; ++jj) {
+      const int nj = clamp1(IX[jj], n);
+      if (sf[jj - 1] & 1) {
         k2 -= 1;
         CT[nj] = 4;
         IP[k2] = nj;
-        if (j == n) { bdone = true; break; }
       } else {
         pj = nj;
         break;
       }
     }
-    if (!bdone) {
-      while (jj < n) {
-        jj += 1;
-        const int nj = IX[jj];
-        if (rho * fabs(Z[nj]) <= tol) {
-          k2 -= 1;
-          CT[nj] = 4;
-          IP[k2] = nj;
+    bool rotated = false;
+    for (jj = jj + 1; jj <= n; ++jj) {
+      const int nj = clamp1(IX[jj], n);
+      const int f = sf[jj - 1];
+      if (f & 1) {
+        k2 -= 1;
+        CT[nj] = 4;
+        IP[k2] = nj;
+        continue;
+      }
+      double c, sv, tau;
+      bool close;
+      if (!rotated) {
+        c = sc[jj - 1];
+        sv = ss[jj - 1];
+        tau = st[jj - 1];
+        close = (f & 2) != 0;
+      } else {
+        sv = Z[pj];
+        c = Z[nj];
+        tau = hypot(c, sv);
+        const double t = D[nj] - D[pj];
+        c /= tau;
+        sv = -sv / tau;
+        close = fabs(t * c * sv) <= tol;
+      }
+      if (close) {
+        Z[nj] = tau;
+        Z[pj] = 0.0;
+        if (CT[nj] != CT[pj]) CT[nj] = 2;
+        CT[pj] = 4;
+        rp[nrot] = pj;
+        rn[nrot] = nj;
+        rc[nrot] = c;
+        rs[nrot] = sv;
+        ++nrot;
+        const double t = D[pj] * (c * c) + D[nj] * (sv * sv);
+        D[nj] = D[pj] * (sv * sv) + D[nj] * (c * c);
+        D[pj] = t;
+        k2 -= 1;
+        int i = 1;
+        if (k2 + i > n) {
+          IP[k2 + i - 1] = pj;
         } else {
-          double s = Z[pj], c = Z[nj];
-          const double tau = hypot(c, s);
-          double t = D[nj] - D[pj];
-          c /= tau;
-          s = -s / tau;
-          if (fabs(t * c * s) <= tol) {
-            Z[nj] = tau;
-            Z[pj] = 0.0;
-            if (CT[nj] != CT[pj]) CT[nj] = 2;
-            CT[pj] = 4;
-            rp[nrot] = pj;
-            rn[nrot] = nj;
-            rc[nrot] = c;
-            rs[nrot] = s;
-            ++nrot;
-            t = D[pj] * (c * c) + D[nj] * (s * s);
-            D[nj] = D[pj] * (s * s) + D[nj] * (c * c);
-            D[pj] = t;
-            k2 -= 1;
-            int i = 1;
-            if (k2 + i > n) {
-              IP[k2 + i - 1] = pj;
+          while (k2 + i <= n) {
+            if (D[pj] < D[clamp1(IP[k2 + i], n)]) {
+              IP[k2 + i - 1] = IP[k2 + i];
+              IP[k2 + i] = pj;
+              i += 1;
             } else {
-              while (k2 + i <= n) {
-                if (D[pj] < D[clamp1(IP[k2 + i], n)]) {
-                  IP[k2 + i - 1] = IP[k2 + i];
-                  IP[k2 + i] = pj;
-                  i += 1;
-                } else {
-                  IP[k2 + i - 1] = pj;
-                  break;
-                }
-              }
+              IP[k2 + i - 1] = pj;
+              break;
             }
-            pj = nj;
-          } else {
-            k += 1;
-            L[k] = D[pj];
-            Wv[k] = Z[pj];
-            IP[k] = pj;
-            pj = nj;
           }
         }
+        pj = nj;
+        rotated = true;
+      } else {
+        k += 1;
+        L[k] = D[pj];
+        Wv[k] = Z[pj];
+        IP[k] = pj;
+        pj = nj;
+        rotated = false;
       }
     }
+    if (pj < 1) pj = 1;  // every z small: the trivial branch above takes that case (NaN input aside)
     k += 1;
     L[k] = D[pj];
     Wv[k] = Z[pj];
     IP[k] = pj;
-    int cc[5] = {0, 0, 0, 0, 0};
-    for (int j = 1; j <= n; ++j) {
-      const int ct = CT[j];
-      cc[(ct >= 1 && ct <= 4) ? ct : 4] += 1;
-    }
-    int psm[5] = {0, 1, 1 + cc[1], 1 + cc[1] + cc[2], 1 + cc[1] + cc[2] + cc[3]};
-    int* IC = indexc - 1;
-    for (int j = 1; j <= n; ++j) {
-      const int js = clamp1(IP[j], n);
-      int ct = CT[js];
-      if (ct < 1 || ct > 4) ct = 4;
-      if (psm[ct] <= n) {
-        IX[psm[ct]] = js;
-        IC[psm[ct]] = j;
-      }
-      psm[ct] += 1;
-    }
-    I.k = n - cc[4];
-    I.c1 = cc[1];
-    I.c2 = cc[2];
-    I.c3 = cc[3];
-    I.c4 = cc[4];
-    I.nrot = nrot;
-    info[blockIdx.x] = I;
-    sh[0] = I.k; sh[1] = cc[1]; sh[2] = cc[2]; sh[3] = cc[3]; sh[4] = cc[4]; sh[5] = nrot;
+    sh[5] = nrot;
   }
   __syncthreads();
-  const int k = sh[0], c1 = sh[1], c2 = sh[2], c3 = sh[3], c4 = sh[4], nrot = sh[5];
+  // pass 4: the column-type counts and the stable partition of the positions by type
+  // (_dcdeflate! 372-382), four ballot scans per tile
+  __shared__ int s_cnt[4], s_wt[4][kDcT / 32], s_base[4];
+  if (tid < 4) s_cnt[tid] = 0;
+  __syncthreads();
+  for (int j = tid; j < n; j += kDcT) {
+    int ct = coltype[j];
+    if (ct < 1 || ct > 4) ct = 4;
+    atomicAdd(&s_cnt[ct - 1], 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    s_base[0] = 1;
+    s_base[1] = 1 + s_cnt[0];
+    s_base[2] = 1 + s_cnt[0] + s_cnt[1];
+    s_base[3] = 1 + s_cnt[0] + s_cnt[1] + s_cnt[2];
+  }
+  __syncthreads();
+  for (int t0 = 0; t0 < n; t0 += kDcT) {
+    const int j = t0 + tid;  // 0-based position in indexp order
+    int js = 1, ct = 0;
+    if (j < n) {
+      js = clamp1(indexp[j], n);
+      ct = coltype[js - 1];
+      if (ct < 1 || ct > 4) ct = 4;
+    }
+    unsigned mask[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) mask[t] = __ballot_sync(FULL, ct == t + 1);
+    if (lane == 0)
+#pragma unroll
+      for (int t = 0; t < 4; ++t) s_wt[t][wid] = __popc(mask[t]);
+    __syncthreads();
+    if (j < n) {
+      const int t = ct - 1;
+      int before = 0;
+      for (int q = 0; q < wid; ++q) before += s_wt[t][q];
+      const int pos = s_base[t] + before + __popc(mask[t] & ((1u << lane) - 1u));
+      if (pos <= n) {
+        index[pos - 1] = js;
+        indexc[pos - 1] = j + 1;
+      }
+    }
+    __syncthreads();
+    if (tid < 4) {
+      int tot = 0;
+      for (int q = 0; q < kDcT / 32; ++q) tot += s_wt[tid][q];
+      s_base[tid] += tot;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    I.c1 = s_cnt[0];
+    I.c2 = s_cnt[1];
+    I.c3 = s_cnt[2];
+    I.c4 = s_cnt[3];
+    I.k = n - I.c4;
+    I.nrot = sh[5];
+    info[blockIdx.x] = I;
+    sh[0] = I.k; sh[1] = I.c1; sh[2] = I.c2; sh[3] = I.c3; sh[4] = I.c4;
+  }
+  __syncthreads();
+  const int k = sh[0], nrot = sh[5];
   // rmul!(Q, Givens(pj, nj, c, s)') for the recorded rotations, in order, row by row
   if (nrot > 0)
     for (int r = tid; r < n; r += kDcT)
@@ -722,33 +831,71 @@ __global__ void __launch_bounds__(kDcT) k_dc_deflate(const DcMerge* __restrict__
         *b = -a1 * s + a2 * c;
       }
   __syncthreads();
+  if (k == 0)
+    for (int j = tid; j < n; j += kDcT) indexq[j] = j + 1;
+}
+
+// The gathers of _dcdeflate! (393-421): the merge's columns of Q in column-type order into
+// [Q2_1 Q2_2] (rows 1:n1 of types 1, 2), [Q2_3 Q2_4] (rows n1+1:n of types 2, 3) and Q2_5 (all
+// rows of the deflated type 4), and z <- d in that order; for a trivial merge (every z
+// negligible) the columns in sorted order into the scratch.  One warp per column, lanes
+// over rows, all merges of the level at once.
+constexpr int kDcGW = 8;  // warps (columns) per CTA of the gather / place kernels
+__global__ void __launch_bounds__(32 * kDcGW) k_dc_gather(const DcMerge* __restrict__ mg,
+                                                          const DcInfo* __restrict__ info, const double* __restrict__ dg,
+                                                          const double* __restrict__ Q, long long ld,
+                                                          const int* __restrict__ indexg, double* zg, double* Q2) {
+  const DcMerge M = mg[blockIdx.x];
+  const DcInfo I = info[blockIdx.x];
+  const int n = M.n, n1 = M.n1, n2 = n - n1, lane = threadIdx.x & 31;
+  const int i = blockIdx.y * kDcGW + (threadIdx.x >> 5);
+  if (i >= n) return;
+  const double* Qb = Q + M.off + (size_t)M.off * ld;
+  double* W2 = Q2 + M.qoff;
+  const int js = clamp1(indexg[M.off + i], n) - 1;
+  const double* src = Qb + (size_t)js * ld;
+  if (I.trivial) {
+    for (int r = lane; r < n; r += 32) W2[r + (size_t)i * n] = src[r];
+    return;
+  }
+  const int c1 = I.c1, c2 = I.c2, c3 = I.c3, k = I.k;
   double* Q12 = W2;
   double* Q34 = W2 + (size_t)n1 * n1;
   double* Q5 = Q34 + (size_t)n2 * n2;
-  for (size_t x = tid; x < (size_t)n * n; x += kDcT) {
-    const int r = (int)(x % n), i = (int)(x / n);  // row r of column i (0-based, type order)
-    const int js = clamp1(index[i], n) - 1;
-    const double v = Qb[r + (size_t)js * ld];
-    if (i < c1 + c2) {
-      if (r < n1) Q12[r + (size_t)i * n1] = v;
-      else if (i >= c1) Q34[(r - n1) + (size_t)(i - c1) * n2] = v;
-    } else if (i < c1 + c2 + c3) {
-      if (r >= n1) Q34[(r - n1) + (size_t)(i - c1) * n2] = v;
-    } else {
-      Q5[r + (size_t)(i - k) * n] = v;
-    }
+  if (i < c1 + c2) {
+    for (int r = lane; r < n1; r += 32) Q12[r + (size_t)i * n1] = src[r];
+    if (i >= c1)
+      for (int r = lane; r < n2; r += 32) Q34[r + (size_t)(i - c1) * n2] = src[n1 + r];
+  } else if (i < c1 + c2 + c3) {
+    for (int r = lane; r < n2; r += 32) Q34[r + (size_t)(i - c1) * n2] = src[n1 + r];
+  } else {
+    for (int r = lane; r < n; r += 32) Q5[r + (size_t)(i - k) * n] = src[r];
   }
-  for (int i = tid; i < n; i += kDcT) z[i] = d[clamp1(index[i], n) - 1];
-  __syncthreads();
-  if (k < n) {
-    for (size_t x = tid; x < (size_t)n * c4; x += kDcT) {
-      const int r = (int)(x % n), j = (int)(x / n);
-      Qb[r + (size_t)(k + j) * ld] = Q5[x];
-    }
-    for (int j = tid; j < c4; j += kDcT) d[k + j] = z[k + j];
+  if (lane == 0) zg[M.off + i] = dg[M.off + js];
+}
+
+// The deflated columns and values to the end of the merge's block (_dcdeflate! 415-421);
+// for a trivial merge the sorted columns back into Q.
+__global__ void __launch_bounds__(32 * kDcGW) k_dc_place(const DcMerge* __restrict__ mg,
+                                                         const DcInfo* __restrict__ info, double* dg, double* Q,
+                                                         long long ld, const double* __restrict__ zg,
+                                                         const double* __restrict__ Q2) {
+  const DcMerge M = mg[blockIdx.x];
+  const DcInfo I = info[blockIdx.x];
+  const int n = M.n, n1 = M.n1, n2 = n - n1, lane = threadIdx.x & 31;
+  const int j = blockIdx.y * kDcGW + (threadIdx.x >> 5);
+  double* Qb = Q + M.off + (size_t)M.off * ld;
+  const double* W2 = Q2 + M.qoff;
+  if (I.trivial) {
+    if (j >= n) return;
+    for (int r = lane; r < n; r += 32) Qb[r + (size_t)j * ld] = W2[r + (size_t)j * n];
+    return;
   }
-  if (k == 0)
-    for (int j = tid; j < n; j += kDcT) indexq[j] = j + 1;
+  const int k = I.k;
+  if (k >= n || j >= I.c4) return;
+  const double* Q5 = W2 + (size_t)n1 * n1 + (size_t)n2 * n2;
+  for (int r = lane; r < n; r += 32) Qb[r + (size_t)(k + j) * ld] = Q5[r + (size_t)j * n];
+  if (lane == 0) dg[M.off + k + j] = zg[M.off + k + j];
 }
 
 // the secular equation's roots: d[j] and delta in column j of the merge's block of Q
@@ -871,8 +1018,8 @@ __global__ void k_dc_or_err(int* status, const int* err) {
 
 // ---- workspace ------------------------------------------------------------------------------
 struct DcWs {
-  double *Qc, *Zt, *Q2, *S, *z, *lam, *w, *w2, *rc, *rs, *orgnrm;
-  int *indexq, *indexc, *index, *indexp, *coltype, *rp, *rn, *brk, *ioff, *imsz, *cuts, *status;
+  double *Qc, *Zt, *Q2, *S, *z, *lam, *w, *w2, *rc, *rs, *orgnrm, *sc, *ss, *st;
+  int *indexq, *indexc, *index, *indexp, *coltype, *rp, *rn, *brk, *ioff, *imsz, *cuts, *status, *sf, *sprev;
   DcMerge* mg;
   DcInfo* info;
   char* gemm;
@@ -900,6 +1047,11 @@ DcWs dc_ws(int n, int zcplx, char* base) {
   W.rc = (double*)take(n * D);
   W.rs = (double*)take(n * D);
   W.orgnrm = (double*)take(D);
+  W.sc = (double*)take(n * D);
+  W.ss = (double*)take(n * D);
+  W.st = (double*)take(n * D);
+  W.sf = (int*)take(n * I);
+  W.sprev = (int*)take(n * I);
   W.indexq = (int*)take(n * I);
   W.indexc = (int*)take(n * I);
   W.index = (int*)take(n * I);
@@ -1014,7 +1166,11 @@ cudaError_t dc_core(int m, double* d, double* e, const DcWs& W, int num_sms, cud
     k_dc_rank<<<gr, 256, 0, s>>>(W.mg, W.info, W.lam, W.indexc, 0);
     DC_CK(cudaGetLastError());
     k_dc_deflate<<<nm, kDcT, 0, s>>>(W.mg, W.info, d, W.Qc, m, W.indexq, W.z, W.lam, W.w, W.indexc, W.index, W.indexp,
-                                     W.coltype, W.rp, W.rn, W.rc, W.rs, W.Q2);
+                                     W.coltype, W.rp, W.rn, W.rc, W.rs, W.Q2, W.sf, W.sprev, W.sc, W.ss, W.st);
+    DC_CK(cudaGetLastError());
+    const dim3 gg(nm, (nmax + kDcGW - 1) / kDcGW);
+    k_dc_gather<<<gg, 32 * kDcGW, 0, s>>>(W.mg, W.info, d, W.Qc, m, W.index, W.z, W.Q2);
+    k_dc_place<<<gg, 32 * kDcGW, 0, s>>>(W.mg, W.info, d, W.Qc, m, W.z, W.Q2);
     DC_CK(cudaGetLastError());
     info.resize(nm);
     DC_CK(cudaMemcpyAsync(info.data(), W.info, sizeof(DcInfo) * nm, cudaMemcpyDeviceToHost, s));
