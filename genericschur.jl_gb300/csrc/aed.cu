@@ -290,7 +290,7 @@ __device__ bool swap_blocks(const AedCtx<T>& a, int j1, int n1, int n2) {
   }
   __syncthreads();
   const int ok = sh.ok, kind = sh.kind;
-  __syncthreads();  // everyone has read the verdict before thread 0 may write the next one
+  __syncthreads();  // everyone has read the decision before thread 0 may write the next one
   if (!ok) return false;
   if (kind == 12) {
     refl_left(a, sh.u1, sh.tau1, j1, j1, nw);

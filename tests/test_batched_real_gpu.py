@@ -1,6 +1,6 @@
 """GPU parity tests of the real FP64 Schur kernels against the CPU oracle.
 
-Criteria (spec parity bar, restating the reference's schurtest checks):
+Criteria (the parity bar, restating the reference's schurtest checks):
 T upper quasi-triangular with standard-form 2x2 blocks (test/real.jl:3-33),
 ||A - Z T Z^T||_F / ||A||_F <= 10 n eps, ||Z^T Z - I||_F <= 10 n eps, eigenvalues
 consistent with T (test/testfuncs.jl:57-86) and matched to the oracle's within

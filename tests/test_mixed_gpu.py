@@ -1,5 +1,5 @@
 """GPU tests of the mixed-precision form: FP32 Schur + FP64 Newton refinement.
-Same acceptance as the FP64 path (spec: equal backward error <= 10 n eps_64):
+Same acceptance as the FP64 path (equal backward error <= 10 n eps_64):
 standard-form quasi-triangular T, ||A - Z T Z^T||_F/||A||_F <= 10 n eps,
 ||Z^T Z - I||_F <= 10 n eps, eigenvalues matched to the oracle's."""
 import numpy as np
