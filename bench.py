@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--dc-only", action="store_true",
                     help="only the divide-and-conquer tridiagonal eigensolver (n = --dc-n); prints its JSON object")
     ap.add_argument("--dc-n", type=int, default=4096)
+    ap.add_argument("--gcond-only", action="store_true",
+                    help="only the generalized condition estimates of a complex triangular pair (n = --gcond-n, "
+                         "split in half); prints its JSON object")
+    ap.add_argument("--gcond-n", type=int, default=1200)
     return ap.parse_args()
 
 
@@ -573,6 +577,36 @@ def measure_stedc(ctx, n, reps=3):
             "ms_median": float(np.median(times)), "eigenvalue_err_n_eps_T": ev_err, "orth_err_n_eps": orth}
 
 
+def measure_gcond(ctx, n, reps=3):
+    """eigvalscond / subspacesep of a seeded random complex triangular pair (S, T), n x n,
+    split in half (the generalized Sylvester wavefront of gcondition.cu): device times."""
+    import genericschur_gb300 as gs
+    rng = np.random.default_rng(7600)
+    cn = lambda: (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2)
+    S = np.triu(cn(), 1) / np.sqrt(n) + np.diag(cn()[0])
+    T = np.triu(cn(), 1) / np.sqrt(n) + np.diag(1 + 0.5 * rng.random(n))
+    G = gs.GeneralizedSchur(S, T, np.diag(S), np.diag(T), np.eye(n), np.eye(n))
+    k = n // 2
+    te, ts = [], []
+    for _ in range(reps + 1):
+        pl, pr = gs.eigvalscond(G, k, ctx=ctx)
+        te.append(ctx.last_kernel_ms())
+        sep = gs.subspacesep(G, k, ctx=ctx)
+        ts.append(ctx.last_kernel_ms())
+    return {"n": n, "nsub": k, "eigvalscond_ms": float(min(te[1:])), "subspacesep_ms": float(min(ts[1:])),
+            "pl": float(pl), "pr": float(pr), "sep": [float(x) for x in sep]}
+
+
+def run_gcond_only(args):
+    import torch
+    import build_lib
+    torch.cuda.set_device(0)
+    build_lib.build()
+    import genericschur_gb300 as gs
+    ctx = gs.Context(0)
+    print(json.dumps(measure_gcond(ctx, args.gcond_n)))
+
+
 def run_dc_only(args):
     import torch
     import build_lib
@@ -615,6 +649,9 @@ def main():
         return
     if args.dc_only:
         run_dc_only(args)
+        return
+    if args.gcond_only:
+        run_gcond_only(args)
         return
     if args.impl == "reference":
         run_reference(args)
