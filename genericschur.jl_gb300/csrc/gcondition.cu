@@ -17,11 +17,12 @@
 // Each element pulls the updates the reference pushes into it, in the reference's order:
 // forward: the L terms l = 0 .. j-1, then the R terms k = m-1 .. i+1; adjoint: C from the
 // rows above in ascending order, F from the columns to the right in descending order.
-// FP64 instructions are the bound on this part (an SM sub-partition issues one FP64 warp
-// instruction in tens of cycles), so an element is a warp: the lanes form the complex
-// products of 32 terms at once and four lanes add them to the four real components of the
-// sums, one FP64 add per term on the serial path instead of sixteen FP64 operations.  The
-// elements of a level go to the CTAs' first warps before any SM takes a second one.
+// An SM sub-partition issues one FP64 warp instruction in tens of cycles, so an element is
+// a warp: the lanes form the complex products of 32 terms at once and four lanes add them
+// to the four real components of the sums, one FP64 add per term on the serial path instead
+// of sixteen FP64 operations.  What remains is the dependency structure: one level after
+// another, each as long as its longest element's serial sum.  The elements of a level go to
+// the CTAs' first warps before any SM takes a second one.
 // Products and sums are plain IEEE operations (no contraction) with the reference's
 // complex formulas, so the result is the reference's to the bit on the same inputs, apart
 // from hypot in the pivot tests.
