@@ -67,3 +67,35 @@ def test_pack_unpack_roundtrip():
     for a, b in zip(mats, back):
         np.testing.assert_array_equal(a, b)
     assert list(woffs) == [0, 1, 4, 12, 12]
+
+
+def test_algorithm_selection():
+    """geigen!/geigvals!/_gschur! take QRIteration() (the default) or DivideAndConquer()
+    (GenericSchur.jl:119-161); RobustRepresentations falls back to QRIteration with a warning
+    (symtridiag.jl:12-26) and any other algorithm raises ArgumentError (symtridiag.jl:61-67)."""
+    import warnings
+    import genericschur_gb300 as gs
+    assert gs._alg(None) == "QR" and gs._alg("QRIteration") == "QR"
+    assert gs._alg("DivideAndConquer") == "DC"
+
+    class DivideAndConquer:
+        pass
+
+    assert gs._alg(DivideAndConquer()) == "DC"
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        assert gs._alg("RobustRepresentations") == "QR"
+        assert any("falling back to QRIteration" in str(x.message) for x in w)
+    with pytest.raises(gs.ArgumentError):
+        gs._alg("Jacobi")
+
+
+def test_generalized_sylvester_shape_checks():
+    """trsylvester!(A, B, C, D, E, F) checks its dimensions before any GPU work
+    (gsylvester.jl:29-47)."""
+    import genericschur_gb300 as gs
+    with pytest.raises(gs.DimensionMismatch):
+        gs.trsylvester(np.eye(3), np.eye(2), np.zeros((3, 2)), np.eye(2), np.eye(2), np.zeros((3, 2)),
+                       ctx=object())
+    with pytest.raises(gs.DimensionMismatch):
+        gs.trsylvester(np.eye(3), np.eye(2), np.zeros((2, 2)), ctx=object())
