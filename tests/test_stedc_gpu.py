@@ -66,7 +66,7 @@ def test_stedc_matches_oracle(gs, n):
 
 
 @pytest.mark.parametrize("cplx", [False, True])
-@pytest.mark.parametrize("n", [40, 300, 1000])
+@pytest.mark.parametrize("n", [1, 7, 25, 26, 40, 300, 1000])
 def test_geigen_hermitian_dc(gs, n, cplx):
     rng = np.random.default_rng(3300 + n + cplx)
     A = rng.standard_normal((n, n)) + (1j * rng.standard_normal((n, n)) if cplx else 0)
