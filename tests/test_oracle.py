@@ -372,3 +372,22 @@ def test_oracle_ggordschur_real_checkord(seed):
         S2, T2, a, b, Q2, Z2, st = po.ggordschur_real(S, T, Q, Z, sel)
         assert st == 0
         check_gordschur_real(A, B, al / be, sel, S2, T2, a, b, Q2, Z2)
+
+
+def test_oracle_gsubspacesep_onenorm_vs_tgsen():
+    """subspacesep(.; pnorm = 1) restated with the solves applied in place: its Difu equals
+    LAPACK ztgsen's one-norm estimate (ijob = 5) on these pencils, where both estimators reach
+    the exact 1 / |Zu^-1|_1 (Difl differs: the estimators take different steps there)."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    rng = np.random.default_rng(5)
+    for n, k in ((8, 3), (16, 1), (20, 10), (30, 29), (24, 5)):
+        A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        B = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        S, T, al, be, Q, Z, st = po.ggschur(A, B)
+        assert st == 0
+        sel = np.zeros(n, np.int32)
+        sel[:k] = 1
+        r = lapack.ztgsen(sel, S, T, Q, Z, ijob=5, lwork=2 * n * n + 4, liwork=2 * n * n + 8)
+        assert r[-1] == 0
+        sep = po.gsubspacesep1(S, T, k)
+        assert abs(sep[0] - r[9][0]) <= 1e-10 * r[9][0]
