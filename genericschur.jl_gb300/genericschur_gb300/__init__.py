@@ -240,16 +240,20 @@ def _eigsortby(w):
 
 def eigvals(A, B=None, sortby="default", **kw):
     """Eigenvalues via gschur!(A; wantZ=false) (pirates.jl:17-27); for a Hermitian or
-    SymTridiagonal argument, geigvals! (GenericSchur.jl:138-146, symtridiag.jl:51-57); for a
-    pencil (A, B), alpha ./ beta of ggschur! in the Schur form's order."""
+    SymTridiagonal argument, geigvals! with alg= (GenericSchur.jl:138-146, symtridiag.jl:51-57,
+    pirates.jl:170-197); for a pencil (A, B), alpha ./ beta of ggschur! in the Schur form's
+    order."""
+    alg = kw.pop("alg", None)
     if B is not None:
         G = ggschur(A, B, wantQ=False, wantZ=False, ctx=kw.get("ctx"))
         with np.errstate(divide="ignore", invalid="ignore"):
             return G.alpha / G.beta
     if isinstance(A, Hermitian):
-        return geigvals(A, sortby=sortby, **kw)
+        return geigvals(A, alg=alg, sortby=sortby, **kw)
     if isinstance(A, SymTridiagonal):
-        return _st_eig(A, False, sortby, kw.get("ctx"))[0]
+        return _st_eig(A, False, sortby, kw.get("ctx"), alg)[0]
+    if alg is not None:
+        raise ArgumentError("alg applies to Hermitian and SymTridiagonal arguments")
     S = gschur(A, wantZ=False, **kw)
     w = S.values
     if sortby is None:
@@ -857,7 +861,8 @@ def hessenberg_hermitian(H, ctx=None):
     return HermitianHessenberg(A, tau[:max(n - 1, 0)], d[:n], e[:max(n - 1, 0)], uplo)
 
 
-def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, jcv=False, ctx=None):
+def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jce=False, jcv=False, ctx=None,
+          alg=None):
     """Eigen decomposition (pirates.jl:63-160): balance! (permute/scale, as the reference's
     defaults), Schur form, triangularize for real input, right eigenvectors (and left
     ones with jvl or jce), the Balancer's lmul!/ldiv!, _enormalize!, sort.  With jce the
@@ -866,10 +871,14 @@ def eigen(A, permute=True, scale=True, sortby="default", jvr=True, jvl=False, jc
     a copy of the Schur form and its subspacesep (and, with jce as well, its
     eigvalscond, which then replaces the vector-based value) is computed, as the
     reference's (expensive) loop does.  Returns Eigen(values, vectors), or, when jvl, jce
-    or jcv is asked for, EigenFull(values, vectors, vectorsl, rconde, rcondv)."""
+    or jcv is asked for, EigenFull(values, vectors, vectorsl, rconde, rcondv).
+    For a Hermitian or SymTridiagonal argument, geigen! with alg (QRIteration by default,
+    or DivideAndConquer; pirates.jl:162-184)."""
     if isinstance(A, (Hermitian, SymTridiagonal)):
-        # eigen!(::Hermitian) / eigen!(::SymTridiagonal) (pirates.jl:162-184)
-        return geigen(A, sortby=sortby, ctx=ctx)
+        # eigen!(::Hermitian; alg) / eigen!(::SymTridiagonal; alg) (pirates.jl:162-184)
+        return geigen(A, alg=alg, sortby=sortby, ctx=ctx)
+    if alg is not None:
+        raise ArgumentError("alg applies to Hermitian and SymTridiagonal arguments")
     A = np.asarray(A)
     B = None
     if permute or scale:

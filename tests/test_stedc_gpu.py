@@ -141,3 +141,20 @@ def test_stedc_timing(gs):
         assert np.abs(np.sort(d) - np.linalg.eigvalsh(T)).max() <= 20 * n * EPS * np.abs(T).max()
         assert np.abs(Z.T @ Z - np.eye(n)).max() <= 20 * n * EPS
     print("n=%d tridiagonal eigenvectors: QR %.1f ms, divide and conquer %.1f ms" % (n, times["QRIteration"], times[DC]))
+
+
+def test_eigen_alg_keyword(gs):
+    """eigen!/eigvals!(::Hermitian; alg) and (::SymTridiagonal; alg) (pirates.jl:162-197)
+    reach divide and conquer; the default stays QRIteration."""
+    rng = np.random.default_rng(3700)
+    n = 60
+    A = rng.standard_normal((n, n))
+    A = (A + A.T) / 2
+    ref = np.linalg.eigvalsh(A)
+    for alg in (None, DC):
+        E = gs.eigen(gs.Hermitian(A, "L"), alg=alg)
+        assert np.abs(E.values - ref).max() <= 30 * n * EPS * np.abs(A).max()
+        assert np.abs(gs.eigvals(gs.Hermitian(A, "U"), alg=alg) - ref).max() <= 30 * n * EPS * np.abs(A).max()
+    D, E2 = rng.standard_normal(n), rng.standard_normal(n - 1)
+    w = gs.eigvals(gs.SymTridiagonal(D.copy(), E2.copy()), alg=DC)
+    assert np.abs(w - np.linalg.eigvalsh(_tri(D, E2))).max() <= 20 * n * EPS * np.abs(_tri(D, E2)).max()
