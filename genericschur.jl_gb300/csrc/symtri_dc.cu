@@ -18,8 +18,9 @@
 //                     column-type counts and partition by ballot scans
 //       k_dc_gather / k_dc_place  the gathers of Q2 by column type and the deflated columns
 //                     to the end, one warp per column over all the level's merges
-//       k_dc_secular  the roots of the secular equation, one thread per root (_dcroot!,
-//                     777-927, with _dcroot2!, _dcnewton and the i = n / i < n helpers)
+//       k_dc_secular  the roots of the secular equation, one warp per root (_dcroot!,
+//                     777-927, with _dcroot2!, _dcnewton and the i = n / i < n helpers;
+//                     the lanes split the sums over the poles)
 //       k_dc_lowner / k_dc_vecs   the eigenvectors of the rank-one problem (_dcsecular!,
 //                     441-472)
 //       the update Q = Q2 S (_dcsecular!, 474-488) as two GEMMs per merge: the FP64 product on
@@ -435,6 +436,256 @@ __device__ double dc_root(int n, int i, const double* __restrict__ dd, const dou
     else dltub = fmin(dltub, tau);
     eta = step(niter, switch3, sw);
     for (int j = 1; j <= n; ++j) delta[j] = delta[j] - eta;
+    tau += eta;
+    prev_w = w;
+    update(0.0);
+    if ((w * prev_w > 0) && (fabs(w) > fabs(prev_w) / 10.0)) sw = !sw;
+  }
+  *conv = false;
+  return dorg + tau;
+}
+
+// The same root with one warp: lanes split the sums over the poles and the updates of
+// delta; the butterfly sums leave the same value in every lane, so the scalar steps run
+// identically in all lanes.  The running erretm sums of the reference (erretm += psi after
+// each term) are the weighted sums sum_i t_i (ii - i + 1) and sum_i t_i (i - ii).
+__device__ __forceinline__ double wsum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ double dc_root_warp(int n, int i, const double* __restrict__ dd, const double* __restrict__ zz,
+                               double* __restrict__ dl, double rho, bool* conv, int lane) {
+  const int maxit = 30;
+  const double* d = dd - 1;
+  const double* z = zz - 1;
+  double* delta = dl - 1;
+  *conv = true;
+  if (n <= 2) {
+    double lam = 0.0;
+    if (lane == 0) lam = dc_root(n, i, dd, zz, dl, rho, conv);
+    __syncwarp();
+    lam = __shfl_sync(0xffffffffu, lam, 0);
+    return lam;
+  }
+  const double rhoinv = 1.0 / rho;
+  double dltlb, dltub, w, tau, erretm;
+  auto set_delta = [&](double org, double sh) {
+    for (int j = 1 + lane; j <= n; j += 32) delta[j] = (d[j] - org) - sh;
+    __syncwarp();
+  };
+  auto shift_delta = [&](double eta) {
+    for (int j = 1 + lane; j <= n; j += 32) delta[j] = delta[j] - eta;
+    __syncwarp();
+  };
+  if (i == n) {
+    const int ii = n - 1;
+    const double midpt = rho / 2.0;
+    set_delta(d[i], midpt);
+    {
+      double ps = 0.0;
+      for (int j = 1 + lane; j <= n - 2; j += 32) ps += dsq(z[j]) / delta[j];
+      const double psi = wsum(ps);
+      const double c = rhoinv + psi;
+      w = c + dsq(z[ii]) / delta[ii] + dsq(z[n]) / delta[n];
+      const double D = d[n] - d[n - 1];
+      const double a = -c * D + dsq(z[n - 1]) + dsq(z[n]);
+      const double b = dsq(z[n]) * D;
+      const double q = a < 0 ? 2.0 * b / (sqrt(a * a + 4.0 * b * c) - a) : (a + sqrt(a * a + 4.0 * b * c)) / (2.0 * c);
+      if (w <= 0) {
+        const double t = dsq(z[n - 1]) / (d[n] - d[n - 1] + rho) + dsq(z[n]) / rho;
+        tau = (c <= t) ? rho : q;
+        dltlb = midpt;
+        dltub = rho;
+      } else {
+        tau = q;
+        dltlb = 0.0;
+        dltub = midpt;
+      }
+    }
+    set_delta(d[i], tau);
+    double dpsi = 0.0, dphi = 0.0;
+    auto update_n = [&]() {
+      double ps = 0.0, dps = 0.0, er = 0.0;
+      for (int j = 1 + lane; j <= ii; j += 32) {
+        const double t = z[j] / delta[j];
+        const double zt = z[j] * t;
+        ps += zt;
+        dps += t * t;
+        er += zt * (double)(ii - j + 1);
+      }
+      const double psi = wsum(ps);
+      dpsi = wsum(dps);
+      erretm = fabs(wsum(er));
+      const double t = z[n] / delta[n];
+      const double phi = z[n] * t;
+      dphi = t * t;
+      erretm = 8.0 * (-phi - psi) + erretm - phi + rhoinv + fabs(tau) * (dpsi + dphi);
+      w = rhoinv + phi + psi;
+    };
+    auto step_n = [&](int iter) {
+      double c = w - delta[n - 1] * dpsi - delta[n] * dphi;
+      if (iter <= 2) c = fabs(c);
+      const double a = (delta[n - 1] + delta[n]) * w - delta[n - 1] * delta[n] * (dpsi + dphi);
+      const double b = delta[n - 1] * delta[n] * w;
+      double eta;
+      if (c == 0) eta = dltub - tau;
+      else if (a >= 0) eta = (a + sqrt(fabs(a * a - 4.0 * b * c))) / (2.0 * c);
+      else eta = 2.0 * b / (a - sqrt(fabs(a * a - 4.0 * b * c)));
+      if (w * eta > 0) eta = -w / (dpsi + dphi);
+      const double t = tau + eta;
+      if (t > dltub || t < dltlb) eta = w < 0 ? (dltub - tau) / 2.0 : (dltlb - tau) / 2.0;
+      return eta;
+    };
+    update_n();
+    if (fabs(w) < kDcEps * erretm) return d[i] + tau;
+    if (w <= 0) dltlb = fmax(dltlb, tau);
+    else dltub = fmin(dltub, tau);
+    double eta = step_n(2);
+    shift_delta(eta);
+    tau += eta;
+    update_n();
+    for (int niter = 3; niter <= maxit; ++niter) {
+      if (fabs(w) < kDcEps * erretm) return d[i] + tau;
+      if (w <= 0) dltlb = fmax(dltlb, tau);
+      else dltub = fmin(dltub, tau);
+      eta = step_n(niter);
+      shift_delta(eta);
+      tau += eta;
+      update_n();
+    }
+    *conv = false;
+    return d[i] + tau;
+  }
+  const int ip1 = i + 1;
+  const double D = d[ip1] - d[i];
+  const double midpt = D / 2.0;
+  set_delta(d[i], midpt);
+  bool orig;
+  {
+    double ps = 0.0, ph = 0.0;
+    for (int j = 1 + lane; j <= n; j += 32) {
+      if (j <= i - 1) ps += dsq(z[j]) / delta[j];
+      else if (j >= i + 2) ph += dsq(z[j]) / delta[j];
+    }
+    const double psi = wsum(ps), phi = wsum(ph);
+    const double c = rhoinv + psi + phi;
+    w = c + dsq(z[i]) / delta[i] + dsq(z[ip1]) / delta[ip1];
+    orig = w > 0;
+    if (orig) {
+      const double a = c * D + dsq(z[i]) + dsq(z[ip1]);
+      const double b = dsq(z[i]) * D;
+      tau = a > 0 ? 2.0 * b / (a + sqrt(fabs(a * a - 4.0 * b * c))) : (a - sqrt(fabs(a * a - 4.0 * b * c))) / (2.0 * c);
+      dltlb = 0.0;
+      dltub = midpt;
+    } else {
+      const double a = c * D - dsq(z[i]) - dsq(z[ip1]);
+      const double b = dsq(z[ip1]) * D;
+      tau = a < 0 ? 2.0 * b / (a - sqrt(fabs(a * a + 4.0 * b * c))) : -(a + sqrt(fabs(a * a + 4.0 * b * c))) / (2.0 * c);
+      dltlb = -midpt;
+      dltub = 0.0;
+    }
+  }
+  const int ii = orig ? i : i + 1;
+  const double dorg = d[ii];
+  set_delta(dorg, tau);
+  double Ppsi = 0.0, Pphi = 0.0, Pdpsi = 0.0, Pdphi = 0.0, Pdw = 0.0, w0 = 0.0;
+  auto update = [&](double etaq) {
+    double ps = 0.0, dps = 0.0, erp = 0.0, ph = 0.0, dph = 0.0, erf = 0.0;
+    for (int j = 1 + lane; j <= n; j += 32) {
+      if (j == ii) continue;
+      const double t = z[j] / delta[j];
+      const double zt = z[j] * t;
+      if (j < ii) {
+        ps += zt;
+        dps += t * t;
+        erp += zt * (double)(ii - j);
+      } else {
+        ph += zt;
+        dph += t * t;
+        erf += zt * (double)(j - ii);
+      }
+    }
+    const double psi = wsum(ps), dpsi = wsum(dps), phi = wsum(ph), dphi = wsum(dph);
+    erretm = fabs(wsum(erp)) + wsum(erf);
+    w0 = rhoinv + phi + psi;
+    double t = z[ii] / delta[ii];
+    const double dw = dpsi + dphi + t * t;
+    t = z[ii] * t;
+    w = rhoinv + phi + psi + t;
+    erretm = 8.0 * (phi - psi) + erretm + 2.0 * rhoinv + 3.0 * fabs(t) + fabs(tau + etaq) * dw;
+    Ppsi = psi; Pphi = phi; Pdpsi = dpsi; Pdphi = dphi; Pdw = dw;
+  };
+  auto step = [&](int niter, bool switch3, bool sw) {
+    double dpsi = Pdpsi, dphi = Pdphi;
+    const double dw = Pdw;
+    const int iip1 = ii + 1, iim1 = ii - 1;
+    double eta;
+    if (!switch3) {
+      double c;
+      if (!sw) {
+        if (orig) c = w - delta[ip1] * dw - (d[i] - d[ip1]) * dsq(z[i] / delta[i]);
+        else c = w - delta[i] * dw - (d[ip1] - d[i]) * dsq(z[ip1] / delta[ip1]);
+      } else {
+        const double t = z[ii] / delta[ii];
+        if (orig) dpsi += t * t;
+        else dphi += t * t;
+        c = w - delta[i] * dpsi - delta[ip1] * dphi;
+      }
+      double a = (delta[i] + delta[ip1]) * w - delta[i] * delta[ip1] * dw;
+      const double b = delta[i] * delta[ip1] * w;
+      if (c == 0) {
+        if (a == 0) {
+          if (orig) a = dsq(z[i]) + dsq(delta[ip1]) * (dpsi + dphi);
+          else a = dsq(z[ip1]) + dsq(delta[i]) * (dpsi + dphi);
+        }
+        eta = b / a;
+      } else if (a <= 0) {
+        eta = (a - sqrt(fabs(a * a - 4.0 * b * c))) / (2.0 * c);
+      } else {
+        eta = 2.0 * b / (a + sqrt(fabs(a * a - 4.0 * b * c)));
+      }
+    } else {
+      const double t = rhoinv + Ppsi + Pphi;
+      double c, z3[3];
+      if (orig) {
+        const double t1 = dsq(z[iim1] / delta[iim1]);
+        c = t - delta[iip1] * (dpsi + dphi) - (d[iim1] - d[iip1]) * t1;
+        z3[0] = dsq(z[iim1]);
+        z3[2] = dsq(delta[iip1]) * ((dpsi - t1) + dphi);
+      } else {
+        const double t1 = dsq(z[iip1] / delta[iip1]);
+        c = t - delta[iim1] * (dpsi + dphi) - (d[iip1] - d[iim1]) * t1;
+        z3[0] = dsq(delta[iim1]) * (dpsi + (dphi - t1));
+        z3[2] = dsq(z[iip1]);
+      }
+      z3[1] = dsq(z[ii]);
+      const double d3[3] = {delta[iim1], delta[ii], delta[iip1]};
+      eta = dc_newton(niter, orig, c, d3, z3, w);
+    }
+    if (w * eta > 0) eta = -w / dw;
+    const double t = tau + eta;
+    if (t > dltub || t < dltlb) eta = w < 0 ? (dltub - tau) / 2.0 : (dltlb - tau) / 2.0;
+    return eta;
+  };
+  update(0.0);
+  bool switch3 = orig ? (w0 < 0) : (w0 > 0);
+  if (ii == 1 || ii == n) switch3 = false;
+  if (fabs(w) < kDcEps * erretm) return dorg + tau;
+  if (w <= 0) dltlb = fmax(dltlb, tau);
+  else dltub = fmin(dltub, tau);
+  double eta = step(2, switch3, false);
+  double prev_w = w;
+  shift_delta(eta);
+  update(eta);
+  bool sw = orig ? (-w > fabs(prev_w) / 10.0) : (w > fabs(prev_w) / 10.0);
+  tau += eta;
+  for (int niter = 3; niter <= maxit; ++niter) {
+    if (fabs(w) < kDcEps * erretm) return dorg + tau;
+    if (w <= 0) dltlb = fmax(dltlb, tau);
+    else dltub = fmin(dltub, tau);
+    eta = step(niter, switch3, sw);
+    shift_delta(eta);
     tau += eta;
     prev_w = w;
     update(0.0);
@@ -898,18 +1149,26 @@ __global__ void __launch_bounds__(32 * kDcGW) k_dc_place(const DcMerge* __restri
   if (lane == 0) dg[M.off + k + j] = zg[M.off + k + j];
 }
 
-// the secular equation's roots: d[j] and delta in column j of the merge's block of Q
-__global__ void __launch_bounds__(128) k_dc_secular(const DcMerge* __restrict__ mg, const DcInfo* __restrict__ info,
-                                                    const double* __restrict__ lam, const double* __restrict__ w,
-                                                    double* d, double* Q, long long ld, int* status) {
+// the secular equation's roots: d[j] and delta in column j of the merge's block of Q; one
+// warp per root (kDcRW roots per CTA)
+constexpr int kDcRW = 4;
+__global__ void __launch_bounds__(32 * kDcRW) k_dc_secular(const DcMerge* __restrict__ mg,
+                                                           const DcInfo* __restrict__ info,
+                                                           const double* __restrict__ lam,
+                                                           const double* __restrict__ w, double* d, double* Q,
+                                                           long long ld, int* status) {
   const DcMerge M = mg[blockIdx.x];
   const DcInfo I = info[blockIdx.x];
-  const int j = blockIdx.y * 128 + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.y * kDcRW + (threadIdx.x >> 5);
   if (j >= I.k) return;
   const int o = M.off;
   bool conv = true;
-  d[o + j] = dc_root(I.k, j + 1, lam + o, w + o, Q + o + (size_t)(o + j) * ld, I.rho, &conv);
-  if (!conv) atomicOr(status, 1);
+  const double lamj = dc_root_warp(I.k, j + 1, lam + o, w + o, Q + o + (size_t)(o + j) * ld, I.rho, &conv, lane);
+  if (lane == 0) {
+    d[o + j] = lamj;
+    if (!conv) atomicOr(status, 1);
+  }
 }
 
 // w[i] = sign(w0[i]) sqrt(-Q[i,i] prod_{j != i} Q[i,j] / (lam[i] - lam[j])) for k >= 3
@@ -1179,7 +1438,8 @@ cudaError_t dc_core(int m, double* d, double* e, const DcWs& W, int num_sms, cud
     for (const DcInfo& I : info) kmax = std::max(kmax, I.k);
     if (kmax > 0) {
       const dim3 gk(nm, (kmax + 127) / 128);
-      k_dc_secular<<<gk, 128, 0, s>>>(W.mg, W.info, W.lam, W.w, d, W.Qc, m, W.status);
+      k_dc_secular<<<dim3(nm, (kmax + kDcRW - 1) / kDcRW), 32 * kDcRW, 0, s>>>(W.mg, W.info, W.lam, W.w, d, W.Qc,
+                                                                                  m, W.status);
       k_dc_lowner<<<gk, 128, 0, s>>>(W.mg, W.info, W.lam, W.w, W.w2, W.Qc, m);
       k_dc_vecs<<<gk, 128, 0, s>>>(W.mg, W.info, W.w2, W.indexc, W.Qc, m, W.S);
       DC_CK(cudaGetLastError());
