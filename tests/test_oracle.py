@@ -391,3 +391,29 @@ def test_oracle_gsubspacesep_onenorm_vs_tgsen():
         assert r[-1] == 0
         sep = po.gsubspacesep1(S, T, k)
         assert abs(sep[0] - r[9][0]) <= 1e-10 * r[9][0]
+
+
+def test_oracle_ggordschur_real_vs_tgsen():
+    """The real-pencil reordering restated (rordschur.jl:542-1178, after dtgexc / dtgex2)
+    against LAPACK dtgsen (ijob = 0) on the same generalized Schur pair and selection: the
+    same eigenvalue order and the same leading deflating subspaces."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    from common import selected_with_pairs
+    rng = np.random.default_rng(9)
+    for trial in range(6):
+        n = 16 if trial < 3 else 30
+        A = rng.random((n, n))
+        B = rng.random((n, n)) - 0.5 + np.eye(n)
+        S, T, al, be, Q, Z, st = po.ggschur_real(A, B)
+        assert st == 0
+        sel = rng.integers(0, 2, n).astype(np.int32)
+        S2, T2, a2, b2, Q2, Z2, st2 = po.ggordschur_real(S, T, Q, Z, sel)
+        assert st2 == 0
+        r = lapack.dtgsen(sel, S, T, Q, Z, ijob=0, lwork=4 * n * n + 4 * n + 16, liwork=n + 8)
+        assert r[-1] == 0
+        lv = (r[2] + 1j * r[3]) / r[4]
+        ov = a2 / b2
+        assert np.abs(lv - ov).max() <= 1e-12 * np.abs(ov).max()
+        k = int(selected_with_pairs(al / be, sel).sum())
+        for Mo, Ml in ((Z2, r[6]), (Q2, r[5])):
+            assert np.abs(Mo[:, :k] @ Mo[:, :k].T - Ml[:, :k] @ Ml[:, :k].T).max() <= 1e-12
