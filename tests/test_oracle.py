@@ -417,3 +417,27 @@ def test_oracle_ggordschur_real_vs_tgsen():
         k = int(selected_with_pairs(al / be, sel).sum())
         for Mo, Ml in ((Z2, r[6]), (Q2, r[5])):
             assert np.abs(Mo[:, :k] @ Mo[:, :k].T - Ml[:, :k] @ Ml[:, :k].T).max() <= 1e-12
+
+
+def test_oracle_ggordschur_cplx_vs_tgsen():
+    """The complex-pencil reordering restated (ordschur.jl:147-305, after ztgexc / ztgex2)
+    against LAPACK ztgsen (ijob = 0): the same eigenvalue order and leading deflating
+    subspaces."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    rng = np.random.default_rng(10)
+    for trial in range(4):
+        n = 16 if trial < 2 else 30
+        A = randn_matrix(rng, n, True)
+        B = randn_matrix(rng, n, True)
+        S, T, al, be, Q, Z, st = po.ggschur(A, B)
+        assert st == 0
+        sel = rng.integers(0, 2, n).astype(np.int32)
+        S2, T2, a2, b2, Q2, Z2, st2 = po.ggordschur(S, T, Q, Z, sel)
+        assert st2 == 0
+        r = lapack.ztgsen(sel, S, T, Q, Z, ijob=0, lwork=4 * n * n + 16, liwork=n + 8)
+        assert r[-1] == 0
+        ov = a2 / b2
+        assert np.abs(r[2] / r[3] - ov).max() <= 1e-12 * np.abs(ov).max()
+        k = int(sel.sum())
+        for Mo, Ml in ((Z2, r[5]), (Q2, r[4])):
+            assert np.abs(Mo[:, :k] @ Mo[:, :k].conj().T - Ml[:, :k] @ Ml[:, :k].conj().T).max() <= 1e-12
