@@ -441,3 +441,48 @@ def test_oracle_ggordschur_cplx_vs_tgsen():
         k = int(sel.sum())
         for Mo, Ml in ((Z2, r[5]), (Q2, r[4])):
             assert np.abs(Mo[:, :k] @ Mo[:, :k].conj().T - Ml[:, :k] @ Ml[:, :k].conj().T).max() <= 1e-12
+
+
+def _match_sets(a, b):
+    from scipy.optimize import linear_sum_assignment
+    C = np.abs(a[:, None] - b[None, :]) / np.maximum(1.0, np.abs(b[None, :]))
+    r, c = linear_sum_assignment(C)
+    return float(C[r, c].max())
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_oracle_hermitian_and_qz_vs_lapack(cplx):
+    """The Hermitian (hessenberg.jl, symtridiag.jl) and QZ (generalized.jl, rgeneralized.jl)
+    restatements against LAPACK on the same inputs: eigenvalues (eigh / ggev), the
+    decompositions' backward errors, and the generalized eigenvectors' residuals
+    (vectors.jl:723-1513): beta A v = alpha B v, u^H (beta A - alpha B) = 0."""
+    import scipy.linalg
+    rng = np.random.default_rng(8800 + cplx)
+    n = 24
+    H = randn_matrix(rng, n, cplx)
+    H = (H + H.conj().T) / 2
+    for uplo in ("L", "U"):
+        w, V, st = po.heev(H, uplo)
+        assert st == 0
+        assert np.abs(w - np.linalg.eigvalsh(H)).max() <= 20 * n * EPS * np.abs(H).max()
+        assert np.abs(H @ V - V * w).max() <= 20 * n * EPS * np.abs(H).max()
+    A = randn_matrix(rng, n, cplx)
+    B = randn_matrix(rng, n, cplx)
+    if cplx:
+        S, T, al, be, Q, Z, st = po.ggschur(A, B)
+        VR = po.ggeigvecs(S, T, Z)
+        VL = po.ggeigvecs(S, T, Q, left=True)
+    else:
+        S, T, al, be, Q, Z, st = po.ggschur_real(A, B)
+        VR = po.rgeigvecs(S, T, Z)
+        VL = po.rgeigvecs(S, T, Q, left=True)
+    assert st == 0
+    nA, nB = np.linalg.norm(A), np.linalg.norm(B)
+    assert np.linalg.norm(A - Q @ S @ Z.conj().T) <= 20 * n * EPS * nA
+    assert np.linalg.norm(B - Q @ T @ Z.conj().T) <= 20 * n * EPS * nB
+    assert _match_sets(al / be, scipy.linalg.eigvals(A, B)) < 1e-8
+    for j in range(n):
+        r = be[j] * (A @ VR[:, j]) - al[j] * (B @ VR[:, j])
+        assert np.linalg.norm(r) <= 1e3 * n * EPS * (abs(be[j]) * nA + abs(al[j]) * nB) * np.linalg.norm(VR[:, j])
+        l = VL[:, j].conj() @ (be[j] * A - al[j] * B)
+        assert np.linalg.norm(l) <= 1e3 * n * EPS * (abs(be[j]) * nA + abs(al[j]) * nB) * np.linalg.norm(VL[:, j])
