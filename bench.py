@@ -69,6 +69,25 @@ def dist_env():
     return world, rank, local
 
 
+def rank_seed(rank):
+    """Each rank factors its own batch (weak scaling, no data-path collective)."""
+    return SEED + rank
+
+
+def reduce_max_ms(torch, ms, world, device):
+    """The per-step time as the job sees it: the maximum over ranks."""
+    if world <= 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, count, ms):
+    """Matrices per second of the whole job: every rank's batch over the slowest rank's step."""
+    return world * count / (ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -221,7 +240,7 @@ def run_ours(args):
     from genericschur_gb300.workloads import batched_real, real_flops
 
     ctx = gs.Context(local)
-    packed, ns, offs, woffs = batched_real(count=args.count, seed=SEED + rank)
+    packed, ns, offs, woffs = batched_real(count=args.count, seed=rank_seed(rank))
     nw = int(ns.sum())
     count = len(ns)
     flops = real_flops(ns)
@@ -277,12 +296,8 @@ def run_ours(args):
         step()
         torch.cuda.synchronize()
         kms.append(ctx.last_kernel_ms())
-    ms = ms_total / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * count / (ms * 1e-3)
+    ms = reduce_max_ms(torch, ms_total / args.steps, world, dev)
+    value = job_throughput(world, count, ms)
 
     e2e = None
     if not args.no_e2e:
