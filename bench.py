@@ -34,6 +34,18 @@ COUNT, SEED = 20000, 4
 WORKLOAD = "batched real FP64 Schur (T, Z, eigenvalues): 20000 matrices, n~U{8..128}, N(0,1), seed 4"
 
 
+def bench_config(count):
+    """The workload's config object, identical in both arms."""
+    return {"workload": WORKLOAD, "batch": count, "seed": SEED,
+            "l2": "inputs larger than L2 (%.0f MB of A per step); A restored from a pristine copy each step"
+                  % (8e-6 * float(np.sum(np.asarray(_sizes(count), dtype=np.float64) ** 2)))}
+
+
+def _sizes(count):
+    from genericschur_gb300.workloads import batch_sizes
+    return batch_sizes(count, SEED)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -217,7 +229,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.mean([s["seconds"] for s in samples]) * 1e3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "batch": args.count, "seed": SEED},
+           "config": bench_config(args.count),
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": samples[0]["cores"], "kind": "port",
                             "sample": samples[0]["sample"] + "; C++ restatement of GenericSchur.jl's gschur! "
                                       "(Julia is absent on this machine), OpenMP over the batch"},
@@ -335,9 +347,7 @@ def run_ours(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "batch_per_gpu": count, "seed": SEED,
-                      "l2": "inputs (%.0f MB of A per step) larger than L2; A restored from a pristine copy each "
-                            "step" % (packed.nbytes / 1e6), "graph": not args.no_graph},
+           "config": bench_config(args.count), "graph": not args.no_graph,
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
            "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
            "large": large, "gemm_f64_tc": gemm_tc, "stedc": stedc, **secondary}

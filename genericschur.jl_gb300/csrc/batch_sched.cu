@@ -1,7 +1,10 @@
 // Work-queue construction for the persistent batched kernels: a counting sort of
 // the matrices by order, largest first, split into the size bins of kBinMax.
 // Runs on the device so that the whole batched pipeline is graph-capturable and
-// needs no host round trip to read the orders.
+// needs no host round trip to read the orders.  Orders outside [0, kSmallMax] (possible
+// when the orders live in device memory and were never checked on the host) are counted
+// in the nearest end bin; the solve kernels see the true order there and write ST_BADARG
+// for it without touching the matrix.
 #include "gs_internal.h"
 
 namespace gsk {

@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(NT) k_eig_adjoint(AdjBatch ab) {
   const int tid = threadIdx.x;
   for (int b = blockIdx.x; b < ab.count; b += gridDim.x) {
     const int n = ab.ns[b];
-    if (n <= 0) continue;
+    if (n <= 0 || n > kSmallMax) continue;  // shared memory is sized for kSmallMax; device orders are unchecked
     const long long off = ab.offs[b];
     const double2* __restrict__ X = ab.VR + off;
     const double2* __restrict__ Y = ab.VL + off;

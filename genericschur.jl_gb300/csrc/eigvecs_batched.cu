@@ -237,7 +237,7 @@ template <int NT>
 __device__ void eigvecs_one(const EigBatch& eb, int b, double2* smem) {
   const int tid = threadIdx.x;
   const int n = eb.ns[b];
-  if (n <= 0) return;
+  if (n <= 0 || n > kSmallMax) return;  // shared memory is sized for kSmallMax; device orders are unchecked
   const long long off = eb.offs[b];
   const double2* __restrict__ Tg = eb.T + off;
   const double2* __restrict__ Zg = eb.Z ? eb.Z + off : nullptr;

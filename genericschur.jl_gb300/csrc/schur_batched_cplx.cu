@@ -148,14 +148,17 @@ __device__ void hessenberg_cplx(int n, double2* A, int ld, double2* tau, double*
 #undef AA
 }
 
+// nmax: the largest order the launch sized its buffers for (the bin's maximum, or the
+// single large matrix's order).  An order outside [0, nmax] read from device memory gets
+// ST_BADARG before anything is read or written.
 template <int NT, bool HSMEM, bool HGLOB>
-__device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
+__device__ void solve_cplx(const CplxBatch& bt, int b, int nmax, double2* smem, CtlC& c) {
   constexpr bool PACKED = !HSMEM;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int n = bt.ns[b];
-  if (n <= 0) {
-    if (tid == 0) bt.status[b] = ST_OK;
+  if (n <= 0 || n > nmax) {
+    if (tid == 0) bt.status[b] = (n == 0) ? ST_OK : ST_BADARG;
     return;
   }
   double2* __restrict__ Ag = bt.A + bt.offs[b];
@@ -525,7 +528,7 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, double2* smem, CtlC& c) {
 
 template <int NT, bool HSMEM, bool HGLOB>
 __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __restrict__ order,
-                                                   int* __restrict__ sched, int bin) {
+                                                   int* __restrict__ sched, int bin, int nmax) {
   extern __shared__ double2 smemz[];
   __shared__ CtlC c;
   __shared__ int s_job;
@@ -536,7 +539,7 @@ __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __re
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_cplx<NT, HSMEM, HGLOB>(bt, order[job], smemz, c);
+    solve_cplx<NT, HSMEM, HGLOB>(bt, order[job], nmax, smemz, c);
   }
 }
 
@@ -551,7 +554,7 @@ cudaError_t launch_bin_c(const CplxBatch& bt, const int* order, int* sched, int 
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM, false>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  k_schur_cplx<NT, HSMEM, false><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin);
+  k_schur_cplx<NT, HSMEM, false><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin, nmax);
   return cudaGetLastError();
 }
 
@@ -564,7 +567,7 @@ cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* or
   const size_t smem = sizeof(double2) * (4 * (size_t)nmax) + 32 * sizeof(double) + 64;
   cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<256, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_schur_cplx<256, false, true><<<1, 256, smem, s>>>(bt, order, sched, kNumBins - 1);
+  k_schur_cplx<256, false, true><<<1, 256, smem, s>>>(bt, order, sched, kNumBins - 1, nmax);
   return cudaGetLastError();
 }
 

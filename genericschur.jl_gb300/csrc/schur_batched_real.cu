@@ -183,13 +183,16 @@ __device__ __forceinline__ void make_refl(T* H, int k, int iend, Refl<T>& out, T
   l[0] = t1; l[1] = out.t2; l[2] = out.t3; l[3] = x1; l[4] = x2;
 }
 
+// nmax: the largest order the launch sized shared memory for.  Orders come from device
+// memory (GS_DEVICE calls are not checked on the host), so an order outside [0, nmax]
+// gets ST_BADARG before anything is read or written.
 template <class T, class W, int NT, bool HSMEM>
-__device__ void solve_real(const RealBatchT<T, W>& bt, int b, T* smem, Ctl<T>& c) {
+__device__ void solve_real(const RealBatchT<T, W>& bt, int b, int nmax, T* smem, Ctl<T>& c) {
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int n = bt.ns[b];
-  if (n <= 0) {
-    if (tid == 0) bt.status[b] = ST_OK;
+  if (n <= 0 || n > nmax) {
+    if (tid == 0) bt.status[b] = (n == 0) ? ST_OK : ST_BADARG;
     return;
   }
   T* __restrict__ Ag = bt.A + bt.offs[b];
@@ -525,7 +528,7 @@ __global__ void __launch_bounds__(NT) k_schur_real(RealBatchT<T, W> bt, const in
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_real<T, W, NT, HSMEM>(bt, order[job], smem, c);
+    solve_real<T, W, NT, HSMEM>(bt, order[job], bin_max(bin), smem, c);
   }
 }
 

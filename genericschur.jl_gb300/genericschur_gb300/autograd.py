@@ -37,6 +37,18 @@ class BatchedEigvals(torch.autograd.Function):
                                               GS_WANTZ | GS_SCALE | GS_DEVICE)
         if rc != 0:
             raise RuntimeError("gs_schur_batched_c64: %s" % lib_ctx.last_error())
+        # per-matrix status: a matrix that hit the iteration limit has no Schur form to
+        # differentiate, and the reference raises UnconvergedException for it
+        # (GenericSchur.jl:39-45, 553-556); an order the kernel rejected is an ArgumentError
+        bad = torch.nonzero(st != 0).flatten().cpu()
+        if bad.numel():
+            from . import ArgumentError, UnconvergedException
+            b0 = int(bad[0])
+            code = int(st[b0].item())
+            msg = "matrix %d of the batch (%d failed): status %d" % (b0, bad.numel(), code)
+            if code == _capi.GS_UNCONVERGED:
+                raise UnconvergedException("Convergence failure; " + msg)
+            raise ArgumentError(msg)
         ctx_.save_for_backward(T, Z, ns, offs, woffs)
         return w.view(batch, n)
 

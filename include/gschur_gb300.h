@@ -113,7 +113,10 @@ GS_API int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, doub
  * with leading dimension ns[b] at element offset offs[b] of A and Z; its
  * eigenvalues start at element woffs[b] of wr/wi (or of w, complex).  status[b]
  * receives GS_OK or GS_UNCONVERGED.  Returns GS_UNCONVERGED if any matrix failed
- * (host-pointer mode) — the other matrices are still valid.
+ * (host-pointer mode) — the other matrices are still valid.  Host-pointer calls check
+ * every order and offset before launching (GS_BADARG).  With GS_DEVICE the orders are
+ * read on the device only: a matrix whose order lies outside [0, 128] is left untouched
+ * and gets status[b] = GS_BADARG; offsets are the caller's responsibility. 
  * ------------------------------------------------------------------------- */
 GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* wr, double* wi,

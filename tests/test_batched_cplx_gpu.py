@@ -95,3 +95,51 @@ def test_unconverged_status(gs):
     A = randn_matrix(rng, 20, cplx=True)
     with pytest.raises(gs.UnconvergedException):
         gs.gschur(A, maxiter=3)
+
+
+@pytest.mark.parametrize("bad_n", [129, -1])
+def test_device_orders_out_of_range(gs, bad_n):
+    """GS_DEVICE complex batches: an order outside [0, 128] read on the device gives
+    that matrix status GS_BADARG and leaves it untouched; the others are decomposed."""
+    torch = pytest.importorskip("torch")
+    from genericschur_gb300 import _capi
+    rng = np.random.default_rng(78)
+    ns = np.array([16, bad_n, 128, 45], dtype=np.int32)
+    room = np.maximum(ns, 0).astype(np.int64) ** 2
+    offs = np.concatenate([[0], np.cumsum(room)[:-1]]).astype(np.int64)
+    woffs = np.concatenate([[0], np.cumsum(np.maximum(ns, 0))[:-1]]).astype(np.int64)
+    m = int(room.sum())
+    packed = (rng.standard_normal(m) + 1j * rng.standard_normal(m)) / np.sqrt(2)
+    dev = torch.device("cuda", 0)
+    ctx = gs.get_context(0)
+    stream = torch.cuda.Stream(dev)
+    A = torch.from_numpy(packed.view(np.float64).copy()).to(dev)
+    Z = torch.zeros_like(A)
+    w = torch.zeros(2 * int(np.maximum(ns, 0).sum()), dtype=torch.float64, device=dev)
+    st = torch.full((len(ns),), -1, dtype=torch.int32, device=dev)
+    dns, doffs, dwoffs = (torch.from_numpy(x).to(dev) for x in (ns, offs, woffs))
+    torch.cuda.synchronize()
+    ctx.set_stream(stream.cuda_stream)
+    try:
+        rc = ctx.lib.gs_schur_batched_c64(ctx.handle, len(ns), dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
+                                          A.data_ptr(), Z.data_ptr(), w.data_ptr(), st.data_ptr(),
+                                          _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE)
+        assert rc == 0
+        stream.synchronize()
+    finally:
+        ctx.set_stream(None)
+    status = st.cpu().numpy()
+    T = A.cpu().numpy().view(np.complex128)
+    Zh = Z.cpu().numpy().view(np.complex128)
+    wh = w.cpu().numpy().view(np.complex128)
+    for b, n in enumerate(ns):
+        o = int(offs[b])
+        if n < 0 or n > 128:
+            assert status[b] == _capi.GS_BADARG
+            np.testing.assert_array_equal(T[o:o + room[b]], packed[o:o + room[b]])
+            continue
+        assert status[b] == 0
+        A0 = packed[o:o + n * n].reshape(n, n, order="F")
+        q = int(woffs[b])
+        assert_schur_cplx(A0, T[o:o + n * n].reshape(n, n, order="F"), Zh[o:o + n * n].reshape(n, n, order="F"),
+                          wh[q:q + n])

@@ -123,3 +123,54 @@ def test_unconverged_status(gs):
     A = rng.standard_normal((20, 20))
     with pytest.raises(gs.UnconvergedException):
         gs.gschur(A, maxiter=3)
+
+
+@pytest.mark.parametrize("bad_n", [129, 300, -3])
+def test_device_orders_out_of_range(gs, bad_n):
+    """GS_DEVICE batches: orders are read on the device only.  An order outside
+    [0, 128] must give that matrix status GS_BADARG (the reference raises
+    ArgumentError/DimensionMismatch for bad sizes) and leave it untouched, while the
+    other matrices are decomposed as usual."""
+    torch = pytest.importorskip("torch")
+    from genericschur_gb300 import _capi
+    rng = np.random.default_rng(77)
+    ns = np.array([20, 128, 7, bad_n, 64, 100], dtype=np.int32)
+    room = np.maximum(ns, 0).astype(np.int64) ** 2
+    offs = np.concatenate([[0], np.cumsum(room)[:-1]]).astype(np.int64)
+    woffs = np.concatenate([[0], np.cumsum(np.maximum(ns, 0))[:-1]]).astype(np.int64)
+    packed = rng.standard_normal(int(room.sum()))
+    dev = torch.device("cuda", 0)
+    ctx = gs.get_context(0)
+    stream = torch.cuda.Stream(dev)
+    A = torch.from_numpy(packed).to(dev)
+    Z = torch.zeros_like(A)
+    nw = int(np.maximum(ns, 0).sum())
+    wr = torch.zeros(nw, dtype=torch.float64, device=dev)
+    wi = torch.zeros(nw, dtype=torch.float64, device=dev)
+    st = torch.full((len(ns),), -1, dtype=torch.int32, device=dev)
+    dns, doffs, dwoffs = (torch.from_numpy(x).to(dev) for x in (ns, offs, woffs))
+    torch.cuda.synchronize()
+    ctx.set_stream(stream.cuda_stream)
+    try:
+        rc = ctx.lib.gs_schur_batched_f64(ctx.handle, len(ns), dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
+                                          A.data_ptr(), Z.data_ptr(), wr.data_ptr(), wi.data_ptr(), st.data_ptr(),
+                                          _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE)
+        assert rc == 0
+        stream.synchronize()
+    finally:
+        ctx.set_stream(None)
+    status = st.cpu().numpy()
+    T = A.cpu().numpy()
+    Zh = Z.cpu().numpy()
+    w = wr.cpu().numpy() + 1j * wi.cpu().numpy()
+    for b, n in enumerate(ns):
+        o = int(offs[b])
+        if n < 0 or n > 128:
+            assert status[b] == _capi.GS_BADARG
+            np.testing.assert_array_equal(T[o:o + room[b]], packed[o:o + room[b]])
+            continue
+        assert status[b] == 0
+        A0 = packed[o:o + n * n].reshape(n, n, order="F")
+        q = int(woffs[b])
+        assert_schur_real(A0, T[o:o + n * n].reshape(n, n, order="F"), Zh[o:o + n * n].reshape(n, n, order="F"),
+                          w[q:q + n])
