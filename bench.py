@@ -337,11 +337,17 @@ def run_ours(args):
     per_matrix = measure_per_matrix(ctx, packed, ns, offs)
     secondary = measure_complex_and_adjoint(ctx, torch, dev, stream)
     large = None
+    large_small = None
+    precision = None
+    c1 = None
     gemm_tc = None
     stedc = None
     if not args.no_large:
         ctx.set_stream(None)
         large = measure_large(ctx, torch, dev, args.large_n)
+        large_small = [measure_large(ctx, torch, dev, m) for m in (1024, 2048)]
+        precision = measure_precision(ctx, torch, dev)
+        c1 = measure_c1(ctx)
         gemm_tc = measure_gemm_tc(ctx, torch, dev, args.large_n)
         stedc = measure_stedc(ctx, args.dc_n)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -350,7 +356,8 @@ def run_ours(args):
            "config": bench_config(args.count), "graph": not args.no_graph,
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
            "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
-           "large": large, "gemm_f64_tc": gemm_tc, "stedc": stedc, **secondary}
+           "large": large, "large_1024_2048": large_small, "precision": precision, "complex256": c1,
+           "gemm_f64_tc": gemm_tc, "stedc": stedc, **secondary}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -396,6 +403,69 @@ def measure_large(ctx, torch, dev, n, mode="both"):
     return out
 
 
+def _schur_errors(torch, dev, A, S):
+    """||A - Z T Z^T||_F / ||A||_F and ||Z^T Z - I||_F in units of n eps (FP64 on the GPU)."""
+    n = A.shape[0]
+    eps = np.finfo(np.float64).eps
+    cm = lambda M: torch.from_numpy(np.ascontiguousarray(M)).to(dev)
+    dA, T, Z = cm(A), cm(S.T), cm(S.Z)
+    be = torch.linalg.norm(dA - Z @ T @ Z.T) / torch.linalg.norm(dA)
+    oe = torch.linalg.norm(Z.T @ Z - torch.eye(n, dtype=torch.float64, device=dev))
+    return float(be) / (n * eps), float(oe) / (n * eps)
+
+
+def measure_precision(ctx, torch, dev, n=2048):
+    """The precision workload's own matrix: A = V diag(l) V^-1, l real with |l| log-uniform
+    in [1e-3, 1e3] and random signs, cond(V) = 1e3, seed 6, n = 2048.  The plain FP64 path
+    and the FP32 + FP64-refinement entry point, each through the C-ABI with host buffers,
+    with their backward errors.  On this law FP32's own backward error (eps32 ||A||_F ~
+    0.07) exceeds half of the eigenvalues' gaps, so the refinement has nothing to converge
+    to and the entry point recomputes in FP64 (info iterations = -1); the line records
+    what that costs."""
+    import genericschur_gb300 as gs
+    from genericschur_gb300.workloads import conditioned_matrix
+    A = conditioned_matrix(n, seed=6)
+    t = time.perf_counter()
+    S = gs.gschur(A, ctx=ctx)
+    fp64_s = time.perf_counter() - t
+    be64, oe64 = _schur_errors(torch, dev, A, S)
+    t = time.perf_counter()
+    S2, info = gs.gschur_mixed(A, ctx=ctx, return_info=True)
+    mixed_s = time.perf_counter() - t
+    be, oe = _schur_errors(torch, dev, A, S2)
+    return {"workload": "A = V diag(l) V^-1, n=2048, |l| log-uniform [1e-3,1e3], random signs, cond(V)=1e3, seed 6",
+            "norm_fro": float(np.linalg.norm(A)), "fp64_s": fp64_s, "fp64_backward_err_n_eps": be64,
+            "fp64_orth_err_n_eps": oe64, "mixed_s": mixed_s, "mixed_backward_err_n_eps": be,
+            "mixed_orth_err_n_eps": oe, "mixed_info": info,
+            "note": "iterations -1: FP64 recomputation (FP32 cannot separate this law's eigenvalues)"}
+
+
+def measure_c1(ctx, n=256):
+    """The plain CPU-runnable workload: one 256 x 256 ComplexF64 matrix, re/im iid
+    N(0, 1/2), seed 0, Z accumulated, no balancing.  GPU time of gs_schur_c64 (host
+    buffers, median of 3 after a warm-up) beside the oracle (the C++ restatement of the
+    reference's complex gschur!, one core) on the same matrix."""
+    import genericschur_gb300 as gs
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(0)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2)
+    ts = []
+    for _ in range(4):
+        t = time.perf_counter()
+        S = gs.gschur(A, ctx=ctx)
+        ts.append(time.perf_counter() - t)
+    gpu_s = float(np.median(ts[1:]))
+    kernel_ms = ctx.last_kernel_ms()
+    t = time.perf_counter()
+    po.gschur(A)
+    cpu_s = time.perf_counter() - t
+    eps = np.finfo(np.float64).eps
+    be = np.linalg.norm(A - S.Z @ S.T @ S.Z.conj().T) / np.linalg.norm(A) / (n * eps)
+    return {"workload": "256x256 ComplexF64, re/im N(0,1/2), seed 0, Z accumulated", "gpu_s": gpu_s,
+            "gpu_kernel_ms": kernel_ms, "cpu_oracle_s": cpu_s, "cpu_oracle_cores": 1,
+            "backward_err_n_eps": float(be), "flops_100n3": 100.0 * n ** 3}
+
+
 def measure_per_matrix(ctx, packed, ns, offs, sample=200):
     """The plain FP64 path one matrix per call (gs_schur_f64 with device buffers,
     synchronised per call) on the first `sample` matrices of the batch: what a caller
@@ -431,6 +501,8 @@ def measure_complex_and_adjoint(ctx, torch, dev, stream, steps=3):
     from genericschur_gb300 import _capi
     from genericschur_gb300.workloads import adjoint_batch, batched_cplx, cplx_flops, logsumexp_loss
     out = {}
+    # the library must launch on the stream the events are recorded on
+    ctx.set_stream(stream.cuda_stream)
 
     def timed(fn, k):
         for _ in range(2):
@@ -491,6 +563,7 @@ def measure_complex_and_adjoint(ctx, torch, dev, stream, steps=3):
                          "ms_per_step": ms,
                          "workload": "4096 ComplexF64 64x64, entries complex N(0,1/2)/8, seed 7, "
                                      "loss sum logsumexp(Re(l)/0.1)"}
+    ctx.set_stream(None)
     return out
 
 
