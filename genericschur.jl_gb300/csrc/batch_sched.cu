@@ -1,5 +1,6 @@
 // Work-queue construction for the persistent batched kernels: a counting sort of
-// the matrices by order, largest first, split into the size bins of kBinMax.
+// the matrices by order, largest first, split into the size bins (bounds: the largest
+// order of each bin, ascending).
 // Runs on the device so that the whole batched pipeline is graph-capturable and
 // needs no host round trip to read the orders.  Orders outside [0, kSmallMax] (possible
 // when the orders live in device memory and were never checked on the host) are counted
@@ -11,7 +12,8 @@ namespace gsk {
 namespace {
 
 __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, int count,
-                                                   int* __restrict__ order, int* __restrict__ sched) {
+                                                   int* __restrict__ order, int* __restrict__ sched,
+                                                   BinBounds bounds) {
   __shared__ int hist[kSmallMax + 1];
   __shared__ int pos[kSmallMax + 1];
   for (int i = threadIdx.x; i <= kSmallMax; i += blockDim.x) hist[i] = 0;
@@ -27,7 +29,7 @@ __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, i
     int bin = kNumBins - 1;
     sched[3 * bin] = 0;
     for (int n = kSmallMax; n >= 0; --n) {
-      while (bin > 0 && n <= bin_max(bin - 1)) {
+      while (bin > 0 && n <= bounds.b[bin - 1]) {
         sched[3 * bin + 1] = run;
         --bin;
         sched[3 * bin] = run;
@@ -53,9 +55,35 @@ __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, i
 
 }  // namespace
 
-cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s) {
-  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched);
+cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, const BinBounds& bounds,
+                            cudaStream_t s) {
+  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched, bounds);
   return cudaGetLastError();
+}
+
+cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s) {
+  BinBounds d;
+  for (int i = 0; i < kNumBins; ++i) d.b[i] = bin_max(i);
+  return launch_bin_sort(ns, count, order, sched, d, s);
+}
+
+BinTuning default_tuning_real() {
+  return BinTuning{{32, 64, 96, 128}, {64, 64, 128, 128}, {1, 1, 0, 0}, {0, 0, 0, 0}};
+}
+BinTuning default_tuning_cplx() {
+  return BinTuning{{32, 64, 96, 128}, {64, 64, 128, 128}, {1, 1, 0, 0}, {0, 0, 0, 0}};
+}
+
+// Largest dynamic shared memory a CTA may use on sm_103 (227 KiB), less the kernels'
+// static shared memory.
+static constexpr size_t kMaxDynSmem = 227 * 1024 - 1024;
+
+bool tuning_shape_ok(bool cplx, int nmax, int nt, int hsmem) {
+  bool known = false;
+  for (int t : kTuneThreads) known |= (t == nt);
+  if (!known || nmax < 1 || nmax > kSmallMax) return false;
+  const size_t b = cplx ? cplx_bin_smem_bytes(nmax, hsmem) : real_bin_smem_bytes(nmax, hsmem);
+  return b <= kMaxDynSmem;
 }
 
 }  // namespace gsk

@@ -397,19 +397,52 @@ cudaError_t launch_absmax(const double* A, size_t cnt, unsigned long long* out, 
 // [start, end) range of that bin inside the sorted work order and a queue ticket
 // counter: sched[3*bin + {0,1,2}].
 constexpr int kNumBins = 4;
-__host__ __device__ constexpr int bin_max(int bin) { return 32 * (bin + 1); }  // 32, 64, 96, 128
+__host__ __device__ constexpr int bin_max(int bin) { return 32 * (bin + 1); }  // 32, 64, 96, 128 (defaults)
+
+// Launch shape of the persistent batched kernels, per size bin: the largest order of
+// the bin (ascending, the last one kSmallMax), threads per CTA, whether the
+// Hessenberg phase runs on a full copy of the matrix in shared memory, and a cap on
+// resident CTAs per SM (0: as many as fit).  Chosen per GPU by the tuner
+// (tune.py) and loaded with gs_set_tuning; the defaults are the hand-picked shapes.
+struct BinTuning {
+  int bounds[kNumBins];
+  int nt[kNumBins];
+  int hsmem[kNumBins];
+  int ctas[kNumBins];
+};
+BinTuning default_tuning_real();
+BinTuning default_tuning_cplx();
+// Thread counts compiled for the FP64 real and the complex kernels (the tuner's
+// candidates); other values are rejected by the table parser.
+constexpr int kTuneThreads[] = {64, 96, 128, 160, 192, 256};
+// Whether (nt, hsmem) is a compiled shape whose shared memory fits for orders up to
+// nmax: real FP64 (cplx = false) or complex (cplx = true).
+bool tuning_shape_ok(bool cplx, int nmax, int nt, int hsmem);
+size_t real_bin_smem_bytes(int nmax, int hsmem);
+size_t cplx_bin_smem_bytes(int nmax, int hsmem);
+struct BinBounds {
+  int b[kNumBins];
+};
 
 // Sorting/binning kernel: order[] lists matrix indices grouped by bin, largest
 // order first inside a bin; sched[] receives the bin ranges and zeroed counters.
+// Without `bounds`, the default bins (bin_max).
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s);
+cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, const BinBounds& bounds,
+                            cudaStream_t s);
 
 // T = double: the FP64 batched kernel; T = float: the same algorithm in FP32 (the
 // Float32 entry points and the FP32 stage of the mixed-precision form).  W is the
-// type of the eigenvalue outputs.
+// type of the eigenvalue outputs.  Without `tun`, the default shapes; the FP32
+// instances always run the default shapes.
 template <class T, class W>
 cudaError_t launch_schur_batched_real(const RealBatchT<T, W>& bt, const int* order, int* sched,
                                       int num_sms, cudaStream_t* streams, int nstreams);
+cudaError_t launch_schur_batched_real_tuned(const RealBatchT<double, double>& bt, const int* order, int* sched,
+                                            int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun);
 cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched,
                                       int num_sms, cudaStream_t* streams, int nstreams);
+cudaError_t launch_schur_batched_cplx_tuned(const CplxBatch& bt, const int* order, int* sched, int num_sms,
+                                            cudaStream_t* streams, int nstreams, const BinTuning& tun);
 
 }  // namespace gsk

@@ -35,6 +35,11 @@ struct gs_context {
   // cached graph of the batched launch sequence
   cudaGraphExec_t gexec = nullptr;
   std::vector<long long> gkey;
+  // launch shapes of the batched kernels (gs_set_tuning); tun_gen changes with them
+  BinTuning tun_real = default_tuning_real();
+  BinTuning tun_cplx = default_tuning_cplx();
+  long long tun_gen = 0;
+  std::string tun_source = "built-in defaults";
 };
 
 namespace {
@@ -185,17 +190,107 @@ int gs_host_free(gs_context* ctx, void* ptr) {
 }
 
 // ---------------------------------------------------------------------------
+// tuning table of the batched kernels
+// ---------------------------------------------------------------------------
+static std::string tuning_text(const gs_context* ctx) {
+  std::string t = "# gschur_gb300 batched tuning (" + ctx->tun_source + ")\n# kind bin nmax threads hsmem ctas_per_sm\n";
+  char line[128];
+  for (int k = 0; k < 2; ++k) {
+    const BinTuning& b = k ? ctx->tun_cplx : ctx->tun_real;
+    for (int i = 0; i < kNumBins; ++i) {
+      snprintf(line, sizeof(line), "%s %d %d %d %d %d\n", k ? "complex_f64" : "real_f64", i, b.bounds[i], b.nt[i],
+               b.hsmem[i], b.ctas[i]);
+      t += line;
+    }
+  }
+  return t;
+}
+
+int gs_set_tuning(gs_context* ctx, const char* path) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  BinTuning tr = default_tuning_real(), tc = default_tuning_cplx();
+  std::string source = "built-in defaults";
+  if (path && path[0]) {
+    FILE* f = fopen(path, "r");
+    if (!f) return set_err(ctx, GS_BADARG, "tuning table %s: cannot open", path);
+    char line[512];
+    int lineno = 0, rc = GS_OK;
+    while (rc == GS_OK && fgets(line, sizeof(line), f)) {
+      ++lineno;
+      char* p = line;
+      while (*p == ' ' || *p == '\t') ++p;
+      if (*p == '#' || *p == '\n' || *p == '\r' || *p == 0) continue;
+      char kind[64];
+      int bin, nmax, nt, hs, ctas;
+      if (sscanf(p, "%63s %d %d %d %d %d", kind, &bin, &nmax, &nt, &hs, &ctas) != 6) {
+        rc = set_err(ctx, GS_BADARG, "tuning table %s:%d: expected 'kind bin nmax threads hsmem ctas_per_sm'", path,
+                     lineno);
+        break;
+      }
+      const int k = !strcmp(kind, "real_f64") ? 0 : (!strcmp(kind, "complex_f64") ? 1 : -1);
+      if (k < 0 || bin < 0 || bin >= kNumBins || ctas < 0 || (hs != 0 && hs != 1) ||
+          !tuning_shape_ok(k == 1, nmax, nt, hs)) {
+        rc = set_err(ctx, GS_BADARG, "tuning table %s:%d: unknown kind, bin, or a shape that is not compiled or does "
+                     "not fit in shared memory", path, lineno);
+        break;
+      }
+      BinTuning& b = k ? tc : tr;
+      b.bounds[bin] = nmax;
+      b.nt[bin] = nt;
+      b.hsmem[bin] = hs;
+      b.ctas[bin] = ctas;
+    }
+    fclose(f);
+    if (rc != GS_OK) return rc;
+    for (int k = 0; k < 2; ++k) {
+      const BinTuning& b = k ? tc : tr;
+      for (int i = 0; i < kNumBins; ++i)
+        if (b.bounds[i] < 1 || (i > 0 && b.bounds[i] <= b.bounds[i - 1]))
+          return set_err(ctx, GS_BADARG, "tuning table %s: bin bounds must increase", path);
+      if (b.bounds[kNumBins - 1] != kSmallMax)
+        return set_err(ctx, GS_BADARG, "tuning table %s: the last bin must end at %d", path, kSmallMax);
+      for (int i = 0; i < kNumBins; ++i)  // a bin whose bound moved must still fit its shape
+        if (!tuning_shape_ok(k == 1, b.bounds[i], b.nt[i], b.hsmem[i]))
+          return set_err(ctx, GS_BADARG, "tuning table %s: bin %d shape does not fit", path, i);
+    }
+    source = path;
+  }
+  ctx->tun_real = tr;
+  ctx->tun_cplx = tc;
+  ctx->tun_source = source;
+  ++ctx->tun_gen;
+  return GS_OK;
+}
+
+int gs_get_tuning(const gs_context* ctx, char* buf, size_t len) {
+  if (!ctx || !buf || len == 0) return GS_BADARG;
+  const std::string t = tuning_text(ctx);
+  const size_t m = std::min(len - 1, t.size());
+  memcpy(buf, t.data(), m);
+  buf[m] = 0;
+  return t.size() < len ? GS_OK : GS_BADARG;
+}
+
+// ---------------------------------------------------------------------------
 // batched real
 // ---------------------------------------------------------------------------
 }  // extern "C"
 template <class T, class W>
 static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* order, int* sched, unsigned flags,
                             bool use_graph, const std::vector<long long>& key) {
+  // FP64 runs the context's tuned shapes; the FP32 instances the defaults
+  constexpr bool tuned = sizeof(T) == 8 && sizeof(W) == 8;
+  BinBounds bounds;
+  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
   auto enqueue = [&](cudaStream_t s) -> int {
-    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, s);
+    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, bounds, s);
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
     return fork_join(ctx, s, [&](cudaStream_t* aux) {
-      return launch_schur_batched_real(bt, order, sched, ctx->num_sms, aux, kNumBins);
+      if constexpr (tuned)
+        return launch_schur_batched_real_tuned(bt, order, sched, ctx->num_sms, aux, kNumBins, ctx->tun_real);
+      else
+        return launch_schur_batched_real(bt, order, sched, ctx->num_sms, aux, kNumBins);
     });
   };
   CK(cudaEventRecord(ctx->t0, ctx->stream));
@@ -296,7 +391,7 @@ static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t
   }
   std::vector<long long> key = {(long long)sizeof(T), (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
                                 (long long)(uintptr_t)bt.ns, (long long)(uintptr_t)bt.wr,
-                                (long long)(uintptr_t)order, (long long)flags};
+                                (long long)(uintptr_t)order, (long long)flags, ctx->tun_gen};
   rc = run_batched_real(ctx, bt, order, sched, flags, (flags & GS_GRAPH) != 0, key);
   if (rc) return rc;
   if (dev) return GS_OK;
@@ -460,11 +555,13 @@ int gs_schur_f32(gs_context* ctx, int64_t n, float* A, int64_t lda, float* Z, in
 // ---------------------------------------------------------------------------
 static int run_batched_cplx(gs_context* ctx, const CplxBatch& bt, int* order, int* sched, bool use_graph,
                             const std::vector<long long>& key) {
+  BinBounds bounds;
+  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = ctx->tun_cplx.bounds[i];
   auto enqueue = [&](cudaStream_t s) -> int {
-    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, s);
+    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, bounds, s);
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
     return fork_join(ctx, s, [&](cudaStream_t* aux) {
-      return launch_schur_batched_cplx(bt, order, sched, ctx->num_sms, aux, kNumBins);
+      return launch_schur_batched_cplx_tuned(bt, order, sched, ctx->num_sms, aux, kNumBins, ctx->tun_cplx);
     });
   };
   CK(cudaEventRecord(ctx->t0, ctx->stream));
@@ -562,7 +659,7 @@ int gs_schur_batched_c64(gs_context* ctx, int64_t count, const int32_t* ns, cons
   }
   std::vector<long long> key = {2, (long long)count, (long long)(uintptr_t)bt.A, (long long)(uintptr_t)bt.Z,
                                 (long long)(uintptr_t)bt.ns, (long long)(uintptr_t)bt.w,
-                                (long long)(uintptr_t)order, (long long)flags};
+                                (long long)(uintptr_t)order, (long long)flags, ctx->tun_gen};
   rc = run_batched_cplx(ctx, bt, order, sched, (flags & GS_GRAPH) != 0, key);
   if (rc) return rc;
   if (dev) return GS_OK;

@@ -543,19 +543,37 @@ __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __re
   }
 }
 
+size_t cbin_smem_bytes(int nmax, bool hsmem) {
+  const size_t hsize = hsmem ? (size_t)nmax * (nmax | 1) : (size_t)pk_off(nmax + 1);
+  return sizeof(double2) * (hsize + 4 * (size_t)nmax) + 32 * sizeof(double) + 64;
+}
+
 template <int NT, bool HSMEM>
-cudaError_t launch_bin_c(const CplxBatch& bt, const int* order, int* sched, int bin, int num_sms, cudaStream_t s) {
-  const int nmax = bin_max(bin);
-  const size_t hsize = HSMEM ? (size_t)nmax * (nmax | 1) : (size_t)pk_off(nmax + 1);
-  const size_t smem = sizeof(double2) * (hsize + 4 * nmax) + 32 * sizeof(double) + 64;
+cudaError_t launch_bin_c(const CplxBatch& bt, const int* order, int* sched, int bin, int nmax, int ctas, int num_sms,
+                         cudaStream_t s) {
+  const size_t smem = cbin_smem_bytes(nmax, HSMEM);
   cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<NT, HSMEM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM, false>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
+  if (ctas > 0 && per_sm > ctas) per_sm = ctas;
   k_schur_cplx<NT, HSMEM, false><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin, nmax);
   return cudaGetLastError();
+}
+
+// One bin with the requested shape (every shape of kTuneThreads, with and without the
+// shared-memory Hessenberg phase).
+cudaError_t launch_shape_c(const CplxBatch& bt, const int* order, int* sched, int bin, int nmax, int nt, int hsmem,
+                           int ctas, int num_sms, cudaStream_t s) {
+#define GS_SHAPE(NTV, HS) \
+  if (nt == NTV && (hsmem != 0) == HS) return launch_bin_c<NTV, HS>(bt, order, sched, bin, nmax, ctas, num_sms, s);
+  GS_SHAPE(64, true) GS_SHAPE(64, false) GS_SHAPE(96, true) GS_SHAPE(96, false)
+  GS_SHAPE(128, true) GS_SHAPE(128, false) GS_SHAPE(160, true) GS_SHAPE(160, false)
+  GS_SHAPE(192, true) GS_SHAPE(192, false) GS_SHAPE(256, true) GS_SHAPE(256, false)
+#undef GS_SHAPE
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -573,14 +591,23 @@ cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* or
 
 size_t cplx_large_hws_elems(int n) { return (size_t)pk_off(n + 1); }
 
-cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched, int num_sms,
-                                      cudaStream_t* streams, int nstreams) {
-  cudaError_t e;
-  if ((e = launch_bin_c<128, false>(bt, order, sched, 3, num_sms, streams[0 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin_c<128, false>(bt, order, sched, 2, num_sms, streams[1 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin_c<64, true>(bt, order, sched, 1, num_sms, streams[2 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin_c<64, true>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
+cudaError_t launch_schur_batched_cplx_tuned(const CplxBatch& bt, const int* order, int* sched, int num_sms,
+                                            cudaStream_t* streams, int nstreams, const BinTuning& t) {
+  // largest bin first: it carries most of the work
+  for (int i = 0; i < kNumBins; ++i) {
+    const int bin = kNumBins - 1 - i;
+    cudaError_t e = launch_shape_c(bt, order, sched, bin, t.bounds[bin], t.nt[bin], t.hsmem[bin], t.ctas[bin],
+                                   num_sms, streams[i % nstreams]);
+    if (e != cudaSuccess) return e;
+  }
   return cudaSuccess;
 }
+
+cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched, int num_sms,
+                                      cudaStream_t* streams, int nstreams) {
+  return launch_schur_batched_cplx_tuned(bt, order, sched, num_sms, streams, nstreams, default_tuning_cplx());
+}
+
+size_t cplx_bin_smem_bytes(int nmax, int hsmem) { return cbin_smem_bytes(nmax, hsmem != 0); }
 
 }  // namespace gsk

@@ -411,10 +411,15 @@ __device__ void solve_real(const RealBatchT<T, W>& bt, int b, int nmax, T* smem,
           __syncwarp();
           if (lane == 0) make_refl(H, k + 1, iend, c.r[cur ^ 1], lg);
         } else {
+          // one task list: far columns k+3..n (left), then far rows 1..k-1 (right)
           const int ft = tid - 32;
           constexpr int NF = NT - 32;
-          for (int j = k + 3 + ft; j <= n; j += NF) left3(H, k, j, r);
-          for (int i = 1 + ft; i <= k - 1; i += NF) right3(H, k, i, r);
+          const int nl = n - k - 2;
+          const int ntask = nl + k - 1;
+          for (int t = ft; t < ntask; t += NF) {
+            if (t < nl) left3(H, k, k + 3 + t, r);
+            else right3(H, k, t - nl + 1, r);
+          }
         }
         __syncthreads();
         cur ^= 1;
@@ -516,7 +521,7 @@ __device__ void solve_real(const RealBatchT<T, W>& bt, int b, int nmax, T* smem,
 
 template <class T, class W, int NT, bool HSMEM>
 __global__ void __launch_bounds__(NT) k_schur_real(RealBatchT<T, W> bt, const int* __restrict__ order,
-                                                   int* __restrict__ sched, int bin) {
+                                                   int* __restrict__ sched, int bin, int nmax) {
   extern __shared__ double smem_raw[];
   T* smem = (T*)smem_raw;
   __shared__ Ctl<T> c;
@@ -528,38 +533,73 @@ __global__ void __launch_bounds__(NT) k_schur_real(RealBatchT<T, W> bt, const in
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_real<T, W, NT, HSMEM>(bt, order[job], bin_max(bin), smem, c);
+    solve_real<T, W, NT, HSMEM>(bt, order[job], nmax, smem, c);
   }
 }
 
-template <class T, class W, int NT, bool HSMEM>
-cudaError_t launch_bin(const RealBatchT<T, W>& bt, const int* order, int* sched, int bin, int num_sms, cudaStream_t s) {
-  const int nmax = bin_max(bin);
-  const size_t full = HSMEM ? (size_t)nmax * (nmax | 1) : 0;
+// Dynamic shared memory of one CTA for orders up to nmax: the packed H of the QR phase
+// (or the full matrix of the Hessenberg phase, hsmem), tau, the reflector log and the
+// reduction scratch.
+size_t bin_smem_elems(int nmax, bool hsmem) {
+  const size_t full = hsmem ? (size_t)nmax * (nmax | 1) : 0;
   const size_t hreg = full > (size_t)rpk(nmax + 1) ? full : (size_t)rpk(nmax + 1);
-  const size_t smem = sizeof(T) * (hreg + 6 * nmax + 32);
+  return hreg + 6 * (size_t)nmax + 32;
+}
+
+template <class T, class W, int NT, bool HSMEM>
+cudaError_t launch_bin(const RealBatchT<T, W>& bt, const int* order, int* sched, int bin, int nmax, int ctas,
+                       int num_sms, cudaStream_t s) {
+  const size_t smem = sizeof(T) * bin_smem_elems(nmax, HSMEM);
   cudaError_t e = cudaFuncSetAttribute(k_schur_real<T, W, NT, HSMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_real<T, W, NT, HSMEM>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  k_schur_real<T, W, NT, HSMEM><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin);
+  if (ctas > 0 && per_sm > ctas) per_sm = ctas;
+  k_schur_real<T, W, NT, HSMEM><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin, nmax);
   return cudaGetLastError();
+}
+
+// One bin with the requested shape.  FP64 compiles every shape of kTuneThreads with
+// and without the shared-memory Hessenberg phase; FP32 only the default shapes.
+template <class T, class W>
+cudaError_t launch_shape(const RealBatchT<T, W>& bt, const int* order, int* sched, int bin, int nmax, int nt,
+                         int hsmem, int ctas, int num_sms, cudaStream_t s) {
+#define GS_SHAPE(NTV, HS) \
+  if (nt == NTV && (hsmem != 0) == HS) return launch_bin<T, W, NTV, HS>(bt, order, sched, bin, nmax, ctas, num_sms, s);
+  if constexpr (sizeof(T) == 8) {
+    GS_SHAPE(64, true) GS_SHAPE(64, false) GS_SHAPE(96, true) GS_SHAPE(96, false)
+    GS_SHAPE(128, true) GS_SHAPE(128, false) GS_SHAPE(160, true) GS_SHAPE(160, false)
+    GS_SHAPE(192, true) GS_SHAPE(192, false) GS_SHAPE(256, true) GS_SHAPE(256, false)
+  } else {
+    GS_SHAPE(64, true) GS_SHAPE(128, false)
+  }
+#undef GS_SHAPE
+  return cudaErrorInvalidValue;
+}
+
+template <class T, class W>
+cudaError_t launch_all_bins(const RealBatchT<T, W>& bt, const int* order, int* sched, int num_sms,
+                            cudaStream_t* streams, int nstreams, const BinTuning& t) {
+  // largest bin first: it carries most of the work
+  for (int i = 0; i < kNumBins; ++i) {
+    const int bin = kNumBins - 1 - i;
+    cudaError_t e = launch_shape(bt, order, sched, bin, t.bounds[bin], t.nt[bin], t.hsmem[bin], t.ctas[bin], num_sms,
+                                 streams[i % nstreams]);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
 
+size_t real_bin_smem_bytes(int nmax, int hsmem) { return sizeof(double) * bin_smem_elems(nmax, hsmem != 0); }
+
 template <class T, class W>
 cudaError_t launch_schur_batched_real(const RealBatchT<T, W>& bt, const int* order, int* sched, int num_sms,
                                       cudaStream_t* streams, int nstreams) {
-  cudaError_t e;
-  // largest bin first: it carries most of the work
-  if ((e = launch_bin<T, W, 128, false>(bt, order, sched, 3, num_sms, streams[0 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<T, W, 128, false>(bt, order, sched, 2, num_sms, streams[1 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<T, W, 64, true>(bt, order, sched, 1, num_sms, streams[2 % nstreams])) != cudaSuccess) return e;
-  if ((e = launch_bin<T, W, 64, true>(bt, order, sched, 0, num_sms, streams[3 % nstreams])) != cudaSuccess) return e;
-  return cudaSuccess;
+  return launch_all_bins(bt, order, sched, num_sms, streams, nstreams, default_tuning_real());
 }
 template cudaError_t launch_schur_batched_real<double, double>(const RealBatchT<double, double>&, const int*, int*, int,
                                                                cudaStream_t*, int);
@@ -567,5 +607,10 @@ template cudaError_t launch_schur_batched_real<float, double>(const RealBatchT<f
                                                               cudaStream_t*, int);
 template cudaError_t launch_schur_batched_real<float, float>(const RealBatchT<float, float>&, const int*, int*, int,
                                                              cudaStream_t*, int);
+
+cudaError_t launch_schur_batched_real_tuned(const RealBatchT<double, double>& bt, const int* order, int* sched,
+                                            int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun) {
+  return launch_all_bins(bt, order, sched, num_sms, streams, nstreams, tun);
+}
 
 }  // namespace gsk

@@ -10,6 +10,9 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "lib", "libgschur_gb300.so")
+# launch shapes of the batched kernels chosen by tune.py on a GB300 (sm_103a, the only
+# target this library is built for)
+DEFAULT_TUNING = os.path.join(HERE, "tuning", "sm_103a.tsv")
 
 GS_OK = 0
 GS_UNCONVERGED = 1
@@ -40,6 +43,8 @@ SIGNATURES = {
     "gs_last_kernel_ms": (ctypes.c_float, [_p]),
     "gs_host_alloc": (_i, [_p, ctypes.POINTER(_p), ctypes.c_size_t]),
     "gs_host_free": (_i, [_p, _p]),
+    "gs_set_tuning": (_i, [_p, ctypes.c_char_p]),
+    "gs_get_tuning": (_i, [_p, ctypes.c_char_p, ctypes.c_size_t]),
     "gs_schur_f64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
     "gs_schur_f32": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
     "gs_schur_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _u, _i64, _i64]),
@@ -133,10 +138,26 @@ class Context:
             msg = self.last_error()
             raise GSError(rc, "gs_create failed: %s" % msg)
         self.device = device
+        # the committed table of tuned launch shapes (GS_TUNING overrides; "" keeps the defaults)
+        path = os.environ.get("GS_TUNING", DEFAULT_TUNING)
+        if path and os.path.exists(path):
+            self.set_tuning(path)
 
     def last_error(self):
         s = self.lib.gs_last_error(self.handle)
         return s.decode() if s else ""
+
+    def set_tuning(self, path):
+        """Load a batched-kernel tuning table (None: the built-in shapes)."""
+        rc = self.lib.gs_set_tuning(self.handle, path.encode() if path else None)
+        if rc != GS_OK:
+            raise GSError(rc, self.last_error())
+
+    def tuning(self):
+        """The active tuning table as text."""
+        buf = ctypes.create_string_buffer(4096)
+        self.lib.gs_get_tuning(self.handle, buf, ctypes.c_size_t(len(buf)))
+        return buf.value.decode()
 
     def set_stream(self, stream_ptr):
         self.lib.gs_set_stream(self.handle, _p(stream_ptr) if stream_ptr else None)

@@ -71,6 +71,20 @@ GS_API const char* gs_last_error(const gs_context* ctx);
  * (CUDA events on the context stream; host<->device copies excluded). */
 GS_API float gs_last_kernel_ms(const gs_context* ctx);
 
+/* Launch shapes of the batched kernels (no reference counterpart: the reference has no
+ * batched form).  gs_set_tuning loads a table written by the project's tuner
+ * (genericschur.jl_gb300/tune.py) for this context: per size bin of the real FP64 and
+ * the complex batched Schur kernels, the bin's largest order, threads per CTA, whether
+ * the Hessenberg phase runs in shared memory, and a cap on CTAs per SM.  Text lines
+ * "kind bin nmax threads hsmem ctas_per_sm" (kind real_f64 or complex_f64; '#' starts a
+ * comment; bins not listed keep their defaults).  path NULL or "" restores the built-in
+ * defaults.  GS_BADARG (message in gs_last_error) for an unreadable file, a shape that is
+ * not compiled or does not fit in shared memory, or bounds that do not increase to 128;
+ * the context keeps its previous shapes then.  Results do not depend on the shapes
+ * beyond rounding.  gs_get_tuning writes the active table (same format) into buf. */
+GS_API int gs_set_tuning(gs_context* ctx, const char* path);
+GS_API int gs_get_tuning(const gs_context* ctx, char* buf, size_t len);
+
 /* Pinned host memory for fast host<->device staging. */
 GS_API int gs_host_alloc(gs_context* ctx, void** ptr, size_t bytes);
 GS_API int gs_host_free(gs_context* ctx, void* ptr);
