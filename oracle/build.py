@@ -26,8 +26,32 @@ def _stale():
     return False
 
 
+MP_LIB = os.path.join(OUT_DIR, "liboracle_mpfr.so")
+MP_SOURCES = ["oracle_mpfr.cpp"]
+MP_HEADERS = ["scalar.hpp", "mp256.hpp", "gschur_oracle.hpp"]
+
+
+def build_mpfr(force=False):
+    """The 256-bit (BigFloat-precision) instance of the Schur restatement, linked against
+    libmpfr.so.6.  Optional: it only generates the committed high-precision fixtures, so a
+    machine without MPFR skips it.  Returns the library path or None."""
+    if not force and os.path.exists(MP_LIB) and all(
+            os.path.getmtime(os.path.join(HERE, f)) <= os.path.getmtime(MP_LIB)
+            for f in MP_SOURCES + MP_HEADERS + ["build.py"]):
+        return MP_LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    cmd = ["g++", "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", MP_LIB + ".tmp"] + \
+        [os.path.join(HERE, s) for s in MP_SOURCES] + ["-l:libmpfr.so.6"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    os.replace(MP_LIB + ".tmp", MP_LIB)
+    return MP_LIB
+
+
 def build(force=False):
     """Compile the oracle shared library if it is missing or stale; return its path."""
+    build_mpfr(force)
     if not force and not _stale():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)

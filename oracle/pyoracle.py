@@ -165,6 +165,52 @@ def gschur_cplx_quad(A):
     return T, Z, w, tuple(res)
 
 
+_mplib = None
+
+
+def mplib():
+    """The 256-bit MPFR instance (oracle/_build/liboracle_mpfr.so), built on demand."""
+    global _mplib
+    if _mplib is None:
+        path = _build.build_mpfr()
+        if path is None:
+            raise OSError("the 256-bit oracle needs libmpfr.so.6")
+        _mplib = ctypes.CDLL(path)
+        for name in ("or_gschur_mp", "or_gschur_zmp"):
+            getattr(_mplib, name).restype = ctypes.c_int
+    return _mplib
+
+
+def gschur_mp(A):
+    """Real Schur in 256-bit arithmetic (BigFloat precision).  Returns (T, Z, w,
+    (backward_err, orth_err)) with T, Z, w rounded to FP64."""
+    A = _f(A, np.float64)
+    n = A.shape[0]
+    T = np.zeros((n, n), order="F")
+    Z = np.zeros((n, n), order="F")
+    wr = np.zeros(n)
+    wi = np.zeros(n)
+    res = np.zeros(2)
+    st = mplib().or_gschur_mp(ctypes.c_int(n), _ptr(A), _ptr(T), _ptr(Z), _ptr(wr), _ptr(wi), _ptr(res))
+    if st:
+        raise Unconverged("iteration limit reached")
+    return T, Z, wr + 1j * wi, tuple(res)
+
+
+def gschur_cplx_mp(A):
+    """Complex Schur in 256-bit arithmetic (BigFloat precision)."""
+    A = _f(A, np.complex128)
+    n = A.shape[0]
+    T = np.zeros((n, n), dtype=np.complex128, order="F")
+    Z = np.zeros((n, n), dtype=np.complex128, order="F")
+    w = np.zeros(n, dtype=np.complex128)
+    res = np.zeros(2)
+    st = mplib().or_gschur_zmp(ctypes.c_int(n), _ptr(A), _ptr(T), _ptr(Z), _ptr(w), _ptr(res))
+    if st:
+        raise Unconverged("iteration limit reached")
+    return T, Z, w, tuple(res)
+
+
 def eigvecs(T, Z, left=False, normalize=True):
     """Eigenvectors from a Schur pair (vectors.jl:12-20 -> _geigvecs!/_gleigvecs!)."""
     n = T.shape[0]

@@ -10,7 +10,8 @@ environment, so these fixtures pin the oracle against regressions only; the
 oracle's agreement with the reference rests on the reference's own known answers
 and property tests (tests/test_oracle.py).
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [mp256]
+(mp256 alone regenerates only tests/golden/mp256_n256.npz, the 256-bit fixture.)
 """
 import os
 import sys
@@ -56,5 +57,27 @@ def quad():
     print("quad residuals", resc, resr)
 
 
+def mp256():
+    """tests/golden/mp256_n256.npz: the same two n = 256 inputs decomposed by the oracle in
+    256-bit MPFR arithmetic -- BigFloat's default precision, which the reference's own
+    high-precision Schur runs use -- eigenvalues rounded to FP64, and that run's
+    backward and orthogonality errors (needs libmpfr.so.6; about ten minutes)."""
+    sys.path.insert(0, os.path.join(ROOT, "genericschur.jl_gb300"))
+    from genericschur_gb300.workloads import conditioned_matrix
+    n = 256
+    rng = np.random.default_rng(0)
+    Ac = np.asfortranarray((rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2))
+    _, _, wc, resc = po.gschur_cplx_mp(Ac)
+    Ar = conditioned_matrix(n, seed=6)
+    _, _, wr, resr = po.gschur_mp(Ar)
+    np.savez_compressed(os.path.join(HERE, "mp256_n256.npz"), A_c256=Ac, w_c256=wc, res_c256=np.array(resc),
+                        A_cond256=Ar, w_cond256=wr, res_cond256=np.array(resr))
+    print("256-bit residuals", resc, resr)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "mp256":
+        mp256()
+    else:
+        main()
+        mp256()

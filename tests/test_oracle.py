@@ -46,6 +46,66 @@ def test_godunov_complex_quad():
     assert np.allclose(got, vals, atol=max(t, 1e-12))
 
 
+def _mp_available():
+    try:
+        po.mplib()
+        return True
+    except OSError:
+        return False
+
+
+@pytest.mark.skipif(not _mp_available(), reason="the 256-bit oracle needs libmpfr.so.6")
+def test_godunov_256bit():
+    """Godunov's known answer at BigFloat precision (256 bits), as the reference's BigFloat
+    tests run it: with delta ~ 2^-256 ||A|| the eigenvalues (condition ~7e16) are exact to
+    far below FP64 rounding, so they round to {-4, -2, -1, 0, 1, 2, 4} (test/real.jl:142-157,
+    test/testfuncs.jl:127-142), real and complex drivers alike."""
+    A, vals, econd = godunov()
+    for fn, M in ((po.gschur_mp, A), (po.gschur_cplx_mp, A.astype(np.complex128))):
+        T, Z, w, (be, oe) = fn(M)
+        assert be < 100 * 2.0 ** -255 and oe < 100 * 2.0 ** -255
+        t = 3 * be * np.linalg.norm(A) * econd
+        assert t < 1e-50
+        got = w[np.lexsort((w.imag, w.real))]
+        assert np.all(np.abs(got.imag) <= 1e-50)
+        assert np.allclose(got.real, vals, rtol=0, atol=1e-50)
+
+
+@pytest.mark.skipif(not _mp_available(), reason="the 256-bit oracle needs libmpfr.so.6")
+@pytest.mark.parametrize("n", [5, 24])
+def test_oracle_256bit_vs_113bit(n):
+    """The 256-bit and 113-bit instances of the same restatement agree on random inputs
+    (to FP64 rounding of the 113-bit eigenvalues), with residuals at their own precision."""
+    rng = np.random.default_rng(7100 + n)
+    A = rng.standard_normal((n, n))
+    _, _, wm, (bm, om) = po.gschur_mp(A)
+    _, _, wq, (bq, oq) = po.gschur_quad(A)
+    assert bm < 1e-74 and om < 1e-74 and bq < 1e-31
+    assert np.max(np.abs(np.sort_complex(wm) - np.sort_complex(wq))) <= 1e-14 * np.abs(wq).max()
+
+
+def test_mp256_fixture_pins_fp64_oracle():
+    """The 256-bit fixture of the n = 256 inputs (BigFloat precision): residuals at that
+    precision, agreement with the 113-bit fixture, and the FP64 oracle's eigenvalues
+    within the parity tolerance of it."""
+    from common import eig_tolerances, match_eigenvalues
+    path = os.path.join(GOLDEN, "mp256_n256.npz")
+    if not os.path.exists(path):
+        pytest.skip("no 256-bit fixture")
+    G = np.load(path)
+    Q = np.load(os.path.join(GOLDEN, "quad_256.npz"))
+    assert max(G["res_c256"]) < 1e-70 and max(G["res_cond256"]) < 1e-70
+    for key in ("c256", "cond256"):
+        np.testing.assert_array_equal(G["A_" + key], Q["A_" + key])
+        A = G["A_" + key]
+        w, tol = eig_tolerances(A, po)
+        ok, worst = match_eigenvalues(w, G["w_" + key], tol)
+        assert ok, "%s: worst err/tol %.3g" % (key, worst)
+        # the 113-bit eigenvalues are the 256-bit ones to far below the parity tolerance
+        ok, worst = match_eigenvalues(Q["w_" + key], G["w_" + key], tol * 1e-10)
+        assert ok, "%s: 113-bit vs 256-bit worst err/tol %.3g" % (key, worst)
+
+
 @pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 32, 64])
 def test_oracle_real_random(n):
     rng = np.random.default_rng(100 + n)
