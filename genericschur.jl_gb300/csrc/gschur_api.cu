@@ -18,6 +18,8 @@
 using namespace gsk;
 
 static constexpr int kCplxLargeMax = 2048;  // single-CTA complex path for 128 < n <= this
+static constexpr int kPipeChunks = 4;       // chunks of a pipelined host-buffer batched call
+static constexpr int64_t kPipeMinCount = 2048;
 
 struct gs_context {
   int device = 0;
@@ -40,6 +42,11 @@ struct gs_context {
   BinTuning tun_cplx = default_tuning_cplx();
   long long tun_gen = 0;
   std::string tun_source = "built-in defaults";
+  // host-buffer batched calls: chunks whose copies overlap the other chunks' kernels
+  bool pipe_ready = false;
+  cudaStream_t pipe_s[kPipeChunks] = {}, pipe_aux[kPipeChunks][kNumBins] = {}, pipe_d2h = nullptr;
+  cudaEvent_t pipe_h2d[kPipeChunks] = {}, pipe_fork[kPipeChunks] = {}, pipe_join[kPipeChunks][kNumBins] = {},
+              pipe_done[kPipeChunks] = {}, pipe_out = nullptr;
 };
 
 namespace {
@@ -155,6 +162,20 @@ int gs_destroy(gs_context* ctx) {
   if (ctx->t0) cudaEventDestroy(ctx->t0);
   if (ctx->t1) cudaEventDestroy(ctx->t1);
   if (ctx->cap) cudaStreamDestroy(ctx->cap);
+  if (ctx->pipe_ready) {
+    for (int c = 0; c < kPipeChunks; ++c) {
+      cudaStreamDestroy(ctx->pipe_s[c]);
+      cudaEventDestroy(ctx->pipe_h2d[c]);
+      cudaEventDestroy(ctx->pipe_fork[c]);
+      cudaEventDestroy(ctx->pipe_done[c]);
+      for (int i = 0; i < kNumBins; ++i) {
+        cudaStreamDestroy(ctx->pipe_aux[c][i]);
+        cudaEventDestroy(ctx->pipe_join[c][i]);
+      }
+    }
+    cudaStreamDestroy(ctx->pipe_d2h);
+    cudaEventDestroy(ctx->pipe_out);
+  }
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return GS_OK;
@@ -318,6 +339,137 @@ static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* or
   return GS_OK;
 }
 
+static int pipe_setup(gs_context* ctx) {
+  if (ctx->pipe_ready) return GS_OK;
+  for (int c = 0; c < kPipeChunks; ++c) {
+    CK(cudaStreamCreateWithFlags(&ctx->pipe_s[c], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->pipe_h2d[c], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->pipe_fork[c], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->pipe_done[c], cudaEventDisableTiming));
+    for (int i = 0; i < kNumBins; ++i) {
+      CK(cudaStreamCreateWithFlags(&ctx->pipe_aux[c][i], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&ctx->pipe_join[c][i], cudaEventDisableTiming));
+    }
+  }
+  CK(cudaStreamCreateWithFlags(&ctx->pipe_d2h, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->pipe_out, cudaEventDisableTiming));
+  ctx->pipe_ready = true;
+  return GS_OK;
+}
+
+// Host-buffer batched call as a pipeline: the batch is cut into kPipeChunks runs of
+// consecutive matrices (the first and last small, so that little copying is exposed),
+// each run's inputs are copied on the context stream, its bin sort and size-bin kernels
+// run on a stream of its own once its copy has landed, and its outputs are copied back on
+// a separate stream once its kernels are done.  So the copies of one run overlap the
+// kernels of the others, and the runs' kernels overlap each other's tails.  Requires the
+// matrices to be stored in order (offsets increasing, not overlapping), which makes each
+// run one contiguous range of every buffer.  Device layout as the unpipelined call.
+template <class T>
+static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>& bt, int64_t count,
+                                        const int32_t* ns, const int64_t* offs, const int64_t* woffs, T* A, T* Z,
+                                        T* wr, T* wi, int32_t* status, int* order, int* sched, long long na,
+                                        long long nw) {
+  int rc = pipe_setup(ctx);
+  if (rc) return rc;
+  constexpr bool tuned = sizeof(T) == 8;
+  BinBounds bounds;
+  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
+  // run boundaries by cumulative n^3 work: 10%, 40%, 40%, 10%
+  double tot = 0.0;
+  for (int64_t b = 0; b < count; ++b) tot += (double)ns[b] * ns[b] * ns[b];
+  const double cut[kPipeChunks - 1] = {0.1, 0.5, 0.9};
+  int64_t edge[kPipeChunks + 1];
+  edge[0] = 0;
+  edge[kPipeChunks] = count;
+  {
+    double run = 0.0;
+    int k = 0;
+    for (int64_t b = 0; b < count && k < kPipeChunks - 1; ++b) {
+      run += (double)ns[b] * ns[b] * ns[b];
+      while (k < kPipeChunks - 1 && run >= cut[k] * tot) edge[++k] = b + 1;
+    }
+    while (k < kPipeChunks - 1) edge[++k] = count;
+  }
+  cudaStream_t s = ctx->stream;
+  // metadata for the whole batch first (small), then the runs' matrices in order
+  CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  auto a_lo = [&](int64_t b) { return (long long)offs[b]; };
+  auto a_hi = [&](int64_t b) { return (long long)offs[b - 1] + (long long)ns[b - 1] * ns[b - 1]; };
+  auto w_lo = [&](int64_t b) { return (long long)woffs[b]; };
+  auto w_hi = [&](int64_t b) { return (long long)woffs[b - 1] + ns[b - 1]; };
+  for (int c = 0; c < kPipeChunks; ++c) {
+    const int64_t b0 = edge[c], b1 = edge[c + 1];
+    if (b1 > b0) {
+      const long long lo = a_lo(b0), hi = a_hi(b1);
+      CK(cudaMemcpyAsync(bt.A + lo, A + lo, sizeof(T) * (hi - lo), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaEventRecord(ctx->pipe_h2d[c], s));
+  }
+  bool timed = false;
+  for (int c = 0; c < kPipeChunks; ++c) {
+    const int64_t b0 = edge[c], b1 = edge[c + 1];
+    cudaStream_t cs = ctx->pipe_s[c];
+    CK(cudaStreamWaitEvent(cs, ctx->pipe_h2d[c], 0));
+    if (b1 > b0) {
+      if (!timed) { CK(cudaEventRecord(ctx->t0, cs)); timed = true; }
+      RealBatchT<T, T> bc = bt;
+      bc.count = (int)(b1 - b0);
+      bc.ns = bt.ns + b0;
+      bc.offs = bt.offs + b0;
+      bc.woffs = bt.woffs + b0;
+      bc.status = bt.status + b0;
+      int* oc = order + b0;  // each run sorts its own slice of the order array
+      int* sc = sched + 3 * kNumBins * c;
+      cudaError_t e = launch_bin_sort(bc.ns, bc.count, oc, sc, bounds, cs);
+      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
+      CK(cudaEventRecord(ctx->pipe_fork[c], cs));
+      for (int i = 0; i < kNumBins; ++i) CK(cudaStreamWaitEvent(ctx->pipe_aux[c][i], ctx->pipe_fork[c], 0));
+      if constexpr (tuned)
+        e = launch_schur_batched_real_tuned(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins, ctx->tun_real);
+      else
+        e = launch_schur_batched_real(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins);
+      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+      for (int i = 0; i < kNumBins; ++i) {
+        CK(cudaEventRecord(ctx->pipe_join[c][i], ctx->pipe_aux[c][i]));
+        CK(cudaStreamWaitEvent(cs, ctx->pipe_join[c][i], 0));
+      }
+    }
+    CK(cudaEventRecord(ctx->pipe_done[c], cs));
+  }
+  // kernel time: from the first run's start to the end of every run's kernels
+  cudaStream_t last = ctx->pipe_s[kPipeChunks - 1];
+  for (int c = 0; c < kPipeChunks - 1; ++c) CK(cudaStreamWaitEvent(last, ctx->pipe_done[c], 0));
+  if (timed) {
+    CK(cudaEventRecord(ctx->t1, last));
+    ctx->timed = true;
+  }
+  cudaStream_t d = ctx->pipe_d2h;
+  for (int c = 0; c < kPipeChunks; ++c) {
+    const int64_t b0 = edge[c], b1 = edge[c + 1];
+    CK(cudaStreamWaitEvent(d, ctx->pipe_done[c], 0));
+    if (b1 <= b0) continue;
+    const long long lo = a_lo(b0), hi = a_hi(b1), wlo = w_lo(b0), whi = w_hi(b1);
+    CK(cudaMemcpyAsync(A + lo, bt.A + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
+    if (bt.Z) CK(cudaMemcpyAsync(Z + lo, bt.Z + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
+    if (whi > wlo) {
+      CK(cudaMemcpyAsync(wr + wlo, bt.wr + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
+      CK(cudaMemcpyAsync(wi + wlo, bt.wi + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
+    }
+    CK(cudaMemcpyAsync(status + b0, bt.status + b0, sizeof(int) * (b1 - b0), cudaMemcpyDeviceToHost, d));
+  }
+  CK(cudaEventRecord(ctx->pipe_out, d));
+  CK(cudaStreamWaitEvent(s, ctx->pipe_out, 0));
+  CK(cudaStreamSynchronize(s));
+  (void)na;
+  (void)nw;
+  for (int64_t b = 0; b < count; ++b)
+    if (status[b] != GS_OK) return set_err(ctx, GS_UNCONVERGED, "matrix %lld: iteration limit reached", (long long)b);
+  return GS_OK;
+}
+
 template <class T>
 static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                                    const int64_t* woffs, T* A, T* Z, T* wr, T* wi, int32_t* status, unsigned flags) {
@@ -337,18 +489,22 @@ static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t
   bt.maxiter_mult = 100;
   Arena ar;
   long long na = 0, nw = 0;
+  bool in_order = true;  // matrices stored one after another (the pipelined copy needs it)
   if (!dev) {
     for (int64_t b = 0; b < count; ++b) {
       const int n = ns[b];
       if (n < 0 || n > kSmallMax)
         return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
       if (offs[b] < 0 || woffs[b] < 0) return set_err(ctx, GS_BADARG, "matrix %lld: negative offset", (long long)b);
+      if (b > 0 && (offs[b] < offs[b - 1] + (long long)ns[b - 1] * ns[b - 1] || woffs[b] < woffs[b - 1] + ns[b - 1]))
+        in_order = false;
       na = std::max(na, (long long)offs[b] + (long long)n * n);
       nw = std::max(nw, (long long)woffs[b] + n);
     }
   }
+  const bool pipelined = !dev && !(flags & GS_GRAPH) && in_order && count >= kPipeMinCount;
   const size_t o_order = ar.take<int>(count);
-  const size_t o_sched = ar.take<int>(3 * kNumBins);
+  const size_t o_sched = ar.take<int>(3 * kNumBins * kPipeChunks);
   size_t o_A = 0, o_Z = 0, o_wr = 0, o_wi = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
   if (!dev) {
     o_A = ar.take<T>(na);
@@ -375,6 +531,9 @@ static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t
     bt.wr = (T*)(base + o_wr);
     bt.wi = (T*)(base + o_wi);
     bt.status = (int*)(base + o_st);
+    if (pipelined)
+      return schur_batched_real_pipelined<T>(ctx, bt, count, ns, offs, woffs, A, Z, wr, wi, status, order, sched, na,
+                                             nw);
     CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));

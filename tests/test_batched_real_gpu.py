@@ -174,3 +174,32 @@ def test_device_orders_out_of_range(gs, bad_n):
         q = int(woffs[b])
         assert_schur_real(A0, T[o:o + n * n].reshape(n, n, order="F"), Zh[o:o + n * n].reshape(n, n, order="F"),
                           w[q:q + n])
+
+
+def test_host_buffer_pipeline_matches(gs):
+    """Host-buffer calls of 2,048 or more matrices stored in order run as a pipeline
+    (runs of matrices whose copies overlap the other runs' kernels).  Each matrix's
+    computation does not depend on how the batch is cut, so the results equal those of
+    the unpipelined call (the graph-replayed one) bit for bit; a batch stored out of order
+    takes the unpipelined path and is correct too."""
+    from genericschur_gb300.workloads import batched_real
+    packed, ns, offs, woffs = batched_real(3000, seed=9)
+    T1, Z1, w1, s1 = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs)
+    T2, Z2, w2, s2 = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs, graph=True)
+    assert np.all(s1 == 0) and np.all(s2 == 0)
+    np.testing.assert_array_equal(T1, T2)
+    np.testing.assert_array_equal(Z1, Z2)
+    np.testing.assert_array_equal(w1, w2)
+    # reversed storage order: offsets decrease, so no pipeline
+    rev = np.arange(len(ns))[::-1]
+    T3, Z3, w3, s3 = gs.gschur_batched(packed=packed, ns=ns[rev].copy(), offs=offs[rev].copy(),
+                                       woffs=woffs[rev].copy())
+    assert np.all(s3 == 0)
+    np.testing.assert_array_equal(T3, T1)
+    np.testing.assert_array_equal(w3, w1)
+    for b in range(0, len(ns), 97):
+        n = int(ns[b])
+        o, q = int(offs[b]), int(woffs[b])
+        A = packed[o:o + n * n].reshape(n, n, order="F")
+        assert_schur_real(A, T1[o:o + n * n].reshape(n, n, order="F"), Z1[o:o + n * n].reshape(n, n, order="F"),
+                          w1[q:q + n])
