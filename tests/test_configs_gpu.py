@@ -108,12 +108,13 @@ def test_complex256_workload(gs):
     """The plain CPU-runnable workload as configured: one 256 x 256 ComplexF64 matrix,
     real and imaginary parts iid N(0, 1/2), seed 0, no balancing, Z accumulated.
     Schur properties, eigenvalues matched to the oracle's FP64 run (tolerance from the
-    oracle's eigenvectors) and to the oracle's 113-bit run (committed fixture)."""
+    oracle's eigenvectors) and to the oracle's 256-bit (BigFloat-precision) run (committed
+    fixture)."""
     import os
     n = 256
     rng = np.random.default_rng(0)
     A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(2)
-    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "quad_256.npz"))
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "mp256_n256.npz"))
     np.testing.assert_array_equal(A, G["A_c256"])
     S = gs.gschur(A)
     assert_schur_cplx(A, S.T, S.Z, S.values)
@@ -121,7 +122,7 @@ def test_complex256_workload(gs):
     ok, worst = match_eigenvalues(S.values, w_ref, tol)
     assert ok, "vs FP64 oracle: worst err/tol %.3g" % worst
     ok, worst = match_eigenvalues(S.values, G["w_c256"], tol)
-    assert ok, "vs 113-bit oracle: worst err/tol %.3g" % worst
+    assert ok, "vs 256-bit oracle: worst err/tol %.3g" % worst
 
 
 def test_differentiation_workload_plain_central_differences(gs):
