@@ -53,6 +53,13 @@ struct CplxBatch {
 };
 cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* order, int* sched, cudaStream_t s);
 size_t cplx_large_hws_elems(int n);
+// One complex matrix of order n > 128 on the whole GPU (schur_large_cplx.cu): Hessenberg
+// reduction, multishift QR, blocks <= 128 by the batched kernel.  A (device, ld n) <- T,
+// Z (or null) <- the unitary factor, w <- diag(T).  Returns ST_OK, ST_UNCONVERGED (sweep
+// limit maxsweeps, <= 0: 100 n; or a non-finite entry), or -1 with *cerr on a CUDA error.
+size_t schur_large_cplx_ws_bytes(int n);
+int schur_large_cplx_run(double2* A, double2* Z, double2* w, int n, int scale, long long maxsweeps, void* ws,
+                         int num_sms, cudaStream_t s, cudaError_t* cerr);
 
 // Eigenvectors of complex Schur factors (T upper triangular), batched.  Matrix b
 // has order ns[b] <= 128 at element offset offs[b] of T, Z, VR, VL and scratch.

@@ -17,7 +17,6 @@
 
 using namespace gsk;
 
-static constexpr int kCplxLargeMax = 2048;  // single-CTA complex path for 128 < n <= this
 static constexpr int kPipeChunks = 4;       // chunks of a pipelined host-buffer batched call
 static constexpr int64_t kPipeMinCount = 2048;
 
@@ -842,13 +841,13 @@ int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
     return set_err(ctx, GS_BADARG, "leading dimension smaller than n");
   if (n == 0) return GS_OK;
   if (!A || !w || (wantz && !Z)) return set_err(ctx, GS_BADARG, "null array argument");
-  if (n > kCplxLargeMax) return set_err(ctx, GS_BADARG, "order %lld > %d not supported for complex input", (long long)n, kCplxLargeMax);
+  if (n > (1 << 20)) return set_err(ctx, GS_BADARG, "order %lld too large", (long long)n);
   CK(cudaSetDevice(ctx->device));
   const bool dev = flags & GS_DEVICE;
   const bool large = n > kSmallMax;
   Arena ar;
   const size_t o_A = ar.take<double2>(n * n), o_Z = ar.take<double2>(n * n), o_w = ar.take<double2>(n);
-  const size_t o_h = ar.take<double2>(large ? cplx_large_hws_elems((int)n) : 1);
+  const size_t o_h = ar.take<char>(large ? schur_large_cplx_ws_bytes((int)n) : 1);
   const size_t o_meta = ar.take<long long>(4), o_st = ar.take<int>(2);
   const size_t o_order = ar.take<int>(1), o_sched = ar.take<int>(3 * kNumBins);
   int rc = ensure_ws(ctx, ar.off);
@@ -881,13 +880,14 @@ int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   bt.maxinner_mult = 30;
   bt.maxiter_abs = maxiter > 0 ? maxiter : 0;
   bt.maxinner_abs = maxinner > 0 ? maxinner : 0;
+  int st = 0;
   if (large) {
-    // one CTA, packed H in global memory (any order up to kCplxLargeMax)
-    bt.hws = (double2*)(base + o_h);
+    // the whole GPU: Hessenberg reduction and multishift QR (schur_large_cplx.cu)
     CK(cudaEventRecord(ctx->t0, s));
-    cudaError_t e = launch_bin_sort(bt.ns, 1, (int*)(base + o_order), (int*)(base + o_sched), s);
-    if (e == cudaSuccess) e = launch_schur_cplx_large(bt, (int)n, (int*)(base + o_order), (int*)(base + o_sched), s);
-    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "complex large launch: %s", cudaGetErrorString(e));
+    cudaError_t ce = cudaSuccess;
+    st = schur_large_cplx_run(dA, wantz ? dZ : nullptr, bt.w, (int)n, bt.scale, maxiter > 0 ? maxiter : 0,
+                              base + o_h, ctx->num_sms, s, &ce);
+    if (st < 0) return set_err(ctx, GS_CUDA, "complex large path: %s", cudaGetErrorString(ce));
     CK(cudaEventRecord(ctx->t1, s));
     ctx->timed = true;
   } else {
@@ -897,8 +897,7 @@ int gs_schur_c64(gs_context* ctx, int64_t n, double* A, int64_t lda, double* Z, 
   CK(cudaMemcpy2DAsync(A, lda * es, dA, n * es, n * es, n, out, s));
   if (wantz) CK(cudaMemcpy2DAsync(Z, ldz * es, dZ, n * es, n * es, n, out, s));
   CK(cudaMemcpyAsync(w, bt.w, n * es, out, s));
-  int st = 0;
-  CK(cudaMemcpyAsync(&st, bt.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!large) CK(cudaMemcpyAsync(&st, bt.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (st != GS_OK) return set_err(ctx, GS_UNCONVERGED, "iteration limit reached");
   return GS_OK;

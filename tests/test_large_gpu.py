@@ -157,3 +157,67 @@ def test_large_nonfinite_input_terminates(gs):
     except (gs.UnconvergedException, gs.ArgumentError):
         return
     assert not np.all(np.isfinite(S.T))
+
+
+@pytest.mark.parametrize("n", [130, 200, 300])
+def test_large_complex_multishift(gs, n):
+    """Complex orders above 128 on the whole GPU (Hessenberg reduction, multishift QR,
+    trailing blocks by the batched kernel): Schur properties and the oracle's eigenvalues."""
+    from common import assert_schur_cplx
+    rng = np.random.default_rng(9750 + n)
+    A = randn_matrix(rng, n, cplx=True)
+    S = gs.gschur(A)
+    assert_schur_cplx(A, S.T, S.Z, S.values)
+    w_ref, tol = eig_tolerances(A, po)
+    ok, worst = match_eigenvalues(S.values, w_ref, tol)
+    assert ok, "worst err/tol %.3g" % worst
+
+
+def test_large_complex_600_vs_lapack(gs):
+    import scipy.linalg
+    from common import assert_schur_cplx, rconde
+    n = 600
+    rng = np.random.default_rng(9760)
+    A = randn_matrix(rng, n, cplx=True)
+    S = gs.gschur(A)
+    assert_schur_cplx(A, S.T, S.Z, S.values)
+    w, VL, VR = scipy.linalg.eig(A, left=True, right=True)
+    tol = 1e2 * n * EPS * np.linalg.norm(A) / np.maximum(rconde(VL, VR), 1e-300)
+    ok, worst = match_eigenvalues(S.values, w, tol)
+    assert ok, "worst err/tol %.3g" % worst
+
+
+@pytest.mark.parametrize("kind", ["zero", "triangular", "blockdiag", "companion", "jordan", "unitary", "scaled"])
+def test_large_complex_structured(gs, kind):
+    """Structured complex inputs of order > 128 end in a Schur form within the FP64 bounds."""
+    from common import assert_schur_cplx
+    n = 180
+    rng = np.random.default_rng(9770)
+    if kind == "unitary":
+        Q, R = np.linalg.qr(randn_matrix(rng, n, cplx=True))
+        A = Q @ np.diag(np.sign(np.diag(R)))
+    elif kind == "scaled":
+        A = 1e300 * randn_matrix(rng, n, cplx=True)
+    else:
+        A = _structured(n, kind, rng).astype(np.complex128)
+        if kind in ("triangular", "blockdiag"):
+            A = A + 1j * _structured(n, kind, np.random.default_rng(9771))
+    S = gs.gschur(A)
+    assert np.all(np.tril(S.T, -1) == 0)
+    nA = max(np.linalg.norm(A), 1e-300)
+    assert np.linalg.norm(A - S.Z @ S.T @ S.Z.conj().T) / nA <= 10 * n * EPS
+    assert np.linalg.norm(S.Z.conj().T @ S.Z - np.eye(n)) <= 10 * n * EPS
+    np.testing.assert_array_equal(S.values, np.diag(S.T))
+    if kind in ("zero", "triangular"):
+        np.testing.assert_allclose(np.sort_complex(S.values), np.sort_complex(np.diag(A)), atol=10 * n * EPS * nA)
+
+
+def test_large_complex_wantz_false(gs):
+    rng = np.random.default_rng(9780)
+    A = randn_matrix(rng, 220, cplx=True)
+    S1 = gs.gschur(A)
+    S0 = gs.gschur(A, wantZ=False)
+    from common import match_eigenvalues as mt
+    tol = np.full(220, 1e-9 * np.abs(S1.values).max())
+    ok, worst = mt(S0.values, S1.values, tol)
+    assert ok, worst
