@@ -53,7 +53,41 @@ __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, i
   }
 }
 
+// The queue of a single matrix: order[0] = 0, bin `bin` holds [0, 1), the other bins are
+// empty, all ticket counters zero.  meta (when not null) receives iota[0..kSmallMax] in its
+// first ints and zeros after, so that ns = meta + m, offs = woffs = (long long*) zeros.
+__global__ void k_single_queue(int* order, int* sched, int bin) {
+  const int t = threadIdx.x;
+  if (t == 0) order[0] = 0;
+  if (t < kNumBins) {
+    sched[3 * t] = 0;
+    sched[3 * t + 1] = (t == bin) ? 1 : 0;
+    sched[3 * t + 2] = 0;
+  }
+}
+
+__global__ void k_single_meta(int* iota, long long* zeros) {
+  for (int t = threadIdx.x; t <= kSmallMax; t += blockDim.x) iota[t] = t;
+  if (threadIdx.x < 2) zeros[threadIdx.x] = 0;
+}
+
 }  // namespace
+
+int default_bin_of(int m) {
+  for (int b = 0; b < kNumBins; ++b)
+    if (m <= bin_max(b)) return b;
+  return kNumBins - 1;
+}
+
+cudaError_t launch_single_queue(int bin, int* order, int* sched, cudaStream_t s) {
+  k_single_queue<<<1, 32, 0, s>>>(order, sched, bin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_single_meta(int* iota, long long* zeros, cudaStream_t s) {
+  k_single_meta<<<1, 128, 0, s>>>(iota, zeros);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, const BinBounds& bounds,
                             cudaStream_t s) {

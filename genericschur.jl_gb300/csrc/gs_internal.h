@@ -49,10 +49,7 @@ struct CplxBatch {
   int maxinner_mult; // maxinner = maxinner_mult * n (reference default 30)
   long long maxiter_abs;   // when > 0, overrides maxiter_mult
   long long maxinner_abs;  // when > 0, overrides maxinner_mult
-  double2* hws;            // packed-H workspace of the single-matrix large variant
 };
-cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* order, int* sched, cudaStream_t s);
-size_t cplx_large_hws_elems(int n);
 // One complex matrix of order n > 128 on the whole GPU (schur_large_cplx.cu): Hessenberg
 // reduction, multishift QR, blocks <= 128 by the batched kernel.  A (device, ld n) <- T,
 // Z (or null) <- the unitary factor, w <- diag(T).  Returns ST_OK, ST_UNCONVERGED (sweep
@@ -451,5 +448,15 @@ cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int
                                       int num_sms, cudaStream_t* streams, int nstreams);
 cudaError_t launch_schur_batched_cplx_tuned(const CplxBatch& bt, const int* order, int* sched, int num_sms,
                                             cudaStream_t* streams, int nstreams, const BinTuning& tun);
+// One matrix of order m (<= kSmallMax) by one CTA of the default shape of its bin, without
+// the bin sort: launch_single_queue fills order/sched for that bin (default_bin_of(m));
+// launch_single_meta writes iota[0..kSmallMax] and two zero offsets once, so that a batch
+// of one can use ns = iota + m and offs = woffs = zeros with no host copy per call.
+int default_bin_of(int m);
+cudaError_t launch_single_queue(int bin, int* order, int* sched, cudaStream_t s);
+cudaError_t launch_single_meta(int* iota, long long* zeros, cudaStream_t s);
+template <class T, class W>
+cudaError_t launch_schur_real_one(const RealBatchT<T, W>& bt, int m, const int* order, int* sched, cudaStream_t s);
+cudaError_t launch_schur_cplx_one(const CplxBatch& bt, int m, const int* order, int* sched, cudaStream_t s);
 
 }  // namespace gsk

@@ -151,7 +151,7 @@ __device__ void hessenberg_cplx(int n, double2* A, int ld, double2* tau, double*
 // nmax: the largest order the launch sized its buffers for (the bin's maximum, or the
 // single large matrix's order).  An order outside [0, nmax] read from device memory gets
 // ST_BADARG before anything is read or written.
-template <int NT, bool HSMEM, bool HGLOB>
+template <int NT, bool HSMEM>
 __device__ void solve_cplx(const CplxBatch& bt, int b, int nmax, double2* smem, CtlC& c) {
   constexpr bool PACKED = !HSMEM;
   const int tid = threadIdx.x;
@@ -166,9 +166,9 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, int nmax, double2* smem, 
   double2* __restrict__ wg = bt.w + bt.woffs[b];
   const int ldh = HSMEM ? (n | 1) : n;
   const int hsize = HSMEM ? n * ldh : pk_off(n + 1);
-  // packed H of the QR phase: shared memory, or (orders > 128) the global workspace
-  double2* Hs = HGLOB ? bt.hws : smem;
-  double2* tau = HGLOB ? smem : Hs + hsize;  // n
+  // packed H of the QR phase (shared memory)
+  double2* Hs = smem;
+  double2* tau = Hs + hsize;  // n
   double2* lg = tau + n;            // 3 per chase step: t1, v2, (t2, 0)
   double* red = (double*)(lg + 3 * n);
   double2* A = HSMEM ? Hs : Ag;     // where the Hessenberg reduction runs
@@ -526,7 +526,7 @@ __device__ void solve_cplx(const CplxBatch& bt, int b, int nmax, double2* smem, 
   __syncthreads();
 }
 
-template <int NT, bool HSMEM, bool HGLOB>
+template <int NT, bool HSMEM>
 __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __restrict__ order,
                                                    int* __restrict__ sched, int bin, int nmax) {
   extern __shared__ double2 smemz[];
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(NT) k_schur_cplx(CplxBatch bt, const int* __re
     const int job = s_job;
     __syncthreads();
     if (job >= end) break;
-    solve_cplx<NT, HSMEM, HGLOB>(bt, order[job], nmax, smemz, c);
+    solve_cplx<NT, HSMEM>(bt, order[job], nmax, smemz, c);
   }
 }
 
@@ -552,14 +552,14 @@ template <int NT, bool HSMEM>
 cudaError_t launch_bin_c(const CplxBatch& bt, const int* order, int* sched, int bin, int nmax, int ctas, int num_sms,
                          cudaStream_t s) {
   const size_t smem = cbin_smem_bytes(nmax, HSMEM);
-  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<NT, HSMEM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<NT, HSMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM, false>, NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_cplx<NT, HSMEM>, NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   if (ctas > 0 && per_sm > ctas) per_sm = ctas;
-  k_schur_cplx<NT, HSMEM, false><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin, nmax);
+  k_schur_cplx<NT, HSMEM><<<num_sms * per_sm, NT, smem, s>>>(bt, order, sched, bin, nmax);
   return cudaGetLastError();
 }
 
@@ -578,18 +578,6 @@ cudaError_t launch_shape_c(const CplxBatch& bt, const int* order, int* sched, in
 
 }  // namespace
 
-// One complex matrix of order n > 128: a single CTA of 256 threads, with the packed
-// H of the QR phase in the global workspace bt.hws (pk_off(n+1) entries).  The
-// matrix has gone through launch_bin_sort, which places it in the last bin.
-cudaError_t launch_schur_cplx_large(const CplxBatch& bt, int nmax, const int* order, int* sched, cudaStream_t s) {
-  const size_t smem = sizeof(double2) * (4 * (size_t)nmax) + 32 * sizeof(double) + 64;
-  cudaError_t e = cudaFuncSetAttribute(k_schur_cplx<256, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_schur_cplx<256, false, true><<<1, 256, smem, s>>>(bt, order, sched, kNumBins - 1, nmax);
-  return cudaGetLastError();
-}
-
-size_t cplx_large_hws_elems(int n) { return (size_t)pk_off(n + 1); }
 
 cudaError_t launch_schur_batched_cplx_tuned(const CplxBatch& bt, const int* order, int* sched, int num_sms,
                                             cudaStream_t* streams, int nstreams, const BinTuning& t) {
@@ -609,5 +597,11 @@ cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int
 }
 
 size_t cplx_bin_smem_bytes(int nmax, int hsmem) { return cbin_smem_bytes(nmax, hsmem != 0); }
+
+cudaError_t launch_schur_cplx_one(const CplxBatch& bt, int m, const int* order, int* sched, cudaStream_t s) {
+  const BinTuning t = default_tuning_cplx();
+  const int bin = default_bin_of(m);
+  return launch_shape_c(bt, order, sched, bin, t.bounds[bin], t.nt[bin], t.hsmem[bin], 1, 1, s);
+}
 
 }  // namespace gsk

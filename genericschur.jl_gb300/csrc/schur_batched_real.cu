@@ -608,6 +608,17 @@ template cudaError_t launch_schur_batched_real<float, double>(const RealBatchT<f
 template cudaError_t launch_schur_batched_real<float, float>(const RealBatchT<float, float>&, const int*, int*, int,
                                                              cudaStream_t*, int);
 
+template <class T, class W>
+cudaError_t launch_schur_real_one(const RealBatchT<T, W>& bt, int m, const int* order, int* sched, cudaStream_t s) {
+  const BinTuning t = default_tuning_real();
+  const int bin = default_bin_of(m);
+  return launch_shape(bt, order, sched, bin, t.bounds[bin], t.nt[bin], t.hsmem[bin], 1, 1, s);
+}
+template cudaError_t launch_schur_real_one<double, double>(const RealBatchT<double, double>&, int, const int*, int*,
+                                                           cudaStream_t);
+template cudaError_t launch_schur_real_one<float, double>(const RealBatchT<float, double>&, int, const int*, int*,
+                                                          cudaStream_t);
+
 cudaError_t launch_schur_batched_real_tuned(const RealBatchT<double, double>& bt, const int* order, int* sched,
                                             int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun) {
   return launch_all_bins(bt, order, sched, num_sms, streams, nstreams, tun);

@@ -106,7 +106,7 @@ size_t schur_large_ws_bytes(int n, size_t tsize) {
   b += sizeof(int) * 64 * kMaxBulges + tsize * 64 * kMaxBulges * 5 + 512;  // chase log
   b += tsize * 4 * kMaxBulges + 256;                                        // shifts
   b += 3 * sizeof(double) * nb * nb + 4 * sizeof(double) * nb + 1024;       // small solve blk, U, wr, wi, meta
-  b += sizeof(int) * (nb + 3 * kNumBins + 8) + 256;                         // order/sched/status/scan
+  b += sizeof(int) * (2 * nb + 3 * kNumBins + 16) + 512;                    // order/iota/sched/status/scan
   b += 2 * sizeof(double) * nb + sizeof(int) * 4 + 512;                      // AED eigenvalues, results
   b += tsize * (size_t)n * nb * 2 + tsize * nb * nb + 512;                  // GEMM temporaries, U in T
   return b + 16 * 256;
@@ -140,6 +140,7 @@ int schur_large_run(LargeRun<T>& r) {
   double* bwi = (double*)take(sizeof(double) * nb);
   long long* meta = (long long*)take(sizeof(long long) * 4);
   int* order = (int*)take(sizeof(int) * (nb + 8));
+  int* iota = (int*)take(sizeof(int) * (nb + 8));
   int* sched = (int*)take(sizeof(int) * (3 * kNumBins + 4));
   int* bstat = (int*)take(sizeof(int) * 4);
   int* dscan = (int*)take(sizeof(int) * 4);
@@ -194,19 +195,16 @@ int schur_large_run(LargeRun<T>& r) {
   // ---- 3. QR
   // The small-matrix kernel in the working precision T on H[lo:hi, lo:hi] (copied to blk;
   // T_blk back in blk, U in U), or -- eigenvalues only, fp32 set -- in FP32.
+  CKL(launch_single_meta(iota, meta, s));
   auto small_solve = [&](int lo, int hi, bool wantU, double* wr_out, double* wi_out, bool fp32) -> int {
     const int m = hi - lo + 1;
-    long long mh[4] = {0, 0, 0, 0};
-    int m32 = m;
-    CKL(cudaMemcpyAsync(meta, mh, sizeof(mh), cudaMemcpyHostToDevice, s));
-    CKL(cudaMemcpyAsync(meta + 2, &m32, sizeof(int), cudaMemcpyHostToDevice, s));
     if (fp32) {
       CKL(copy2d<T, float>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk32, m, s));
       RealBatchT<float> bt{};
       bt.count = 1;
-      bt.ns = (const int*)(meta + 2);
+      bt.ns = iota + m;
       bt.offs = meta;
-      bt.woffs = meta + 1;
+      bt.woffs = meta;
       bt.A = blk32;
       bt.Z = nullptr;
       bt.wr = wr_out;
@@ -215,16 +213,16 @@ int schur_large_run(LargeRun<T>& r) {
       bt.wantz = 0;
       bt.scale = 0;
       bt.maxiter_mult = 100;
-      CKL(launch_bin_sort(bt.ns, 1, order, sched, s));
-      CKL(launch_schur_batched_real<float, double>(bt, order, sched, r.num_sms, &s, 1));
+      CKL(launch_single_queue(default_bin_of(m), order, sched, s));
+      CKL(launch_schur_real_one<float, double>(bt, m, order, sched, s));
       return 0;
     }
     CKL(copy2d<T, T>(m, m, H + (size_t)(lo - 1) * n + (lo - 1), n, blk, m, s));
     RealBatchT<T> bt{};
     bt.count = 1;
-    bt.ns = (const int*)(meta + 2);
+    bt.ns = iota + m;
     bt.offs = meta;
-    bt.woffs = meta + 1;
+    bt.woffs = meta;
     bt.A = blk;
     bt.Z = wantU ? U : nullptr;
     bt.wr = wr_out;
@@ -233,8 +231,8 @@ int schur_large_run(LargeRun<T>& r) {
     bt.wantz = wantU;
     bt.scale = 0;
     bt.maxiter_mult = 100;
-    CKL(launch_bin_sort(bt.ns, 1, order, sched, s));
-    CKL(launch_schur_batched_real<T, double>(bt, order, sched, r.num_sms, &s, 1));
+    CKL(launch_single_queue(default_bin_of(m), order, sched, s));
+    CKL(launch_schur_real_one<T, double>(bt, m, order, sched, s));
     return 0;
   };
 
