@@ -6,6 +6,8 @@
 // when the orders live in device memory and were never checked on the host) are counted
 // in the nearest end bin; the solve kernels see the true order there and write ST_BADARG
 // for it without touching the matrix.
+#include <algorithm>
+
 #include "gs_internal.h"
 
 namespace gsk {
@@ -13,12 +15,13 @@ namespace {
 
 __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, int count,
                                                    int* __restrict__ order, int* __restrict__ sched,
-                                                   BinBounds bounds) {
+                                                   BinBounds bounds, const int* status, int code) {
   __shared__ int hist[kSmallMax + 1];
   __shared__ int pos[kSmallMax + 1];
   for (int i = threadIdx.x; i <= kSmallMax; i += blockDim.x) hist[i] = 0;
   __syncthreads();
   for (int b = threadIdx.x; b < count; b += blockDim.x) {
+    if (status && status[b] != code) continue;
     int n = ns[b];
     n = n < 0 ? 0 : (n > kSmallMax ? kSmallMax : n);
     atomicAdd(&hist[n], 1);
@@ -47,10 +50,25 @@ __global__ void __launch_bounds__(1024) k_bin_sort(const int* __restrict__ ns, i
   }
   __syncthreads();
   for (int b = threadIdx.x; b < count; b += blockDim.x) {
+    if (status && status[b] != code) continue;
     int n = ns[b];
     n = n < 0 ? 0 : (n > kSmallMax ? kSmallMax : n);
     order[atomicAdd(&pos[n], 1)] = b;
   }
+}
+
+__global__ void k_batch_extent(const int* __restrict__ ns, const long long* __restrict__ offs,
+                               const long long* __restrict__ woffs, int count, unsigned long long* out) {
+  unsigned long long ea = 0, ew = 0;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < count; b += gridDim.x * blockDim.x) {
+    int n = ns[b];
+    n = n < 0 ? 0 : (n > kSmallMax ? kSmallMax : n);
+    const long long a = offs[b] + (long long)n * n, w = woffs[b] + n;
+    ea = a > (long long)ea ? (unsigned long long)a : ea;
+    ew = w > (long long)ew ? (unsigned long long)w : ew;
+  }
+  atomicMax(out, ea);
+  atomicMax(out + 1, ew);
 }
 
 // The queue of a single matrix: order[0] = 0, bin `bin` holds [0, 1), the other bins are
@@ -91,7 +109,20 @@ cudaError_t launch_single_meta(int* iota, long long* zeros, cudaStream_t s) {
 
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, const BinBounds& bounds,
                             cudaStream_t s) {
-  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched, bounds);
+  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched, bounds, nullptr, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bin_sort_status(const int* ns, int count, const int* status, int code, int* order, int* sched,
+                                   const BinBounds& bounds, cudaStream_t s) {
+  k_bin_sort<<<1, 1024, 0, s>>>(ns, count, order, sched, bounds, status, code);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_extent(const int* ns, const long long* offs, const long long* woffs, int count,
+                                unsigned long long* out, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_batch_extent<<<std::min(1024, (count + 255) / 256), 256, 0, s>>>(ns, offs, woffs, count, out);
   return cudaGetLastError();
 }
 
@@ -107,16 +138,22 @@ BinTuning default_tuning_real() {
 BinTuning default_tuning_cplx() {
   return BinTuning{{32, 64, 96, 128}, {64, 64, 128, 128}, {1, 1, 0, 0}, {0, 0, 0, 0}};
 }
+BinTuning default_tuning_mixed32() {
+  return BinTuning{{32, 64, 96, 128}, {64, 64, 128, 128}, {1, 1, 0, 0}, {0, 0, 0, 0}};
+}
 
 // Largest dynamic shared memory a CTA may use on sm_103 (227 KiB), less the kernels'
 // static shared memory.
 static constexpr size_t kMaxDynSmem = 227 * 1024 - 1024;
 
-bool tuning_shape_ok(bool cplx, int nmax, int nt, int hsmem) {
+bool tuning_shape_ok(int kind, int nmax, int nt, int hsmem) {
   bool known = false;
   for (int t : kTuneThreads) known |= (t == nt);
-  if (!known || nmax < 1 || nmax > kSmallMax) return false;
-  const size_t b = cplx ? cplx_bin_smem_bytes(nmax, hsmem) : real_bin_smem_bytes(nmax, hsmem);
+  if (kind == kTuneMixed32 && nt == 160) known = false;
+  if (!known || nmax < 1 || nmax > kSmallMax || kind < 0 || kind > kTuneMixed32) return false;
+  const size_t b = kind == kTuneCplx ? cplx_bin_smem_bytes(nmax, hsmem)
+                                     : (kind == kTuneReal ? real_bin_smem_bytes(nmax, hsmem)
+                                                          : real32_bin_smem_bytes(nmax, hsmem));
   return b <= kMaxDynSmem;
 }
 

@@ -12,6 +12,9 @@ constexpr int kSmallMax = 128;
 
 // Per-matrix status codes (also the C-ABI return codes).
 enum : int { ST_OK = 0, ST_UNCONVERGED = 1, ST_BADARG = 2, ST_CUDA = 3 };
+// Internal per-matrix status of the mixed batched form: the refinement handed the matrix
+// back to the FP64 kernel (which overwrites it with ST_OK / ST_UNCONVERGED).
+constexpr int kStFallback = 7;
 
 // A ragged batch of column-major matrices in one packed buffer.  Matrix b has
 // order ns[b] and starts at element offs[b] of A and Z; its eigenvalues start at
@@ -416,13 +419,18 @@ struct BinTuning {
 };
 BinTuning default_tuning_real();
 BinTuning default_tuning_cplx();
+BinTuning default_tuning_mixed32();  // the FP32 stage of the mixed batched form
 // Thread counts compiled for the FP64 real and the complex kernels (the tuner's
-// candidates); other values are rejected by the table parser.
+// candidates); other values are rejected by the table parser.  The FP32 stage of the
+// mixed form compiles the same counts but 160.
 constexpr int kTuneThreads[] = {64, 96, 128, 160, 192, 256};
-// Whether (nt, hsmem) is a compiled shape whose shared memory fits for orders up to
-// nmax: real FP64 (cplx = false) or complex (cplx = true).
-bool tuning_shape_ok(bool cplx, int nmax, int nt, int hsmem);
+// Table kinds: real FP64 kernel, complex kernel, FP32 stage of the mixed real form.
+enum : int { kTuneReal = 0, kTuneCplx = 1, kTuneMixed32 = 2 };
+// Whether (nt, hsmem) is a compiled shape of that kind whose shared memory fits for
+// orders up to nmax.
+bool tuning_shape_ok(int kind, int nmax, int nt, int hsmem);
 size_t real_bin_smem_bytes(int nmax, int hsmem);
+size_t real32_bin_smem_bytes(int nmax, int hsmem);
 size_t cplx_bin_smem_bytes(int nmax, int hsmem);
 struct BinBounds {
   int b[kNumBins];
@@ -434,6 +442,9 @@ struct BinBounds {
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, cudaStream_t s);
 cudaError_t launch_bin_sort(const int* ns, int count, int* order, int* sched, const BinBounds& bounds,
                             cudaStream_t s);
+// The same over the matrices whose status equals `code` only (the others are left out).
+cudaError_t launch_bin_sort_status(const int* ns, int count, const int* status, int code, int* order, int* sched,
+                                   const BinBounds& bounds, cudaStream_t s);
 
 // T = double: the FP64 batched kernel; T = float: the same algorithm in FP32 (the
 // Float32 entry points and the FP32 stage of the mixed-precision form).  W is the
@@ -444,6 +455,8 @@ cudaError_t launch_schur_batched_real(const RealBatchT<T, W>& bt, const int* ord
                                       int num_sms, cudaStream_t* streams, int nstreams);
 cudaError_t launch_schur_batched_real_tuned(const RealBatchT<double, double>& bt, const int* order, int* sched,
                                             int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun);
+cudaError_t launch_schur_batched_real32_tuned(const RealBatchT<float, float>& bt, const int* order, int* sched,
+                                              int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun);
 cudaError_t launch_schur_batched_cplx(const CplxBatch& bt, const int* order, int* sched,
                                       int num_sms, cudaStream_t* streams, int nstreams);
 cudaError_t launch_schur_batched_cplx_tuned(const CplxBatch& bt, const int* order, int* sched, int num_sms,
@@ -458,5 +471,37 @@ cudaError_t launch_single_meta(int* iota, long long* zeros, cudaStream_t s);
 template <class T, class W>
 cudaError_t launch_schur_real_one(const RealBatchT<T, W>& bt, int m, const int* order, int* sched, cudaStream_t s);
 cudaError_t launch_schur_cplx_one(const CplxBatch& bt, int m, const int* order, int* sched, cudaStream_t s);
+
+// Batched real Schur in mixed precision (refine_batched.cu): FP32 Schur pairs refined to
+// FP64 by Newton steps, matrices the refinement cannot finish recomputed by the FP64
+// kernel (unless nofallback: then ST_UNCONVERGED).  na / nw: element extents of A and of
+// the eigenvalue arrays; order / sched: count and 3 * kNumBins ints.
+struct MixedBatch {
+  int count;
+  const int* ns;
+  const long long* offs;
+  const long long* woffs;
+  double* A;
+  double* Z;  // null: no Schur vectors wanted
+  double* wr;
+  double* wi;
+  int* status;
+  int* order;
+  int* sched;
+  void* ws;   // mixed_batched_ws_bytes(na, nw, Z != null): arrays indexed like A and wr
+  int* iws;   // mixed_batched_iws_ints(count) ints: per-matrix and schedule scratch
+  long long na, nw;
+  int scale;
+  int nofallback;
+};
+size_t mixed_batched_ws_bytes(long long na, long long nw, bool wantz);
+constexpr size_t kMixedSchedInts = 4 * kNumBins + 8;
+inline size_t mixed_batched_iws_ints(long long count) { return 2 * (size_t)count + kMixedSchedInts; }
+cudaError_t launch_mixed_batched(const MixedBatch& m, int num_sms, cudaStream_t s, cudaStream_t* aux, int naux,
+                                 cudaEvent_t fork, cudaEvent_t* join, const BinTuning& tun64, const BinTuning& tun32);
+// Element extents of a device-resident ragged batch: out[0] = max(offs + n^2),
+// out[1] = max(woffs + n) (orders clamped to [0, kSmallMax]); out must be zeroed.
+cudaError_t launch_batch_extent(const int* ns, const long long* offs, const long long* woffs, int count,
+                                unsigned long long* out, cudaStream_t s);
 
 }  // namespace gsk

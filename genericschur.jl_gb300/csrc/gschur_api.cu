@@ -39,6 +39,7 @@ struct gs_context {
   // launch shapes of the batched kernels (gs_set_tuning); tun_gen changes with them
   BinTuning tun_real = default_tuning_real();
   BinTuning tun_cplx = default_tuning_cplx();
+  BinTuning tun_mixed32 = default_tuning_mixed32();
   long long tun_gen = 0;
   std::string tun_source = "built-in defaults";
   // host-buffer batched calls: chunks whose copies overlap the other chunks' kernels
@@ -215,11 +216,11 @@ int gs_host_free(gs_context* ctx, void* ptr) {
 static std::string tuning_text(const gs_context* ctx) {
   std::string t = "# gschur_gb300 batched tuning (" + ctx->tun_source + ")\n# kind bin nmax threads hsmem ctas_per_sm\n";
   char line[128];
-  for (int k = 0; k < 2; ++k) {
-    const BinTuning& b = k ? ctx->tun_cplx : ctx->tun_real;
+  static const char* kinds[3] = {"real_f64", "complex_f64", "mixed_f32"};
+  for (int k = 0; k < 3; ++k) {
+    const BinTuning& b = k == kTuneReal ? ctx->tun_real : (k == kTuneCplx ? ctx->tun_cplx : ctx->tun_mixed32);
     for (int i = 0; i < kNumBins; ++i) {
-      snprintf(line, sizeof(line), "%s %d %d %d %d %d\n", k ? "complex_f64" : "real_f64", i, b.bounds[i], b.nt[i],
-               b.hsmem[i], b.ctas[i]);
+      snprintf(line, sizeof(line), "%s %d %d %d %d %d\n", kinds[k], i, b.bounds[i], b.nt[i], b.hsmem[i], b.ctas[i]);
       t += line;
     }
   }
@@ -229,7 +230,7 @@ static std::string tuning_text(const gs_context* ctx) {
 int gs_set_tuning(gs_context* ctx, const char* path) {
   if (!ctx) return GS_BADARG;
   ctx->err.clear();
-  BinTuning tr = default_tuning_real(), tc = default_tuning_cplx();
+  BinTuning tr = default_tuning_real(), tc = default_tuning_cplx(), tm = default_tuning_mixed32();
   std::string source = "built-in defaults";
   if (path && path[0]) {
     FILE* f = fopen(path, "r");
@@ -248,14 +249,16 @@ int gs_set_tuning(gs_context* ctx, const char* path) {
                      lineno);
         break;
       }
-      const int k = !strcmp(kind, "real_f64") ? 0 : (!strcmp(kind, "complex_f64") ? 1 : -1);
+      const int k = !strcmp(kind, "real_f64")
+                        ? kTuneReal
+                        : (!strcmp(kind, "complex_f64") ? kTuneCplx : (!strcmp(kind, "mixed_f32") ? kTuneMixed32 : -1));
       if (k < 0 || bin < 0 || bin >= kNumBins || ctas < 0 || (hs != 0 && hs != 1) ||
-          !tuning_shape_ok(k == 1, nmax, nt, hs)) {
-        rc = set_err(ctx, GS_BADARG, "tuning table %s:%d: unknown kind, bin, or a shape that is not compiled or does "
-                     "not fit in shared memory", path, lineno);
+          !tuning_shape_ok(k, nmax, nt, hs) || (k == kTuneMixed32 && nmax != bin_max(bin))) {
+        rc = set_err(ctx, GS_BADARG, "tuning table %s:%d: unknown kind, bin, a shape that is not compiled or does "
+                     "not fit in shared memory, or a mixed_f32 bound other than the default", path, lineno);
         break;
       }
-      BinTuning& b = k ? tc : tr;
+      BinTuning& b = k == kTuneReal ? tr : (k == kTuneCplx ? tc : tm);
       b.bounds[bin] = nmax;
       b.nt[bin] = nt;
       b.hsmem[bin] = hs;
@@ -263,21 +266,22 @@ int gs_set_tuning(gs_context* ctx, const char* path) {
     }
     fclose(f);
     if (rc != GS_OK) return rc;
-    for (int k = 0; k < 2; ++k) {
-      const BinTuning& b = k ? tc : tr;
+    for (int k = 0; k < 3; ++k) {
+      const BinTuning& b = k == kTuneReal ? tr : (k == kTuneCplx ? tc : tm);
       for (int i = 0; i < kNumBins; ++i)
         if (b.bounds[i] < 1 || (i > 0 && b.bounds[i] <= b.bounds[i - 1]))
           return set_err(ctx, GS_BADARG, "tuning table %s: bin bounds must increase", path);
       if (b.bounds[kNumBins - 1] != kSmallMax)
         return set_err(ctx, GS_BADARG, "tuning table %s: the last bin must end at %d", path, kSmallMax);
       for (int i = 0; i < kNumBins; ++i)  // a bin whose bound moved must still fit its shape
-        if (!tuning_shape_ok(k == 1, b.bounds[i], b.nt[i], b.hsmem[i]))
+        if (!tuning_shape_ok(k, b.bounds[i], b.nt[i], b.hsmem[i]))
           return set_err(ctx, GS_BADARG, "tuning table %s: bin %d shape does not fit", path, i);
     }
     source = path;
   }
   ctx->tun_real = tr;
   ctx->tun_cplx = tc;
+  ctx->tun_mixed32 = tm;
   ctx->tun_source = source;
   ++ctx->tun_gen;
   return GS_OK;
@@ -296,23 +300,10 @@ int gs_get_tuning(const gs_context* ctx, char* buf, size_t len) {
 // batched real
 // ---------------------------------------------------------------------------
 }  // extern "C"
-template <class T, class W>
-static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* order, int* sched, unsigned flags,
-                            bool use_graph, const std::vector<long long>& key) {
-  // FP64 runs the context's tuned shapes; the FP32 instances the defaults
-  constexpr bool tuned = sizeof(T) == 8 && sizeof(W) == 8;
-  BinBounds bounds;
-  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
-  auto enqueue = [&](cudaStream_t s) -> int {
-    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, bounds, s);
-    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
-    return fork_join(ctx, s, [&](cudaStream_t* aux) {
-      if constexpr (tuned)
-        return launch_schur_batched_real_tuned(bt, order, sched, ctx->num_sms, aux, kNumBins, ctx->tun_real);
-      else
-        return launch_schur_batched_real(bt, order, sched, ctx->num_sms, aux, kNumBins);
-    });
-  };
+// Run `enqueue` on the context stream, or replay it as a CUDA graph cached under `key`
+// (captured on the first call with that key).  Brackets the work with the timing events.
+template <class F>
+static int run_graph_or_direct(gs_context* ctx, bool use_graph, const std::vector<long long>& key, F enqueue) {
   CK(cudaEventRecord(ctx->t0, ctx->stream));
   if (use_graph) {
     if (!ctx->gexec || ctx->gkey != key) {
@@ -338,6 +329,26 @@ static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* or
   return GS_OK;
 }
 
+template <class T, class W>
+static int run_batched_real(gs_context* ctx, const RealBatchT<T, W>& bt, int* order, int* sched, unsigned flags,
+                            bool use_graph, const std::vector<long long>& key) {
+  // FP64 runs the context's tuned shapes; the FP32 instances the defaults
+  constexpr bool tuned = sizeof(T) == 8 && sizeof(W) == 8;
+  BinBounds bounds;
+  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
+  auto enqueue = [&](cudaStream_t s) -> int {
+    cudaError_t e = launch_bin_sort(bt.ns, bt.count, order, sched, bounds, s);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
+    return fork_join(ctx, s, [&](cudaStream_t* aux) {
+      if constexpr (tuned)
+        return launch_schur_batched_real_tuned(bt, order, sched, ctx->num_sms, aux, kNumBins, ctx->tun_real);
+      else
+        return launch_schur_batched_real(bt, order, sched, ctx->num_sms, aux, kNumBins);
+    });
+  };
+  return run_graph_or_direct(ctx, use_graph, key, enqueue);
+}
+
 static int pipe_setup(gs_context* ctx) {
   if (ctx->pipe_ready) return GS_OK;
   for (int c = 0; c < kPipeChunks; ++c) {
@@ -358,22 +369,21 @@ static int pipe_setup(gs_context* ctx) {
 
 // Host-buffer batched call as a pipeline: the batch is cut into kPipeChunks runs of
 // consecutive matrices (the first and last small, so that little copying is exposed),
-// each run's inputs are copied on the context stream, its bin sort and size-bin kernels
-// run on a stream of its own once its copy has landed, and its outputs are copied back on
-// a separate stream once its kernels are done.  So the copies of one run overlap the
-// kernels of the others, and the runs' kernels overlap each other's tails.  Requires the
-// matrices to be stored in order (offsets increasing, not overlapping), which makes each
-// run one contiguous range of every buffer.  Device layout as the unpipelined call.
-template <class T>
-static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>& bt, int64_t count,
-                                        const int32_t* ns, const int64_t* offs, const int64_t* woffs, T* A, T* Z,
-                                        T* wr, T* wi, int32_t* status, int* order, int* sched, long long na,
-                                        long long nw) {
+// each run's inputs are copied on the context stream, its compute (`launch_run(c, b0, b1,
+// stream)`: bin sort and kernels of matrices [b0, b1), forked onto the run's own aux
+// streams) runs on a stream of its own once its copy has landed, and its outputs are
+// copied back on a separate stream once its kernels are done.  So the copies of one run
+// overlap the kernels of the others, and the runs' kernels overlap each other's tails.
+// Requires the matrices to be stored in order (offsets increasing, not overlapping), which
+// makes each run one contiguous range of every buffer.  dA, dZ, dwr, dwi, dst: the device
+// copies (dns, doffs, dwoffs the metadata); device layout as the unpipelined call.
+template <class T, class F>
+static int batched_pipelined(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                             const int64_t* woffs, T* A, T* Z, T* wr, T* wi, int32_t* status, int* dns,
+                             long long* doffs, long long* dwoffs, T* dA, T* dZ, T* dwr, T* dwi, int* dst,
+                             F launch_run) {
   int rc = pipe_setup(ctx);
   if (rc) return rc;
-  constexpr bool tuned = sizeof(T) == 8;
-  BinBounds bounds;
-  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
   // run boundaries by cumulative n^3 work: 10%, 40%, 40%, 10%
   double tot = 0.0;
   for (int64_t b = 0; b < count; ++b) tot += (double)ns[b] * ns[b] * ns[b];
@@ -392,9 +402,9 @@ static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>&
   }
   cudaStream_t s = ctx->stream;
   // metadata for the whole batch first (small), then the runs' matrices in order
-  CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(doffs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dwoffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
   auto a_lo = [&](int64_t b) { return (long long)offs[b]; };
   auto a_hi = [&](int64_t b) { return (long long)offs[b - 1] + (long long)ns[b - 1] * ns[b - 1]; };
   auto w_lo = [&](int64_t b) { return (long long)woffs[b]; };
@@ -403,7 +413,7 @@ static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>&
     const int64_t b0 = edge[c], b1 = edge[c + 1];
     if (b1 > b0) {
       const long long lo = a_lo(b0), hi = a_hi(b1);
-      CK(cudaMemcpyAsync(bt.A + lo, A + lo, sizeof(T) * (hi - lo), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(dA + lo, A + lo, sizeof(T) * (hi - lo), cudaMemcpyHostToDevice, s));
     }
     CK(cudaEventRecord(ctx->pipe_h2d[c], s));
   }
@@ -414,27 +424,8 @@ static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>&
     CK(cudaStreamWaitEvent(cs, ctx->pipe_h2d[c], 0));
     if (b1 > b0) {
       if (!timed) { CK(cudaEventRecord(ctx->t0, cs)); timed = true; }
-      RealBatchT<T, T> bc = bt;
-      bc.count = (int)(b1 - b0);
-      bc.ns = bt.ns + b0;
-      bc.offs = bt.offs + b0;
-      bc.woffs = bt.woffs + b0;
-      bc.status = bt.status + b0;
-      int* oc = order + b0;  // each run sorts its own slice of the order array
-      int* sc = sched + 3 * kNumBins * c;
-      cudaError_t e = launch_bin_sort(bc.ns, bc.count, oc, sc, bounds, cs);
-      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
-      CK(cudaEventRecord(ctx->pipe_fork[c], cs));
-      for (int i = 0; i < kNumBins; ++i) CK(cudaStreamWaitEvent(ctx->pipe_aux[c][i], ctx->pipe_fork[c], 0));
-      if constexpr (tuned)
-        e = launch_schur_batched_real_tuned(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins, ctx->tun_real);
-      else
-        e = launch_schur_batched_real(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins);
-      if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
-      for (int i = 0; i < kNumBins; ++i) {
-        CK(cudaEventRecord(ctx->pipe_join[c][i], ctx->pipe_aux[c][i]));
-        CK(cudaStreamWaitEvent(cs, ctx->pipe_join[c][i], 0));
-      }
+      rc = launch_run(c, b0, b1, cs);
+      if (rc) return rc;
     }
     CK(cudaEventRecord(ctx->pipe_done[c], cs));
   }
@@ -451,22 +442,55 @@ static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>&
     CK(cudaStreamWaitEvent(d, ctx->pipe_done[c], 0));
     if (b1 <= b0) continue;
     const long long lo = a_lo(b0), hi = a_hi(b1), wlo = w_lo(b0), whi = w_hi(b1);
-    CK(cudaMemcpyAsync(A + lo, bt.A + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
-    if (bt.Z) CK(cudaMemcpyAsync(Z + lo, bt.Z + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
+    CK(cudaMemcpyAsync(A + lo, dA + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
+    if (dZ) CK(cudaMemcpyAsync(Z + lo, dZ + lo, sizeof(T) * (hi - lo), cudaMemcpyDeviceToHost, d));
     if (whi > wlo) {
-      CK(cudaMemcpyAsync(wr + wlo, bt.wr + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
-      CK(cudaMemcpyAsync(wi + wlo, bt.wi + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
+      CK(cudaMemcpyAsync(wr + wlo, dwr + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
+      CK(cudaMemcpyAsync(wi + wlo, dwi + wlo, sizeof(T) * (whi - wlo), cudaMemcpyDeviceToHost, d));
     }
-    CK(cudaMemcpyAsync(status + b0, bt.status + b0, sizeof(int) * (b1 - b0), cudaMemcpyDeviceToHost, d));
+    CK(cudaMemcpyAsync(status + b0, dst + b0, sizeof(int) * (b1 - b0), cudaMemcpyDeviceToHost, d));
   }
   CK(cudaEventRecord(ctx->pipe_out, d));
   CK(cudaStreamWaitEvent(s, ctx->pipe_out, 0));
   CK(cudaStreamSynchronize(s));
-  (void)na;
-  (void)nw;
   for (int64_t b = 0; b < count; ++b)
     if (status[b] != GS_OK) return set_err(ctx, GS_UNCONVERGED, "matrix %lld: iteration limit reached", (long long)b);
   return GS_OK;
+}
+
+template <class T>
+static int schur_batched_real_pipelined(gs_context* ctx, const RealBatchT<T, T>& bt, int64_t count,
+                                        const int32_t* ns, const int64_t* offs, const int64_t* woffs, T* A, T* Z,
+                                        T* wr, T* wi, int32_t* status, int* order, int* sched) {
+  constexpr bool tuned = sizeof(T) == 8;
+  BinBounds bounds;
+  for (int i = 0; i < kNumBins; ++i) bounds.b[i] = tuned ? ctx->tun_real.bounds[i] : bin_max(i);
+  return batched_pipelined<T>(
+      ctx, count, ns, offs, woffs, A, Z, wr, wi, status, (int*)bt.ns, (long long*)bt.offs, (long long*)bt.woffs,
+      bt.A, bt.Z, bt.wr, bt.wi, bt.status, [&](int c, int64_t b0, int64_t b1, cudaStream_t cs) -> int {
+        RealBatchT<T, T> bc = bt;
+        bc.count = (int)(b1 - b0);
+        bc.ns = bt.ns + b0;
+        bc.offs = bt.offs + b0;
+        bc.woffs = bt.woffs + b0;
+        bc.status = bt.status + b0;
+        int* oc = order + b0;  // each run sorts its own slice of the order array
+        int* sc = sched + 3 * kNumBins * c;
+        cudaError_t e = launch_bin_sort(bc.ns, bc.count, oc, sc, bounds, cs);
+        if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "bin sort launch: %s", cudaGetErrorString(e));
+        CK(cudaEventRecord(ctx->pipe_fork[c], cs));
+        for (int i = 0; i < kNumBins; ++i) CK(cudaStreamWaitEvent(ctx->pipe_aux[c][i], ctx->pipe_fork[c], 0));
+        if constexpr (tuned)
+          e = launch_schur_batched_real_tuned(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins, ctx->tun_real);
+        else
+          e = launch_schur_batched_real(bc, oc, sc, ctx->num_sms, ctx->pipe_aux[c], kNumBins);
+        if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+        for (int i = 0; i < kNumBins; ++i) {
+          CK(cudaEventRecord(ctx->pipe_join[c][i], ctx->pipe_aux[c][i]));
+          CK(cudaStreamWaitEvent(cs, ctx->pipe_join[c][i], 0));
+        }
+        return GS_OK;
+      });
 }
 
 template <class T>
@@ -531,8 +555,7 @@ static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t
     bt.wi = (T*)(base + o_wi);
     bt.status = (int*)(base + o_st);
     if (pipelined)
-      return schur_batched_real_pipelined<T>(ctx, bt, count, ns, offs, woffs, A, Z, wr, wi, status, order, sched, na,
-                                             nw);
+      return schur_batched_real_pipelined<T>(ctx, bt, count, ns, offs, woffs, A, Z, wr, wi, status, order, sched);
     CK(cudaMemcpyAsync((void*)bt.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)bt.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
@@ -564,10 +587,151 @@ static int schur_batched_real_impl(gs_context* ctx, int64_t count, const int32_t
   return GS_OK;
 }
 
+// GS_MIXED: FP32 Schur pairs refined to FP64 (refine_batched.cu).  Same arguments and
+// results as the FP64 batched call; the workspace grows with the batch (five FP32 and
+// two or three FP64 copies of A), so a device-pointer call first reads the batch's
+// extents back from the device.
+static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
+                                    const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
+                                    int32_t* status, unsigned flags) {
+  if (!ctx) return GS_BADARG;
+  ctx->err.clear();
+  if (count < 0 || count > (1LL << 30)) return set_err(ctx, GS_BADARG, "bad count %lld", (long long)count);
+  if (count == 0) return GS_OK;
+  const bool wantz = flags & GS_WANTZ;
+  if (!ns || !offs || !woffs || !A || !wr || !wi || !status || (wantz && !Z))
+    return set_err(ctx, GS_BADARG, "null array argument");
+  CK(cudaSetDevice(ctx->device));
+  const bool dev = flags & GS_DEVICE;
+  cudaStream_t s = ctx->stream;
+  long long na = 0, nw = 0;
+  if (!dev) {
+    for (int64_t b = 0; b < count; ++b) {
+      const int n = ns[b];
+      if (n < 0 || n > kSmallMax)
+        return set_err(ctx, GS_BADARG, "matrix %lld: order %d outside [0, %d]", (long long)b, n, kSmallMax);
+      if (offs[b] < 0 || woffs[b] < 0) return set_err(ctx, GS_BADARG, "matrix %lld: negative offset", (long long)b);
+      na = std::max(na, (long long)offs[b] + (long long)n * n);
+      nw = std::max(nw, (long long)woffs[b] + n);
+    }
+  } else {
+    Arena ar0;
+    const size_t o_ext = ar0.take<unsigned long long>(2);
+    int rc = ensure_ws(ctx, ar0.off);
+    if (rc) return rc;
+    unsigned long long* dext = (unsigned long long*)(ctx->dws + o_ext);
+    unsigned long long ext[2] = {0, 0};
+    CK(cudaMemsetAsync(dext, 0, sizeof(ext), s));
+    CK(launch_batch_extent(ns, (const long long*)offs, (const long long*)woffs, (int)count, dext, s));
+    CK(cudaMemcpyAsync(ext, dext, sizeof(ext), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    na = (long long)ext[0];
+    nw = (long long)ext[1];
+  }
+  Arena ar;
+  const size_t o_order = ar.take<int>(count);
+  const size_t o_sched = ar.take<int>(3 * kNumBins * kPipeChunks);
+  size_t o_A = 0, o_Z = 0, o_wr = 0, o_wi = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
+  bool in_order = true;  // matrices stored one after another (the pipelined copy needs it)
+  if (!dev) {
+    for (int64_t b = 1; b < count; ++b)
+      if (offs[b] < offs[b - 1] + (long long)ns[b - 1] * ns[b - 1] || woffs[b] < woffs[b - 1] + ns[b - 1])
+        in_order = false;
+    o_A = ar.take<double>(na);
+    o_Z = ar.take<double>(wantz ? na : 1);
+    o_wr = ar.take<double>(nw);
+    o_wi = ar.take<double>(nw);
+    o_ns = ar.take<int>(count);
+    o_offs = ar.take<long long>(count);
+    o_woffs = ar.take<long long>(count);
+    o_st = ar.take<int>(count);
+  }
+  const size_t o_ws = ar.take<char>(mixed_batched_ws_bytes(na, nw, wantz));
+  const size_t o_iws = ar.take<int>(mixed_batched_iws_ints(count) + (kPipeChunks - 1) * kMixedSchedInts);
+  int rc = ensure_ws(ctx, ar.off);
+  if (rc) return rc;
+  char* base = ctx->dws;
+  MixedBatch mb{};
+  mb.count = (int)count;
+  mb.order = (int*)(base + o_order);
+  mb.sched = (int*)(base + o_sched);
+  mb.ws = base + o_ws;
+  mb.iws = (int*)(base + o_iws);
+  mb.na = na;
+  mb.nw = nw;
+  mb.scale = (flags & GS_SCALE) ? 1 : 0;
+  mb.nofallback = (flags & GS_NOFALLBACK) ? 1 : 0;
+  if (!dev) {
+    mb.ns = (const int*)(base + o_ns);
+    mb.offs = (const long long*)(base + o_offs);
+    mb.woffs = (const long long*)(base + o_woffs);
+    mb.A = (double*)(base + o_A);
+    mb.Z = wantz ? (double*)(base + o_Z) : nullptr;
+    mb.wr = (double*)(base + o_wr);
+    mb.wi = (double*)(base + o_wi);
+    mb.status = (int*)(base + o_st);
+    if (!(flags & GS_GRAPH) && in_order && count >= kPipeMinCount) {
+      // each run: the whole mixed sequence on its matrices, with its own slice of the
+      // per-matrix scratch and its own schedules
+      return batched_pipelined<double>(
+          ctx, count, ns, offs, woffs, A, Z, wr, wi, status, (int*)mb.ns, (long long*)mb.offs, (long long*)mb.woffs,
+          mb.A, mb.Z, mb.wr, mb.wi, mb.status, [&](int c, int64_t b0, int64_t b1, cudaStream_t cs) -> int {
+            MixedBatch mc = mb;
+            mc.count = (int)(b1 - b0);
+            mc.ns = mb.ns + b0;
+            mc.offs = mb.offs + b0;
+            mc.woffs = mb.woffs + b0;
+            mc.status = mb.status + b0;
+            mc.order = mb.order + b0;
+            mc.sched = mb.sched + 3 * kNumBins * c;
+            mc.iws = mb.iws + 2 * b0 + (size_t)c * kMixedSchedInts;
+            cudaError_t e = launch_mixed_batched(mc, ctx->num_sms, cs, ctx->pipe_aux[c], kNumBins, ctx->pipe_fork[c],
+                                                 ctx->pipe_join[c], ctx->tun_real, ctx->tun_mixed32);
+            if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
+            return GS_OK;
+          });
+    }
+    CK(cudaMemcpyAsync((void*)mb.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)mb.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)mb.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(mb.A, A, sizeof(double) * na, cudaMemcpyHostToDevice, s));
+  } else {
+    mb.ns = ns;
+    mb.offs = (const long long*)offs;
+    mb.woffs = (const long long*)woffs;
+    mb.A = A;
+    mb.Z = wantz ? Z : nullptr;
+    mb.wr = wr;
+    mb.wi = wi;
+    mb.status = status;
+  }
+  std::vector<long long> key = {-1, (long long)count, (long long)(uintptr_t)mb.A, (long long)(uintptr_t)mb.Z,
+                                (long long)(uintptr_t)mb.ns, (long long)(uintptr_t)mb.wr, (long long)(uintptr_t)mb.ws,
+                                na, nw, (long long)flags, ctx->tun_gen};
+  rc = run_graph_or_direct(ctx, (flags & GS_GRAPH) != 0, key, [&](cudaStream_t st) -> int {
+    cudaError_t e = launch_mixed_batched(mb, ctx->num_sms, st, ctx->aux, kNumBins, ctx->fork, ctx->join, ctx->tun_real,
+                                         ctx->tun_mixed32);
+    if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
+    return GS_OK;
+  });
+  if (rc) return rc;
+  if (dev) return GS_OK;
+  CK(cudaMemcpyAsync(A, mb.A, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
+  if (wantz) CK(cudaMemcpyAsync(Z, mb.Z, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wr, mb.wr, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(wi, mb.wi, sizeof(double) * nw, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(status, mb.status, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int64_t b = 0; b < count; ++b)
+    if (status[b] != GS_OK) return set_err(ctx, GS_UNCONVERGED, "matrix %lld: iteration limit reached", (long long)b);
+  return GS_OK;
+}
+
 extern "C" {
 int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                          const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
                          int32_t* status, unsigned flags) {
+  if (flags & GS_MIXED) return schur_batched_mixed_impl(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
   return schur_batched_real_impl<double>(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
 }
 

@@ -1,0 +1,6 @@
+// Mixed-precision batched refinement, size bin of orders <= 96 (row tile 6 x 16).
+#include "refine_bin_impl.cuh"
+
+namespace gsk {
+template cudaError_t launch_refine_bin<6>(const RefineArgs&, int, int, cudaStream_t);
+}  // namespace gsk

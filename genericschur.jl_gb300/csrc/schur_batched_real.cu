@@ -24,6 +24,8 @@
 // everything step k+1 reads was written by one side or the other before the
 // barrier.  Each sweep's reflectors are logged and applied to the Z rows in one
 // streaming pass afterwards (every thread owns rows of Z).
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "gs_internal.h"
 
@@ -562,7 +564,9 @@ cudaError_t launch_bin(const RealBatchT<T, W>& bt, const int* order, int* sched,
 }
 
 // One bin with the requested shape.  FP64 compiles every shape of kTuneThreads with
-// and without the shared-memory Hessenberg phase; FP32 only the default shapes.
+// and without the shared-memory Hessenberg phase, the FP32 kernel with FP32 eigenvalues
+// (Float32 batches and the FP32 stage of the mixed form) the same but 160 threads, the
+// FP32 kernel with FP64 eigenvalues (the large path's small solves) the default shapes.
 template <class T, class W>
 cudaError_t launch_shape(const RealBatchT<T, W>& bt, const int* order, int* sched, int bin, int nmax, int nt,
                          int hsmem, int ctas, int num_sms, cudaStream_t s) {
@@ -572,6 +576,10 @@ cudaError_t launch_shape(const RealBatchT<T, W>& bt, const int* order, int* sche
     GS_SHAPE(64, true) GS_SHAPE(64, false) GS_SHAPE(96, true) GS_SHAPE(96, false)
     GS_SHAPE(128, true) GS_SHAPE(128, false) GS_SHAPE(160, true) GS_SHAPE(160, false)
     GS_SHAPE(192, true) GS_SHAPE(192, false) GS_SHAPE(256, true) GS_SHAPE(256, false)
+  } else if constexpr (std::is_same_v<W, float>) {
+    GS_SHAPE(64, true) GS_SHAPE(64, false) GS_SHAPE(96, true) GS_SHAPE(96, false)
+    GS_SHAPE(128, true) GS_SHAPE(128, false) GS_SHAPE(192, true) GS_SHAPE(192, false)
+    GS_SHAPE(256, true) GS_SHAPE(256, false)
   } else {
     GS_SHAPE(64, true) GS_SHAPE(128, false)
   }
@@ -595,6 +603,7 @@ cudaError_t launch_all_bins(const RealBatchT<T, W>& bt, const int* order, int* s
 }  // namespace
 
 size_t real_bin_smem_bytes(int nmax, int hsmem) { return sizeof(double) * bin_smem_elems(nmax, hsmem != 0); }
+size_t real32_bin_smem_bytes(int nmax, int hsmem) { return sizeof(float) * bin_smem_elems(nmax, hsmem != 0); }
 
 template <class T, class W>
 cudaError_t launch_schur_batched_real(const RealBatchT<T, W>& bt, const int* order, int* sched, int num_sms,
@@ -621,6 +630,11 @@ template cudaError_t launch_schur_real_one<float, double>(const RealBatchT<float
 
 cudaError_t launch_schur_batched_real_tuned(const RealBatchT<double, double>& bt, const int* order, int* sched,
                                             int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun) {
+  return launch_all_bins(bt, order, sched, num_sms, streams, nstreams, tun);
+}
+
+cudaError_t launch_schur_batched_real32_tuned(const RealBatchT<float, float>& bt, const int* order, int* sched,
+                                              int num_sms, cudaStream_t* streams, int nstreams, const BinTuning& tun) {
   return launch_all_bins(bt, order, sched, num_sms, streams, nstreams, tun);
 }
 

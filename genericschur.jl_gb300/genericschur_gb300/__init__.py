@@ -288,12 +288,15 @@ def unpack_batch(packed, ns, offs):
 
 
 def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ=True, scale=True, graph=False,
-                   ctx=None, raise_on_failure=True):
+                   ctx=None, raise_on_failure=True, mixed=False, fallback=True):
     """gschur! over a ragged batch (orders <= 128) in one launch sequence.
 
     Pass either `mats` (list of square arrays) or the packed form (packed, ns,
     offs, woffs) as produced by pack_batch.  Returns (T_list, Z_list, values_list,
     status) for `mats`, or (T_packed, Z_packed, w_packed, status) for packed input.
+    mixed=True (real Float64 only): FP32 Schur pairs refined to FP64 accuracy by
+    Newton steps; matrices the refinement cannot finish are recomputed in FP64, or,
+    with fallback=False, reported as unconverged.
     """
     ctx = ctx or get_context()
     lists = mats is not None
@@ -314,6 +317,10 @@ def gschur_batched(mats=None, packed=None, ns=None, offs=None, woffs=None, wantZ
     nw = int(ns.sum()) if count else 0
     nw = max(nw, int((woffs + ns).max()) if count else 0)
     flags = (GS_WANTZ if wantZ else 0) | (GS_SCALE if scale else 0) | (GS_GRAPH if graph else 0)
+    if mixed:
+        if cplx or single:
+            raise ArgumentError("gschur_batched: mixed=True applies to real Float64 batches")
+        flags |= _capi.GS_MIXED | (0 if fallback else _capi.GS_NOFALLBACK)
     status = np.zeros(count, dtype=np.int32)
     Z = np.zeros_like(packed) if wantZ else None
     lib = ctx.lib

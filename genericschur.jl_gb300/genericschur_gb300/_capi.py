@@ -27,6 +27,7 @@ GS_RAW = 16
 GS_NOFALLBACK = 32
 GS_BAL_PERMUTE = 64
 GS_DC = 128
+GS_MIXED = 256
 
 _i = ctypes.c_int
 _i64 = ctypes.c_int64

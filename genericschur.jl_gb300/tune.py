@@ -6,7 +6,9 @@ phase runs on a full copy of the matrix in shared memory, and a cap on CTAs per 
 This script times every compiled shape on each bin's share of the benchmark batches --
 20,000 real N(0,1) matrices with orders ~ U{8..128} (seed 4) and 5,000 complex ones
 (seed 5) -- picks the fastest per bin, then tries a few bin boundaries with the chosen
-shapes on the whole batch, and writes the table that gs_set_tuning loads:
+shapes on the whole batch; for the FP32 stage of the mixed real form (GS_MIXED, default
+bins kept) it improves one bin's shape at a time, largest bin first, timing the whole
+mixed call on the real batch.  It writes the table that gs_set_tuning loads:
 
     python genericschur.jl_gb300/tune.py [--out PATH] [--reps 5] [--margin 0.02]
 
@@ -39,10 +41,10 @@ MAX_DYN_SMEM = 227 * 1024 - 1024
 
 def smem_bytes(kind, nmax, hsmem):
     """Dynamic shared memory per CTA, as the kernels size it."""
-    if kind == "real_f64":
+    if kind in ("real_f64", "mixed_f32"):
         full = nmax * (nmax | 1) if hsmem else 0
         rpk = (nmax * (nmax + 7)) // 2  # real packed QR layout: column j keeps rows 1..j+3
-        return 8 * (max(full, rpk) + 6 * nmax + 32)
+        return (8 if kind == "real_f64" else 4) * (max(full, rpk) + 6 * nmax + 32)
     pk = (nmax * (nmax + 5)) // 2  # complex packed QR layout: column j keeps rows 1..j+2
     h = nmax * (nmax | 1) if hsmem else pk
     return 16 * (h + 4 * nmax) + 32 * 8 + 64
@@ -52,7 +54,7 @@ def table_text(shapes, note):
     lines = ["# gschur_gb300 batched tuning table (genericschur.jl_gb300/tune.py)"]
     lines += ["# " + x for x in note]
     lines.append("# kind bin nmax threads hsmem ctas_per_sm")
-    for kind in ("real_f64", "complex_f64"):
+    for kind in ("real_f64", "complex_f64", "mixed_f32"):
         for b, (nmax, nt, hs, ctas) in enumerate(shapes[kind]):
             lines.append("%s %d %d %d %d %d" % (kind, b, nmax, nt, hs, ctas))
     return "\n".join(lines) + "\n"
@@ -61,7 +63,7 @@ def table_text(shapes, note):
 class Runner:
     """Device-resident copy of one batch and a timed call of the batched entry point."""
 
-    def __init__(self, ctx, torch, dev, kind, packed, ns, offs, woffs):
+    def __init__(self, ctx, torch, dev, kind, packed, ns, offs, woffs, mixed=False):
         from genericschur_gb300 import _capi
         self.ctx, self.torch, self.kind, self.count = ctx, torch, kind, len(ns)
         self.cplx = kind == "complex_f64"
@@ -76,6 +78,8 @@ class Runner:
         self.ns, self.offs, self.woffs = (torch.from_numpy(x).to(dev) for x in (ns, offs, woffs))
         # the benchmark's mode: the launch sequence replayed as a CUDA graph
         self.flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | _capi.GS_GRAPH
+        if mixed:
+            self.flags |= _capi.GS_MIXED
         self.stream = torch.cuda.Stream(dev)
 
     def run(self):
@@ -140,7 +144,7 @@ def main():
     ctx = gs.Context(0)
     t_start = time.time()
     base_shapes = [(b, nt, hs, 0) for b, nt, hs in zip(DEFAULT_BOUNDS, DEFAULT_THREADS, DEFAULT_HSMEM)]
-    default = {"real_f64": list(base_shapes), "complex_f64": list(base_shapes)}
+    default = {"real_f64": list(base_shapes), "complex_f64": list(base_shapes), "mixed_f32": list(base_shapes)}
     batches = {"real_f64": batched_real(20000, seed=4), "complex_f64": batched_cplx(5000, seed=5)}
     chosen = {k: list(v) for k, v in default.items()}
     log = []
@@ -207,11 +211,39 @@ def main():
             print(log[-1], flush=True)
             del r
             torch.cuda.empty_cache()
+        # FP32 stage of the mixed form: one bin at a time on the whole mixed call
+        r = Runner(ctx, torch, dev, "real_f64", *batches["real_f64"], mixed=True)
+        apply(ctx, chosen, tmp)
+        base = cur = r.time(args.reps)
+        _, bad = r.eigenvalues()
+        assert bad == 0
+        for b in reversed(range(len(DEFAULT_BOUNDS))):
+            hi = DEFAULT_BOUNDS[b]
+            for nt in THREADS:
+                for hs in (0, 1):
+                    if nt == 160 or smem_bytes("mixed_f32", hi, hs) > MAX_DYN_SMEM or \
+                            (hi, nt, hs, 0) == chosen["mixed_f32"][b]:
+                        continue
+                    cand = {k: list(v) for k, v in chosen.items()}
+                    cand["mixed_f32"][b] = (hi, nt, hs, 0)
+                    apply(ctx, cand, tmp)
+                    ms = r.time(args.reps)
+                    _, bad = r.eigenvalues()
+                    log.append("mixed_f32 bin %d threads %d hsmem %d: whole mixed batch %.2f ms%s"
+                               % (b, nt, hs, ms, "" if bad == 0 else " REJECTED"))
+                    print(log[-1], flush=True)
+                    if bad == 0 and ms < cur * (1.0 - args.margin):
+                        cur = ms
+                        chosen["mixed_f32"][b] = (hi, nt, hs, 0)
+        log.append("mixed_f32 whole mixed batch: default shapes %.2f ms, chosen %.2f ms" % (base, cur))
+        print(log[-1], flush=True)
+        del r
+        torch.cuda.empty_cache()
     note = ["device: %s; tuned %s in %.0f s" % (torch.cuda.get_device_name(0), time.strftime("%Y-%m-%d"),
                                                  time.time() - t_start),
             "workloads: real 20000 N(0,1) n~U{8..128} seed 4; complex 5000 seed 5; CUDA graph replay; "
             "a shape replaces the default only when %.0f%% faster" % (100 * args.margin)] + \
-        [x for x in log if "whole batch" in x]
+        [x for x in log if "whole batch" in x or "whole mixed batch: default" in x]
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     with open(args.out, "w") as f:
         f.write(table_text(chosen, note))

@@ -49,6 +49,7 @@ extern "C" {
 #define GS_NOFALLBACK 32u /* mixed precision: report GS_UNCONVERGED instead of recomputing in FP64   */
 #define GS_BAL_PERMUTE 64u /* balancing: search the row/column permutations (with GS_SCALE: scale too) */
 #define GS_DC 128u         /* Hermitian eigensolver: DivideAndConquer() instead of QRIteration()       */
+#define GS_MIXED 256u      /* batched real FP64: FP32 Schur + FP64 Newton refinement, same accuracy    */
 
 typedef struct gs_context gs_context;
 
@@ -73,15 +74,17 @@ GS_API float gs_last_kernel_ms(const gs_context* ctx);
 
 /* Launch shapes of the batched kernels (no reference counterpart: the reference has no
  * batched form).  gs_set_tuning loads a table written by the project's tuner
- * (genericschur.jl_gb300/tune.py) for this context: per size bin of the real FP64 and
- * the complex batched Schur kernels, the bin's largest order, threads per CTA, whether
- * the Hessenberg phase runs in shared memory, and a cap on CTAs per SM.  Text lines
- * "kind bin nmax threads hsmem ctas_per_sm" (kind real_f64 or complex_f64; '#' starts a
- * comment; bins not listed keep their defaults).  path NULL or "" restores the built-in
- * defaults.  GS_BADARG (message in gs_last_error) for an unreadable file, a shape that is
- * not compiled or does not fit in shared memory, or bounds that do not increase to 128;
- * the context keeps its previous shapes then.  Results do not depend on the shapes
- * beyond rounding.  gs_get_tuning writes the active table (same format) into buf. */
+ * (genericschur.jl_gb300/tune.py) for this context: per size bin of the real FP64, the
+ * complex, and the FP32 stage of the mixed real (GS_MIXED) batched Schur kernels, the
+ * bin's largest order, threads per CTA, whether the Hessenberg phase runs in shared
+ * memory, and a cap on CTAs per SM.  Text lines "kind bin nmax threads hsmem ctas_per_sm"
+ * (kind real_f64, complex_f64 or mixed_f32; '#' starts a comment; bins not listed keep
+ * their defaults; mixed_f32 bins keep the default bounds 32/64/96/128).  path NULL or ""
+ * restores the built-in defaults.  GS_BADARG (message in gs_last_error) for an unreadable
+ * file, a shape that is not compiled or does not fit in shared memory, or bounds that do
+ * not increase to 128; the context keeps its previous shapes then.  Results do not depend
+ * on the shapes beyond rounding.  gs_get_tuning writes the active table (same format)
+ * into buf. */
 GS_API int gs_set_tuning(gs_context* ctx, const char* path);
 GS_API int gs_get_tuning(const gs_context* ctx, char* buf, size_t len);
 
