@@ -1,16 +1,21 @@
-"""Benchmark of the batched real FP64 Schur decomposition (the headline workload).
+"""Benchmark of the batched real Float64 Schur decomposition (the headline workload).
 
 Workload: 20,000 real Float64 matrices, orders iid uniform in [8, 128], entries iid
 N(0,1), seed 4 (one batch per rank); each step is one gschur! over the whole batch
-returning T, Z and the eigenvalues.
+returning T, Z and the eigenvalues at FP64 backward error.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` is matrices/s with the inputs resident in HBM (CUDA events on the launch
-stream; the step includes restoring A, which the decomposition overwrites);
-`e2e` is the same metric through the C-ABI with pinned host buffers, host<->device
-copies inside the timed region.  `--impl reference` times the CPU restatement of
-the reference algorithm (the oracle) on the host cores instead.
+The metric compares the mixed form with the FP64 form at equal backward error: the
+headline `value` is the mixed form (GS_MIXED: FP32 Schur sweeps, FP64 Newton refinement
+of each Schur pair, FP64 recomputation of the matrices the refinement cannot finish),
+`fp64` the plain FP64 batched form on the same inputs, and `accuracy` both forms'
+backward and orthogonality errors on the same sample.  `value` is matrices/s with the
+inputs resident in HBM (CUDA events on the launch stream; the step includes restoring
+A, which the decomposition overwrites); `e2e` is the same metric through the C-ABI with
+pinned host buffers, host<->device copies inside the timed region.  `--impl reference`
+times the CPU restatement of the reference algorithm (the oracle, FP64) on the host
+cores instead.
 """
 import argparse
 import json
@@ -270,69 +275,104 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
-    flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | (0 if args.no_graph else _capi.GS_GRAPH)
+    base_flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | (0 if args.no_graph else _capi.GS_GRAPH)
     lib = ctx.lib
 
-    def step():
-        dA.copy_(dA0)
-        rc = lib.gs_schur_batched_f64(ctx.handle, count, dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
-                                      dA.data_ptr(), dZ.data_ptr(), dwr.data_ptr(), dwi.data_ptr(), dst.data_ptr(),
-                                      flags)
-        if rc != 0:
-            raise RuntimeError("gs_schur_batched_f64 failed: %s" % ctx.last_error())
+    def make_step(flags):
+        def step():
+            dA.copy_(dA0)
+            rc = lib.gs_schur_batched_f64(ctx.handle, count, dns.data_ptr(), doffs.data_ptr(), dwoffs.data_ptr(),
+                                          dA.data_ptr(), dZ.data_ptr(), dwr.data_ptr(), dwi.data_ptr(),
+                                          dst.data_ptr(), flags)
+            if rc != 0:
+                raise RuntimeError("gs_schur_batched_f64 failed: %s" % ctx.last_error())
+        return step
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    bad = int((dst != 0).sum().item())
-    # per-launch kernel time of the batched Schur sequence (dominant kernel), events on its stream
-    kms = []
-    clocks = ClockSampler(local)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms_total = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    # kernel-only time per launch (CUDA events recorded by the library around its kernels)
-    for _ in range(2):
-        step()
+    def timed(flags, sample_clocks):
+        """W warm-up steps, then K steps between a barrier and synchronizes (CUDA events on
+        the library's stream); returns ms per step, the kernel-only ms of two further
+        steps, unconverged count, the clock record, and the results of the last step."""
+        step = make_step(flags)
+        for _ in range(args.warmup):
+            step()
         torch.cuda.synchronize()
-        kms.append(ctx.last_kernel_ms())
-    ms = reduce_max_ms(torch, ms_total / args.steps, world, dev)
-    value = job_throughput(world, count, ms)
+        bad = int((dst != 0).sum().item())
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ms_total = e0.elapsed_time(e1)
+        clk = clocks.stop() if clocks else None
+        kms = []
+        for _ in range(2):
+            step()
+            torch.cuda.synchronize()
+            kms.append(ctx.last_kernel_ms())
+        res = (dA.cpu().numpy(), dZ.cpu().numpy(), dwr.cpu().numpy() + 1j * dwi.cpu().numpy())
+        return ms_total / args.steps, float(np.mean(kms)), bad, clk, res
 
-    e2e = None
+    # headline: the mixed form (FP32 Schur sweeps, FP64 Newton refinement; FP64 accuracy)
+    mixed_flags = base_flags | _capi.GS_MIXED
+    ms_mixed, kms_mixed, bad, clk, res_mixed = timed(mixed_flags, True)
+    info = ctx.mixed_info()  # counters and refinement time of the last (kernel-timed) step
+    # the plain FP64 batched form on the same inputs
+    ms_fp64, kms_fp64, bad64, _, res_fp64 = timed(base_flags, False)
+    ms = reduce_max_ms(torch, ms_mixed, world, dev)
+    value = job_throughput(world, count, ms)
+    value64 = job_throughput(world, count, reduce_max_ms(torch, ms_fp64, world, dev))
+
+    e2e = e2e64 = None
     if not args.no_e2e:
-        e2e = measure_e2e(ctx, packed, ns, offs, woffs, steps=max(1, min(args.steps, 3)))
+        e2e = measure_e2e(ctx, packed, ns, offs, woffs, steps=max(1, min(args.steps, 3)), mixed=True)
+        e2e64 = measure_e2e(ctx, packed, ns, offs, woffs, steps=max(1, min(args.steps, 3)))
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
     peak = fp64_peak_tflops(torch, dev)
-    kernel_ms = float(np.mean(kms))
+    # roofline of the mixed step's dominant phase: the refinement kernels (four size-bin
+    # launches running concurrently), bound by the FP64 pipe; their FP64 FLOPs are counted by
+    # the kernels (algorithmic triangles, not the executed tiles) and timed by CUDA events the
+    # library records around them on its stream
+    ref_s = info["refine_us"] * 1e-6 if info["refine_us"] > 0 else None
+    ach = info["fp64_flops"] / ref_s / 1e12 if ref_s else None
+    roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": (ach / peak) if ach else None, "traffic": None,
+            "kernel": "k_refine_bin<2,4,6,8> (refinement phase of the mixed step)",
+            "phase_ms": info["refine_us"] * 1e-3, "step_kernel_ms": kms_mixed,
+            "algorithmic": "FP64 FLOPs of the refinement: per Newton step 2 n^3 (A Z) + n^3 (lower triangle of "
+                           "Z^T A Z) + n^3 (lower triangle of Z^T Z), plus n^3 for the last step's upper triangle; "
+                           "%.4g FLOP in %d Newton steps over %d matrices" % (info["fp64_flops"], info["newton_steps"],
+                                                                            info["refined"] + info["handed_back"]),
+            "peak_source": "measured: cuBLAS DGEMM 4096^3 in this run (FP64 FMA pipe; no FP64 tensor-core path "
+                           "is faster on GB300)"}
+    kernel_ms = kms_fp64
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     per_matrix_bytes = measured_traffic_per_matrix()
     traffic = per_matrix_bytes * count if per_matrix_bytes else None
-    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": traffic,
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of the 4 size-bin launches of one step, "
-                              "ncu capture of a 6000-matrix case of the same law scaled by matrices "
-                              "(profiles/k_schur_real_traffic.txt); algorithmic bytes 24 n^2 + 16 n per matrix "
-                              "= %.4g per step" % float(np.sum(24.0 * ns.astype(np.float64) ** 2 + 16.0 * ns)),
-            "peak_source": "measured: cuBLAS DGEMM 4096^3 in this run (FP64 FMA pipe; no FP64 tensor-core path "
-                           "is faster on GB300)",
-            "algorithmic": "25 n^3 FLOP per matrix, summed over the batch (%.4g FLOP per launch)" % flops,
-            "kernel_ms": kernel_ms}
+    roof64 = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+              "traffic": traffic, "kernel": "k_schur_real<double> (four size-bin launches)",
+              "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of the 4 size-bin launches of one "
+                                "step, ncu capture of a 6000-matrix case of the same law scaled by matrices "
+                                "(profiles/k_schur_real_traffic.txt); algorithmic bytes 24 n^2 + 16 n per matrix "
+                                "= %.4g per step" % float(np.sum(24.0 * ns.astype(np.float64) ** 2 + 16.0 * ns)),
+              "algorithmic": "25 n^3 FLOP per matrix, summed over the batch (%.4g FLOP per launch)" % flops,
+              "kernel_ms": kernel_ms}
+    accuracy = {"mixed": schur_errors_sample(packed, ns, offs, woffs, res_mixed),
+                "fp64": schur_errors_sample(packed, ns, offs, woffs, res_fp64)}
+    fp64 = {"value": value64, "unit": UNIT, "ms_per_step": ms_fp64, "unconverged": bad64, "roofline": roof64,
+            "e2e": e2e64, "gpu_launches_per_step": 5}
     cpu = None if args.no_cpu else cpu_baseline_sample(args.count, SEED)
     per_matrix = measure_per_matrix(ctx, packed, ns, offs)
     secondary = measure_complex_and_adjoint(ctx, torch, dev, stream)
@@ -352,10 +392,16 @@ def run_ours(args):
         stedc = measure_stedc(ctx, args.dc_n)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "form": "mixed (GS_MIXED): FP32 Schur sweeps, per-matrix FP64 Newton refinement of the Schur pair, "
+                   "FP64 recomputation of matrices the refinement cannot finish; results at FP64 backward error "
+                   "(accuracy: both forms measured on the same sample in this run)",
            "config": bench_config(args.count), "graph": not args.no_graph,
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-           "gpu_launches": 5 * args.steps, "unconverged": bad, "plain_fp64_per_matrix": per_matrix,
+           "gpu_launches": 16 * args.steps, "unconverged": bad, "refinement": info,
+           "fp64": fp64, "mixed_vs_fp64": value / value64,
+           "mixed_vs_fp64_e2e": (e2e["value"] / e2e64["value"]) if (e2e and e2e64) else None,
+           "accuracy": accuracy, "plain_fp64_per_matrix": per_matrix,
            "large": large, "large_1024_2048": large_small, "precision": precision, "complex256": c1,
            "gemm_f64_tc": gemm_tc, "stedc": stedc, **secondary}
     print(json.dumps(out))
@@ -567,7 +613,26 @@ def measure_complex_and_adjoint(ctx, torch, dev, stream, steps=3):
     return out
 
 
-def measure_e2e(ctx, packed, ns, offs, woffs, steps):
+def schur_errors_sample(packed, ns, offs, woffs, res, every=20):
+    """Backward error ||A - Z T Z^T||_F / ||A||_F and orthogonality ||Z^T Z - I||_F, in
+    units of n eps, of every `every`-th matrix of a batch result (numpy, on the host)."""
+    T, Z, _ = res
+    be, oe = [], []
+    for b in range(0, len(ns), every):
+        n = int(ns[b])
+        o = int(offs[b])
+        A = packed[o:o + n * n].reshape((n, n), order="F")
+        Tb = T[o:o + n * n].reshape((n, n), order="F")
+        Zb = Z[o:o + n * n].reshape((n, n), order="F")
+        eps = np.finfo(np.float64).eps
+        be.append(np.linalg.norm(A - Zb @ Tb @ Zb.T) / np.linalg.norm(A) / (n * eps))
+        oe.append(np.linalg.norm(Zb.T @ Zb - np.eye(n)) / (n * eps))
+    return {"backward_max": float(np.max(be)), "backward_median": float(np.median(be)),
+            "orth_max": float(np.max(oe)), "orth_median": float(np.median(oe)), "unit": "n eps",
+            "sample": "every %dth matrix (%d)" % (every, len(be))}
+
+
+def measure_e2e(ctx, packed, ns, offs, woffs, steps, mixed=False):
     """Same metric through the C-ABI with pinned host buffers (copies included)."""
     import ctypes
     from genericschur_gb300 import _capi
@@ -581,7 +646,7 @@ def measure_e2e(ctx, packed, ns, offs, woffs, steps):
         A = np.ctypeslib.as_array((ctypes.c_double * packed.size).from_address(hp[0]))
         Z = np.ctypeslib.as_array((ctypes.c_double * packed.size).from_address(hp[1]))
         ctx.set_stream(None)
-        flags = _capi.GS_WANTZ | _capi.GS_SCALE
+        flags = _capi.GS_WANTZ | _capi.GS_SCALE | (_capi.GS_MIXED if mixed else 0)
         times = []
         for i in range(steps + 1):
             A[:] = packed

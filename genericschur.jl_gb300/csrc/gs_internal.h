@@ -493,6 +493,9 @@ struct MixedBatch {
   long long na, nw;
   int scale;
   int nofallback;
+  unsigned long long* stats;      // null, or 4 counters the caller zeroed: matrices refined,
+                                  // handed back to FP64, Newton steps, FP64 FLOPs of the refinement
+  cudaEvent_t ref0, ref1;         // null, or recorded around the refinement kernels
 };
 size_t mixed_batched_ws_bytes(long long na, long long nw, bool wantz);
 constexpr size_t kMixedSchedInts = 4 * kNumBins + 8;

@@ -30,6 +30,10 @@ struct gs_context {
   cudaEvent_t fork = nullptr, join[kNumBins] = {};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool timed = false;
+  // mixed batched form: refinement counters (device) and events around the refinement
+  unsigned long long* mix_stats = nullptr;
+  cudaEvent_t mix_e0 = nullptr, mix_e1 = nullptr;
+  bool mix_valid = false, mix_timed = false;
   char* dws = nullptr;
   size_t dws_cap = 0;
   std::string err;
@@ -161,6 +165,9 @@ int gs_destroy(gs_context* ctx) {
   if (ctx->fork) cudaEventDestroy(ctx->fork);
   if (ctx->t0) cudaEventDestroy(ctx->t0);
   if (ctx->t1) cudaEventDestroy(ctx->t1);
+  if (ctx->mix_stats) cudaFree(ctx->mix_stats);
+  if (ctx->mix_e0) cudaEventDestroy(ctx->mix_e0);
+  if (ctx->mix_e1) cudaEventDestroy(ctx->mix_e1);
   if (ctx->cap) cudaStreamDestroy(ctx->cap);
   if (ctx->pipe_ready) {
     for (int c = 0; c < kPipeChunks; ++c) {
@@ -657,6 +664,14 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   mb.sched = (int*)(base + o_sched);
   mb.ws = base + o_ws;
   mb.iws = (int*)(base + o_iws);
+  if (!ctx->mix_stats) {
+    CK(cudaMalloc(&ctx->mix_stats, 4 * sizeof(unsigned long long)));
+    CK(cudaEventCreate(&ctx->mix_e0));
+    CK(cudaEventCreate(&ctx->mix_e1));
+  }
+  mb.stats = ctx->mix_stats;
+  ctx->mix_valid = true;
+  ctx->mix_timed = false;
   mb.na = na;
   mb.nw = nw;
   mb.scale = (flags & GS_SCALE) ? 1 : 0;
@@ -672,7 +687,8 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
     mb.status = (int*)(base + o_st);
     if (!(flags & GS_GRAPH) && in_order && count >= kPipeMinCount) {
       // each run: the whole mixed sequence on its matrices, with its own slice of the
-      // per-matrix scratch and its own schedules
+      // per-matrix scratch and its own schedules (the counters add up over the runs)
+      CK(cudaMemsetAsync(mb.stats, 0, 4 * sizeof(unsigned long long), s));
       return batched_pipelined<double>(
           ctx, count, ns, offs, woffs, A, Z, wr, wi, status, (int*)mb.ns, (long long*)mb.offs, (long long*)mb.woffs,
           mb.A, mb.Z, mb.wr, mb.wi, mb.status, [&](int c, int64_t b0, int64_t b1, cudaStream_t cs) -> int {
@@ -708,7 +724,11 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   std::vector<long long> key = {-1, (long long)count, (long long)(uintptr_t)mb.A, (long long)(uintptr_t)mb.Z,
                                 (long long)(uintptr_t)mb.ns, (long long)(uintptr_t)mb.wr, (long long)(uintptr_t)mb.ws,
                                 na, nw, (long long)flags, ctx->tun_gen};
+  mb.ref0 = ctx->mix_e0;
+  mb.ref1 = ctx->mix_e1;
+  ctx->mix_timed = true;
   rc = run_graph_or_direct(ctx, (flags & GS_GRAPH) != 0, key, [&](cudaStream_t st) -> int {
+    CK(cudaMemsetAsync(mb.stats, 0, 4 * sizeof(unsigned long long), st));
     cudaError_t e = launch_mixed_batched(mb, ctx->num_sms, st, ctx->aux, kNumBins, ctx->fork, ctx->join, ctx->tun_real,
                                          ctx->tun_mixed32);
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
@@ -733,6 +753,24 @@ int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* ns, cons
                          int32_t* status, unsigned flags) {
   if (flags & GS_MIXED) return schur_batched_mixed_impl(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
   return schur_batched_real_impl<double>(ctx, count, ns, offs, woffs, A, Z, wr, wi, status, flags);
+}
+
+int gs_mixed_batched_info(gs_context* ctx, int64_t* info) {
+  if (!ctx || !info) return GS_BADARG;
+  ctx->err.clear();
+  if (!ctx->mix_valid) return set_err(ctx, GS_BADARG, "no GS_MIXED batched call on this context yet");
+  unsigned long long st[4] = {0, 0, 0, 0};
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(st, ctx->mix_stats, sizeof(st), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; ++i) info[i] = (int64_t)st[i];
+  info[4] = -1;
+  float ms = 0.0f;
+  if (ctx->mix_timed) {
+    if (cudaEventElapsedTime(&ms, ctx->mix_e0, ctx->mix_e1) == cudaSuccess) info[4] = (int64_t)(1000.0 * ms);
+    else (void)cudaGetLastError();  // not recorded: leave no error behind for the caller's next launch
+  }
+  return GS_OK;
 }
 
 int gs_schur_batched_f32(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,

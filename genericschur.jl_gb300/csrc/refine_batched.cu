@@ -129,11 +129,16 @@ cudaError_t launch_mixed_batched(const MixedBatch& m, int num_sms, cudaStream_t 
   if (e != cudaSuccess) return e;
   // 3. refinement, largest matrices first
   if ((e = cudaMemsetAsync(ticket, 0, sizeof(int) * kNumBins, s)) != cudaSuccess) return e;
+  // under stream capture: external event nodes, so that the graph's replay records them
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if ((e = cudaStreamIsCapturing(s, &cap)) != cudaSuccess) return e;
+  const unsigned evflags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (m.ref0 && (e = cudaEventRecordWithFlags(m.ref0, s, evflags)) != cudaSuccess) return e;
   RefineArgs ra{};
   ra.count = m.count; ra.ns = m.ns; ra.offs = m.offs; ra.woffs = m.woffs;
   ra.A = m.A; ra.Z = Zw; ra.T32 = A32; ra.Z32 = Z32; ra.P = P; ra.Q = Q; ra.M = M; ra.W = W; ra.NF = NF;
   ra.wr = m.wr; ra.wi = m.wi; ra.status = m.status; ra.exps = exps; ra.order = m.order; ra.sched = m.sched;
-  ra.ticket = ticket; ra.nofallback = m.nofallback;
+  ra.ticket = ticket; ra.nofallback = m.nofallback; ra.stats = m.stats;
   // one kernel per default size bin (orders <= 32, 64, 96, 128: row tiles 2, 4, 6, 8 x 16),
   // forked like the Schur bins so that the bins' tails overlap
   static_assert(kNumBins == 4, "the refinement bins follow the default size bins");
@@ -145,6 +150,7 @@ cudaError_t launch_mixed_batched(const MixedBatch& m, int num_sms, cudaStream_t 
     return launch_refine_bin<2>(ra, 0, num_sms, aux[3 % naux]);
   });
   if (e != cudaSuccess) return e;
+  if (m.ref1 && (e = cudaEventRecordWithFlags(m.ref1, s, evflags)) != cudaSuccess) return e;
   if (m.nofallback) return cudaSuccess;
   // 4. the FP64 kernel on the matrices the refinement handed back
   BinBounds bounds;

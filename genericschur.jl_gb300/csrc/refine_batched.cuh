@@ -30,6 +30,7 @@ struct RefineArgs {
   const int* order;
   const int* sched;  // bin ranges of the bin sort (3 ints per bin)
   int* ticket;       // one zeroed counter per bin
+  unsigned long long* stats;  // null, or: refined, handed back, Newton steps, FP64 FLOPs
   int nofallback;
 };
 

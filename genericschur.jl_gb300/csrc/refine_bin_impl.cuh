@@ -286,7 +286,9 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
   __syncthreads();
   const unsigned char* bid = sm.bid;
   bool ok = false;
+  int steps = 0;
   for (int step = 0; step < kMaxSteps && !ok; ++step) {
+    steps = step + 1;
     // FP64: P = A_s Z; the block-lower part of Q = At = Z^T P (its small entries are the
     // signal); NF = (I - Z^T Z) / 2 from the lower triangle.  The block-upper part of At
     // only feeds FP32 solves until the last step, so it is an FP32 product here and the
@@ -371,8 +373,16 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
     }
     __syncthreads();
   }
+  const unsigned long long n3 = (unsigned long long)n * n * n;
   if (!ok) {
-    if (tid == 0) a.status[b] = a.nofallback ? ST_UNCONVERGED : kStFallback;
+    if (tid == 0) {
+      a.status[b] = a.nofallback ? ST_UNCONVERGED : kStFallback;
+      if (a.stats) {
+        atomicAdd(a.stats + 1, 1ull);
+        atomicAdd(a.stats + 2, (unsigned long long)steps);
+        atomicAdd(a.stats + 3, 4ull * steps * n3);
+      }
+    }
     return;
   }
   // standard form of the 2x2 blocks (_gs2x2!) and the eigenvalues
@@ -417,7 +427,14 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
     for (int idx = tid; idx < nn; idx += kRT) A[idx] *= usc;
     for (int i = tid; i < n; i += kRT) { wr[i] *= usc; wi[i] *= usc; }
   }
-  if (tid == 0) a.status[b] = ST_OK;
+  if (tid == 0) {
+    a.status[b] = ST_OK;
+    if (a.stats) {  // FP64 FLOPs: per step A Z (2 n^3) and two triangles (n^3 each), the last upper triangle
+      atomicAdd(a.stats, 1ull);
+      atomicAdd(a.stats + 2, (unsigned long long)steps);
+      atomicAdd(a.stats + 3, (4ull * steps + 1ull) * n3);
+    }
+  }
 }
 
 // One size bin (orders up to 16 RM): persistent CTAs take the bin's matrices, largest
@@ -437,7 +454,10 @@ __global__ void __launch_bounds__(kRT, 2) k_refine_bin(RefineArgs a, int bin) {
     if (n < 1 || n > kSmallMax) continue;  // empty (ST_OK) or order out of range (ST_BADARG)
     const int st = a.status[b];
     if (st != ST_OK) {
-      if (threadIdx.x == 0 && st == ST_UNCONVERGED && !a.nofallback) a.status[b] = kStFallback;
+      if (threadIdx.x == 0 && st == ST_UNCONVERGED) {
+        if (!a.nofallback) a.status[b] = kStFallback;
+        if (a.stats) atomicAdd(a.stats + 1, 1ull);
+      }
       continue;
     }
     refine_one<RM>(a, b, n, sm);

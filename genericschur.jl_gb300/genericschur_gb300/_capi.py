@@ -50,6 +50,7 @@ SIGNATURES = {
     "gs_schur_f32": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _p, _u, _i64]),
     "gs_schur_c64": (_i, [_p, _i64, _p, _i64, _p, _i64, _p, _u, _i64, _i64]),
     "gs_schur_batched_f64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
+    "gs_mixed_batched_info": (_i, [_p, _p]),
     "gs_schur_batched_f32": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_schur_batched_c64": (_i, [_p, _i64, _p, _p, _p, _p, _p, _p, _p, _u]),
     "gs_eigvecs_c64": (_i, [_p, _i64, _p, _p, _p, _p, _u]),
@@ -165,6 +166,16 @@ class Context:
 
     def last_kernel_ms(self):
         return float(self.lib.gs_last_kernel_ms(self.handle))
+
+    def mixed_info(self):
+        """Counters of the last GS_MIXED batched call: refined, handed back to FP64, Newton
+        steps, FP64 FLOPs of the refinement, refinement device time in us (-1 if not timed)."""
+        info = (ctypes.c_int64 * 5)()
+        rc = self.lib.gs_mixed_batched_info(self.handle, info)
+        if rc != GS_OK:
+            raise RuntimeError("gs_mixed_batched_info: %s" % self.last_error())
+        keys = ("refined", "handed_back", "newton_steps", "fp64_flops", "refine_us")
+        return dict(zip(keys, (int(x) for x in info)))
 
     def host_alloc(self, nbytes):
         p = _p()

@@ -139,6 +139,16 @@ GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* n
                          const int64_t* woffs, double* A, double* Z, double* wr, double* wi,
                          int32_t* status, unsigned flags);
 
+/* After a GS_MIXED batched call (GS_MIXED: FP32 Schur pairs refined to FP64 accuracy by
+ * per-matrix Newton steps; matrices the refinement cannot finish are recomputed in FP64,
+ * or with GS_NOFALLBACK reported GS_UNCONVERGED): info[0] matrices finished by the
+ * refinement, info[1] matrices handed back to the FP64 kernel (or reported), info[2]
+ * Newton steps taken, info[3] FP64 FLOPs of the refinement (per step 2 n^3 for A Z and
+ * n^3 for each of two triangles, plus n^3 for the last step's upper triangle), info[4]
+ * device time of the refinement kernels in microseconds (-1 for a pipelined host-buffer
+ * call).  Synchronises the context stream.  GS_BADARG before the first GS_MIXED call. */
+GS_API int gs_mixed_batched_info(gs_context* ctx, int64_t* info);
+
 GS_API int gs_schur_batched_f32(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
                                 const int64_t* woffs, float* A, float* Z, float* wr, float* wi,
                                 int32_t* status, unsigned flags);

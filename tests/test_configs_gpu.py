@@ -54,6 +54,30 @@ def test_batched_real_workload_20000(gs):
         assert ok, "matrix %d (n=%d): worst err/tol %.3g" % (b, n, worst)
 
 
+def test_batched_real_workload_20000_mixed(gs):
+    """The headline batch through the mixed form (GS_MIXED: FP32 Schur sweeps, FP64
+    Newton refinement, FP64 recomputation where the refinement stalls), in one call:
+    status and the Schur-form properties on all 20,000, backward and orthogonality errors
+    within 10 n eps; eigenvalues matched to the oracle's on a seeded sample of 1,000."""
+    from genericschur_gb300.workloads import batched_real
+    packed, ns, offs, woffs = batched_real(20000, seed=4)
+    T, Z, w, st = gs.gschur_batched(packed=packed, ns=ns, offs=offs, woffs=woffs, graph=True, mixed=True)
+    assert np.all(st == 0), np.unique(st, return_counts=True)
+    As, Ts, Zs = _unpack(packed, ns, offs), _unpack(T, ns, offs), _unpack(Z, ns, offs)
+    worst_be = worst_oe = 0.0
+    for b in range(len(ns)):
+        n = int(ns[b])
+        be, oe = assert_schur_real(As[b], Ts[b], Zs[b], w[woffs[b]:woffs[b] + n])
+        worst_be = max(worst_be, be / (n * EPS))
+        worst_oe = max(worst_oe, oe / (n * EPS))
+    assert worst_be <= 10 and worst_oe <= 10
+    for b in _sample(len(ns), 1000, 41):
+        n = int(ns[b])
+        w_ref, tol = eig_tolerances(As[b], po)
+        ok, worst = match_eigenvalues(w[woffs[b]:woffs[b] + n], w_ref, tol)
+        assert ok, "matrix %d (n=%d): worst err/tol %.3g" % (b, n, worst)
+
+
 def test_batched_complex_workload_5000(gs):
     """The complex batch: 5,000 ComplexF64 matrices, orders ~ U{8..128}, re/im iid
     N(0, 1/2), seed 5.  Status and properties on all; eigenvalues matched to the
