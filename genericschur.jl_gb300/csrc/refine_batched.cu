@@ -26,9 +26,10 @@
 //      Z <- Z + Z X, the 2x2 blocks standardised with _gs2x2! (GenericSchur.jl:716-803)
 //      at the unit scale of A_s (its thresholds are absolute: at 1e-300, b c underflows),
 //      then T and the eigenvalues scaled back by 2^e;
-//   4. matrices whose FP32 Schur did not converge, or whose refinement did not reach the
-//      tolerance in kMaxSteps steps (eigenvalues FP32 cannot separate), keep A untouched
-//      and are recomputed by the FP64 batched kernel (or reported unconverged).
+//   4. matrices whose FP32 Schur did not converge, or whose refinement diverges, stops
+//      gaining (from the third step on, less than 4x per step) or has not reached the
+//      tolerance in six steps (eigenvalues FP32 cannot separate), keep A untouched and
+//      are recomputed by the FP64 batched kernel (or reported unconverged).
 // The eigenvalue order is the FP32 run's deflation order; the result satisfies the same
 // backward-error, orthogonality and standard-form conditions as the FP64 path.
 #include <algorithm>

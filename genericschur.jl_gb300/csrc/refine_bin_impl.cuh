@@ -14,7 +14,8 @@ constexpr int kAS = kSmallMax + 4;  // staged op(A) chunk: kKC rows of up to 128
 constexpr int kNC = 2;            // columns per thread in one pass
 constexpr int kPW = 16 * kNC;     // columns per pass
 constexpr int kBS = kPW + 4;      // staged B chunk: kKC rows of kPW entries
-constexpr int kMaxSteps = 4;
+constexpr int kMaxSteps = 6;      // Newton steps before a matrix is handed back
+constexpr float kMinGain = 4.f;    // from the third step on, a step must shrink max|X| this much
 constexpr float kTolFinal = 1e-9f;
 constexpr float kTolDiverge = 1e-1f;
 
@@ -287,6 +288,7 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
   const unsigned char* bid = sm.bid;
   bool ok = false;
   int steps = 0;
+  float xprev = 0.f;
   for (int step = 0; step < kMaxSteps && !ok; ++step) {
     steps = step + 1;
     // FP64: P = A_s Z; the block-lower part of Q = At = Z^T P (its small entries are the
@@ -349,6 +351,8 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
     cta_max3(xmax, d2, d3, sm);
     if (!(xmax <= kTolDiverge)) break;
     ok = xmax <= kTolFinal;
+    if (!ok && step >= 2 && xmax * kMinGain > xprev) break;  // stagnating: hand back
+    xprev = xmax;
     if (ok) {
       // the block-upper part of At in FP64 (the block-lower part is this step's)
       cta_mm<RM, 2, double>(n, n, n, LdT<double, double>{Z, n}, LdNB<double, double>{P, n},
@@ -439,8 +443,10 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
 
 // One size bin (orders up to 16 RM): persistent CTAs take the bin's matrices, largest
 // first, from the bin's ticket counter.
+// Three CTAs per SM (80 registers): measured 327 ms for the 20,000-matrix batch against 350
+// ms with two; four spill the product loops.
 template <int RM>
-__global__ void __launch_bounds__(kRT, 2) k_refine_bin(RefineArgs a, int bin) {
+__global__ void __launch_bounds__(kRT, 3) k_refine_bin(RefineArgs a, int bin) {
   __shared__ Smem sm;
   const int beg = a.sched[3 * bin], end = a.sched[3 * bin + 1];
   for (;;) {
