@@ -76,6 +76,10 @@ def parse():
                     help="only the generalized condition estimates of a complex triangular pair (n = --gcond-n, "
                          "split in half); prints its JSON object")
     ap.add_argument("--gcond-n", type=int, default=1200)
+    ap.add_argument("--case", choices=["mixed_once", "refine_small", "complex256"],
+                    help="profiling cases (no timing, no JSON line): mixed_once = two GS_MIXED calls on the headline "
+                         "batch (device buffers); refine_small = one GS_MIXED call on 600 matrices of orders 97..128; "
+                         "complex256 = two plain complex Schur decompositions of the 256 x 256 workload")
     return ap.parse_args()
 
 
@@ -802,8 +806,56 @@ def run_large_only(args):
     print(json.dumps(measure_large(ctx, torch, dev, args.large_n, args.large_mode)))
 
 
+def run_case(args):
+    """Small fixed cases for ncu launch lists and captures (profiles/)."""
+    import torch
+    import build_lib
+    build_lib.build()
+    import genericschur_gb300 as gs
+    from genericschur_gb300 import _capi
+    if args.case == "complex256":
+        rng = np.random.default_rng(0)
+        A = (rng.standard_normal((256, 256)) + 1j * rng.standard_normal((256, 256))) / np.sqrt(2)
+        for _ in range(2):
+            gs.gschur(A)
+        return
+    if args.case == "refine_small":
+        rng = np.random.default_rng(12)
+        mats = [rng.standard_normal((int(n), int(n))) for n in rng.integers(97, 129, size=600)]
+        _, _, _, st = gs.gschur_batched(mats, mixed=True)
+        assert np.all(st == 0)
+        return
+    from genericschur_gb300.workloads import batched_real
+    dev = torch.device("cuda", 0)
+    ctx = gs.Context(0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    packed, ns, offs, woffs = batched_real(count=COUNT, seed=SEED)
+    dA = torch.from_numpy(packed).to(dev)
+    dZ = torch.empty_like(dA)
+    nw = int(ns.sum())
+    dwr = torch.empty(nw, dtype=torch.float64, device=dev)
+    dwi = torch.empty_like(dwr)
+    dns, doffs, dwo = (torch.from_numpy(x).to(dev) for x in (ns, offs, woffs))
+    dst = torch.empty(len(ns), dtype=torch.int32, device=dev)
+    flags = _capi.GS_WANTZ | _capi.GS_SCALE | _capi.GS_DEVICE | _capi.GS_MIXED
+    for _ in range(2):
+        dA.copy_(torch.from_numpy(packed).to(dev))
+        rc = ctx.lib.gs_schur_batched_f64(ctx.handle, len(ns), dns.data_ptr(), doffs.data_ptr(), dwo.data_ptr(),
+                                          dA.data_ptr(), dZ.data_ptr(), dwr.data_ptr(), dwi.data_ptr(),
+                                          dst.data_ptr(), flags)
+        if rc != 0:
+            raise RuntimeError(ctx.last_error())
+    torch.cuda.synchronize()
+    assert int((dst != 0).sum()) == 0
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args)
+        return
     if args.large_only:
         run_large_only(args)
         return
