@@ -493,13 +493,17 @@ struct MixedBatch {
   long long na, nw;
   int scale;
   int nofallback;
-  unsigned long long* stats;      // null, or 4 counters the caller zeroed: matrices refined,
-                                  // handed back to FP64, Newton steps, FP64 FLOPs of the refinement
+  unsigned long long* stats;      // 4 counters the caller zeroed: matrices refined, handed back
+                                  // to FP64, Newton steps, FP64-accurate product FLOPs
+  int* tc_err;                    // zeroed word, set when a tensor-core wait timed out
   cudaEvent_t ref0, ref1;         // null, or recorded around the refinement kernels
+  cudaEvent_t fp32_wait;  // null, or an event the FP32 stage waits for (a previous run's FP32 stage)
+  cudaEvent_t fp32_done;  // null, or recorded once the FP32 stage has finished
 };
 size_t mixed_batched_ws_bytes(long long na, long long nw, bool wantz);
-constexpr size_t kMixedSchedInts = 4 * kNumBins + 8;
-inline size_t mixed_batched_iws_ints(long long count) { return 2 * (size_t)count + kMixedSchedInts; }
+constexpr size_t kMixedSchedInts = 64;  // schedules and ticket counters of one run
+// per matrix: the scale exponent, the refinement's last step size and the fallback order
+inline size_t mixed_batched_iws_ints(long long count) { return 3 * (size_t)count + kMixedSchedInts; }
 cudaError_t launch_mixed_batched(const MixedBatch& m, int num_sms, cudaStream_t s, cudaStream_t* aux, int naux,
                                  cudaEvent_t fork, cudaEvent_t* join, const BinTuning& tun64, const BinTuning& tun32);
 // Element extents of a device-resident ragged batch: out[0] = max(offs + n^2),

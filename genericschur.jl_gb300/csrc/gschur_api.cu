@@ -51,6 +51,7 @@ struct gs_context {
   cudaStream_t pipe_s[kPipeChunks] = {}, pipe_aux[kPipeChunks][kNumBins] = {}, pipe_d2h = nullptr;
   cudaEvent_t pipe_h2d[kPipeChunks] = {}, pipe_fork[kPipeChunks] = {}, pipe_join[kPipeChunks][kNumBins] = {},
               pipe_done[kPipeChunks] = {}, pipe_out = nullptr;
+  cudaEvent_t pipe_mid[kPipeChunks] = {};  // mixed form: a run's FP32 stage done
 };
 
 namespace {
@@ -175,6 +176,7 @@ int gs_destroy(gs_context* ctx) {
       cudaEventDestroy(ctx->pipe_h2d[c]);
       cudaEventDestroy(ctx->pipe_fork[c]);
       cudaEventDestroy(ctx->pipe_done[c]);
+      cudaEventDestroy(ctx->pipe_mid[c]);
       for (int i = 0; i < kNumBins; ++i) {
         cudaStreamDestroy(ctx->pipe_aux[c][i]);
         cudaEventDestroy(ctx->pipe_join[c][i]);
@@ -363,6 +365,7 @@ static int pipe_setup(gs_context* ctx) {
     CK(cudaEventCreateWithFlags(&ctx->pipe_h2d[c], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->pipe_fork[c], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->pipe_done[c], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->pipe_mid[c], cudaEventDisableTiming));
     for (int i = 0; i < kNumBins; ++i) {
       CK(cudaStreamCreateWithFlags(&ctx->pipe_aux[c][i], cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&ctx->pipe_join[c][i], cudaEventDisableTiming));
@@ -665,11 +668,12 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   mb.ws = base + o_ws;
   mb.iws = (int*)(base + o_iws);
   if (!ctx->mix_stats) {
-    CK(cudaMalloc(&ctx->mix_stats, 4 * sizeof(unsigned long long)));
+    CK(cudaMalloc(&ctx->mix_stats, 5 * sizeof(unsigned long long)));  // 4 counters, the error word
     CK(cudaEventCreate(&ctx->mix_e0));
     CK(cudaEventCreate(&ctx->mix_e1));
   }
   mb.stats = ctx->mix_stats;
+  mb.tc_err = reinterpret_cast<int*>(ctx->mix_stats + 4);
   ctx->mix_valid = true;
   ctx->mix_timed = false;
   mb.na = na;
@@ -688,7 +692,7 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
     if (!(flags & GS_GRAPH) && in_order && count >= kPipeMinCount) {
       // each run: the whole mixed sequence on its matrices, with its own slice of the
       // per-matrix scratch and its own schedules (the counters add up over the runs)
-      CK(cudaMemsetAsync(mb.stats, 0, 4 * sizeof(unsigned long long), s));
+      CK(cudaMemsetAsync(mb.stats, 0, 5 * sizeof(unsigned long long), s));
       return batched_pipelined<double>(
           ctx, count, ns, offs, woffs, A, Z, wr, wi, status, (int*)mb.ns, (long long*)mb.offs, (long long*)mb.woffs,
           mb.A, mb.Z, mb.wr, mb.wi, mb.status, [&](int c, int64_t b0, int64_t b1, cudaStream_t cs) -> int {
@@ -700,7 +704,11 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
             mc.status = mb.status + b0;
             mc.order = mb.order + b0;
             mc.sched = mb.sched + 3 * kNumBins * c;
-            mc.iws = mb.iws + 2 * b0 + (size_t)c * kMixedSchedInts;
+            mc.iws = mb.iws + 3 * b0 + (size_t)c * kMixedSchedInts;
+            // the run's FP32 stage follows the previous run's, so that it runs beside that
+            // run's refinement (FP32 and FP64 pipes) instead of competing with its FP32 stage
+            mc.fp32_wait = c > 0 ? ctx->pipe_mid[c - 1] : nullptr;
+            mc.fp32_done = ctx->pipe_mid[c];
             cudaError_t e = launch_mixed_batched(mc, ctx->num_sms, cs, ctx->pipe_aux[c], kNumBins, ctx->pipe_fork[c],
                                                  ctx->pipe_join[c], ctx->tun_real, ctx->tun_mixed32);
             if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
@@ -728,7 +736,7 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   mb.ref1 = ctx->mix_e1;
   ctx->mix_timed = true;
   rc = run_graph_or_direct(ctx, (flags & GS_GRAPH) != 0, key, [&](cudaStream_t st) -> int {
-    CK(cudaMemsetAsync(mb.stats, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(mb.stats, 0, 5 * sizeof(unsigned long long), st));
     cudaError_t e = launch_mixed_batched(mb, ctx->num_sms, st, ctx->aux, kNumBins, ctx->fork, ctx->join, ctx->tun_real,
                                          ctx->tun_mixed32);
     if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
@@ -759,7 +767,7 @@ int gs_mixed_batched_info(gs_context* ctx, int64_t* info) {
   if (!ctx || !info) return GS_BADARG;
   ctx->err.clear();
   if (!ctx->mix_valid) return set_err(ctx, GS_BADARG, "no GS_MIXED batched call on this context yet");
-  unsigned long long st[4] = {0, 0, 0, 0};
+  unsigned long long st[5] = {0, 0, 0, 0, 0};
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(st, ctx->mix_stats, sizeof(st), cudaMemcpyDeviceToHost));
@@ -770,6 +778,10 @@ int gs_mixed_batched_info(gs_context* ctx, int64_t* info) {
     if (cudaEventElapsedTime(&ms, ctx->mix_e0, ctx->mix_e1) == cudaSuccess) info[4] = (int64_t)(1000.0 * ms);
     else (void)cudaGetLastError();  // not recorded: leave no error behind for the caller's next launch
   }
+  // a tensor-core wait that timed out handed its matrix back to the FP64 kernel (results
+  // stay correct); report it, with the counters filled
+  if ((int)(st[4] & 0xffffffffu) != 0)
+    return set_err(ctx, GS_CUDA, "a tensor-core wait of the refinement timed out (code %d)", (int)(st[4] & 0xffffffffu));
   return GS_OK;
 }
 

@@ -3,6 +3,7 @@
 // waves, the per-matrix Newton loop and the bin kernel.  Included only by the per-bin
 // translation units (refine_bin_r*.cu), so that each compiles one row tile.
 #pragma once
+#include <cstdlib>
 #include "refine_batched.cuh"
 
 namespace gsk {
@@ -14,7 +15,6 @@ constexpr int kAS = kSmallMax + 4;  // staged op(A) chunk: kKC rows of up to 128
 constexpr int kNC = 2;            // columns per thread in one pass
 constexpr int kPW = 16 * kNC;     // columns per pass
 constexpr int kBS = kPW + 4;      // staged B chunk: kKC rows of kPW entries
-constexpr int kMaxSteps = 6;      // Newton steps before a matrix is handed back
 constexpr float kMinGain = 4.f;    // from the third step on, a step must shrink max|X| this much
 constexpr float kTolFinal = 1e-9f;
 constexpr float kTolDiverge = 1e-1f;
@@ -221,14 +221,51 @@ __device__ void sylv_waves(int n, int N, const short* bs, const float* Tf, const
       float r10 = ip == 2 ? R[(size_t)j0 * n + i0 + 1] : 0.f;
       float r01 = jq == 2 ? R[(size_t)(j0 + 1) * n + i0] : 0.f;
       float r11 = (ip == 2 && jq == 2) ? R[(size_t)(j0 + 1) * n + i0 + 1] : 0.f;
-      for (int k = i0 + ip; k < n; ++k) {  // - sum_{r>p} T_pr W_rq
-        const float t0 = Tf[(size_t)k * n + i0], t1 = ip == 2 ? Tf[(size_t)k * n + i0 + 1] : 0.f;
-        const float w0 = W[(size_t)j0 * n + k], w1 = jq == 2 ? W[(size_t)(j0 + 1) * n + k] : 0.f;
+      // The two sums run in k order; their loads are issued kU at a time, so that the
+      // L1/L2 latency is paid once per kU terms rather than once per term.
+      constexpr int kU = 8;
+      const float* Ti0 = Tf + i0;       // row i0 of T: stride n
+      const float* Wj0 = W + (size_t)j0 * n;
+      int k = i0 + ip;
+      for (; k + kU <= n; k += kU) {  // - sum_{r>p} T_pr W_rq
+        float t0[kU], t1[kU], w0[kU], w1[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          t0[u] = Ti0[(size_t)(k + u) * n];
+          t1[u] = ip == 2 ? Ti0[(size_t)(k + u) * n + 1] : 0.f;
+          w0[u] = Wj0[k + u];
+          w1[u] = jq == 2 ? Wj0[n + k + u] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          r00 -= t0[u] * w0[u]; r01 -= t0[u] * w1[u]; r10 -= t1[u] * w0[u]; r11 -= t1[u] * w1[u];
+        }
+      }
+      for (; k < n; ++k) {
+        const float t0 = Ti0[(size_t)k * n], t1 = ip == 2 ? Ti0[(size_t)k * n + 1] : 0.f;
+        const float w0 = Wj0[k], w1 = jq == 2 ? Wj0[n + k] : 0.f;
         r00 -= t0 * w0; r01 -= t0 * w1; r10 -= t1 * w0; r11 -= t1 * w1;
       }
-      for (int k = 0; k < j0; ++k) {  // + sum_{r<q} W_pr T_rq
-        const float w0 = W[(size_t)k * n + i0], w1 = ip == 2 ? W[(size_t)k * n + i0 + 1] : 0.f;
-        const float t0 = Tf[(size_t)j0 * n + k], t1 = jq == 2 ? Tf[(size_t)(j0 + 1) * n + k] : 0.f;
+      const float* Tj0 = Tf + (size_t)j0 * n;  // column j0 of T
+      const float* Wi0 = W + i0;               // row i0 of W: stride n
+      k = 0;
+      for (; k + kU <= j0; k += kU) {  // + sum_{r<q} W_pr T_rq
+        float w0[kU], w1[kU], t0[kU], t1[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          w0[u] = Wi0[(size_t)(k + u) * n];
+          w1[u] = ip == 2 ? Wi0[(size_t)(k + u) * n + 1] : 0.f;
+          t0[u] = Tj0[k + u];
+          t1[u] = jq == 2 ? Tj0[n + k + u] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          r00 += w0[u] * t0[u]; r01 += w0[u] * t1[u]; r10 += w1[u] * t0[u]; r11 += w1[u] * t1[u];
+        }
+      }
+      for (; k < j0; ++k) {
+        const float w0 = Wi0[(size_t)k * n], w1 = ip == 2 ? Wi0[(size_t)k * n + 1] : 0.f;
+        const float t0 = Tj0[k], t1 = jq == 2 ? Tj0[n + k] : 0.f;
         r00 += w0 * t0; r01 += w0 * t1; r10 += w1 * t0; r11 += w1 * t1;
       }
       // (I_q (x) T_pp - T_qq^T (x) I_p) vec(W_pq) = vec(R), vec index a + ip * b
@@ -253,8 +290,10 @@ __device__ void sylv_waves(int n, int N, const short* bs, const float* Tf, const
 }
 
 
+// One Newton step of one matrix: At = Z^T A_s Z and N = (I - Z^T Z) / 2 were formed by
+// the tensor-core products of this step (Q in FP64, its FP32 copy in T32, N in NF).
 template <int RM>
-__device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
+__device__ void refine_step(const RefineArgs& a, int b, int n, int step, Smem& sm) {
   const int tid = threadIdx.x;
   const long long off = a.offs[b];
   double* A = a.A + off;
@@ -268,13 +307,14 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
   float* NF = a.NF + off;
   const int nn = n * n;
   const int e = a.exps[b];
-  const double sc = ldexp(1.0, -e), usc = ldexp(1.0, e);
+  const double usc = ldexp(1.0, e);
   // 1x1 / 2x2 block structure of the FP32 Schur form
   if (tid == 0) {
+    const unsigned char* blk = a.blk + a.woffs[b];
     int N = 0, i = 0;
     while (i < n) {
       sm.bs[N++] = (short)i;
-      i += (i + 1 < n && AtF[(size_t)i * n + i + 1] != 0.f) ? 2 : 1;
+      i += (i + 1 < n && blk[i]) ? 2 : 1;
     }
     sm.bs[N] = (short)n;
     sm.nblk = N;
@@ -283,42 +323,11 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
   const int N = sm.nblk;
   for (int p = tid; p < N; p += kRT)
     for (int i = sm.bs[p]; i < sm.bs[p + 1]; ++i) sm.bid[i] = (unsigned char)p;
-  for (int idx = tid; idx < nn; idx += kRT) Z[idx] = (double)ZF[idx];
   __syncthreads();
   const unsigned char* bid = sm.bid;
-  bool ok = false;
-  int steps = 0;
-  float xprev = 0.f;
-  for (int step = 0; step < kMaxSteps && !ok; ++step) {
-    steps = step + 1;
-    // FP64: P = A_s Z; the block-lower part of Q = At = Z^T P (its small entries are the
-    // signal); NF = (I - Z^T Z) / 2 from the lower triangle.  The block-upper part of At
-    // only feeds FP32 solves until the last step, so it is an FP32 product here and the
-    // FP64 one is formed once the step turns out to be the last.
-    cta_mm<RM, 0, double>(n, n, n, LdN<double, double>{A, n, sc}, LdNB<double, double>{Z, n},
-                          [&](int i, int j, double v) { P[(size_t)j * n + i] = v; }, sm);
-    cta_mm<RM, 1, double>(n, n, n, LdT<double, double>{Z, n}, LdNB<double, double>{P, n},
-                          [&](int i, int j, double v) {
-                            if (bid[i] > bid[j]) {
-                              Q[(size_t)j * n + i] = v;
-                              AtF[(size_t)j * n + i] = (float)v;
-                            }
-                          },
-                          sm);
-    cta_mm<RM, 1, double>(n, n, n, LdT<double, double>{Z, n}, LdNB<double, double>{Z, n},
-                          [&](int i, int j, double v) {
-                            if (i >= j) {
-                              const float h = (float)(0.5 * ((i == j ? 1.0 : 0.0) - v));
-                              NF[(size_t)j * n + i] = h;
-                              NF[(size_t)i * n + j] = h;
-                            }
-                          },
-                          sm);
-    cta_mm<RM, 0, float>(n, n, n, LdT<float, float>{ZF, n}, LdNB<double, float>{P, n},
-                         [&](int i, int j, float v) {
-                           if (bid[i] <= bid[j]) AtF[(size_t)j * n + i] = v;
-                         },
-                         sm);
+  const int steps = step + 1;
+  bool ok = false, fail = false;
+  {
     float tnorm = 0.f, dummy0 = 0.f, dummy1 = 0.f;
     for (int idx = tid; idx < nn; idx += kRT) tnorm = nanmax(tnorm, fabsf(AtF[idx]));
     cta_max3(tnorm, dummy0, dummy1, sm);
@@ -349,18 +358,19 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
     }
     float d2 = 0.f, d3 = 0.f;
     cta_max3(xmax, d2, d3, sm);
-    if (!(xmax <= kTolDiverge)) break;
-    ok = xmax <= kTolFinal;
-    if (!ok && step >= 2 && xmax * kMinGain > xprev) break;  // stagnating: hand back
-    xprev = xmax;
+    const float xprev = step > 0 ? a.xprev[b] : 0.f;
+    if (!(xmax <= kTolDiverge)) {
+      fail = true;
+    } else {
+      ok = xmax <= kTolFinal;
+      if (!ok && (step >= 2 && xmax * kMinGain > xprev)) fail = true;  // stagnating: hand back
+      if (!ok && step == kRefineSteps - 1) fail = true;                 // out of steps
+    }
+    if (!ok && !fail && tid == 0) a.xprev[b] = xmax;
+  }
+  if (!fail) {
     if (ok) {
-      // the block-upper part of At in FP64 (the block-lower part is this step's)
-      cta_mm<RM, 2, double>(n, n, n, LdT<double, double>{Z, n}, LdNB<double, double>{P, n},
-                            [&](int i, int j, double v) {
-                              if (bid[i] <= bid[j]) Q[(size_t)j * n + i] = v;
-                            },
-                            sm);
-      // T = At + X^T At + At X (unit scale), block-lower part zero, into A
+      // T = At + X^T At + At X (unit scale; At in FP64 from the tensor-core product), block-lower part zero, into A
       cta_mm<RM, 0, float>(n, n, 2 * n, LdCatA{W, true, AtF, n}, LdCatB{AtF, W, n},
                         [&](int i, int j, float v) {
                           A[(size_t)j * n + i] = bid[i] > bid[j] ? 0.0 : Q[(size_t)j * n + i] + (double)v;
@@ -376,17 +386,22 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
       ZF[idx] = (float)z;
     }
     __syncthreads();
+    if (!ok) refine_col_exps<kRT>(n, Z, a.exZ + a.woffs[b]);  // for the next step's products
   }
   const unsigned long long n3 = (unsigned long long)n * n * n;
-  if (!ok) {
+  if (fail) {
     if (tid == 0) {
       a.status[b] = a.nofallback ? ST_UNCONVERGED : kStFallback;
       if (a.stats) {
         atomicAdd(a.stats + 1, 1ull);
         atomicAdd(a.stats + 2, (unsigned long long)steps);
-        atomicAdd(a.stats + 3, 4ull * steps * n3);
+        atomicAdd(a.stats + 3, 6ull * steps * n3);
       }
     }
+    return;
+  }
+  if (!ok) {  // next Newton step
+    if (tid == 0) a.status[b] = kStRefining;
     return;
   }
   // standard form of the 2x2 blocks (_gs2x2!) and the eigenvalues
@@ -433,25 +448,26 @@ __device__ void refine_one(const RefineArgs& a, int b, int n, Smem& sm) {
   }
   if (tid == 0) {
     a.status[b] = ST_OK;
-    if (a.stats) {  // FP64 FLOPs: per step A Z (2 n^3) and two triangles (n^3 each), the last upper triangle
+    if (a.stats) {  // FP64-accurate product FLOPs: per step A_s Z, Z^T P and Z^T Z (2 n^3 each)
       atomicAdd(a.stats, 1ull);
       atomicAdd(a.stats + 2, (unsigned long long)steps);
-      atomicAdd(a.stats + 3, (4ull * steps + 1ull) * n3);
+      atomicAdd(a.stats + 3, 6ull * steps * n3);
     }
   }
 }
 
-// One size bin (orders up to 16 RM): persistent CTAs take the bin's matrices, largest
-// first, from the bin's ticket counter.
-// Three CTAs per SM (80 registers): measured 327 ms for the 20,000-matrix batch against 350
-// ms with two; four spill the product loops.
+// One size bin (orders up to 16 RM), Newton step `step`: persistent CTAs take the bin's
+// matrices, largest first, from the step's ticket counter for the bin.
+// Three CTAs per SM (80 registers): measured faster than two on the 20,000-matrix batch;
+// four spill the product loops.
 template <int RM>
-__global__ void __launch_bounds__(kRT, 3) k_refine_bin(RefineArgs a, int bin) {
+__global__ void __launch_bounds__(kRT, 3) k_refine_bin(RefineArgs a, int bin, int step) {
   __shared__ Smem sm;
   const int beg = a.sched[3 * bin], end = a.sched[3 * bin + 1];
+  int* ticket = a.ticket + kRefineTicketsPerStep * step + bin;
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) sm.ticket = beg + atomicAdd(a.ticket + bin, 1);
+    if (threadIdx.x == 0) sm.ticket = beg + atomicAdd(ticket, 1);
     __syncthreads();
     const int t = sm.ticket;
     if (t >= end) break;
@@ -459,25 +475,34 @@ __global__ void __launch_bounds__(kRT, 3) k_refine_bin(RefineArgs a, int bin) {
     const int n = a.ns[b];
     if (n < 1 || n > kSmallMax) continue;  // empty (ST_OK) or order out of range (ST_BADARG)
     const int st = a.status[b];
-    if (st != ST_OK) {
-      if (threadIdx.x == 0 && st == ST_UNCONVERGED) {
-        if (!a.nofallback) a.status[b] = kStFallback;
+    if (st == kStRefining) {  // the step's products are missing (a tensor-core wait timed out)
+      if (threadIdx.x == 0) {
+        a.status[b] = a.nofallback ? ST_UNCONVERGED : kStFallback;
         if (a.stats) atomicAdd(a.stats + 1, 1ull);
       }
       continue;
     }
-    refine_one<RM>(a, b, n, sm);
+    if (st != kStStepReady) continue;
+    refine_step<RM>(a, b, n, step, sm);
   }
 }
 
 }  // namespace
 
 template <int RM>
-cudaError_t launch_refine_bin(const RefineArgs& a, int bin, int num_sms, cudaStream_t s) {
+cudaError_t launch_refine_bin(const RefineArgs& a, int bin, int step, int num_sms, cudaStream_t s) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine_bin<RM>, kRT, 0);
   if (e != cudaSuccess) return e;
-  k_refine_bin<RM><<<num_sms * (per_sm > 0 ? per_sm : 1), kRT, 0, s>>>(a, bin);
+  if (const char* ev = std::getenv("GS_REFINE_CTAS")) {  // tuning runs: CTAs per SM
+    const int c = std::atoi(ev);
+    if (c > 0 && c < per_sm) per_sm = c;
+  }
+  if (const char* ev = std::getenv("GS_REFINE_CARVEOUT")) {  // tuning runs: shared-memory carveout, percent
+    e = cudaFuncSetAttribute(k_refine_bin<RM>, cudaFuncAttributePreferredSharedMemoryCarveout, std::atoi(ev));
+    if (e != cudaSuccess) return e;
+  }
+  k_refine_bin<RM><<<num_sms * (per_sm > 0 ? per_sm : 1), kRT, 0, s>>>(a, bin, step);
   return cudaGetLastError();
 }
 

@@ -2,5 +2,5 @@
 #include "refine_bin_impl.cuh"
 
 namespace gsk {
-template cudaError_t launch_refine_bin<4>(const RefineArgs&, int, int, cudaStream_t);
+template cudaError_t launch_refine_bin<4>(const RefineArgs&, int, int, int, cudaStream_t);
 }  // namespace gsk
