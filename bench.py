@@ -180,6 +180,29 @@ def fp64_peak_tflops(torch, dev):
     return best
 
 
+def fp32_peak_tflops(torch, dev):
+    """Measured FP32 CUDA-core peak: cuBLAS SGEMM 4096^3 with TF32 off (best of 5)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(4096, 4096, dtype=torch.float32, device=dev)
+        b = torch.randn(4096, 4096, dtype=torch.float32, device=dev)
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 0.0
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = max(best, 2 * 4096.0 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return best
+
+
 def measured_traffic_per_matrix():
     """DRAM bytes per matrix of the batched kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_schur_real_traffic.txt")
@@ -345,22 +368,36 @@ def run_ours(args):
             torch.distributed.destroy_process_group()
         return
     peak = fp64_peak_tflops(torch, dev)
-    # roofline of the mixed step's dominant phase: the refinement kernels (four size-bin
-    # launches running concurrently), bound by the FP64 pipe; their FP64 FLOPs are counted by
-    # the kernels (algorithmic triangles, not the executed tiles) and timed by CUDA events the
-    # library records around them on its stream
+    peak32 = fp32_peak_tflops(torch, dev)
+    # roofline of the mixed step's dominant kernel: the FP32 batched Schur kernel
+    # (k_schur_real<float>, four size-bin launches running concurrently), timed by the CUDA
+    # events the library records at the start of the call's kernels and at the start of the
+    # refinement (the conversion k_mixed_prep, ~1% of the stage, is inside that window);
+    # bound by the FP32 FMA pipe (25 n^3 FLOP per matrix), which the bulge chase's
+    # dependent chains and per-step barriers leave mostly idle
+    fp32_s = info["fp32_us"] * 1e-6 if info["fp32_us"] > 0 else None
+    ach32 = flops / fp32_s / 1e12 if fp32_s else None
+    roof = {"bound": "fp32", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
+            "frac": (ach32 / peak32) if ach32 else None, "traffic": None,
+            "kernel": "k_schur_real<float> (FP32 stage of the mixed step, four size-bin launches)",
+            "phase_ms": info["fp32_us"] * 1e-3, "step_kernel_ms": kms_mixed,
+            "algorithmic": "25 n^3 FP32 FLOP per matrix, summed over the batch (%.4g FLOP per launch)" % flops,
+            "peak_source": "measured: cuBLAS SGEMM 4096^3 in this run (FP32 FMA pipe, TF32 off)",
+            "traffic_note": "not the bound: inputs and outputs are 12 n^2 bytes per matrix (ncu: "
+                            "profiles/k_schur_real_f32_600.md)"}
+    # the refinement phase: FP64-accurate products on the tensor cores, the rest of each
+    # Newton step in FP32; its rate in FP64-equivalent FLOPs of those products
     ref_s = info["refine_us"] * 1e-6 if info["refine_us"] > 0 else None
-    ach = info["fp64_flops"] / ref_s / 1e12 if ref_s else None
-    roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-            "frac": (ach / peak) if ach else None, "traffic": None,
-            "kernel": "k_refine_bin<2,4,6,8> (refinement phase of the mixed step)",
-            "phase_ms": info["refine_us"] * 1e-3, "step_kernel_ms": kms_mixed,
-            "algorithmic": "FP64 FLOPs of the refinement: per Newton step 2 n^3 (A Z) + n^3 (lower triangle of "
-                           "Z^T A Z) + n^3 (lower triangle of Z^T Z), plus n^3 for the last step's upper triangle; "
-                           "%.4g FLOP in %d Newton steps over %d matrices" % (info["fp64_flops"], info["newton_steps"],
-                                                                            info["refined"] + info["handed_back"]),
-            "peak_source": "measured: cuBLAS DGEMM 4096^3 in this run (FP64 FMA pipe; no FP64 tensor-core path "
-                           "is faster on GB300)"}
+    refinement = dict(info)
+    refinement.update({
+        "phase_ms": info["refine_us"] * 1e-3,
+        "product_fp64_equiv_tflops": info["product_flops"] / ref_s / 1e12 if ref_s else None,
+        "fp64_peak_tflops": peak,
+        "kernels": "k_refine_tc (tensor cores: A_s Z, Z^T (A Z), Z^T Z per Newton step), k_refine_bin<2,4,6,8> "
+                   "(FP32 Sylvester waves, corrections), one launch each per Newton step (six steps)",
+        "algorithmic": "per Newton step 2 n^3 each for A_s Z, Z^T (A_s Z), Z^T Z; %.4g FLOP in %d Newton steps "
+                       "over %d matrices" % (info["product_flops"], info["newton_steps"],
+                                             info["refined"] + info["handed_back"])})
     kernel_ms = kms_fp64
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     per_matrix_bytes = measured_traffic_per_matrix()
@@ -397,12 +434,13 @@ def run_ours(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-           "form": "mixed (GS_MIXED): FP32 Schur sweeps, per-matrix FP64 Newton refinement of the Schur pair, "
-                   "FP64 recomputation of matrices the refinement cannot finish; results at FP64 backward error "
-                   "(accuracy: both forms measured on the same sample in this run)",
+           "form": "mixed (GS_MIXED): FP32 Schur sweeps, per-matrix Newton refinement of the Schur pair with its "
+                   "FP64-accurate products on the BF16 tensor cores, FP64 recomputation of matrices the refinement "
+                   "cannot finish; results at FP64 backward error (accuracy: both forms measured on the same "
+                   "sample in this run)",
            "config": bench_config(args.count), "graph": not args.no_graph,
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-           "gpu_launches": 16 * args.steps, "unconverged": bad, "refinement": info,
+           "gpu_launches": 42 * args.steps, "unconverged": bad, "refinement": refinement,
            "fp64": fp64, "mixed_vs_fp64": value / value64,
            "mixed_vs_fp64_e2e": (e2e["value"] / e2e64["value"]) if (e2e and e2e64) else None,
            "accuracy": accuracy, "plain_fp64_per_matrix": per_matrix,

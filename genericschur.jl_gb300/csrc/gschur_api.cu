@@ -773,10 +773,14 @@ int gs_mixed_batched_info(gs_context* ctx, int64_t* info) {
   CK(cudaMemcpy(st, ctx->mix_stats, sizeof(st), cudaMemcpyDeviceToHost));
   for (int i = 0; i < 4; ++i) info[i] = (int64_t)st[i];
   info[4] = -1;
+  info[5] = -1;
   float ms = 0.0f;
   if (ctx->mix_timed) {
     if (cudaEventElapsedTime(&ms, ctx->mix_e0, ctx->mix_e1) == cudaSuccess) info[4] = (int64_t)(1000.0 * ms);
     else (void)cudaGetLastError();  // not recorded: leave no error behind for the caller's next launch
+    // the FP32 stage: from the start of the call's kernels to the start of the refinement
+    if (ctx->timed && cudaEventElapsedTime(&ms, ctx->t0, ctx->mix_e0) == cudaSuccess) info[5] = (int64_t)(1000.0 * ms);
+    else (void)cudaGetLastError();
   }
   // a tensor-core wait that timed out handed its matrix back to the FP64 kernel (results
   // stay correct); report it, with the counters filled

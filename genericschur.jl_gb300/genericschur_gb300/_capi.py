@@ -169,12 +169,13 @@ class Context:
 
     def mixed_info(self):
         """Counters of the last GS_MIXED batched call: refined, handed back to FP64, Newton
-        steps, FP64 FLOPs of the refinement, refinement device time in us (-1 if not timed)."""
-        info = (ctypes.c_int64 * 5)()
+        steps, FLOPs of the refinement's FP64-accurate (tensor-core) products, refinement and
+        FP32-stage device times in us (-1 if not timed)."""
+        info = (ctypes.c_int64 * 6)()
         rc = self.lib.gs_mixed_batched_info(self.handle, info)
         if rc != GS_OK:
             raise RuntimeError("gs_mixed_batched_info: %s" % self.last_error())
-        keys = ("refined", "handed_back", "newton_steps", "fp64_flops", "refine_us")
+        keys = ("refined", "handed_back", "newton_steps", "product_flops", "refine_us", "fp32_us")
         return dict(zip(keys, (int(x) for x in info)))
 
     def host_alloc(self, nbytes):

@@ -141,12 +141,14 @@ GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* n
 
 /* After a GS_MIXED batched call (GS_MIXED: FP32 Schur pairs refined to FP64 accuracy by
  * per-matrix Newton steps; matrices the refinement cannot finish are recomputed in FP64,
- * or with GS_NOFALLBACK reported GS_UNCONVERGED): info[0] matrices finished by the
- * refinement, info[1] matrices handed back to the FP64 kernel (or reported), info[2]
- * Newton steps taken, info[3] FP64 FLOPs of the refinement (per step 2 n^3 for A Z and
- * n^3 for each of two triangles, plus n^3 for the last step's upper triangle), info[4]
- * device time of the refinement kernels in microseconds (-1 for a pipelined host-buffer
- * call).  Synchronises the context stream.  GS_BADARG before the first GS_MIXED call. */
+ * or with GS_NOFALLBACK reported GS_UNCONVERGED), info[0..5]: info[0] matrices finished by
+ * the refinement, info[1] matrices handed back to the FP64 kernel (or reported), info[2]
+ * Newton steps taken, info[3] FLOPs of the refinement's FP64-accurate products (per step
+ * 2 n^3 each for A Z, Z^T (A Z) and Z^T Z, run on the tensor cores), info[4] device time
+ * of the refinement in microseconds, info[5] device time of the FP32 stage (conversion,
+ * FP32 Schur) in microseconds (both -1 for a pipelined host-buffer call).  Synchronises
+ * the context stream.  GS_BADARG before the first GS_MIXED call; GS_CUDA (counters
+ * filled) when a tensor-core wait timed out and its matrix was handed back. */
 GS_API int gs_mixed_batched_info(gs_context* ctx, int64_t* info);
 
 GS_API int gs_schur_batched_f32(gs_context* ctx, int64_t count, const int32_t* ns, const int64_t* offs,
