@@ -3,7 +3,6 @@
 // waves, the per-matrix Newton loop and the bin kernel.  Included only by the per-bin
 // translation units (refine_bin_r*.cu), so that each compiles one row tile.
 #pragma once
-#include <cstdlib>
 #include "refine_batched.cuh"
 
 namespace gsk {
@@ -19,16 +18,26 @@ constexpr float kMinGain = 4.f;    // from the third step on, a step must shrink
 constexpr float kTolFinal = 1e-9f;
 constexpr float kTolDiverge = 1e-1f;
 
+// Tiles of the block Sylvester solve: about kTile rows each, never splitting a 2x2 block
+constexpr int kTile = 16;
+constexpr int kMaxTiles = 9;   // orders <= 128 give at most 8 tiles of >= 16 rows
+constexpr int kTS = 17;        // largest tile (a 2x2 block may extend one by a row); smem row stride
+
 struct Smem {
-  double a[kKC * kAS];
+  double a[kKC * kAS];         // product staging; the Sylvester solve's tiles as floats
   double b[kKC * kBS];
   float red[3][kRT / 32];
   double rot[2];
   short bs[kSmallMax + 2];
   unsigned char bid[kSmallMax];
+  short te[kMaxTiles + 1];     // tile row starts
+  short tbk[kMaxTiles + 1];    // tile block starts
   int nblk;
+  int ntile;
   int ticket;
 };
+static_assert(2 * kMaxTiles * kTS * kTS * sizeof(float) <= sizeof(double) * kKC * (kAS + kBS),
+              "the Sylvester tiles fit in the product staging area");
 
 __device__ __forceinline__ float nanmax(float m, float v) { return (v > m || v != v) ? v : m; }
 
@@ -183,112 +192,225 @@ struct LdCatB {
   __device__ bool kfast(int) const { return true; }
 };
 
-// Solve the m x m system K x = r (m <= 4) by Gaussian elimination with partial pivoting;
-// pivots below `floor` in magnitude are replaced by +-floor (bounded correction for
+// Gaussian elimination with partial pivoting on an M x M system held in registers (every
+// index is a compile-time constant: the pivot row is brought up by compare-and-swap steps);
+// pivots below `floor` in magnitude are replaced by +-floor (a bounded correction for
 // eigenvalues that FP32 does not separate; the step then fails the tolerance).
-__device__ void small_solve4(int m, float K[4][4], float r[4], float floor) {
-  for (int c = 0; c < m; ++c) {
-    int piv = c;
-    for (int i = c + 1; i < m; ++i)
-      if (fabsf(K[i][c]) > fabsf(K[piv][c])) piv = i;
-    if (piv != c) {
-      for (int j = 0; j < 4; ++j) { const float t = K[c][j]; K[c][j] = K[piv][j]; K[piv][j] = t; }
-      const float t = r[c]; r[c] = r[piv]; r[piv] = t;
+template <int M>
+__device__ __forceinline__ void gauss_solve(float (&K)[M][M], float (&r)[M], float floor) {
+#pragma unroll
+  for (int c = 0; c < M; ++c) {
+#pragma unroll
+    for (int i = c + 1; i < M; ++i) {
+      const bool sw = fabsf(K[i][c]) > fabsf(K[c][c]);
+#pragma unroll
+      for (int j = c; j < M; ++j) {
+        const float x = K[c][j], y = K[i][j];
+        K[c][j] = sw ? y : x;
+        K[i][j] = sw ? x : y;
+      }
+      const float x = r[c], y = r[i];
+      r[c] = sw ? y : x;
+      r[i] = sw ? x : y;
     }
     if (fabsf(K[c][c]) < floor) K[c][c] = K[c][c] < 0.f ? -floor : floor;
-    for (int i = c + 1; i < m; ++i) {
-      const float f = K[i][c] / K[c][c];
-      for (int j = c; j < m; ++j) K[i][j] -= f * K[c][j];
+    const float inv = 1.f / K[c][c];
+#pragma unroll
+    for (int i = c + 1; i < M; ++i) {
+      const float f = K[i][c] * inv;
+#pragma unroll
+      for (int j = c; j < M; ++j) K[i][j] -= f * K[c][j];
       r[i] -= f * r[c];
     }
   }
-  for (int c = m - 1; c >= 0; --c) {
-    float s = r[c];
-    for (int j = c + 1; j < m; ++j) s -= K[c][j] * r[j];
-    r[c] = s / K[c][c];
+#pragma unroll
+  for (int c = M - 1; c >= 0; --c) {
+    float v = r[c];
+#pragma unroll
+    for (int j = c + 1; j < M; ++j) v -= K[c][j] * r[j];
+    r[c] = v / K[c][c];
   }
 }
 
-// Block-lower W from T (block-upper part of Tf) and the right-hand sides R (block-lower
-// entries of R), by waves D = p - q = N-1 .. 1: block pair (p, q) needs W_rq, r > p, and
-// W_pr, r < q, all of larger D.
-__device__ void sylv_waves(int n, int N, const short* bs, const float* Tf, const float* R, float* W, float floor) {
-  for (int D = N - 1; D >= 1; --D) {
-    for (int q = threadIdx.x; q < N - D; q += kRT) {
-      const int p = q + D;
-      const int i0 = bs[p], ip = bs[p + 1] - i0, j0 = bs[q], jq = bs[q + 1] - j0;
-      float r00 = R[(size_t)j0 * n + i0];
-      float r10 = ip == 2 ? R[(size_t)j0 * n + i0 + 1] : 0.f;
-      float r01 = jq == 2 ? R[(size_t)(j0 + 1) * n + i0] : 0.f;
-      float r11 = (ip == 2 && jq == 2) ? R[(size_t)(j0 + 1) * n + i0 + 1] : 0.f;
-      // The two sums run in k order; their loads are issued kU at a time, so that the
-      // L1/L2 latency is paid once per kU terms rather than once per term.
-      constexpr int kU = 8;
-      const float* Ti0 = Tf + i0;       // row i0 of T: stride n
-      const float* Wj0 = W + (size_t)j0 * n;
-      int k = i0 + ip;
-      for (; k + kU <= n; k += kU) {  // - sum_{r>p} T_pr W_rq
-        float t0[kU], t1[kU], w0[kU], w1[kU];
+// Kronecker system of block pair (p, q) of orders IP, JQ:
+// (I_q (x) T_pp - T_qq^T (x) I_p) vec(W_pq) = vec(r), vec index a + IP b.  tp / tq: the
+// diagonal blocks (row stride ld); r[a][b]: the right-hand side, overwritten by W_pq.
+template <int IP, int JQ>
+__device__ __forceinline__ void pair_solve_t(const float* tp, const float* tq, int ld, float (&r)[2][2], float floor) {
+  constexpr int M = IP * JQ;
+  float K[M][M], rv[M];
 #pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          t0[u] = Ti0[(size_t)(k + u) * n];
-          t1[u] = ip == 2 ? Ti0[(size_t)(k + u) * n + 1] : 0.f;
-          w0[u] = Wj0[k + u];
-          w1[u] = jq == 2 ? Wj0[n + k + u] : 0.f;
-        }
+  for (int u = 0; u < M; ++u)
 #pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          r00 -= t0[u] * w0[u]; r01 -= t0[u] * w1[u]; r10 -= t1[u] * w0[u]; r11 -= t1[u] * w1[u];
-        }
-      }
-      for (; k < n; ++k) {
-        const float t0 = Ti0[(size_t)k * n], t1 = ip == 2 ? Ti0[(size_t)k * n + 1] : 0.f;
-        const float w0 = Wj0[k], w1 = jq == 2 ? Wj0[n + k] : 0.f;
-        r00 -= t0 * w0; r01 -= t0 * w1; r10 -= t1 * w0; r11 -= t1 * w1;
-      }
-      const float* Tj0 = Tf + (size_t)j0 * n;  // column j0 of T
-      const float* Wi0 = W + i0;               // row i0 of W: stride n
-      k = 0;
-      for (; k + kU <= j0; k += kU) {  // + sum_{r<q} W_pr T_rq
-        float w0[kU], w1[kU], t0[kU], t1[kU];
+    for (int v = 0; v < M; ++v) K[u][v] = 0.f;
 #pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          w0[u] = Wi0[(size_t)(k + u) * n];
-          w1[u] = ip == 2 ? Wi0[(size_t)(k + u) * n + 1] : 0.f;
-          t0[u] = Tj0[k + u];
-          t1[u] = jq == 2 ? Tj0[n + k + u] : 0.f;
-        }
+  for (int b = 0; b < JQ; ++b)
 #pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          r00 += w0[u] * t0[u]; r01 += w0[u] * t1[u]; r10 += w1[u] * t0[u]; r11 += w1[u] * t1[u];
-        }
+    for (int a = 0; a < IP; ++a) {
+      const int row = a + IP * b;
+      rv[row] = r[a][b];
+#pragma unroll
+      for (int a2 = 0; a2 < IP; ++a2) K[row][a2 + IP * b] += tp[a * ld + a2];
+#pragma unroll
+      for (int b2 = 0; b2 < JQ; ++b2) K[row][a + IP * b2] -= tq[b2 * ld + b];
+    }
+  gauss_solve<M>(K, rv, floor);
+#pragma unroll
+  for (int b = 0; b < JQ; ++b)
+#pragma unroll
+    for (int a = 0; a < IP; ++a) r[a][b] = rv[a + IP * b];
+}
+
+__device__ __forceinline__ void pair_solve(int ip, int jq, const float* tp, const float* tq, int ld,
+                                           float (&r)[2][2], float floor) {
+  if (ip == 1 && jq == 1) pair_solve_t<1, 1>(tp, tq, ld, r, floor);
+  else if (ip == 2 && jq == 1) pair_solve_t<2, 1>(tp, tq, ld, r, floor);
+  else if (ip == 1) pair_solve_t<1, 2>(tp, tq, ld, r, floor);
+  else pair_solve_t<2, 2>(tp, tq, ld, r, floor);
+}
+
+// Block-lower W of T_pp W_pq - W_pq T_qq = R_pq - sum_{r>p} T_pr W_rq + sum_{r<q} W_pr T_rq
+// (T: block-upper part of Tf; R: block-lower entries of R, overwritten) by tiles of about
+// kTile rows that never split a 2x2 block.  Tile pairs (P, Q), P >= Q, are solved by
+// waves D = P - Q from the bottom-left tile up; the tiles of one wave are solved at once in
+// shared memory (the diagonal tiles of T and the wave's tiles of R/W there), block pair by
+// block pair along local anti-diagonals, with only the within-tile sums; after each wave,
+// the solved tiles' contributions are pushed into the right-hand sides of the tiles that
+// need them (R_PQ -= T_{P,S} W_{S,Q} for the solved tile below in the same tile column,
+// R_PQ += W_{P,S} T_{S,Q} for the solved tile left in the same tile row).  The long sums of
+// the element-wise waves thus become short tile products whose loads are coalesced.
+__device__ void sylv_tiled(int n, int N, const short* bs, const unsigned char* bid, const float* Tf, float* R,
+                           float* W, float floor, Smem& sm) {
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    int nt = 0;
+    sm.te[0] = 0;
+    sm.tbk[0] = 0;
+    for (int p = 0; p < N; ++p)
+      if (bs[p] - sm.te[nt] >= kTile) {
+        ++nt;
+        sm.te[nt] = bs[p];
+        sm.tbk[nt] = (short)p;
       }
-      for (; k < j0; ++k) {
-        const float w0 = Wi0[(size_t)k * n], w1 = ip == 2 ? Wi0[(size_t)k * n + 1] : 0.f;
-        const float t0 = Tj0[k], t1 = jq == 2 ? Tj0[n + k] : 0.f;
-        r00 += w0 * t0; r01 += w0 * t1; r10 += w1 * t0; r11 += w1 * t1;
-      }
-      // (I_q (x) T_pp - T_qq^T (x) I_p) vec(W_pq) = vec(R), vec index a + ip * b
-      const int m = ip * jq;
-      float K[4][4], rv[4];
-      const float rr[2][2] = {{r00, r01}, {r10, r11}};
-      for (int u = 0; u < 4; ++u)
-        for (int v = 0; v < 4; ++v) K[u][v] = 0.f;
-      for (int b = 0; b < jq; ++b)
-        for (int a = 0; a < ip; ++a) {
-          const int row = a + ip * b;
-          rv[row] = rr[a][b];
-          for (int a2 = 0; a2 < ip; ++a2) K[row][a2 + ip * b] += Tf[(size_t)(i0 + a2) * n + i0 + a];
-          for (int b2 = 0; b2 < jq; ++b2) K[row][a + ip * b2] -= Tf[(size_t)(j0 + b) * n + j0 + b2];
+    ++nt;
+    sm.te[nt] = (short)n;
+    sm.tbk[nt] = (short)N;
+    sm.ntile = nt;
+  }
+  __syncthreads();
+  const int nt = sm.ntile;
+  float* sT = reinterpret_cast<float*>(sm.a);       // diagonal tiles of T: [tile][row * kTS + col]
+  float* sW = sT + kMaxTiles * kTS * kTS;            // the wave's tiles of R / W: [Q][row * kTS + col]
+  for (int e = tid; e < nt * kTS * kTS; e += kRT) {
+    const int t = e / (kTS * kTS), l = e - t * kTS * kTS, li = l / kTS, lj = l - li * kTS;
+    const int i = sm.te[t] + li, j = sm.te[t] + lj;
+    sT[e] = (i < sm.te[t + 1] && j < sm.te[t + 1]) ? Tf[(size_t)j * n + i] : 0.f;
+  }
+  for (int D = nt - 1; D >= 0; --D) {
+    const int ntl = nt - D;  // tiles (Q + D, Q), Q < ntl
+    __syncthreads();
+    for (int e = tid; e < ntl * kTS * kTS; e += kRT) {
+      const int Q = e / (kTS * kTS), l = e - Q * kTS * kTS, li = l / kTS, lj = l - li * kTS;
+      const int i = sm.te[Q + D] + li, j = sm.te[Q] + lj;
+      sW[e] = (i < sm.te[Q + D + 1] && j < sm.te[Q + 1]) ? R[(size_t)j * n + i] : 0.f;
+    }
+    int maxw = 0;
+    for (int Q = 0; Q < ntl; ++Q)
+      maxw = max(maxw, (sm.tbk[Q + D + 1] - sm.tbk[Q + D]) + (sm.tbk[Q + 1] - sm.tbk[Q]) - 1);
+    __syncthreads();
+    // local waves: pair (p, q) of tile pair (P, Q) on wave (last block of P - p) + (q - first block of Q)
+    for (int w = 0; w < maxw; ++w) {
+      for (int task = tid; task < ntl * kTS; task += kRT) {
+        const int Q = task / kTS, a = task - Q * kTS, P = Q + D;
+        const int pb = sm.tbk[P], pe = sm.tbk[P + 1], qb = sm.tbk[Q], qe = sm.tbk[Q + 1];
+        const int p = pe - 1 - a, q = qb + (w - a);
+        if (a > w || p < pb || q >= qe) continue;
+        if (D == 0 && p <= q) continue;
+        const int tP = sm.te[P], tQ = sm.te[Q];
+        const int li0 = bs[p] - tP, ip = bs[p + 1] - bs[p], lj0 = bs[q] - tQ, jq = bs[q + 1] - bs[q];
+        const int lpe = sm.te[P + 1] - tP;
+        float* rw = sW + Q * kTS * kTS;
+        const float* tp = sT + P * kTS * kTS;
+        const float* tq = sT + Q * kTS * kTS;
+        float r[2][2];
+        r[0][0] = rw[li0 * kTS + lj0];
+        r[1][0] = ip == 2 ? rw[(li0 + 1) * kTS + lj0] : 0.f;
+        r[0][1] = jq == 2 ? rw[li0 * kTS + lj0 + 1] : 0.f;
+        r[1][1] = (ip == 2 && jq == 2) ? rw[(li0 + 1) * kTS + lj0 + 1] : 0.f;
+        for (int k = li0 + ip; k < lpe; ++k) {  // - sum_{r>p} T_pr W_rq within tile P
+          const float t0 = tp[li0 * kTS + k], t1 = ip == 2 ? tp[(li0 + 1) * kTS + k] : 0.f;
+          const float w0 = rw[k * kTS + lj0], w1 = jq == 2 ? rw[k * kTS + lj0 + 1] : 0.f;
+          r[0][0] -= t0 * w0; r[0][1] -= t0 * w1; r[1][0] -= t1 * w0; r[1][1] -= t1 * w1;
         }
-      small_solve4(m, K, rv, floor);
-      for (int b = 0; b < jq; ++b)
-        for (int a = 0; a < ip; ++a) W[(size_t)(j0 + b) * n + i0 + a] = rv[a + ip * b];
+        for (int k = 0; k < lj0; ++k) {  // + sum_{r<q} W_pr T_rq within tile Q
+          const float w0 = rw[li0 * kTS + k], w1 = ip == 2 ? rw[(li0 + 1) * kTS + k] : 0.f;
+          const float t0 = tq[k * kTS + lj0], t1 = jq == 2 ? tq[k * kTS + lj0 + 1] : 0.f;
+          r[0][0] += w0 * t0; r[0][1] += w0 * t1; r[1][0] += w1 * t0; r[1][1] += w1 * t1;
+        }
+        pair_solve(ip, jq, tp + li0 * kTS + li0, tq + lj0 * kTS + lj0, kTS, r, floor);
+        for (int b = 0; b < jq; ++b)
+          for (int a2 = 0; a2 < ip; ++a2) rw[(li0 + a2) * kTS + lj0 + b] = r[a2][b];
+      }
+      __syncthreads();
+    }
+    // the solved tiles to W (block-lower entries)
+    for (int e = tid; e < ntl * kTS * kTS; e += kRT) {
+      const int Q = e / (kTS * kTS), l = e - Q * kTS * kTS, li = l / kTS, lj = l - li * kTS;
+      const int i = sm.te[Q + D] + li, j = sm.te[Q] + lj;
+      if (i < sm.te[Q + D + 1] && j < sm.te[Q + 1] && bid[i] > bid[j]) W[(size_t)j * n + i] = sW[e];
+    }
+    if (D == 0) break;
+    // right-looking update, term 1: for each tile column Q < ntl, rows of tiles Q .. Q+D-1:
+    // R(i, j) -= sum_{k in tile Q+D} T(i, k) W(k, j)
+    {
+      int tot = 0;
+      for (int Q = 0; Q < ntl; ++Q) tot += (sm.te[Q + D] - sm.te[Q]) * (sm.te[Q + 1] - sm.te[Q]);
+      for (int e = tid; e < tot; e += kRT) {
+        int Q = 0, l = e;
+        for (;; ++Q) {
+          const int sz = (sm.te[Q + D] - sm.te[Q]) * (sm.te[Q + 1] - sm.te[Q]);
+          if (l < sz) break;
+          l -= sz;
+        }
+        const int rows = sm.te[Q + D] - sm.te[Q];
+        const int i = sm.te[Q] + l % rows, lj = l / rows, j = sm.te[Q] + lj;
+        const int k0 = sm.te[Q + D], kn = sm.te[Q + D + 1] - k0;
+        const float* ws = sW + Q * kTS * kTS + lj;  // W(k0 + kk, j) = ws[kk * kTS]
+        float acc = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < kTS; ++kk)
+          if (kk < kn) acc += Tf[(size_t)(k0 + kk) * n + i] * ws[kk * kTS];
+        R[(size_t)j * n + i] -= acc;
+      }
     }
     __syncthreads();
+    // term 2: for each tile row P >= D, columns of tiles P-D+1 .. P:
+    // R(i, j) += sum_{k in tile P-D} W(i, k) T(k, j)
+    {
+      int tot = 0;
+      for (int P = D; P < nt; ++P) tot += (sm.te[P + 1] - sm.te[P]) * (sm.te[P + 1] - sm.te[P - D + 1]);
+      for (int e = tid; e < tot; e += kRT) {
+        int P = D, l = e;
+        for (;; ++P) {
+          const int sz = (sm.te[P + 1] - sm.te[P]) * (sm.te[P + 1] - sm.te[P - D + 1]);
+          if (l < sz) break;
+          l -= sz;
+        }
+        const int rows = sm.te[P + 1] - sm.te[P];
+        const int li = l % rows, i = sm.te[P] + li, j = sm.te[P - D + 1] + l / rows;
+        const int k0 = sm.te[P - D], kn = sm.te[P - D + 1] - k0;
+        const float* ws = sW + (P - D) * kTS * kTS + li * kTS;  // W(i, k0 + kk) = ws[kk]
+        const float* tc = Tf + (size_t)j * n + k0;                // T(k0 + kk, j) = tc[kk]
+        float acc = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < kTS; ++kk)
+          if (kk < kn) acc += ws[kk] * tc[kk];
+        R[(size_t)j * n + i] += acc;
+      }
+    }
   }
+  __syncthreads();
 }
-
 
 // One Newton step of one matrix: At = Z^T A_s Z and N = (I - Z^T Z) / 2 were formed by
 // the tensor-core products of this step (Q in FP64, its FP32 copy in T32, N in NF).
@@ -340,7 +462,7 @@ __device__ void refine_step(const RefineArgs& a, int b, int n, int step, Smem& s
     }
     __syncthreads();
     const float floor = 8.f * 1.2e-7f * (tnorm > 0.f ? tnorm : 1.f);
-    sylv_waves(n, N, sm.bs, AtF, M, W, floor);
+    sylv_tiled(n, N, sm.bs, bid, AtF, M, W, floor, sm);
     // X = N + W - W^T (W block-lower); each block-lower entry's thread writes its mirror
     float xmax = 0.f;
     for (int idx = tid; idx < nn; idx += kRT) {
@@ -458,8 +580,8 @@ __device__ void refine_step(const RefineArgs& a, int b, int n, int step, Smem& s
 
 // One size bin (orders up to 16 RM), Newton step `step`: persistent CTAs take the bin's
 // matrices, largest first, from the step's ticket counter for the bin.
-// Three CTAs per SM (80 registers): measured faster than two on the 20,000-matrix batch;
-// four spill the product loops.
+// Three CTAs per SM (80 registers): measured faster than two or one (also with the L1 share
+// raised for the Sylvester waves) on the 20,000-matrix batch; four spill the product loops.
 template <int RM>
 __global__ void __launch_bounds__(kRT, 3) k_refine_bin(RefineArgs a, int bin, int step) {
   __shared__ Smem sm;
@@ -494,14 +616,6 @@ cudaError_t launch_refine_bin(const RefineArgs& a, int bin, int step, int num_sm
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine_bin<RM>, kRT, 0);
   if (e != cudaSuccess) return e;
-  if (const char* ev = std::getenv("GS_REFINE_CTAS")) {  // tuning runs: CTAs per SM
-    const int c = std::atoi(ev);
-    if (c > 0 && c < per_sm) per_sm = c;
-  }
-  if (const char* ev = std::getenv("GS_REFINE_CARVEOUT")) {  // tuning runs: shared-memory carveout, percent
-    e = cudaFuncSetAttribute(k_refine_bin<RM>, cudaFuncAttributePreferredSharedMemoryCarveout, std::atoi(ev));
-    if (e != cudaSuccess) return e;
-  }
   k_refine_bin<RM><<<num_sms * (per_sm > 0 ? per_sm : 1), kRT, 0, s>>>(a, bin, step);
   return cudaGetLastError();
 }
