@@ -9,11 +9,11 @@ namespace gsk {
 namespace {
 
 constexpr int kRT = 256;          // threads per CTA (16 x 16 product layout)
-constexpr int kKC = 16;           // contraction chunk staged in shared memory
-constexpr int kAS = kSmallMax + 4;  // staged op(A) chunk: kKC rows of up to 128 entries
-constexpr int kNC = 2;            // columns per thread in one pass
+constexpr int kKC = 32;           // contraction chunk staged in shared memory
+constexpr int kAS = kSmallMax + 1;  // staged op(A) chunk: kKC rows of up to 128 entries (odd stride)
+constexpr int kNC = 4;            // columns per thread in one pass
 constexpr int kPW = 16 * kNC;     // columns per pass
-constexpr int kBS = kPW + 4;      // staged B chunk: kKC rows of kPW entries
+constexpr int kBS = kPW + 1;      // staged B chunk: kKC rows of kPW entries
 constexpr float kMinGain = 4.f;    // from the third step on, a step must shrink max|X| this much
 constexpr float kTolFinal = 1e-9f;
 constexpr float kTolDiverge = 1e-1f;
@@ -24,8 +24,8 @@ constexpr int kMaxTiles = 9;   // orders <= 128 give at most 8 tiles of >= 16 ro
 constexpr int kTS = 17;        // largest tile (a 2x2 block may extend one by a row); smem row stride
 
 struct Smem {
-  double a[kKC * kAS];         // product staging; the Sylvester solve's tiles as floats
-  double b[kKC * kBS];
+  float a[kKC * kAS];          // product staging; the Sylvester solve's tiles
+  float b[kKC * kBS];
   float red[3][kRT / 32];
   double rot[2];
   short bs[kSmallMax + 2];
@@ -36,7 +36,7 @@ struct Smem {
   int ntile;
   int ticket;
 };
-static_assert(2 * kMaxTiles * kTS * kTS * sizeof(float) <= sizeof(double) * kKC * (kAS + kBS),
+static_assert(2 * kMaxTiles * kTS * kTS <= kKC * (kAS + kBS),
               "the Sylvester tiles fit in the product staging area");
 
 __device__ __forceinline__ float nanmax(float m, float v) { return (v > m || v != v) ? v : m; }
@@ -59,99 +59,77 @@ __device__ void cta_max3(float& x, float& y, float& z, Smem& sm) {
 }
 
 // ------------------------------------------------------------------------------------
-// CTA matrix product C (n x ncols) = sum_{k < kdim} opA(i, k) B(k, j), computed in CT.
-// Threads form a 16 x 16 grid; in each pass over kPW columns [j0, j0 + kPW) thread
-// (tx, ty) owns rows rb + tx + 16 r (r < RMP) and columns j0 + ty + 16 c (c < kNC) (the
-// FP64 pipe, not the register tile, bounds the FP64 products, so the tile stays small
-// and nothing spills).  Chunks of kKC contraction indices are staged in shared memory
-// (zero beyond n / kdim); the loaders say whether consecutive k are contiguous in memory
-// (kfast), which picks the coalesced staging order.  The store functor receives every
-// (i, j, value) with i < n, j < ncols of the pass's rows.
-// PART 0: all rows; PART 1: rows from the 16-row group holding j0 down (covers i >= j);
-// PART 2: rows up to j0 + kPW (covers i <= j + 1), so that a triangle costs about half.
+// CTA matrix product C (n x ncols) = sum_{k < kdim} opA(i, k) B(k, j) in FP32.  Threads
+// form a 16 x 16 grid; in each pass over kPW columns [j0, j0 + kPW) thread (tx, ty) owns
+// rows tx + 16 r (r < RMP) and columns j0 + ty + 16 c (c < kNC).  Chunks of kKC
+// contraction indices are staged in shared memory (zero beyond n / kdim); the loaders say
+// whether consecutive k are contiguous in memory (kfast), which picks the coalesced
+// staging order.  The store functor receives every (i, j, value) with i < n, j < ncols.
 // ------------------------------------------------------------------------------------
-template <int RMP, class CT, class LA, class LB, class ST>
-__device__ void mm_pass(int n, int ncols, int kdim, int rb, int j0, const LA& la, const LB& lb, const ST& st,
-                        Smem& sm) {
-  CT* sa = reinterpret_cast<CT*>(sm.a);
-  CT* sb = reinterpret_cast<CT*>(sm.b);
+template <int RMP, class LA, class LB, class ST>
+__device__ void mm_pass(int n, int ncols, int kdim, int j0, const LA& la, const LB& lb, const ST& st, Smem& sm) {
+  float* sa = sm.a;
+  float* sb = sm.b;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int nrow = RMP * 16;
+  constexpr int nrow = RMP * 16;
   const int cm = min(kNC, (ncols - j0 + 15) >> 4);
-  CT acc[RMP][kNC];
+  float acc[RMP][kNC];
 #pragma unroll
   for (int r = 0; r < RMP; ++r)
 #pragma unroll
-    for (int c = 0; c < kNC; ++c) acc[r][c] = CT(0);
+    for (int c = 0; c < kNC; ++c) acc[r][c] = 0.f;
   for (int k0 = 0; k0 < kdim; k0 += kKC) {
     __syncthreads();
     if (la.kfast(k0)) {
       for (int e = tid; e < kKC * nrow; e += kRT) {
-        const int kk = e & (kKC - 1), i = rb + (e >> 4), k = k0 + kk;
-        sa[kk * kAS + (i - rb)] = (i < n && k < kdim) ? la(i, k) : CT(0);
+        const int kk = e & (kKC - 1), i = e / kKC, k = k0 + kk;
+        sa[kk * kAS + i] = (i < n && k < kdim) ? la(i, k) : 0.f;
       }
     } else {
       for (int e = tid; e < kKC * nrow; e += kRT) {
-        const int kk = e / nrow, ii = e - kk * nrow, i = rb + ii, k = k0 + kk;
-        sa[kk * kAS + ii] = (i < n && k < kdim) ? la(i, k) : CT(0);
+        const int kk = e / nrow, i = e - kk * nrow, k = k0 + kk;
+        sa[kk * kAS + i] = (i < n && k < kdim) ? la(i, k) : 0.f;
       }
     }
     if (lb.kfast(k0)) {
       for (int e = tid; e < kKC * kPW; e += kRT) {
-        const int kk = e & (kKC - 1), jj = e >> 4, j = j0 + jj, k = k0 + kk;
-        sb[kk * kBS + jj] = (j < ncols && k < kdim) ? lb(k, j) : CT(0);
+        const int kk = e & (kKC - 1), jj = e / kKC, j = j0 + jj, k = k0 + kk;
+        sb[kk * kBS + jj] = (j < ncols && k < kdim) ? lb(k, j) : 0.f;
       }
     } else {
       for (int e = tid; e < kKC * kPW; e += kRT) {
         const int kk = e / kPW, jj = e % kPW, j = j0 + jj, k = k0 + kk;
-        sb[kk * kBS + jj] = (j < ncols && k < kdim) ? lb(k, j) : CT(0);
+        sb[kk * kBS + jj] = (j < ncols && k < kdim) ? lb(k, j) : 0.f;
       }
     }
     __syncthreads();
-#pragma unroll 2
-    for (int kk = 0; kk < kKC; ++kk) {
-      CT av[RMP], bv[kNC];
+    const int kn = min(kKC, kdim - k0);
+#pragma unroll 4
+    for (int kk = 0; kk < kn; ++kk) {
+      float av[RMP], bv[kNC];
 #pragma unroll
       for (int r = 0; r < RMP; ++r) av[r] = sa[kk * kAS + tx + 16 * r];
 #pragma unroll
       for (int c = 0; c < kNC; ++c) bv[c] = sb[kk * kBS + ty + 16 * c];
-      if (cm == kNC) {
 #pragma unroll
-        for (int r = 0; r < RMP; ++r)
+      for (int r = 0; r < RMP; ++r)
 #pragma unroll
-          for (int c = 0; c < kNC; ++c) acc[r][c] = fma(av[r], bv[c], acc[r][c]);
-      } else {
-#pragma unroll
-        for (int r = 0; r < RMP; ++r) acc[r][0] = fma(av[r], bv[0], acc[r][0]);
-      }
+        for (int c = 0; c < kNC; ++c)
+          if (c < cm) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
     }
   }
 #pragma unroll
   for (int r = 0; r < RMP; ++r)
 #pragma unroll
     for (int c = 0; c < kNC; ++c) {
-      const int i = rb + tx + 16 * r, j = j0 + ty + 16 * c;
+      const int i = tx + 16 * r, j = j0 + ty + 16 * c;
       if (i < n && j < ncols) st(i, j, acc[r][c]);
     }
 }
 
-template <int RM, int PART, class CT, class LA, class LB, class ST>
+template <int RM, class LA, class LB, class ST>
 __device__ void cta_mm(int n, int ncols, int kdim, const LA& la, const LB& lb, const ST& st, Smem& sm) {
-  for (int j0 = 0; j0 < ncols; j0 += kPW) {
-    if constexpr (PART == 0) {
-      mm_pass<RM, CT>(n, ncols, kdim, 0, j0, la, lb, st, sm);
-    } else {
-      const int rb = PART == 1 ? (j0 & ~15) : 0;
-      const int re = PART == 1 ? n : min(n, j0 + kPW + 1);
-      const int rm = (((re - rb + 15) >> 4) + 1) & ~1;  // even row-group counts only
-      switch (rm) {
-        case 2: mm_pass<2, CT>(n, ncols, kdim, rb, j0, la, lb, st, sm); break;
-        case 4: if constexpr (RM >= 4) mm_pass<4, CT>(n, ncols, kdim, rb, j0, la, lb, st, sm); break;
-        case 6: if constexpr (RM >= 6) mm_pass<6, CT>(n, ncols, kdim, rb, j0, la, lb, st, sm); break;
-        default: if constexpr (RM >= 8) mm_pass<8, CT>(n, ncols, kdim, rb, j0, la, lb, st, sm); break;
-      }
-    }
-  }
+  for (int j0 = 0; j0 < ncols; j0 += kPW) mm_pass<RM>(n, ncols, kdim, j0, la, lb, st, sm);
   __syncthreads();
 }
 
@@ -299,7 +277,7 @@ __device__ void sylv_tiled(int n, int N, const short* bs, const unsigned char* b
   }
   __syncthreads();
   const int nt = sm.ntile;
-  float* sT = reinterpret_cast<float*>(sm.a);       // diagonal tiles of T: [tile][row * kTS + col]
+  float* sT = sm.a;       // diagonal tiles of T: [tile][row * kTS + col]
   float* sW = sT + kMaxTiles * kTS * kTS;            // the wave's tiles of R / W: [Q][row * kTS + col]
   for (int e = tid; e < nt * kTS * kTS; e += kRT) {
     const int t = e / (kTS * kTS), l = e - t * kTS * kTS, li = l / kTS, lj = l - li * kTS;
@@ -454,7 +432,7 @@ __device__ void refine_step(const RefineArgs& a, int b, int n, int step, Smem& s
     for (int idx = tid; idx < nn; idx += kRT) tnorm = nanmax(tnorm, fabsf(AtF[idx]));
     cta_max3(tnorm, dummy0, dummy1, sm);
     // M = N At + At N (FP32), then the right-hand sides -(L + M) on the block-lower part
-    cta_mm<RM, 0, float>(n, n, 2 * n, LdCatA{NF, false, AtF, n}, LdCatB{AtF, NF, n},
+    cta_mm<RM>(n, n, 2 * n, LdCatA{NF, false, AtF, n}, LdCatB{AtF, NF, n},
                       [&](int i, int j, float v) { M[(size_t)j * n + i] = v; }, sm);
     for (int idx = tid; idx < nn; idx += kRT) {
       const int i = idx % n, j = idx / n;
@@ -493,14 +471,14 @@ __device__ void refine_step(const RefineArgs& a, int b, int n, int step, Smem& s
   if (!fail) {
     if (ok) {
       // T = At + X^T At + At X (unit scale; At in FP64 from the tensor-core product), block-lower part zero, into A
-      cta_mm<RM, 0, float>(n, n, 2 * n, LdCatA{W, true, AtF, n}, LdCatB{AtF, W, n},
+      cta_mm<RM>(n, n, 2 * n, LdCatA{W, true, AtF, n}, LdCatB{AtF, W, n},
                         [&](int i, int j, float v) {
                           A[(size_t)j * n + i] = bid[i] > bid[j] ? 0.0 : Q[(size_t)j * n + i] + (double)v;
                         },
                         sm);
     }
     // Z <- Z + Z X (product in FP32), through P
-    cta_mm<RM, 0, float>(n, n, n, LdN<float, float>{ZF, n, 1.f}, LdNB<float, float>{W, n},
+    cta_mm<RM>(n, n, n, LdN<float, float>{ZF, n, 1.f}, LdNB<float, float>{W, n},
                       [&](int i, int j, float v) { P[(size_t)j * n + i] = Z[(size_t)j * n + i] + (double)v; }, sm);
     for (int idx = tid; idx < nn; idx += kRT) {
       const double z = P[idx];
