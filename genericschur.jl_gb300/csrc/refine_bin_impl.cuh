@@ -176,6 +176,7 @@ struct LdCatB {
 // eigenvalues that FP32 does not separate; the step then fails the tolerance).
 template <int M>
 __device__ __forceinline__ void gauss_solve(float (&K)[M][M], float (&r)[M], float floor) {
+  float inv[M];
 #pragma unroll
   for (int c = 0; c < M; ++c) {
 #pragma unroll
@@ -192,10 +193,10 @@ __device__ __forceinline__ void gauss_solve(float (&K)[M][M], float (&r)[M], flo
       r[i] = sw ? x : y;
     }
     if (fabsf(K[c][c]) < floor) K[c][c] = K[c][c] < 0.f ? -floor : floor;
-    const float inv = 1.f / K[c][c];
+    inv[c] = __frcp_rn(K[c][c]);  // one reciprocal per pivot, reused by the back substitution
 #pragma unroll
     for (int i = c + 1; i < M; ++i) {
-      const float f = K[i][c] * inv;
+      const float f = K[i][c] * inv[c];
 #pragma unroll
       for (int j = c; j < M; ++j) K[i][j] -= f * K[c][j];
       r[i] -= f * r[c];
@@ -206,7 +207,7 @@ __device__ __forceinline__ void gauss_solve(float (&K)[M][M], float (&r)[M], flo
     float v = r[c];
 #pragma unroll
     for (int j = c + 1; j < M; ++j) v -= K[c][j] * r[j];
-    r[c] = v / K[c][c];
+    r[c] = v * inv[c];
   }
 }
 
