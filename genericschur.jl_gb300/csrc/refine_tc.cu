@@ -21,7 +21,7 @@
 //     of the row maximum) and the dropped levels (s + t >= 10) stay below the rounding
 //     error of an FP64 dot product of the same length.
 //
-// Kernel k_refine_tc: persistent CTAs of 256 threads (one per SM: the eight level
+// Kernel k_refine_tc: persistent CTAs of 512 threads (one per SM: the eight level
 // accumulators fill the SM's 512 TMEM columns), each taking the matrices still being
 // refined from a ticket counter, largest first.  Per product, per 64-column panel of Y:
 // chunks of 32 contraction indices are split by all threads straight into shared memory
@@ -29,10 +29,11 @@
 // contiguous bytes, K-adjacent core matrices 128 B apart, 8-row groups 512 B apart),
 // double-buffered so that one chunk is split while the MMAs of the previous one run;
 // thread 0 issues the 36 slice products per 16-wide K step (tcgen05.mma, M = 128,
-// N = 64, K = 16) into the accumulator of their level; after the panel's last chunk all
-// eight warps drain the levels with tcgen05.ld.  Every wait is bounded: a timeout hands
-// the matrix to the FP64 kernel (status kStFallback), records the error, waits for the
-// CTA's MMAs, frees TMEM and ends the CTA.
+// N = 64, K = 16) into the accumulator of their level; after the panel's last chunk the
+// sixteen warps (four per TMEM lane quarter, 16 columns each) drain the levels with
+// tcgen05.ld.  Every wait is bounded: a timeout hands the matrix to the FP64 kernel
+// (status kStFallback), records the error, waits for the CTA's MMAs, frees TMEM and ends
+// the CTA.
 #include <cstdint>
 
 #include "refine_batched.cuh"
@@ -49,7 +50,7 @@ constexpr int kQLevels = 8;                        // levels s + t = 0 .. 7 (0-b
 constexpr int kQM = 128;                           // MMA M (rows of op(X), zero-padded)
 constexpr int kQN = 64;                            // MMA N: panel width of Y
 constexpr int kQK = 32;                            // contraction indices per chunk
-constexpr int kQThreads = 256;
+constexpr int kQThreads = 512;
 constexpr int kQXSlice = kQM * kQK * 2;            // bytes of one X slice of a chunk (8 KiB)
 constexpr int kQYSlice = kQN * kQK * 2;            // bytes of one Y slice of a chunk (4 KiB)
 constexpr int kQStage = kQSlices * (kQXSlice + kQYSlice);  // 96 KiB
@@ -168,7 +169,7 @@ __device__ bool tc_product(int n, const double* X, const double* Y, const int* e
       // rows of op(X) and columns of Y beyond n only reach outputs that are not stored, so
       // they are skipped; contraction indices beyond n are zero in both operands
       constexpr int kXItems = kQM * (kQK / 8), kItems = kXItems + kQN * (kQK / 8);
-      constexpr int kPer = kItems / kQThreads;  // 3
+      constexpr int kPer = (kItems + kQThreads - 1) / kQThreads;  // 2
       double v[kPer][8];
       int eit[kPer];
       unsigned char* dst[kPer];
@@ -176,8 +177,11 @@ __device__ bool tc_product(int n, const double* X, const double* Y, const int* e
 #pragma unroll
       for (int u = 0; u < kPer; ++u) {
         const int it = tid + u * kQThreads;
-        int row, kg, e = kQExpZero;
-        if (it < kXItems) {
+        int row = 0, kg = 0, e = kQExpZero;
+        if (it >= kItems) {
+          live[u] = false;
+          dst[u] = xs;
+        } else if (it < kXItems) {
           row = it & (kQM - 1); kg = it >> 7;
           live[u] = row < n;
           dst[u] = xs + (((row >> 3) * (kQK / 8) + kg) * 64 + (row & 7) * 8) * 2;
@@ -245,19 +249,18 @@ __device__ bool tc_product(int n, const double* X, const double* Y, const int* e
     if (ctl.fail) return false;
     tc_fence_after();
     {
-      const int q = warp & 3, h = warp >> 2;  // TMEM lane quarter, column half of the panel
+      const int q = warp & 3, cq = warp >> 2;  // TMEM lane quarter, 16-column quarter of the panel
       const int i = q * 32 + lane;
-      const int jb = j0 + h * 32;
-      // G = Z^T Z is symmetric: its panels' rows above the panel are not needed
-      const bool need = KIND != 2 || q * 32 + 32 > j0;
+      const int jb = j0 + cq * 16;
+      // G = Z^T Z is symmetric: only the lower triangle is formed (and mirrored)
+      const bool need = KIND != 2 || q * 32 + 32 > jb;
       if (jb < n && q * 32 < n && need) {  // warp-uniform
         // the eight exact level sums, as integers, combined in two 64-bit Horner sums of
         // four levels each (below 2^46, so their FP64 conversions are exact)
-        long long hs[32], ls[32];
+        long long hs[16], ls[16];
 #pragma unroll
-        for (int x = 0; x < 32; ++x) { hs[x] = 0; ls[x] = 0; }
-        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 32);
-        const bool two = jb + 16 < n;  // warp-uniform
+        for (int x = 0; x < 16; ++x) { hs[x] = 0; ls[x] = 0; }
+        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cq * 16);
 #pragma unroll 1
         for (int L = 0; L < kQLevels; ++L) {  // most significant level first
           uint32_t v[16];
@@ -270,22 +273,11 @@ __device__ bool tc_product(int n, const double* X, const double* Y, const int* e
 #pragma unroll
             for (int x = 0; x < 16; ++x) ls[x] = ls[x] * 128 + level_int(v[x]);
           }
-          if (two) {
-            tc_ld16(tb + L * kQN + 16, v);
-            tc_wait_ld();
-            if (L < 4) {
-#pragma unroll
-              for (int x = 0; x < 16; ++x) hs[16 + x] = hs[16 + x] * 128 + level_int(v[x]);
-            } else {
-#pragma unroll
-              for (int x = 0; x < 16; ++x) ls[16 + x] = ls[16 + x] * 128 + level_int(v[x]);
-            }
-          }
         }
         if (i < n) {
           const int ei = ex[i];
 #pragma unroll
-          for (int x = 0; x < 32; ++x) {
+          for (int x = 0; x < 16; ++x) {
             const int j = jb + x;
             if (j < n && (KIND != 2 || i >= j)) {
               const int fj = fy[j];
