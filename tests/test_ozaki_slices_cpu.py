@@ -4,8 +4,8 @@ refinement (genericschur.jl_gb300/csrc/refine_tc.cu).
 The kernel forms FP64-accurate products C = op(X) Y of n x n matrices (n <= 128) from BF16
 slice products: rows of op(X) and columns of Y are scaled by powers of two (max |x| < 2^e),
 cut into eight 7-bit slices (56 bits), every slice product is summed over k in an FP32
-accumulator per level s + t, and the eight level sums are combined as integers: adjacent
-levels never overflow, the two 64-bit Horner sums stay below 2^46, and
+accumulator per level s + t, and the eight level sums are combined as integers in two
+64-bit Horner sums of four levels each, which stay below 2^46, and
 
     C_ij = 2^(e_i + f_j - 14) (hs 2^-21 + ls 2^-49).
 
@@ -121,9 +121,8 @@ def test_level_bound_at_the_largest_order():
     for L in range(LEVELS):
         pairs = sum(1 for s in range(SLICES) for t in range(SLICES) if s + t == L)
         assert pairs * worst_pair < 2 ** 24
-    # adjacent levels paired in 32 bits and the two 64-bit Horner sums
+    # the two 64-bit Horner sums
     lev = [sum(1 for s in range(SLICES) for t in range(SLICES) if s + t == L) * worst_pair for L in range(LEVELS)]
-    assert max(lev[L] * 128 + lev[L + 1] for L in range(0, LEVELS, 2)) < 2 ** 31
     hs = ((lev[0] * 128 + lev[1]) * 128 + lev[2]) * 128 + lev[3]
     ls = ((lev[4] * 128 + lev[5]) * 128 + lev[6]) * 128 + lev[7]
     assert max(hs, ls) < 2 ** 46
