@@ -497,8 +497,6 @@ struct MixedBatch {
                                   // to FP64, Newton steps, FP64-accurate product FLOPs
   int* tc_err;                    // zeroed word, set when a tensor-core wait timed out
   cudaEvent_t ref0, ref1;         // null, or recorded around the refinement kernels
-  cudaEvent_t fp32_wait;  // null, or an event the FP32 stage waits for (a previous run's FP32 stage)
-  cudaEvent_t fp32_done;  // null, or recorded once the FP32 stage has finished
 };
 size_t mixed_batched_ws_bytes(long long na, long long nw, bool wantz);
 constexpr size_t kMixedSchedInts = 64;  // schedules and ticket counters of one run

@@ -51,7 +51,6 @@ struct gs_context {
   cudaStream_t pipe_s[kPipeChunks] = {}, pipe_aux[kPipeChunks][kNumBins] = {}, pipe_d2h = nullptr;
   cudaEvent_t pipe_h2d[kPipeChunks] = {}, pipe_fork[kPipeChunks] = {}, pipe_join[kPipeChunks][kNumBins] = {},
               pipe_done[kPipeChunks] = {}, pipe_out = nullptr;
-  cudaEvent_t pipe_mid[kPipeChunks] = {};  // mixed form: a run's FP32 stage done
 };
 
 namespace {
@@ -176,7 +175,6 @@ int gs_destroy(gs_context* ctx) {
       cudaEventDestroy(ctx->pipe_h2d[c]);
       cudaEventDestroy(ctx->pipe_fork[c]);
       cudaEventDestroy(ctx->pipe_done[c]);
-      cudaEventDestroy(ctx->pipe_mid[c]);
       for (int i = 0; i < kNumBins; ++i) {
         cudaStreamDestroy(ctx->pipe_aux[c][i]);
         cudaEventDestroy(ctx->pipe_join[c][i]);
@@ -365,7 +363,6 @@ static int pipe_setup(gs_context* ctx) {
     CK(cudaEventCreateWithFlags(&ctx->pipe_h2d[c], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->pipe_fork[c], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->pipe_done[c], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ctx->pipe_mid[c], cudaEventDisableTiming));
     for (int i = 0; i < kNumBins; ++i) {
       CK(cudaStreamCreateWithFlags(&ctx->pipe_aux[c][i], cudaStreamNonBlocking));
       CK(cudaEventCreateWithFlags(&ctx->pipe_join[c][i], cudaEventDisableTiming));
@@ -642,11 +639,7 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   const size_t o_order = ar.take<int>(count);
   const size_t o_sched = ar.take<int>(3 * kNumBins * kPipeChunks);
   size_t o_A = 0, o_Z = 0, o_wr = 0, o_wi = 0, o_ns = 0, o_offs = 0, o_woffs = 0, o_st = 0;
-  bool in_order = true;  // matrices stored one after another (the pipelined copy needs it)
   if (!dev) {
-    for (int64_t b = 1; b < count; ++b)
-      if (offs[b] < offs[b - 1] + (long long)ns[b - 1] * ns[b - 1] || woffs[b] < woffs[b - 1] + ns[b - 1])
-        in_order = false;
     o_A = ar.take<double>(na);
     o_Z = ar.take<double>(wantz ? na : 1);
     o_wr = ar.take<double>(nw);
@@ -657,7 +650,7 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
     o_st = ar.take<int>(count);
   }
   const size_t o_ws = ar.take<char>(mixed_batched_ws_bytes(na, nw, wantz));
-  const size_t o_iws = ar.take<int>(mixed_batched_iws_ints(count) + (kPipeChunks - 1) * kMixedSchedInts);
+  const size_t o_iws = ar.take<int>(mixed_batched_iws_ints(count));
   int rc = ensure_ws(ctx, ar.off);
   if (rc) return rc;
   char* base = ctx->dws;
@@ -689,32 +682,6 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
     mb.wr = (double*)(base + o_wr);
     mb.wi = (double*)(base + o_wi);
     mb.status = (int*)(base + o_st);
-    if (!(flags & GS_GRAPH) && in_order && count >= kPipeMinCount) {
-      // each run: the whole mixed sequence on its matrices, with its own slice of the
-      // per-matrix scratch and its own schedules (the counters add up over the runs)
-      CK(cudaMemsetAsync(mb.stats, 0, 5 * sizeof(unsigned long long), s));
-      return batched_pipelined<double>(
-          ctx, count, ns, offs, woffs, A, Z, wr, wi, status, (int*)mb.ns, (long long*)mb.offs, (long long*)mb.woffs,
-          mb.A, mb.Z, mb.wr, mb.wi, mb.status, [&](int c, int64_t b0, int64_t b1, cudaStream_t cs) -> int {
-            MixedBatch mc = mb;
-            mc.count = (int)(b1 - b0);
-            mc.ns = mb.ns + b0;
-            mc.offs = mb.offs + b0;
-            mc.woffs = mb.woffs + b0;
-            mc.status = mb.status + b0;
-            mc.order = mb.order + b0;
-            mc.sched = mb.sched + 3 * kNumBins * c;
-            mc.iws = mb.iws + 3 * b0 + (size_t)c * kMixedSchedInts;
-            // the run's FP32 stage follows the previous run's, so that it runs beside that
-            // run's refinement (FP32 and FP64 pipes) instead of competing with its FP32 stage
-            mc.fp32_wait = c > 0 ? ctx->pipe_mid[c - 1] : nullptr;
-            mc.fp32_done = ctx->pipe_mid[c];
-            cudaError_t e = launch_mixed_batched(mc, ctx->num_sms, cs, ctx->pipe_aux[c], kNumBins, ctx->pipe_fork[c],
-                                                 ctx->pipe_join[c], ctx->tun_real, ctx->tun_mixed32);
-            if (e != cudaSuccess) return set_err(ctx, GS_CUDA, "mixed batched launch: %s", cudaGetErrorString(e));
-            return GS_OK;
-          });
-    }
     CK(cudaMemcpyAsync((void*)mb.ns, ns, sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)mb.offs, offs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)mb.woffs, woffs, sizeof(long long) * count, cudaMemcpyHostToDevice, s));
@@ -735,7 +702,13 @@ static int schur_batched_mixed_impl(gs_context* ctx, int64_t count, const int32_
   mb.ref0 = ctx->mix_e0;
   mb.ref1 = ctx->mix_e1;
   ctx->mix_timed = true;
-  rc = run_graph_or_direct(ctx, (flags & GS_GRAPH) != 0, key, [&](cudaStream_t st) -> int {
+  // Host-buffer calls: all inputs in, the whole sequence as one CUDA graph (captured on the
+  // first call with these extents), all outputs out.  Runs of matrices whose copies overlap
+  // the other runs' kernels (the FP64 form's pipeline) were measured slower here: each run
+  // repeats the stages' tails (a large matrix's FP32 Schur and each Newton step), which
+  // costs more than the 14 ms of copies it hides.
+  const bool use_graph = (flags & GS_GRAPH) != 0 || !dev;
+  rc = run_graph_or_direct(ctx, use_graph, key, [&](cudaStream_t st) -> int {
     CK(cudaMemsetAsync(mb.stats, 0, 5 * sizeof(unsigned long long), st));
     cudaError_t e = launch_mixed_batched(mb, ctx->num_sms, st, ctx->aux, kNumBins, ctx->fork, ctx->join, ctx->tun_real,
                                          ctx->tun_mixed32);

@@ -187,10 +187,8 @@ cudaError_t launch_mixed_batched(const MixedBatch& m, int num_sms, cudaStream_t 
     }
     return cudaSuccess;
   };
-  if (m.fp32_wait && (e = cudaStreamWaitEvent(s, m.fp32_wait, 0)) != cudaSuccess) return e;
   e = forked([&]() { return launch_schur_batched_real32_tuned(b32, m.order, m.sched, num_sms, aux, naux, tun32); });
   if (e != cudaSuccess) return e;
-  if (m.fp32_done && (e = cudaEventRecord(m.fp32_done, s)) != cudaSuccess) return e;
   // 3. refinement, largest matrices first: per Newton step the tensor-core products, then
   // one kernel per default size bin (orders <= 32, 64, 96, 128: row tiles 2, 4, 6, 8 x 16),
   // forked like the Schur bins so that the bins' tails overlap

@@ -146,7 +146,7 @@ GS_API int gs_schur_batched_f64(gs_context* ctx, int64_t count, const int32_t* n
  * Newton steps taken, info[3] FLOPs of the refinement's FP64-accurate products (per step
  * 2 n^3 each for A Z, Z^T (A Z) and Z^T Z, run on the tensor cores), info[4] device time
  * of the refinement in microseconds, info[5] device time of the FP32 stage (conversion,
- * FP32 Schur) in microseconds (both -1 for a pipelined host-buffer call).  Synchronises
+ * FP32 Schur) in microseconds (both -1 if not timed).  Synchronises
  * the context stream.  GS_BADARG before the first GS_MIXED call; GS_CUDA (counters
  * filled) when a tensor-core wait timed out and its matrix was handed back. */
 GS_API int gs_mixed_batched_info(gs_context* ctx, int64_t* info);
